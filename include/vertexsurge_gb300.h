@@ -1,0 +1,233 @@
+/*
+ * vertexsurge_gb300 — C ABI of the GB300 (sm_103a) implementation of
+ * VertexSurge's variable-length graph pattern matching hot path:
+ * the bit-matrix multi-source BFS expand (VExpand), the vertex-id hash join
+ * (HashJoin), the multi-way intersection (Mintersect) and the glue operators
+ * between them (MatrixTableSelect, TableConvert, Count).
+ *
+ * Conventions
+ *  - Every call returns a status (VS_OK == 0); vs_last_error() gives the
+ *    message of the calling thread's last failure.
+ *  - Handles own device memory.  Pointers passed in (sources, columns, maps)
+ *    may be host or device memory; they are borrowed for the duration of the
+ *    call only.
+ *  - Calls are ordered on the stream passed (a cudaStream_t, NULL = legacy
+ *    default stream).  Calls that return a host-visible result (counts,
+ *    downloads, statistics) synchronise that stream.
+ *  - A handle is not thread-safe; independent handles are.
+ *
+ * Logical matrices.  A bit matrix has `rows` x `cols` logical elements;
+ * column c is stored as `wpc` consecutive uint64 words (wpc >= ceil(rows/64),
+ * even), element (r, c) is bit r % 64 of word c * wpc + r / 64.  An expand
+ * result has one row per source (in input order) and one column per vertex:
+ * column v is the set of sources that reach v.  Downloads produce the packed
+ * logical form with ceil(rows/64) words per column.
+ */
+#ifndef VERTEXSURGE_GB300_H
+#define VERTEXSURGE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference reports errors with assert/exit, e.g.
+ *      src/objects/operator/vexpand.cpp:88-91, join.cpp:82-85) ------------ */
+#define VS_OK 0
+#define VS_ERR_ARG 1         /* invalid argument or shape                   */
+#define VS_ERR_OOM 2         /* device allocation failed                    */
+#define VS_ERR_CUDA 3        /* a CUDA runtime call failed                  */
+#define VS_ERR_TIMEOUT 4     /* a bounded device-side wait gave up          */
+#define VS_ERR_UNSUPPORTED 5 /* combination the operator does not support   */
+#define VS_ERR_CAPACITY 6    /* output exceeded the caller's row bound      */
+
+/* Direction (src/include/common/common.hh, rules src/objects/meta/schema.cpp:261-302) */
+#define VS_DIR_FORWARD 0
+#define VS_DIR_BACKWARD 1
+#define VS_DIR_BOTH 2
+
+/* ExpandPathType (src/include/operator/expand.hh:24-28) */
+#define VS_PATH_ANY 0
+#define VS_PATH_SHORTEST 1
+#define VS_PATH_FIND_SHORTEST 2
+
+/* Per-hop expansion strategy */
+#define VS_STRAT_AUTO 0   /* fixed planner, or the learned picker when enabled */
+#define VS_STRAT_PULL 1   /* dense: every vertex ORs its active in-neighbour rows */
+#define VS_STRAT_PUSH 2   /* active rows OR-ed into out-neighbours with atomics */
+#define VS_STRAT_SPARSE 3 /* (vertex, source) pair lists, one bit per edge */
+
+/* Table kinds (src/include/execution/tuple.hh:9-18 TableType) */
+#define VS_KIND_VARROW 1
+#define VS_KIND_COLMAIN 2
+
+/* Flat column types (src/include/meta/type.hh: VID = uint32, Int64) */
+#define VS_T_VID 0
+#define VS_T_I64 1
+
+typedef void *vs_stream_t;
+typedef struct vs_graph vs_graph;
+typedef struct vs_bitmat vs_bitmat;
+typedef struct vs_flat vs_flat;
+typedef struct vs_expand_plan vs_expand_plan;
+
+const char *vs_last_error(void);
+/* Select the CUDA device for the calling thread and set up the stream-ordered
+ * allocator pool. */
+int vs_init(int device);
+const char *vs_version(void);
+
+/* ---- graph (replaces Graph::load + Graph::get_edges_refs CSR requests,
+ *      src/objects/storage/graph_store.cpp:48-73, :75-110, :142-189) ------
+ * fwd: out-lists (u -> v), rev: in-lists (v <- u), both int64 offsets [V+1]
+ * and uint32 ids, every list sorted.  directed == 0 marks an undirected edge
+ * type stored both ways, for which direction has no effect. */
+int vs_graph_upload(uint32_t V, uint64_t E, const int64_t *fwd_off, const uint32_t *fwd_dst,
+                    const int64_t *rev_off, const uint32_t *rev_src, int directed,
+                    vs_stream_t stream, vs_graph **out);
+int vs_graph_info(const vs_graph *g, uint32_t *V, uint64_t *E, int *directed);
+int vs_graph_free(vs_graph *g);
+
+/* ---- bit matrices (replaces DenseVarStackMatrix / DenseColMainMatrix and
+ *      VarRowMatrixTable / ColMainMatrixTable, src/include/storage/bitmap.hh:262-425,
+ *      src/include/execution/matrix_table.hh) ------------------------------ */
+typedef struct vs_bitmat_info {
+  uint32_t rows, cols, wpc;
+  int32_t kind;
+  int32_t has_row_map, has_col_map;
+  uint64_t *words; /* device pointer, cols * wpc words (borrowed) */
+} vs_bitmat_info;
+
+int vs_bitmat_create(uint32_t rows, uint32_t cols, int kind, vs_stream_t stream, vs_bitmat **out);
+int vs_bitmat_upload(vs_bitmat *m, const uint64_t *logical_words, vs_stream_t stream);
+int vs_bitmat_download(const vs_bitmat *m, uint64_t *logical_words, vs_stream_t stream);
+/* row_map[r] / col_map[c] give the vertex id of a physical row / column
+ * (MatrixTable::row_map / col_map); NULL leaves the map absent. */
+int vs_bitmat_set_maps(vs_bitmat *m, const uint32_t *row_map, const uint32_t *col_map,
+                       vs_stream_t stream);
+int vs_bitmat_get_maps(const vs_bitmat *m, uint32_t *row_map, uint32_t *col_map,
+                       vs_stream_t stream);
+int vs_bitmat_get_info(const vs_bitmat *m, vs_bitmat_info *info);
+int vs_bitmat_free(vs_bitmat *m);
+
+/* Count / Table::tuple_count on a matrix table: popcount
+ * (src/objects/operator/big_operators2.cpp:5-14, bitmap.cpp:1098-1125). */
+int vs_bitmat_count(const vs_bitmat *m, uint64_t *count, vs_stream_t stream);
+
+/* MatrixTableSelect on a VarRow table (big_operators2.cpp:138-213): the
+ * result keeps columns targets[0..T) (duplicates kept) and has col_map =
+ * targets, row_map inherited. */
+int vs_matrix_select(const vs_bitmat *m, const uint32_t *targets, uint32_t T, vs_bitmat **out,
+                     vs_stream_t stream);
+
+/* TableConvert VarRow -> ColMain (big_operators2.cpp:16-86); transpose
+ * swaps rows and columns together with their maps. */
+int vs_table_convert(const vs_bitmat *m, int transpose, vs_bitmat **out, vs_stream_t stream);
+
+/* TableConvert(Flat) / matrix iterators (bit_matrix_table.cpp:133-289):
+ * one (row value, column value) VID pair per set bit, maps applied. */
+int vs_bitmat_to_flat(const vs_bitmat *m, vs_flat **out, vs_stream_t stream);
+
+/* ---- flat tables (replaces FlatTable, src/include/execution/flat_table.hh) */
+int vs_flat_create(uint32_t ncols, const int32_t *types, uint64_t nrows, vs_flat **out);
+int vs_flat_upload(vs_flat *f, uint32_t col, const void *data, vs_stream_t stream);
+int vs_flat_download(const vs_flat *f, uint32_t col, void *data, vs_stream_t stream);
+int vs_flat_info(const vs_flat *f, uint32_t *ncols, uint64_t *nrows, int32_t *types);
+int vs_flat_free(vs_flat *f);
+
+/* ---- expand (replaces VExpand + Expand<DenseVarStackMatrix> with
+ *      ExpandStrategy::Dense: src/objects/operator/vexpand.cpp:45-483,
+ *      src/objects/operator/expand.cpp:210-414,
+ *      src/include/operator/expand_impl.hh:135-277) ----------------------- */
+typedef struct vs_expand_params {
+  uint32_t k_min, k_max;   /* hop range [k_min, k_max]; FindShortest uses k_max as the cap */
+  int32_t path_type;       /* VS_PATH_* */
+  int32_t direction;       /* VS_DIR_* */
+  int32_t strategy;        /* VS_STRAT_*: AUTO lets the planner choose per hop */
+  int32_t use_picker;      /* 1: the learned picker chooses under AUTO (when loaded) */
+  uint32_t hub_threshold;  /* in-degree above which a vertex gets a whole CTA (0 = tuned default) */
+  uint32_t slice_words;    /* source words per pass (0 = whole row up to 256 words) */
+  uint64_t pair_capacity;  /* sparse (vertex, source) list capacity (0 = default) */
+} vs_expand_params;
+
+#define VS_MAX_HOPS 64
+typedef struct vs_expand_stats {
+  uint32_t hops_run;              /* k_actual_max of the reference */
+  uint32_t found;                 /* FindShortest: targets found */
+  uint64_t visit_count;           /* Shortest: visited bits at the end */
+  uint64_t new_bits[VS_MAX_HOPS + 1];       /* bits set in layer h (Shortest: new bits) */
+  uint64_t active_vertices[VS_MAX_HOPS + 1];/* non-zero columns of layer h */
+  uint64_t active_edges[VS_MAX_HOPS + 1];   /* edges leaving non-zero columns of layer h-1 */
+  uint64_t pairs[VS_MAX_HOPS + 1];          /* sparse hops: pairs produced */
+  int32_t strategy[VS_MAX_HOPS + 1];        /* strategy run at hop h */
+} vs_expand_stats;
+
+/* A plan owns the frontier, next, visited and accumulator matrices for S
+ * sources and can be re-run; vs_expand_plan_run enqueues work only (no host
+ * synchronisation, no allocation), so it may be captured in a CUDA graph when
+ * sources/targets/distances are device pointers. */
+int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
+                          vs_expand_plan **out);
+int vs_expand_plan_run(vs_expand_plan *plan, const uint32_t *sources, const uint32_t *targets,
+                       int32_t *distances, vs_stream_t stream);
+/* Result of the last run as a borrowed VarRow matrix view (rows = sources,
+ * row_map = sources, cols = vertices), valid until the next run or free. */
+int vs_expand_plan_result(vs_expand_plan *plan, vs_bitmat **view);
+int vs_expand_plan_stats(vs_expand_plan *plan, vs_expand_stats *stats, vs_stream_t stream);
+int vs_expand_plan_free(vs_expand_plan *plan);
+
+/* One-shot expand: plan, run, hand the result matrix to the caller.
+ * FindShortest: targets[i] is the target of source i, distances[i] receives
+ * the hop count (0 when source == target, -1 when not found) and *out may be
+ * NULL. */
+int vs_expand(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_params *p,
+              const uint32_t *targets, int32_t *distances, vs_bitmat **out,
+              vs_expand_stats *stats, vs_stream_t stream);
+
+/* ---- hash join (replaces HashJoin, src/objects/operator/join.cpp:26-449) --
+ * A table operand is a flat table with the key in column key_col, or a
+ * ColMain matrix whose column variable is the key (rows are its payload).
+ * The result has join_schema order (src/objects/execution/tuple.cpp:317-342):
+ * every column of a, then every non-key column of b; a matrix operand
+ * contributes the columns (row value, key).  count is always the exact
+ * number of result tuples; at most max_rows are written to *out (the result
+ * holds min(count, max_rows) rows and the call returns VS_ERR_CAPACITY when
+ * it had to drop tuples).  only_count != 0 computes count only. */
+typedef struct vs_table_ref {
+  const vs_flat *flat;
+  const vs_bitmat *mat;
+  uint32_t key_col;
+} vs_table_ref;
+
+int vs_hash_join(vs_table_ref a, vs_table_ref b, int only_count, uint64_t max_rows,
+                 vs_flat **out, uint64_t *count, vs_stream_t stream);
+
+/* ---- multi-way intersection (replaces Mintersect,
+ *      src/objects/operator/mintersect.cpp:14-345) ---------------------------
+ * base: flat table or VarRow matrix (columns row value, column value).
+ * Each dependency supplies, for the vertex u found in base column base_col,
+ * a set of new vertices: a ColMain matrix (rows = new vertex, columns = u,
+ * maps optional), a flat edge table (columns u_col -> nv_col) or the graph's
+ * adjacency (u's out-list along direction).  For every base tuple the
+ * intersection of its dependencies' sets is emitted as (base columns...,
+ * new vertex); new_vertex_count bounds the new vertex ids when no dependency
+ * is a matrix. */
+typedef struct vs_isect_dep {
+  const vs_bitmat *mat;
+  const vs_flat *flat;
+  const vs_graph *graph;
+  int32_t direction;
+  uint32_t u_col, nv_col;
+  uint32_t base_col;
+} vs_isect_dep;
+
+int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
+                  uint32_t new_vertex_count, int only_count, uint64_t max_rows, vs_flat **out,
+                  uint64_t *count, vs_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VERTEXSURGE_GB300_H */

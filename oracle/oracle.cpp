@@ -1,0 +1,803 @@
+// ORACLE — test infrastructure only (see oracle.h for scope and citations).
+//
+// CPU restatement of VertexSurge's operators following the reference's scalar
+// branches.  Every function names the reference lines it restates.
+#include "oracle.h"
+
+#include <omp.h>
+
+#include <algorithm>
+#include <bit>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+int g_threads = 0;
+
+inline int nthreads() { return g_threads > 0 ? g_threads : omp_get_max_threads(); }
+
+inline size_t align_to(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// ---------------------------------------------------------------------------
+// DenseVarStackMatrix restated (bitmap.hh:329-425, set_derived bitmap.cpp:910-920).
+// Rows are grouped into stacks of R rows; a stack stores, for every column,
+// R/64 consecutive words (column-major inside the stack).
+struct StackMatrix {
+  static constexpr size_t V_ALIGN = 8;  // 512-bit alignment of the reference
+  size_t row_count, col_count, R, v_per_stack_col, v_per_stack, stack_count, total;
+  std::vector<uint64_t> bits;
+
+  StackMatrix(size_t rows, size_t cols, size_t stack_rows)
+      : row_count(rows), col_count(cols), R(stack_rows) {
+    v_per_stack_col = R / 64;
+    v_per_stack = align_to(v_per_stack_col * col_count, V_ALIGN);
+    stack_count = align_to(row_count, R) / R;
+    total = align_to(v_per_stack * stack_count, V_ALIGN);
+    bits.assign(total, 0);
+  }
+  // get_v_idx, bitmap.hh:350-353
+  inline size_t vidx(size_t r, size_t c) const {
+    return (r / R) * v_per_stack + c * v_per_stack_col + (r % R) / 64;
+  }
+  inline bool get(size_t r, size_t c) const { return (bits[vidx(r, c)] >> (r % 64)) & 1; }
+  inline void set(size_t r, size_t c, bool to) {
+    if (to)
+      bits[vidx(r, c)] |= 1ULL << (r % 64);
+    else
+      bits[vidx(r, c)] &= ~(1ULL << (r % 64));
+  }
+  // or_stack_col_from scalar branch, bitmap.cpp:1206-1213
+  inline void or_stack_col_from(size_t si, size_t c, const StackMatrix &o, size_t oc) {
+    size_t r = si * R;
+    uint64_t *p = &bits[vidx(r, c)];
+    const uint64_t *q = &o.bits[o.vidx(r, oc)];
+    for (size_t i = 0; i < v_per_stack_col; i++) p[i] = p[i] | q[i];
+  }
+  // dedup_and_update_visit_and_count scalar branch, bitmap.cpp:1078-1095
+  static size_t dedup_and_update_visit_and_count(StackMatrix &vis, StackMatrix &out) {
+    size_t re = 0;
+    uint64_t *v = vis.bits.data(), *o = out.bits.data();
+    const size_t n = vis.total;
+#pragma omp parallel for reduction(+ : re) num_threads(nthreads()) schedule(static)
+    for (size_t i = 0; i < n; i++) {
+      uint64_t x = v[i] & o[i];
+      o[i] = o[i] ^ x;
+      v[i] = v[i] | o[i];
+      re += std::popcount(v[i]);
+    }
+    return re;
+  }
+  // operator|= scalar branch, bitmap.cpp:995-1001
+  void or_from(const StackMatrix &o) {
+    uint64_t *v = bits.data();
+    const uint64_t *q = o.bits.data();
+#pragma omp parallel for num_threads(nthreads()) schedule(static)
+    for (size_t i = 0; i < total; i++) v[i] = v[i] | q[i];
+  }
+  // count scalar branch, bitmap.cpp:1113-1124
+  size_t count() const {
+    size_t re = 0;
+    const uint64_t *p = bits.data();
+#pragma omp parallel for reduction(+ : re) num_threads(nthreads()) schedule(static)
+    for (size_t i = 0; i < total; i++) re += std::popcount(p[i]);
+    return re;
+  }
+  bool col_nonzero(size_t si, size_t c) const {
+    const uint64_t *q = &bits[vidx(si * R, c)];
+    for (size_t i = 0; i < v_per_stack_col; i++)
+      if (q[i]) return true;
+    return false;
+  }
+  void to_logical(uint64_t *out) const {
+    const size_t wpc = (row_count + 63) / 64;
+#pragma omp parallel for num_threads(nthreads()) schedule(static)
+    for (size_t c = 0; c < col_count; c++)
+      for (size_t w = 0; w < wpc; w++) out[c * wpc + w] = bits[vidx(w * 64, c)];
+  }
+  void from_logical(const uint64_t *in) {
+    const size_t wpc = (row_count + 63) / 64;
+    for (size_t c = 0; c < col_count; c++)
+      for (size_t w = 0; w < wpc; w++) bits[vidx(w * 64, c)] = in[c * wpc + w];
+  }
+};
+
+// DenseColMainMatrix restated (bitmap.hh:262-326, bitmap.cpp:580-609): every
+// column holds v_per_col words, v_per_col aligned to 8 words.
+struct ColMain {
+  size_t row_count, col_count, v_per_col;
+  std::vector<uint64_t> bits;
+  ColMain(size_t rows, size_t cols) : row_count(rows), col_count(cols) {
+    v_per_col = align_to(align_to(rows, 64) / 64, 8);
+    bits.assign(v_per_col * cols, 0);
+  }
+  inline bool get(size_t r, size_t c) const { return (bits[c * v_per_col + r / 64] >> (r % 64)) & 1; }
+  inline void set(size_t r, size_t c, bool to) {
+    if (to)
+      bits[c * v_per_col + r / 64] |= 1ULL << (r % 64);
+    else
+      bits[c * v_per_col + r / 64] &= ~(1ULL << (r % 64));
+  }
+  uint64_t *col(size_t c) { return &bits[c * v_per_col]; }
+  const uint64_t *col(size_t c) const { return &bits[c * v_per_col]; }
+  // set_col_to scalar branch, bitmap.cpp:829-841
+  void set_col_to(size_t c, bool to) {
+    uint64_t *p = col(c);
+    for (size_t i = 0; i < v_per_col; i++) p[i] = to ? ~0ULL : 0ULL;
+  }
+  // and_col_from scalar branch, bitmap.cpp:874-879
+  void and_col_from(size_t c, const ColMain &o, size_t oc) {
+    uint64_t *p = col(c);
+    const uint64_t *q = o.col(oc);
+    for (size_t i = 0; i < v_per_col; i++) p[i] = p[i] & q[i];
+  }
+  // count_bits_in_col scalar branch, bitmap.cpp:655-666
+  size_t count_bits_in_col(size_t c) const {
+    size_t re = 0;
+    const uint64_t *p = col(c);
+    for (size_t i = 0; i < v_per_col; i++) re += std::popcount(p[i]);
+    return re;
+  }
+  void from_logical(const uint64_t *in) {
+    const size_t wpc = (row_count + 63) / 64;
+    for (size_t c = 0; c < col_count; c++)
+      for (size_t w = 0; w < wpc; w++) bits[c * v_per_col + w] = in[c * wpc + w];
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Edge sets of one expand step: the lists of "base" vertices u whose column is
+// OR-ed into target column v (out[v] |= base[u]).  Direction rules follow
+// EdgeSchema::check_src_or_dst_for_edge_ref (schema.cpp:261-302): directed
+// Forward uses src->dst, Backward uses dst->src, Both uses both; undirected
+// edge types are stored both ways and use the src->dst list.
+struct InLists {
+  const int64_t *off[2];
+  const uint32_t *adj[2];
+  int n = 0;
+};
+
+InLists in_lists(const int64_t *fwd_off, const uint32_t *fwd_dst, const int64_t *rev_off,
+                 const uint32_t *rev_src, int directed, int dir) {
+  InLists L;
+  bool use_fwd = !directed || dir == OR_FORWARD || dir == OR_BOTH;
+  bool use_bwd = directed && (dir == OR_BACKWARD || dir == OR_BOTH);
+  // out[v] |= base[u] for u->v means v's in-list (reverse CSR)
+  if (use_fwd) {
+    L.off[L.n] = rev_off;
+    L.adj[L.n] = rev_src;
+    L.n++;
+  }
+  // moving against u->v: out[u] |= base[v], i.e. u's out-list
+  if (use_bwd) {
+    L.off[L.n] = fwd_off;
+    L.adj[L.n] = fwd_dst;
+    L.n++;
+  }
+  return L;
+}
+
+// One dense hop, Expand<DenseVarStackMatrix>::expand_dense (expand.cpp:210-344):
+// edges are owned by their target column (the BlockHilbert dst partitions);
+// within a partition every stack is processed in turn.
+void expand_dense(const InLists &L, uint32_t V, const StackMatrix &base, StackMatrix &out) {
+#pragma omp parallel for num_threads(nthreads()) schedule(dynamic, 256)
+  for (size_t v = 0; v < V; v++) {
+    for (size_t si = 0; si < base.stack_count; si++) {
+      for (int l = 0; l < L.n; l++) {
+        for (int64_t j = L.off[l][v]; j < L.off[l][v + 1]; j++) {
+          out.or_stack_col_from(si, v, base, L.adj[l][j]);
+        }
+      }
+    }
+  }
+}
+
+uint64_t active_edges(const InLists &L, uint32_t V, const StackMatrix &base) {
+  uint64_t n = 0;
+#pragma omp parallel for reduction(+ : n) num_threads(nthreads()) schedule(dynamic, 256)
+  for (size_t v = 0; v < V; v++) {
+    for (int l = 0; l < L.n; l++) {
+      for (int64_t j = L.off[l][v]; j < L.off[l][v + 1]; j++) {
+        uint32_t u = L.adj[l][j];
+        bool nz = false;
+        for (size_t si = 0; si < base.stack_count && !nz; si++) nz = base.col_nonzero(si, u);
+        n += nz;
+      }
+    }
+  }
+  return n;
+}
+
+}  // namespace
+
+extern "C" {
+
+void oracle_set_threads(int n) { g_threads = n; }
+int oracle_get_threads(void) { return nthreads(); }
+
+// VExpand with ExpandStrategy::Dense over DenseVarStackMatrix:
+//   ExpandStatus init        expand_impl.hh:135-169 (stack size), :252-277 (layer 0 + visit)
+//   hop loop                  PhysicalOperator::run (physical_operator.cpp:62-101) with
+//                             VExpand::after_child (vexpand.cpp:222-284)
+//   one hop + dedup           expand.cpp:263-344
+//   result                    VExpand::merge_to_MT (vexpand.cpp:298-354)
+int oracle_vexpand(uint32_t V, const int64_t *fwd_off, const uint32_t *fwd_dst,
+                   const int64_t *rev_off, const uint32_t *rev_src, int directed,
+                   const uint32_t *sources, uint32_t S, uint32_t k_min, uint32_t k_max,
+                   int path_type, int dir, uint32_t stack_row_count, const uint32_t *targets,
+                   int32_t *dist, uint64_t *out_words, uint64_t *hop_stats) {
+  if (V == 0 || (S > 0 && !sources) || k_min > k_max || k_max > 64) return 1;
+  if (path_type < OR_ANY || path_type > OR_FIND_SHORTEST || dir < 0 || dir > 2) return 1;
+  if (path_type == OR_FIND_SHORTEST && (!targets || !dist)) return 1;
+  for (uint32_t i = 0; i < S; i++)
+    if (sources[i] >= V || (targets && targets[i] >= V)) return 1;
+  const size_t R = stack_row_count ? stack_row_count : 1024;  // decide_k0, expand.cpp:416-417
+  if (R % 512 != 0) return 1;
+  const size_t W = (S + 63) / 64;
+  if (S == 0) return 0;  // VExpand::before_execution returns false: empty result
+  InLists L = in_lists(fwd_off, fwd_dst, rev_off, rev_src, directed, dir);
+  const bool dedup = path_type != OR_ANY;
+
+  std::vector<std::unique_ptr<StackMatrix>> layers;
+  auto layer = [&](size_t i) -> StackMatrix & {
+    while (layers.size() <= i) layers.emplace_back(new StackMatrix(S, V, R));
+    return *layers[i];
+  };
+  std::unique_ptr<StackMatrix> visit;
+  if (dedup) visit.reset(new StackMatrix(S, V, R));
+  // init_first_m_layer (expand_impl.hh:252-277)
+  for (size_t i = 0; i < S; i++) {
+    layer(0).set(i, sources[i], true);
+    if (dedup) visit->set(i, sources[i], true);
+  }
+  size_t visit_count = S;
+  size_t last_visit_count = visit_count;
+  size_t found = 0;
+  if (path_type == OR_FIND_SHORTEST) {  // VExpand::before_execution, vexpand.cpp:179-195
+    for (size_t r = 0; r < S; r++) {
+      dist[r] = -1;
+      if (sources[r] == targets[r]) {
+        dist[r] = 0;
+        found++;
+      }
+    }
+  }
+  layer(std::max<size_t>(3, k_max) - 1);  // init_multiple_m_layer, vexpand.cpp:213-214
+  size_t k_actual_max = 0;
+  for (size_t i = 0; i < k_max; i++) {
+    StackMatrix &base = layer(i);
+    StackMatrix &out = layer(i + 1);
+    if (hop_stats) hop_stats[2 * 64 + i + 1] = active_edges(L, V, base);
+    expand_dense(L, V, base, out);
+    if (dedup) visit_count = StackMatrix::dedup_and_update_visit_and_count(*visit, out);
+    if (hop_stats) {
+      hop_stats[0 * 64 + i + 1] = visit_count;
+      hop_stats[1 * 64 + i + 1] = out.count();
+    }
+    k_actual_max = i + 1;  // after_child
+    bool cont = true;
+    if (path_type == OR_SHORTEST) {
+      if (last_visit_count == visit_count) cont = false;
+      last_visit_count = visit_count;
+    } else if (path_type == OR_FIND_SHORTEST) {
+      const int32_t d = (int32_t)(i + 1);
+      for (size_t r = 0; r < S; r++) {
+        if (dist[r] == -1 && out.get(r, targets[r])) {
+          dist[r] = d;
+          found++;
+        }
+      }
+      if (found == S)
+        cont = false;
+      else if (last_visit_count == visit_count)
+        cont = false;
+      last_visit_count = visit_count;
+    }
+    if (!cont) break;
+  }
+  if (hop_stats) hop_stats[3 * 64] = k_actual_max;
+  if (path_type == OR_FIND_SHORTEST || !out_words) return 0;
+  // merge_to_MT
+  if (path_type == OR_SHORTEST && k_min == 0) {
+    visit->to_logical(out_words);
+    return 0;
+  }
+  StackMatrix merged(S, V, R);
+  for (size_t i = k_min; i <= k_actual_max; i++) merged.or_from(layer(i));
+  merged.to_logical(out_words);
+  (void)W;
+  return 0;
+}
+
+uint64_t oracle_matrix_count(uint32_t rows, uint32_t cols, const uint64_t *words,
+                             uint32_t stack_row_count) {
+  StackMatrix m(rows, cols, stack_row_count ? stack_row_count : 1024);
+  m.from_logical(words);
+  return m.count();
+}
+
+// MatrixTableSelect::run_internal, VarRowMatrix branch (big_operators2.cpp:152-213)
+int oracle_matrix_select(uint32_t rows, uint32_t cols, const uint64_t *words,
+                         uint32_t stack_row_count, const uint32_t *targets, uint32_t T,
+                         uint64_t *out_words) {
+  const size_t R = stack_row_count ? stack_row_count : 1024;
+  for (uint32_t i = 0; i < T; i++)
+    if (targets[i] >= cols) return 1;
+  StackMatrix old(rows, cols, R);
+  old.from_logical(words);
+  StackMatrix nm(rows, T, R);
+#pragma omp parallel for num_threads(nthreads())
+  for (size_t ci = 0; ci < T; ci++)
+    for (size_t si = 0; si < nm.stack_count; si++) nm.or_stack_col_from(si, ci, old, targets[ci]);
+  nm.to_logical(out_words);
+  return 0;
+}
+
+// TableConvert::run_internal, VarRow -> ColMain (big_operators2.cpp:28-61)
+int oracle_table_convert(uint32_t rows, uint32_t cols, const uint64_t *words,
+                         uint32_t stack_row_count, int transpose, uint64_t *out_words) {
+  StackMatrix src(rows, cols, stack_row_count ? stack_row_count : 1024);
+  src.from_logical(words);
+  if (transpose) {
+    ColMain dst(cols, rows);
+#pragma omp parallel for num_threads(nthreads())
+    for (size_t r = 0; r < rows; r++)
+      for (size_t c = 0; c < cols; c++) dst.set(c, r, src.get(r, c));
+    const size_t wpc = ((size_t)cols + 63) / 64;
+    for (size_t c = 0; c < rows; c++)
+      for (size_t w = 0; w < wpc; w++) out_words[c * wpc + w] = dst.bits[c * dst.v_per_col + w];
+  } else {
+    // copy_from_variable_row_mat has no scalar path (bitmap.cpp:896-899); its
+    // SIMD path copies each stack column verbatim, i.e. an identical logical matrix.
+    ColMain dst(rows, cols);
+    const size_t wpc = ((size_t)rows + 63) / 64;
+    for (size_t c = 0; c < cols; c++)
+      for (size_t w = 0; w < wpc; w++) dst.bits[c * dst.v_per_col + w] = src.bits[src.vidx(w * 64, c)];
+    for (size_t c = 0; c < cols; c++)
+      for (size_t w = 0; w < wpc; w++) out_words[c * wpc + w] = dst.bits[c * dst.v_per_col + w];
+  }
+  return 0;
+}
+
+// VarRowMatrixTable::Iterator::next (bit_matrix_table.cpp:133-188) over every
+// stack; BitmapIterator::next (bitmap.hh:108-123) is the ctz loop.
+uint64_t oracle_matrix_iterate(uint32_t rows, uint32_t cols, const uint64_t *words,
+                               uint32_t stack_row_count, const uint32_t *row_map,
+                               const uint32_t *col_map, uint32_t *out_r, uint32_t *out_c) {
+  StackMatrix m(rows, cols, stack_row_count ? stack_row_count : 1024);
+  m.from_logical(words);
+  uint64_t n = 0;
+  for (size_t si = 0; si < m.stack_count; si++) {
+    const uint64_t *start = &m.bits[m.vidx(si * m.R, 0)];
+    const size_t nw = m.v_per_stack_col * cols;
+    for (size_t wi = 0; wi < nw; wi++) {
+      uint64_t d = start[wi];
+      while (d) {
+        size_t bitpos = wi * 64 + std::countr_zero(d);
+        d &= d - 1;
+        uint32_t r = (uint32_t)(bitpos % m.R + si * m.R);
+        uint32_t c = (uint32_t)(wi / m.v_per_stack_col);
+        if (row_map) r = row_map[r];
+        if (col_map) c = col_map[c];
+        if (out_r) {
+          out_r[n] = r;
+          out_c[n] = c;
+        }
+        n++;
+      }
+    }
+  }
+  return n;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Tables for HashJoin and Mintersect.
+namespace {
+
+struct Schema {
+  std::vector<int32_t> var, type;
+  int index(int32_t v) const {
+    for (size_t i = 0; i < var.size(); i++)
+      if (var[i] == v) return (int)i;
+    return -1;
+  }
+};
+
+// TableSchema::join_schema (tuple.cpp:317-342)
+Schema join_schema(const Schema &a, const Schema &b, int32_t key) {
+  Schema r = a;
+  for (size_t i = 0; i < b.var.size(); i++)
+    if (b.var[i] != key) {
+      r.var.push_back(b.var[i]);
+      r.type.push_back(b.type[i]);
+    }
+  return r;
+}
+
+// TableSchema::map_to (tuple.cpp:289-300)
+std::vector<int> map_to(const Schema &from, const Schema &to) {
+  std::vector<int> m;
+  for (auto v : from.var) m.push_back(to.index(v));
+  return m;
+}
+
+Schema schema_of(const or_table *t) {
+  Schema s;
+  for (uint32_t i = 0; i < t->ncols; i++) {
+    s.var.push_back(t->var[i]);
+    s.type.push_back(t->kind == OR_FLAT ? t->type[i] : OR_T_VID);
+  }
+  return s;
+}
+
+inline uint64_t flat_get(const or_table *t, uint64_t row, uint32_t col) {
+  if (t->type[col] == OR_T_I64) return (uint64_t)((const int64_t *)t->cols[col])[row];
+  return ((const uint32_t *)t->cols[col])[row];
+}
+
+uint64_t tuple_count(const or_table *t) {
+  if (t->kind == OR_FLAT) return t->nrows;
+  const size_t wpc = ((size_t)t->mrows + 63) / 64;
+  uint64_t n = 0;
+  for (size_t i = 0; i < wpc * t->mcols; i++) n += std::popcount(t->words[i]);
+  return n;
+}
+
+struct ColMainView {
+  const or_table *t;
+  ColMain m;
+  std::unordered_map<uint32_t, uint32_t> col_hash, row_hash;
+  explicit ColMainView(const or_table *tt) : t(tt), m(tt->mrows, tt->mcols) {
+    m.from_logical(tt->words);
+    if (tt->col_map)
+      for (uint32_t i = 0; i < tt->mcols; i++) col_hash.emplace(tt->col_map[i], i);
+    if (tt->row_map)
+      for (uint32_t i = 0; i < tt->mrows; i++) row_hash.emplace(tt->row_map[i], i);
+  }
+  uint32_t col_value(size_t c) const { return t->col_map ? t->col_map[c] : (uint32_t)c; }
+  uint32_t row_value(size_t r) const { return t->row_map ? t->row_map[r] : (uint32_t)r; }
+  // MatrixTable::find_col_idx (bit_matrix_table.cpp:53-61)
+  bool find_col_idx(uint32_t v, size_t *out) const {
+    if (!t->col_map) {
+      if (v < t->mcols) {
+        *out = v;
+        return true;
+      }
+      return false;
+    }
+    auto it = col_hash.find(v);
+    if (it == col_hash.end()) return false;
+    *out = it->second;
+    return true;
+  }
+  // ColMainMatrixTable::Iterator over one column (bit_matrix_table.cpp:242-289)
+  template <typename F> void for_rows(size_t c, F f) const {
+    const uint64_t *p = m.col(c);
+    for (size_t w = 0; w < m.v_per_col; w++) {
+      uint64_t d = p[w];
+      while (d) {
+        size_t r = w * 64 + std::countr_zero(d);
+        d &= d - 1;
+        f(row_value(r));
+      }
+    }
+  }
+};
+
+struct ResultBuilder {
+  Schema s;
+  std::vector<std::vector<uint64_t>> cols;
+  explicit ResultBuilder(const Schema &sc) : s(sc), cols(sc.var.size()) {}
+  void finish(or_result *out) {
+    out->ncols = (uint32_t)s.var.size();
+    out->nrows = cols.empty() ? 0 : cols[0].size();
+    for (size_t i = 0; i < s.var.size(); i++) {
+      out->var[i] = s.var[i];
+      out->type[i] = s.type[i];
+      if (s.type[i] == OR_T_I64) {
+        int64_t *p = (int64_t *)std::malloc(sizeof(int64_t) * (out->nrows + 1));
+        for (uint64_t r = 0; r < out->nrows; r++) p[r] = (int64_t)cols[i][r];
+        out->cols[i] = p;
+      } else {
+        uint32_t *p = (uint32_t *)std::malloc(sizeof(uint32_t) * (out->nrows + 1));
+        for (uint64_t r = 0; r < out->nrows; r++) p[r] = (uint32_t)cols[i][r];
+        out->cols[i] = p;
+      }
+    }
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+void oracle_free_result(or_result *r) {
+  if (!r) return;
+  for (uint32_t i = 0; i < r->ncols && i < 16; i++) std::free(r->cols[i]);
+  std::memset(r, 0, sizeof(*r));
+}
+
+// HashJoin::build + HashJoin::probe (join.cpp:26-444).  The reference's hash
+// maps are tbb::concurrent_hash_map keyed by XXH64 of a TupleValue; the hash
+// function is unobservable, so std::unordered_map stands in.
+int oracle_hash_join(const or_table *a, const or_table *b, int32_t key_var, int only_count,
+                     or_result *out) {
+  std::memset(out, 0, sizeof(*out));
+  if (a->kind == OR_VARROW || b->kind == OR_VARROW) return 1;  // not supported (join.cpp:73-77)
+  Schema sa = schema_of(a), sb = schema_of(b);
+  int ka = sa.index(key_var), kb = sb.index(key_var);
+  if (ka < 0 || kb < 0 || sa.type[ka] != sb.type[kb]) return 1;
+  Schema rs = only_count ? Schema{{-1}, {OR_T_I64}} : join_schema(sa, sb, key_var);
+  if (rs.var.size() > 16) return 1;
+
+  const or_table *build = a, *probe = b;
+  auto col_count = [](const or_table *t) -> uint64_t { return t->mcols; };
+  // build-side choice, join.cpp:39-72
+  if (build->kind == OR_FLAT && probe->kind == OR_FLAT) {
+    if (build->nrows < probe->nrows) std::swap(build, probe);
+  } else if (build->kind == OR_FLAT && probe->kind == OR_COLMAIN) {
+    if (build->nrows < col_count(probe)) std::swap(build, probe);
+  } else if (build->kind == OR_COLMAIN && probe->kind == OR_FLAT) {
+    if (col_count(build) < probe->nrows) std::swap(build, probe);
+  } else {
+    if (col_count(build) < col_count(probe)) std::swap(build, probe);
+  }
+  Schema bs = schema_of(build), ps = schema_of(probe);
+  const int bk = bs.index(key_var), pk = ps.index(key_var);
+  if ((build->kind == OR_COLMAIN && bk != 1) || (probe->kind == OR_COLMAIN && pk != 1)) return 1;
+
+  std::unordered_map<uint64_t, std::vector<uint64_t>> flat_map;  // key -> build rows
+  std::unordered_map<uint64_t, uint64_t> count_map;              // key -> multiplicity
+  std::unique_ptr<ColMainView> bview, pview;
+  if (build->kind == OR_COLMAIN) bview.reset(new ColMainView(build));
+  if (probe->kind == OR_COLMAIN) pview.reset(new ColMainView(probe));
+
+  // build (join.cpp:86-155)
+  if (build->kind == OR_FLAT) {
+    for (uint64_t i = 0; i < build->nrows; i++) {
+      uint64_t k = flat_get(build, i, bk);
+      if (only_count)
+        count_map[k]++;
+      else
+        flat_map[k].push_back(i);
+    }
+  } else if (only_count) {
+    for (size_t c = 0; c < build->mcols; c++)
+      count_map.emplace(bview->col_value(c), bview->m.count_bits_in_col(c));  // insert keeps the first
+  }
+
+  ResultBuilder res(rs);
+  int64_t total = 0;
+  auto push_row = [&](std::vector<uint64_t> &vals) {
+    for (size_t i = 0; i < vals.size(); i++) res.cols[i].push_back(vals[i]);
+  };
+  const std::vector<int> pmap = map_to(ps, rs), bmap = map_to(bs, rs);
+
+  if (probe->kind == OR_FLAT) {
+    if (only_count) {  // join.cpp:266-278
+      for (uint64_t i = 0; i < probe->nrows; i++) {
+        auto it = count_map.find(flat_get(probe, i, pk));
+        if (it != count_map.end()) total += (int64_t)it->second;
+      }
+    } else if (build->kind == OR_FLAT) {  // join.cpp:183-225
+      std::vector<uint64_t> vals(rs.var.size());
+      for (uint64_t pi = 0; pi < probe->nrows; pi++) {
+        auto it = flat_map.find(flat_get(probe, pi, pk));
+        if (it == flat_map.end()) continue;
+        for (uint64_t bi : it->second) {
+          for (size_t c = 0; c < pmap.size(); c++)
+            if (pmap[c] >= 0 && (int)c != pk) vals[pmap[c]] = flat_get(probe, pi, c);
+          for (size_t c = 0; c < bmap.size(); c++)
+            if (bmap[c] >= 0) vals[bmap[c]] = flat_get(build, bi, c);
+          push_row(vals);
+        }
+      }
+    } else {  // Flat probe x ColMain build, join.cpp:226-262
+      std::vector<uint64_t> vals(rs.var.size());
+      const int payload = bmap[0];
+      for (uint64_t i = 0; i < probe->nrows; i++) {
+        uint32_t vid = (uint32_t)flat_get(probe, i, pk);
+        size_t col;
+        // the reference dereferences a failed lookup (join.cpp:241-244); a
+        // missing key contributes no tuple here
+        if (!bview->find_col_idx(vid, &col)) continue;
+        bview->for_rows(col, [&](uint32_t r) {
+          for (size_t c = 0; c < pmap.size(); c++)
+            if (pmap[c] >= 0) vals[pmap[c]] = flat_get(probe, i, c);
+          vals[payload] = r;
+          push_row(vals);
+        });
+      }
+    }
+  } else {  // probe is ColMain
+    if (only_count) {  // join.cpp:406-430
+      for (size_t c = 0; c < probe->mcols; c++) {
+        auto it = count_map.find(pview->col_value(c));
+        if (it != count_map.end()) total += (int64_t)(it->second * pview->m.count_bits_in_col(c));
+      }
+    } else if (build->kind == OR_FLAT) {  // join.cpp:281-331
+      std::vector<uint64_t> vals(rs.var.size());
+      for (size_t c = 0; c < probe->mcols; c++) {
+        auto it = flat_map.find(pview->col_value(c));
+        if (it == flat_map.end()) continue;
+        pview->for_rows(c, [&](uint32_t prow) {
+          for (uint64_t bri : it->second) {
+            vals[pmap[0]] = prow;
+            for (size_t bc = 0; bc < bmap.size(); bc++)
+              if (bmap[bc] >= 0) vals[bmap[bc]] = flat_get(build, bri, bc);
+            push_row(vals);
+          }
+        });
+      }
+    } else {  // ColMain x ColMain, join.cpp:333-401
+      std::vector<uint64_t> vals(rs.var.size());
+      const int payload = bmap[0];
+      for (size_t c = 0; c < probe->mcols; c++) {
+        uint32_t key = pview->col_value(c);
+        size_t bcol;
+        if (!bview->find_col_idx(key, &bcol)) continue;
+        std::vector<uint32_t> brows;
+        bview->for_rows(bcol, [&](uint32_t r) { brows.push_back(r); });
+        pview->for_rows(c, [&](uint32_t pr) {
+          for (uint32_t br : brows) {
+            vals[pmap[0]] = pr;
+            vals[pmap[1]] = key;
+            vals[payload] = br;
+            push_row(vals);
+          }
+        });
+      }
+    }
+  }
+  if (only_count) {
+    out->ncols = 1;
+    out->nrows = 1;
+    out->var[0] = -1;
+    out->type[0] = OR_T_I64;
+    int64_t *p = (int64_t *)std::malloc(sizeof(int64_t));
+    *p = total;
+    out->cols[0] = p;
+    out->count = total;
+    return 0;
+  }
+  res.finish(out);
+  out->count = (int64_t)out->nrows;
+  return 0;
+}
+
+// Mintersect::finishAddingDependency + run_internal (mintersect.cpp:14-345).
+int oracle_mintersect(const or_table *base, const or_table *deps, uint32_t ndeps,
+                      int32_t new_var, uint32_t new_type_vertex_count, int only_count,
+                      or_result *out) {
+  std::memset(out, 0, sizeof(*out));
+  if (ndeps == 0 || base->kind == OR_COLMAIN) return 1;
+  Schema bsch = schema_of(base);
+  std::vector<int> var_base_idx(ndeps), edges_u_idx(ndeps), edges_nv_idx(ndeps);
+  for (uint32_t i = 0; i < ndeps; i++) {
+    const or_table *d = &deps[i];
+    if (d->ncols != 2 || d->kind == OR_VARROW) return 1;
+    Schema ds = schema_of(d);
+    int nv = ds.index(new_var);
+    if (nv < 0 || ds.type[nv] != OR_T_VID) return 1;
+    edges_nv_idx[i] = nv;
+    edges_u_idx[i] = 1 - nv;
+    var_base_idx[i] = bsch.index(ds.var[1 - nv]);
+    if (var_base_idx[i] < 0) return 1;
+    // a ColMain dependency has the new vertex as its row variable (mintersect.cpp:59)
+    if (d->kind == OR_COLMAIN && nv != 0) return 1;
+  }
+  Schema rs;
+  if (only_count) {
+    rs = Schema{{-1}, {OR_T_I64}};
+  } else {
+    rs = bsch;
+    rs.var.push_back(new_var);
+    rs.type.push_back(OR_T_VID);
+  }
+  // cache rows: the ColMain row count when every dependency is a matrix
+  size_t ncm = 0, cm_rows = 0;
+  std::vector<std::unique_ptr<ColMainView>> views(ndeps);
+  const uint32_t *target_row_map = nullptr;
+  for (uint32_t i = 0; i < ndeps; i++) {
+    if (deps[i].kind == OR_COLMAIN) {
+      views[i].reset(new ColMainView(&deps[i]));
+      if (ncm && cm_rows != deps[i].mrows) return 1;
+      cm_rows = deps[i].mrows;
+      if (!ncm) target_row_map = deps[i].row_map;
+      ncm++;
+    }
+  }
+  const size_t cache_rows = (ncm == ndeps) ? cm_rows : new_type_vertex_count;
+
+  // base tuples: Flat rows or the (row, col) pairs of a VarRow matrix
+  std::vector<std::vector<uint64_t>> base_rows;
+  if (base->kind == OR_FLAT) {
+    base_rows.resize(base->nrows);
+    for (uint64_t i = 0; i < base->nrows; i++)
+      for (uint32_t c = 0; c < base->ncols; c++) base_rows[i].push_back(flat_get(base, i, c));
+  } else {
+    uint64_t n = oracle_matrix_iterate(base->mrows, base->mcols, base->words, 1024, nullptr,
+                                       nullptr, nullptr, nullptr);
+    std::vector<uint32_t> r(n), c(n);
+    oracle_matrix_iterate(base->mrows, base->mcols, base->words, 1024, base->row_map,
+                          base->col_map, r.data(), c.data());
+    base_rows.resize(n);
+    for (uint64_t i = 0; i < n; i++) base_rows[i] = {r[i], c[i]};
+  }
+
+  ResultBuilder res(rs);
+  int64_t total = 0;
+  const size_t nbase = base_rows.size();
+  const int nt = nthreads();
+  std::vector<std::vector<std::vector<uint64_t>>> per_thread(nt);
+#pragma omp parallel num_threads(nt) reduction(+ : total)
+  {
+    const int t = omp_get_thread_num();
+    ColMain ir(cache_rows, 2);  // col 0 = result, col 1 = flat scratch
+#pragma omp for schedule(dynamic, 64)
+    for (size_t bi = 0; bi < nbase; bi++) {
+      ir.set_col_to(0, true);
+      for (uint32_t di = 0; di < ndeps; di++) {
+        uint32_t bvid = (uint32_t)base_rows[bi][var_base_idx[di]];
+        const or_table *d = &deps[di];
+        if (d->kind == OR_COLMAIN) {
+          size_t col;
+          if (views[di]->find_col_idx(bvid, &col))
+            ir.and_col_from(0, views[di]->m, col);
+          else
+            ir.set_col_to(0, false);
+        } else {
+          // linear scan of the flat dependency (mintersect.cpp:149-165);
+          // the dependency's own u column is used for both base kinds
+          ir.set_col_to(1, false);
+          for (uint64_t i = 0; i < d->nrows; i++) {
+            if ((uint32_t)flat_get(d, i, edges_u_idx[di]) != bvid) continue;
+            uint64_t payload = flat_get(d, i, edges_nv_idx[di]);
+            if (payload < cache_rows) ir.set(payload, 1, true);
+          }
+          ir.and_col_from(0, ir, 1);
+        }
+      }
+      size_t num = ir.count_bits_in_col(0);
+      total += (int64_t)num;
+      if (num == 0 || only_count) continue;
+      const uint64_t *p = ir.col(0);
+      for (size_t w = 0; w < ir.v_per_col; w++) {
+        uint64_t dd = p[w];
+        while (dd) {
+          uint32_t x = (uint32_t)(w * 64 + std::countr_zero(dd));
+          dd &= dd - 1;
+          if (target_row_map) x = target_row_map[x];
+          std::vector<uint64_t> row = base_rows[bi];
+          row.push_back(x);
+          per_thread[t].push_back(std::move(row));
+        }
+      }
+    }
+  }
+  if (only_count) {
+    out->ncols = 1;
+    out->nrows = 1;
+    out->var[0] = -1;
+    out->type[0] = OR_T_I64;
+    int64_t *p = (int64_t *)std::malloc(sizeof(int64_t));
+    *p = total;
+    out->cols[0] = p;
+    out->count = total;
+    return 0;
+  }
+  for (auto &v : per_thread)
+    for (auto &row : v)
+      for (size_t i = 0; i < row.size(); i++) res.cols[i].push_back(row[i]);
+  res.finish(out);
+  out->count = (int64_t)out->nrows;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,157 @@
+"""GPU parity of the expand (VExpand) against the CPU oracle, bit-exact,
+through the C ABI.  Covers every path type, direction, hop range, every
+pull kernel variant (row widths from 1 to 256 words), forced strategies,
+hub CTAs, multi-slice rows, duplicate sources and FindShortest."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from tests import graphs as G
+from vertexsurge_gb300 import graphgen
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def graphs(vs):
+    hg = G.small_graphs()
+    return {k: (g, vs.DeviceGraph.from_host(g)) for k, g in hg.items()}
+
+
+def run_both(vs, g, dg, src, k_min, k_max, path, direction, **kw):
+    m, _, st = vs.expand(dg, src, k_min, k_max, path, direction, stats=True, **kw)
+    got = m.download()
+    exp, _, _ = O.vexpand(g, src, k_min, k_max, path, direction)
+    return got, exp, st
+
+
+@pytest.mark.parametrize("path", ["any", "shortest"])
+@pytest.mark.parametrize("direction", ["forward", "backward", "both"])
+@pytest.mark.parametrize("krange", [(0, 2), (1, 3), (2, 4), (1, 1)])
+def test_expand_parity_paths(vs, graphs, path, direction, krange):
+    for name, (g, dg) in graphs.items():
+        src = graphgen.sample_sources(g.V, 96, seed=7)
+        got, exp, st = run_both(vs, g, dg, src, krange[0], krange[1], path, direction)
+        assert np.array_equal(got, exp), (name, path, direction, krange, st)
+
+
+@pytest.mark.parametrize("S", [1, 31, 64, 65, 128, 200, 512, 1000, 2048, 4096, 8192, 16384])
+def test_expand_parity_row_widths(vs, graphs, S):
+    g, dg = graphs["rmat11_skew"]
+    src = graphgen.sample_sources(g.V, min(S, g.V), seed=S)
+    if S > g.V:
+        src = np.resize(src, S).astype(np.uint32)  # repeated sources are independent rows
+    for path in ("any", "shortest"):
+        got, exp, _ = run_both(vs, g, dg, src, 1, 3, path, "forward")
+        assert np.array_equal(got, exp), (S, path)
+
+
+@pytest.mark.parametrize("strategy", ["pull", "sparse", "push", "auto"])
+@pytest.mark.parametrize("path", ["any", "shortest"])
+def test_expand_forced_strategies(vs, graphs, strategy, path):
+    for name, (g, dg) in graphs.items():
+        src = graphgen.sample_sources(g.V, 150, seed=3)
+        got, exp, st = run_both(vs, g, dg, src, 1, 4, path, "forward", strategy=strategy)
+        assert np.array_equal(got, exp), (name, strategy, path, st)
+
+
+def test_expand_hub_ctas_and_slices(vs, graphs):
+    for name, (g, dg) in graphs.items():
+        src = graphgen.sample_sources(g.V, 300, seed=9)
+        for kw in ({"hub_threshold": 8}, {"slice_words": 2}, {"slice_words": 4, "hub_threshold": 16},
+                   {"strategy": "pull", "slice_words": 2}):
+            for path in ("any", "shortest"):
+                got, exp, _ = run_both(vs, g, dg, src, 1, 3, path, "both", **kw)
+                assert np.array_equal(got, exp), (name, kw, path)
+
+
+def test_expand_sparse_overflow_falls_back(vs, graphs):
+    g, dg = graphs["rmat10"]
+    src = graphgen.sample_sources(g.V, 200, seed=5)
+    for path in ("any", "shortest"):
+        got, exp, st = run_both(vs, g, dg, src, 1, 4, path, "forward", strategy="sparse",
+                                pair_capacity=300)
+        assert np.array_equal(got, exp), st
+
+
+def test_expand_duplicate_sources(vs, graphs):
+    g, dg = graphs["rmat10"]
+    src = np.array([5, 5, 17, 900, 5, 17, 0, 0], dtype=np.uint32)
+    for path in ("any", "shortest"):
+        for kr in ((0, 3), (1, 3), (2, 5)):
+            got, exp, _ = run_both(vs, g, dg, src, kr[0], kr[1], path, "forward")
+            assert np.array_equal(got, exp), (path, kr)
+
+
+def test_expand_early_stop_hops_run(vs, graphs):
+    g, dg = graphs["rmat10"]
+    src = graphgen.sample_sources(g.V, 64, seed=1)
+    m, _, st = vs.expand(dg, src, 1, 30, "shortest", "forward", stats=True)
+    _, _, ost = O.vexpand(g, src, 1, 30, "shortest", "forward", hop_stats=True)
+    assert st["hops_run"] == ost["hops_run"] < 30
+    assert st["visit_count"] == ost["visit_count"][-1]
+    exp, _, _ = O.vexpand(g, src, 1, 30, "shortest", "forward")
+    assert np.array_equal(m.download(), exp)
+
+
+def test_expand_find_shortest(vs, graphs):
+    for name, (g, dg) in graphs.items():
+        S = 120
+        src = graphgen.sample_sources(g.V, S, seed=31)
+        tgt = graphgen.sample_sources(g.V, S, seed=32)
+        tgt[:7] = src[:7]
+        _, dist, _ = vs.expand(dg, src, 1, 50, "find_shortest", "forward", targets=tgt)
+        _, odist, _ = O.vexpand(g, src, 1, 50, "find_shortest", "forward", targets=tgt)
+        assert np.array_equal(dist, odist), name
+
+
+def test_expand_stats_active_edges(vs, graphs):
+    g, dg = graphs["zipf3000"]
+    src = graphgen.sample_sources(g.V, 256, seed=2)
+    for path in ("any", "shortest"):
+        _, _, st = vs.expand(dg, src, 1, 3, path, "forward", stats=True)
+        _, _, ost = O.vexpand(g, src, 1, 3, path, "forward", hop_stats=True)
+        assert st["active_edges"][1:] == ost["active_edges"][1:], (path, st, ost)
+
+
+def test_plan_rerun_is_clean(vs, graphs):
+    """A reused plan must give the same answer for a different source set."""
+    g, dg = graphs["rmat11_skew"]
+    p = vs.make_params(1, 3, "shortest", "forward")
+    plan = vs.ExpandPlan(dg, 256, p)
+    for seed in (1, 2, 1):
+        src = graphgen.sample_sources(g.V, 256, seed=seed)
+        plan.run(src)
+        got = plan.result().download()
+        exp, _, _ = O.vexpand(g, src, 1, 3, "shortest", "forward")
+        assert np.array_equal(got, exp), seed
+
+
+def test_expand_empty_and_isolated(vs):
+    # a graph with isolated vertices and a single edge
+    g = graphgen.from_edges(10, [1], [2])
+    dg = vs.DeviceGraph.from_host(g)
+    src = np.array([0, 1, 2, 9], dtype=np.uint32)
+    for path in ("any", "shortest"):
+        m, _, _ = vs.expand(dg, src, 0, 3, path, "both")
+        exp, _, _ = O.vexpand(g, src, 0, 3, path, "both")
+        assert np.array_equal(m.download(), exp)
+    m, _, _ = vs.expand(dg, np.zeros(0, np.uint32), 1, 3, "any", "forward")
+    assert m.shape == (0, 10) and m.count() == 0
+
+
+def test_expand_rejects_bad_arguments(vs, graphs):
+    g, dg = graphs["rmat10"]
+    with pytest.raises(vs.VsError):
+        vs.expand(dg, np.array([1], np.uint32), 3, 2, "any", "forward")
+    with pytest.raises(vs.VsError):
+        vs.expand(dg, np.array([1], np.uint32), 1, 65, "any", "forward")
+
+
+def test_expand_rejects_out_of_range_ids(vs, graphs):
+    g, dg = graphs["rmat10"]
+    with pytest.raises(vs.VsError):
+        vs.expand(dg, np.array([1, g.V + 5], np.uint32), 1, 2, "shortest", "forward")
+    with pytest.raises(vs.VsError):
+        vs.expand(dg, np.array([1, 2], np.uint32), 1, 5, "find_shortest", "forward",
+                  targets=np.array([3, g.V], np.uint32))

@@ -1,0 +1,458 @@
+"""ctypes binding of the C ABI in include/vertexsurge_gb300.h.
+
+This is the Python-side view of the drop-in boundary: every call goes to
+libvsgb300.so (hand-written sm_103a CUDA).  There is no fallback: if the
+library is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libvsgb300.so"
+
+VS_OK, VS_ERR_ARG, VS_ERR_OOM, VS_ERR_CUDA, VS_ERR_TIMEOUT, VS_ERR_UNSUPPORTED, VS_ERR_CAPACITY = range(7)
+DIR_FORWARD, DIR_BACKWARD, DIR_BOTH = 0, 1, 2
+PATH_ANY, PATH_SHORTEST, PATH_FIND_SHORTEST = 0, 1, 2
+STRAT_AUTO, STRAT_PULL, STRAT_PUSH, STRAT_SPARSE = 0, 1, 2, 3
+KIND_VARROW, KIND_COLMAIN = 1, 2
+T_VID, T_I64 = 0, 1
+MAX_HOPS = 64
+
+_DIRS = {"forward": DIR_FORWARD, "backward": DIR_BACKWARD, "both": DIR_BOTH}
+_PATHS = {"any": PATH_ANY, "shortest": PATH_SHORTEST, "find_shortest": PATH_FIND_SHORTEST}
+_STRATS = {"auto": STRAT_AUTO, "pull": STRAT_PULL, "push": STRAT_PUSH, "sparse": STRAT_SPARSE}
+
+
+class VsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"vertexsurge_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class ExpandParams(C.Structure):
+    _fields_ = [("k_min", C.c_uint32), ("k_max", C.c_uint32), ("path_type", C.c_int32),
+                ("direction", C.c_int32), ("strategy", C.c_int32), ("use_picker", C.c_int32),
+                ("hub_threshold", C.c_uint32), ("slice_words", C.c_uint32),
+                ("pair_capacity", C.c_uint64)]
+
+
+class ExpandStats(C.Structure):
+    _fields_ = [("hops_run", C.c_uint32), ("found", C.c_uint32), ("visit_count", C.c_uint64),
+                ("new_bits", C.c_uint64 * (MAX_HOPS + 1)),
+                ("active_vertices", C.c_uint64 * (MAX_HOPS + 1)),
+                ("active_edges", C.c_uint64 * (MAX_HOPS + 1)),
+                ("pairs", C.c_uint64 * (MAX_HOPS + 1)),
+                ("strategy", C.c_int32 * (MAX_HOPS + 1))]
+
+    def as_dict(self) -> dict:
+        n = self.hops_run + 1
+        return {"hops_run": self.hops_run, "found": self.found, "visit_count": self.visit_count,
+                "new_bits": list(self.new_bits[:n]), "active_vertices": list(self.active_vertices[:n]),
+                "active_edges": list(self.active_edges[:n]), "pairs": list(self.pairs[:n]),
+                "strategy": list(self.strategy[:n])}
+
+
+class BitmatInfo(C.Structure):
+    _fields_ = [("rows", C.c_uint32), ("cols", C.c_uint32), ("wpc", C.c_uint32), ("kind", C.c_int32),
+                ("has_row_map", C.c_int32), ("has_col_map", C.c_int32), ("words", C.c_void_p)]
+
+
+class TableRef(C.Structure):
+    _fields_ = [("flat", C.c_void_p), ("mat", C.c_void_p), ("key_col", C.c_uint32)]
+
+
+class IsectDep(C.Structure):
+    _fields_ = [("mat", C.c_void_p), ("flat", C.c_void_p), ("graph", C.c_void_p),
+                ("direction", C.c_int32), ("u_col", C.c_uint32), ("nv_col", C.c_uint32),
+                ("base_col", C.c_uint32)]
+
+
+_lib = None
+
+# (name, restype, argtypes) for every entry point of the header
+_SIGS = [
+    ("vs_last_error", C.c_char_p, []),
+    ("vs_version", C.c_char_p, []),
+    ("vs_init", C.c_int, [C.c_int]),
+    ("vs_graph_upload", C.c_int, [C.c_uint32, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("vs_graph_info", C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64),
+                                C.POINTER(C.c_int)]),
+    ("vs_graph_free", C.c_int, [C.c_void_p]),
+    ("vs_bitmat_create", C.c_int, [C.c_uint32, C.c_uint32, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("vs_bitmat_upload", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("vs_bitmat_download", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("vs_bitmat_set_maps", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("vs_bitmat_get_maps", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("vs_bitmat_get_info", C.c_int, [C.c_void_p, C.POINTER(BitmatInfo)]),
+    ("vs_bitmat_free", C.c_int, [C.c_void_p]),
+    ("vs_bitmat_count", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.c_void_p]),
+    ("vs_matrix_select", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p), C.c_void_p]),
+    ("vs_table_convert", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_void_p]),
+    ("vs_bitmat_to_flat", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_void_p]),
+    ("vs_flat_create", C.c_int, [C.c_uint32, C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    ("vs_flat_upload", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("vs_flat_download", C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    ("vs_flat_info", C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64), C.c_void_p]),
+    ("vs_flat_free", C.c_int, [C.c_void_p]),
+    ("vs_expand_plan_create", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(ExpandParams),
+                                        C.POINTER(C.c_void_p)]),
+    ("vs_expand_plan_run", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("vs_expand_plan_result", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("vs_expand_plan_stats", C.c_int, [C.c_void_p, C.POINTER(ExpandStats), C.c_void_p]),
+    ("vs_expand_plan_free", C.c_int, [C.c_void_p]),
+    ("vs_expand", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(ExpandParams), C.c_void_p,
+                            C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(ExpandStats), C.c_void_p]),
+    ("vs_hash_join", C.c_int, [TableRef, TableRef, C.c_int, C.c_uint64, C.POINTER(C.c_void_p),
+                               C.POINTER(C.c_uint64), C.c_void_p]),
+    ("vs_mintersect", C.c_int, [TableRef, C.POINTER(IsectDep), C.c_uint32, C.c_uint32, C.c_int,
+                                C.c_uint64, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_void_p]),
+]
+
+# entry points beyond the header's operator set (tuning and learned picker)
+_EXTRA_SIGS = [
+    ("vs_expand_plan_set_tuning", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int]),
+    ("vs_expand_plan_set_picker", C.c_int, [C.c_void_p, C.c_void_p]),
+]
+
+HEADER_SYMBOLS = [s[0] for s in _SIGS]
+
+
+def lib() -> C.CDLL:
+    """Load libvsgb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: run vertexsurge_gb300.build.build_all() "
+                               "(the CUDA extension is required; there is no CPU fallback)")
+        L = C.CDLL(str(LIB_PATH))
+        for name, res, args in _SIGS + _EXTRA_SIGS:
+            f = getattr(L, name, None)
+            if f is None:
+                continue
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> int:
+    if rc not in (VS_OK,):
+        raise VsError(rc, lib().vs_last_error().decode())
+    return rc
+
+
+def init(device: int = 0) -> None:
+    check(lib().vs_init(device))
+
+
+def _ptr(a) -> C.c_void_p:
+    """Pointer of a numpy array (host) or a torch tensor (host or device)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"]
+        return C.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    if isinstance(a, int):
+        return C.c_void_p(a)
+    raise TypeError(type(a))
+
+
+def _stream(s) -> C.c_void_p:
+    if s is None:
+        return None
+    if hasattr(s, "cuda_stream"):
+        return C.c_void_p(s.cuda_stream)
+    return C.c_void_p(int(s))
+
+
+class DeviceGraph:
+    """A CSR graph resident in HBM (vs_graph)."""
+
+    def __init__(self, V, E, fwd_off, fwd_dst, rev_off, rev_src, directed=True, stream=None):
+        h = C.c_void_p()
+        check(lib().vs_graph_upload(V, E, _ptr(fwd_off), _ptr(fwd_dst), _ptr(rev_off), _ptr(rev_src),
+                                    1 if directed else 0, _stream(stream), C.byref(h)))
+        self.h = h
+        self.V, self.E, self.directed = int(V), int(E), bool(directed)
+
+    @classmethod
+    def from_host(cls, g, stream=None) -> "DeviceGraph":
+        return cls(g.V, g.E, g.fwd_off, g.fwd_dst, g.rev_off, g.rev_src, g.directed, stream)
+
+    def free(self):
+        if self.h:
+            lib().vs_graph_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class BitMatrix:
+    """A device bit matrix handle (vs_bitmat)."""
+
+    def __init__(self, h: C.c_void_p, owner=None):
+        self.h = h
+        self._owner = owner  # keeps a plan alive for borrowed views
+
+    @classmethod
+    def create(cls, rows, cols, kind=KIND_VARROW, stream=None):
+        h = C.c_void_p()
+        check(lib().vs_bitmat_create(rows, cols, kind, _stream(stream), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_logical(cls, words: np.ndarray, rows: int, cols: int, kind=KIND_VARROW,
+                     row_map=None, col_map=None, stream=None):
+        m = cls.create(rows, cols, kind, stream)
+        words = np.ascontiguousarray(words, dtype=np.uint64)
+        assert words.size == cols * ((rows + 63) // 64)
+        check(lib().vs_bitmat_upload(m.h, _ptr(words), _stream(stream)))
+        if row_map is not None or col_map is not None:
+            rm = None if row_map is None else np.ascontiguousarray(row_map, dtype=np.uint32)
+            cm = None if col_map is None else np.ascontiguousarray(col_map, dtype=np.uint32)
+            check(lib().vs_bitmat_set_maps(m.h, _ptr(rm), _ptr(cm), _stream(stream)))
+        return m
+
+    def info(self) -> BitmatInfo:
+        inf = BitmatInfo()
+        check(lib().vs_bitmat_get_info(self.h, C.byref(inf)))
+        return inf
+
+    @property
+    def shape(self):
+        i = self.info()
+        return i.rows, i.cols
+
+    def download(self, stream=None) -> np.ndarray:
+        """Logical words, shape (cols, ceil(rows/64))."""
+        i = self.info()
+        out = np.zeros((i.cols, (i.rows + 63) // 64), dtype=np.uint64)
+        check(lib().vs_bitmat_download(self.h, _ptr(out), _stream(stream)))
+        return out
+
+    def maps(self, stream=None):
+        i = self.info()
+        rm = np.zeros(i.rows, np.uint32) if i.has_row_map else None
+        cm = np.zeros(i.cols, np.uint32) if i.has_col_map else None
+        check(lib().vs_bitmat_get_maps(self.h, _ptr(rm), _ptr(cm), _stream(stream)))
+        return rm, cm
+
+    def count(self, stream=None) -> int:
+        c = C.c_uint64()
+        check(lib().vs_bitmat_count(self.h, C.byref(c), _stream(stream)))
+        return int(c.value)
+
+    def select(self, targets: np.ndarray, stream=None) -> "BitMatrix":
+        t = np.ascontiguousarray(targets, dtype=np.uint32)
+        h = C.c_void_p()
+        check(lib().vs_matrix_select(self.h, _ptr(t), len(t), C.byref(h), _stream(stream)))
+        return BitMatrix(h)
+
+    def convert(self, transpose: bool, stream=None) -> "BitMatrix":
+        h = C.c_void_p()
+        check(lib().vs_table_convert(self.h, 1 if transpose else 0, C.byref(h), _stream(stream)))
+        return BitMatrix(h)
+
+    def to_flat(self, stream=None) -> "FlatTable":
+        h = C.c_void_p()
+        check(lib().vs_bitmat_to_flat(self.h, C.byref(h), _stream(stream)))
+        return FlatTable(h)
+
+    def free(self):
+        if self.h:
+            lib().vs_bitmat_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class FlatTable:
+    """A device flat table handle (vs_flat): columns of uint32 (VID) or int64."""
+
+    def __init__(self, h: C.c_void_p):
+        self.h = h
+
+    @classmethod
+    def from_columns(cls, cols, stream=None) -> "FlatTable":
+        types = []
+        arrs = []
+        for c in cols:
+            c = np.ascontiguousarray(c)
+            if c.dtype == np.int64:
+                types.append(T_I64)
+            else:
+                c = c.astype(np.uint32)
+                types.append(T_VID)
+            arrs.append(np.ascontiguousarray(c))
+        n = len(arrs[0])
+        assert all(len(a) == n for a in arrs)
+        t = (C.c_int32 * len(types))(*types)
+        h = C.c_void_p()
+        check(lib().vs_flat_create(len(arrs), t, n, C.byref(h)))
+        f = cls(h)
+        for i, a in enumerate(arrs):
+            check(lib().vs_flat_upload(h, i, _ptr(a), _stream(stream)))
+        return f
+
+    def info(self):
+        nc = C.c_uint32()
+        nr = C.c_uint64()
+        types = (C.c_int32 * 16)()
+        check(lib().vs_flat_info(self.h, C.byref(nc), C.byref(nr), types))
+        return int(nc.value), int(nr.value), list(types[: nc.value])
+
+    def columns(self, stream=None) -> list:
+        nc, nr, types = self.info()
+        out = []
+        for i, t in enumerate(types):
+            a = np.zeros(nr, dtype=np.int64 if t == T_I64 else np.uint32)
+            check(lib().vs_flat_download(self.h, i, _ptr(a), _stream(stream)))
+            out.append(a)
+        return out
+
+    def free(self):
+        if self.h:
+            lib().vs_flat_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def make_params(k_min, k_max, path="any", direction="forward", strategy="auto", use_picker=False,
+                hub_threshold=0, slice_words=0, pair_capacity=0) -> ExpandParams:
+    p = ExpandParams()
+    p.k_min, p.k_max = int(k_min), int(k_max)
+    p.path_type = _PATHS[path] if isinstance(path, str) else int(path)
+    p.direction = _DIRS[direction] if isinstance(direction, str) else int(direction)
+    p.strategy = _STRATS[strategy] if isinstance(strategy, str) else int(strategy)
+    p.use_picker = 1 if use_picker else 0
+    p.hub_threshold = int(hub_threshold)
+    p.slice_words = int(slice_words)
+    p.pair_capacity = int(pair_capacity)
+    return p
+
+
+class ExpandPlan:
+    """Reusable expand workspace (vs_expand_plan)."""
+
+    def __init__(self, graph: DeviceGraph, S: int, params: ExpandParams):
+        h = C.c_void_p()
+        check(lib().vs_expand_plan_create(graph.h, S, C.byref(params), C.byref(h)))
+        self.h = h
+        self.graph = graph
+        self.S = S
+        self.params = params
+
+    def set_tuning(self, sparse_frac=-1.0, push_frac=-1.0, collect_stats=False):
+        check(lib().vs_expand_plan_set_tuning(self.h, sparse_frac, push_frac, 1 if collect_stats else 0))
+
+    def run(self, sources, targets=None, distances=None, stream=None):
+        check(lib().vs_expand_plan_run(self.h, _ptr(sources), _ptr(targets), _ptr(distances),
+                                       _stream(stream)))
+
+    def result(self) -> BitMatrix:
+        h = C.c_void_p()
+        check(lib().vs_expand_plan_result(self.h, C.byref(h)))
+        return BitMatrix(h, owner=self)
+
+    def stats(self, stream=None) -> dict:
+        s = ExpandStats()
+        check(lib().vs_expand_plan_stats(self.h, C.byref(s), _stream(stream)))
+        return s.as_dict()
+
+    def free(self):
+        if self.h:
+            lib().vs_expand_plan_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def expand(graph: DeviceGraph, sources, k_min, k_max, path="any", direction="forward",
+           strategy="auto", targets=None, stream=None, stats=False, **kw):
+    """One-shot VExpand. Returns (BitMatrix or None, distances or None, stats dict or None)."""
+    src = np.ascontiguousarray(sources, dtype=np.uint32)
+    p = make_params(k_min, k_max, path, direction, strategy, **kw)
+    S = len(src)
+    dist = None
+    tg = None
+    if p.path_type == PATH_FIND_SHORTEST:
+        tg = np.ascontiguousarray(targets, dtype=np.uint32)
+        dist = np.zeros(S, dtype=np.int32)
+    out = C.c_void_p()
+    st = ExpandStats() if stats else None
+    check(lib().vs_expand(graph.h, _ptr(src), S, C.byref(p), _ptr(tg), _ptr(dist),
+                          None if p.path_type == PATH_FIND_SHORTEST else C.byref(out),
+                          C.byref(st) if st is not None else None, _stream(stream)))
+    m = BitMatrix(out) if out.value else None
+    return m, dist, (st.as_dict() if st is not None else None)
+
+
+def hash_join(a, b, key_a=0, key_b=0, only_count=False, max_rows=1 << 62, stream=None):
+    """HashJoin over two operands (FlatTable with key column, or a ColMain BitMatrix).
+    Returns (FlatTable or None, exact count, truncated flag)."""
+    ra, rb = TableRef(), TableRef()
+    for r, t, k in ((ra, a, key_a), (rb, b, key_b)):
+        if isinstance(t, FlatTable):
+            r.flat = t.h
+        else:
+            r.mat = t.h
+        r.key_col = k
+    out = C.c_void_p()
+    cnt = C.c_uint64()
+    rc = lib().vs_hash_join(ra, rb, 1 if only_count else 0, max_rows,
+                            None if only_count else C.byref(out), C.byref(cnt), _stream(stream))
+    truncated = rc == VS_ERR_CAPACITY
+    if not truncated:
+        check(rc)
+    return (FlatTable(out) if out.value else None), int(cnt.value), truncated
+
+
+def mintersect(base, deps, new_vertex_count=0, only_count=False, max_rows=1 << 62, stream=None):
+    """Mintersect. deps: list of dicts with keys mat/flat/graph, direction, u_col, nv_col, base_col."""
+    rb = TableRef()
+    if isinstance(base, FlatTable):
+        rb.flat = base.h
+    else:
+        rb.mat = base.h
+    arr = (IsectDep * len(deps))()
+    for i, d in enumerate(deps):
+        arr[i].mat = d["mat"].h if d.get("mat") is not None else None
+        arr[i].flat = d["flat"].h if d.get("flat") is not None else None
+        arr[i].graph = d["graph"].h if d.get("graph") is not None else None
+        arr[i].direction = _DIRS.get(d.get("direction", "forward"), 0) if isinstance(
+            d.get("direction", "forward"), str) else int(d["direction"])
+        arr[i].u_col = d.get("u_col", 0)
+        arr[i].nv_col = d.get("nv_col", 1)
+        arr[i].base_col = d.get("base_col", 0)
+    out = C.c_void_p()
+    cnt = C.c_uint64()
+    rc = lib().vs_mintersect(rb, arr, len(deps), new_vertex_count, 1 if only_count else 0, max_rows,
+                             None if only_count else C.byref(out), C.byref(cnt), _stream(stream))
+    truncated = rc == VS_ERR_CAPACITY
+    if not truncated:
+        check(rc)
+    return (FlatTable(out) if out.value else None), int(cnt.value), truncated

@@ -1,0 +1,351 @@
+// Handles, errors, allocation, graph upload, bit-matrix and flat-table basics.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+#include "vs_internal.cuh"
+
+namespace vs {
+
+static thread_local std::string g_last_error;
+
+void set_error(const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+
+int fail(int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
+  set_error("%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();  // clear the sticky-free allocation error
+    return VS_ERR_OOM;
+  }
+  return VS_ERR_CUDA;
+}
+
+int dalloc(void **p, size_t bytes, cudaStream_t st) {
+  cudaError_t e = cudaMallocAsync(p, bytes, st);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    *p = nullptr;
+    return fail(VS_ERR_OOM, "device allocation of %zu bytes failed", bytes);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync", __FILE__, __LINE__);
+  return VS_OK;
+}
+
+void dfree(void *p, cudaStream_t st) {
+  if (p) cudaFreeAsync(p, st);
+}
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+int flat_alloc(uint32_t ncols, const int32_t *types, uint64_t nrows, cudaStream_t st,
+               vs_flat **out) {
+  if (ncols == 0 || ncols > 16) return fail(VS_ERR_ARG, "flat table needs 1..16 columns");
+  vs_flat *f = new vs_flat();
+  f->ncols = ncols;
+  f->nrows = nrows;
+  for (uint32_t i = 0; i < ncols; i++) {
+    if (types[i] != VS_T_VID && types[i] != VS_T_I64) {
+      delete f;
+      return fail(VS_ERR_ARG, "column %u has unknown type %d", i, types[i]);
+    }
+    f->types[i] = types[i];
+    int rc = dalloc(&f->cols[i], type_size(types[i]) * (nrows ? nrows : 1), st);
+    if (rc != VS_OK) {
+      for (uint32_t j = 0; j < i; j++) dfree(f->cols[j], st);
+      delete f;
+      return rc;
+    }
+  }
+  *out = f;
+  return VS_OK;
+}
+
+int bitmat_alloc(uint32_t rows, uint32_t cols, int kind, cudaStream_t st, vs_bitmat **out) {
+  if (kind != VS_KIND_VARROW && kind != VS_KIND_COLMAIN)
+    return fail(VS_ERR_ARG, "unknown matrix kind %d", kind);
+  vs_bitmat *m = new vs_bitmat();
+  m->rows = rows;
+  m->cols = cols;
+  m->wpc = words_per_col(rows);
+  m->kind = kind;
+  m->owns_words = true;
+  size_t n = (size_t)m->wpc * cols;
+  int rc = dalloc_n(&m->words, n, st);
+  if (rc != VS_OK) {
+    delete m;
+    return rc;
+  }
+  cudaError_t e = cudaMemsetAsync(m->words, 0, sizeof(uint64_t) * (n ? n : 1), st);
+  if (e != cudaSuccess) {
+    dfree(m->words, st);
+    delete m;
+    return cuda_fail(e, "cudaMemsetAsync", __FILE__, __LINE__);
+  }
+  *out = m;
+  return VS_OK;
+}
+
+// popcount over a word array, 64-bit result accumulated with one atomic per block
+__global__ void popcount_kernel(const uint64_t *__restrict__ w, size_t n,
+                                unsigned long long *__restrict__ out) {
+  unsigned long long s = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    s += __popcll(w[i]);
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ unsigned long long part[32];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < blockDim.x / 32 ? part[threadIdx.x] : 0;
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0 && s) atomicAdd(out, s);
+  }
+}
+
+__global__ void mask_last_word_kernel(uint64_t *w, uint32_t cols, uint32_t wpc, uint32_t last,
+                                      uint64_t mask) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x)
+    w[(size_t)c * wpc + last] &= mask;
+}
+
+int popcount_words(const uint64_t *w, size_t n, uint64_t *count, cudaStream_t st) {
+  unsigned long long *d;
+  VS_TRY(dalloc_n(&d, 1, st));
+  VS_CK(cudaMemsetAsync(d, 0, sizeof(*d), st));
+  if (n) {
+    int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 8);
+    popcount_kernel<<<blocks, 256, 0, st>>>(w, n, d);
+    VS_CK(cudaGetLastError());
+  }
+  unsigned long long h = 0;
+  VS_CK(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st));
+  dfree(d, st);
+  VS_CK(cudaStreamSynchronize(st));
+  *count = h;
+  return VS_OK;
+}
+
+}  // namespace vs
+
+using namespace vs;
+
+extern "C" {
+
+const char *vs_last_error(void) { return g_last_error.c_str(); }
+
+const char *vs_version(void) { return "vertexsurge_gb300 0.1 sm_103a"; }
+
+int vs_init(int device) {
+  VS_CK(cudaSetDevice(device));
+  cudaMemPool_t pool;
+  VS_CK(cudaDeviceGetDefaultMemPool(&pool, device));
+  uint64_t threshold = UINT64_MAX;  // keep freed blocks for reuse
+  VS_CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold));
+  sm_count();
+  return VS_OK;
+}
+
+int vs_graph_upload(uint32_t V, uint64_t E, const int64_t *fwd_off, const uint32_t *fwd_dst,
+                    const int64_t *rev_off, const uint32_t *rev_src, int directed,
+                    vs_stream_t stream, vs_graph **out) {
+  if (!out || V == 0 || !fwd_off || !rev_off || (E && (!fwd_dst || !rev_src)))
+    return fail(VS_ERR_ARG, "vs_graph_upload: missing CSR arrays");
+  cudaStream_t st = S(stream);
+  vs_graph *g = new vs_graph();
+  g->V = V;
+  g->E = E;
+  g->directed = directed ? 1 : 0;
+  int rc = VS_OK;
+  if ((rc = dalloc_n(&g->fwd_off, (size_t)V + 1, st)) != VS_OK ||
+      (rc = dalloc_n(&g->rev_off, (size_t)V + 1, st)) != VS_OK ||
+      (rc = dalloc_n(&g->fwd_dst, E, st)) != VS_OK ||
+      (rc = dalloc_n(&g->rev_src, E, st)) != VS_OK ||
+      (rc = copy_in(g->fwd_off, fwd_off, (size_t)V + 1, st)) != VS_OK ||
+      (rc = copy_in(g->rev_off, rev_off, (size_t)V + 1, st)) != VS_OK ||
+      (rc = copy_in(g->fwd_dst, fwd_dst, E, st)) != VS_OK ||
+      (rc = copy_in(g->rev_src, rev_src, E, st)) != VS_OK) {
+    vs_graph_free(g);
+    return rc;
+  }
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    vs_graph_free(g);
+    return cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
+  }
+  *out = g;
+  return VS_OK;
+}
+
+int vs_graph_info(const vs_graph *g, uint32_t *V, uint64_t *E, int *directed) {
+  if (!g) return fail(VS_ERR_ARG, "null graph");
+  if (V) *V = g->V;
+  if (E) *E = g->E;
+  if (directed) *directed = g->directed;
+  return VS_OK;
+}
+
+int vs_graph_free(vs_graph *g) {
+  if (!g) return VS_OK;
+  cudaFree(g->fwd_off);
+  cudaFree(g->rev_off);
+  cudaFree(g->fwd_dst);
+  cudaFree(g->rev_src);
+  delete g;
+  return VS_OK;
+}
+
+int vs_bitmat_create(uint32_t rows, uint32_t cols, int kind, vs_stream_t stream, vs_bitmat **out) {
+  if (!out) return fail(VS_ERR_ARG, "null output");
+  return bitmat_alloc(rows, cols, kind, S(stream), out);
+}
+
+int vs_bitmat_upload(vs_bitmat *m, const uint64_t *logical_words, vs_stream_t stream) {
+  if (!m || (!logical_words && m->rows && m->cols)) return fail(VS_ERR_ARG, "null argument");
+  cudaStream_t st = S(stream);
+  const size_t lw = (m->rows + 63) / 64;
+  VS_CK(cudaMemsetAsync(m->words, 0, sizeof(uint64_t) * (size_t)m->wpc * m->cols, st));
+  if (lw && m->cols) {
+    VS_CK(cudaMemcpy2DAsync(m->words, m->wpc * 8, logical_words, lw * 8, lw * 8, m->cols,
+                            cudaMemcpyDefault, st));
+    if (m->rows % 64) {  // bits past the last row must stay zero
+      const uint64_t mask = (1ull << (m->rows % 64)) - 1;
+      mask_last_word_kernel<<<std::max(1u, std::min((m->cols + 255) / 256, 4096u)), 256, 0, st>>>(
+          m->words, m->cols, m->wpc, (uint32_t)(lw - 1), mask);
+      VS_CK(cudaGetLastError());
+    }
+  }
+  return VS_OK;
+}
+
+int vs_bitmat_download(const vs_bitmat *m, uint64_t *logical_words, vs_stream_t stream) {
+  if (!m || (!logical_words && m->rows && m->cols)) return fail(VS_ERR_ARG, "null argument");
+  cudaStream_t st = S(stream);
+  const size_t lw = (m->rows + 63) / 64;
+  if (lw && m->cols)
+    VS_CK(cudaMemcpy2DAsync(logical_words, lw * 8, m->words, m->wpc * 8, lw * 8, m->cols,
+                            cudaMemcpyDefault, st));
+  VS_CK(cudaStreamSynchronize(st));
+  return VS_OK;
+}
+
+int vs_bitmat_set_maps(vs_bitmat *m, const uint32_t *row_map, const uint32_t *col_map,
+                       vs_stream_t stream) {
+  if (!m) return fail(VS_ERR_ARG, "null matrix");
+  cudaStream_t st = S(stream);
+  if (row_map) {
+    if (!m->row_map) VS_TRY(dalloc_n(&m->row_map, m->rows, st));
+    VS_TRY(copy_in(m->row_map, row_map, m->rows, st));
+  }
+  if (col_map) {
+    if (!m->col_map) VS_TRY(dalloc_n(&m->col_map, m->cols, st));
+    VS_TRY(copy_in(m->col_map, col_map, m->cols, st));
+  }
+  return VS_OK;
+}
+
+int vs_bitmat_get_maps(const vs_bitmat *m, uint32_t *row_map, uint32_t *col_map,
+                       vs_stream_t stream) {
+  if (!m) return fail(VS_ERR_ARG, "null matrix");
+  cudaStream_t st = S(stream);
+  if (row_map && m->row_map)
+    VS_CK(cudaMemcpyAsync(row_map, m->row_map, 4ull * m->rows, cudaMemcpyDefault, st));
+  if (col_map && m->col_map)
+    VS_CK(cudaMemcpyAsync(col_map, m->col_map, 4ull * m->cols, cudaMemcpyDefault, st));
+  VS_CK(cudaStreamSynchronize(st));
+  return VS_OK;
+}
+
+int vs_bitmat_get_info(const vs_bitmat *m, vs_bitmat_info *info) {
+  if (!m || !info) return fail(VS_ERR_ARG, "null argument");
+  info->rows = m->rows;
+  info->cols = m->cols;
+  info->wpc = m->wpc;
+  info->kind = m->kind;
+  info->has_row_map = m->row_map != nullptr;
+  info->has_col_map = m->col_map != nullptr;
+  info->words = m->words;
+  return VS_OK;
+}
+
+int vs_bitmat_free(vs_bitmat *m) {
+  if (!m) return VS_OK;
+  if (!m->view) {
+    if (m->owns_words) cudaFree(m->words);
+    cudaFree(m->row_map);
+    cudaFree(m->col_map);
+  }
+  delete m;
+  return VS_OK;
+}
+
+int vs_bitmat_count(const vs_bitmat *m, uint64_t *count, vs_stream_t stream) {
+  if (!m || !count) return fail(VS_ERR_ARG, "null argument");
+  return popcount_words(m->words, (size_t)m->wpc * m->cols, count, S(stream));
+}
+
+int vs_flat_create(uint32_t ncols, const int32_t *types, uint64_t nrows, vs_flat **out) {
+  if (!out || !types) return fail(VS_ERR_ARG, "null argument");
+  return flat_alloc(ncols, types, nrows, 0, out);
+}
+
+int vs_flat_upload(vs_flat *f, uint32_t col, const void *data, vs_stream_t stream) {
+  if (!f || col >= f->ncols || (!data && f->nrows)) return fail(VS_ERR_ARG, "bad column");
+  if (f->nrows)
+    VS_CK(cudaMemcpyAsync(f->cols[col], data, type_size(f->types[col]) * f->nrows,
+                          cudaMemcpyDefault, S(stream)));
+  return VS_OK;
+}
+
+int vs_flat_download(const vs_flat *f, uint32_t col, void *data, vs_stream_t stream) {
+  if (!f || col >= f->ncols || (!data && f->nrows)) return fail(VS_ERR_ARG, "bad column");
+  if (f->nrows)
+    VS_CK(cudaMemcpyAsync(data, f->cols[col], type_size(f->types[col]) * f->nrows,
+                          cudaMemcpyDefault, S(stream)));
+  VS_CK(cudaStreamSynchronize(S(stream)));
+  return VS_OK;
+}
+
+int vs_flat_info(const vs_flat *f, uint32_t *ncols, uint64_t *nrows, int32_t *types) {
+  if (!f) return fail(VS_ERR_ARG, "null table");
+  if (ncols) *ncols = f->ncols;
+  if (nrows) *nrows = f->nrows;
+  if (types)
+    for (uint32_t i = 0; i < f->ncols; i++) types[i] = f->types[i];
+  return VS_OK;
+}
+
+int vs_flat_free(vs_flat *f) {
+  if (!f) return VS_OK;
+  for (uint32_t i = 0; i < f->ncols; i++) cudaFree(f->cols[i]);
+  delete f;
+  return VS_OK;
+}
+
+}  // extern "C"

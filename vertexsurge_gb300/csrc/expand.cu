@@ -1,0 +1,1041 @@
+// Multi-source bit-matrix expand: VExpand + Expand<DenseVarStackMatrix>
+// (src/objects/operator/vexpand.cpp, src/objects/operator/expand.cpp,
+// src/include/operator/expand_impl.hh) re-designed for sm_103a.
+//
+// Data layout in HBM.  Every matrix is vertex-major: vertex v owns W
+// consecutive uint64 words (W = ceil(S/64) rounded up to even), bit i of the
+// row is source i.  This is the reference's DenseVarStackMatrix with a single
+// stack as tall as S (rows padded to 128 instead of 1024), so one hop gathers
+// 8W bytes per active edge instead of a padded 128-byte stack slice per stack.
+//
+// Buffers: two frontier buffers (layer h-1 and layer h ping-pong), the
+// visited matrix (Shortest/FindShortest) and the accumulator (the union of
+// layers k_min..k_max when it differs from visited).  Each frontier buffer
+// has one uint32 flag per vertex with the invariant "flag == 0 => row is
+// zero", which lets a hop skip inactive rows and clear only what it wrote.
+//
+// Per hop one of three strategies runs; the choice is made ON THE DEVICE by a
+// one-block decide kernel from the previous hop's counters, so a whole query
+// is a fixed launch sequence that can be captured in a CUDA graph:
+//   SPARSE  (vertex, source) pair lists, one atomicOr per (pair, edge): the
+//           reference's CSR strategy (expand.cpp:43-131) as an exact
+//           bit-matrix update; used from the sources and while frontiers are tiny.
+//   PULL    every vertex ORs the rows of its active in-neighbours with 16-byte
+//           coalesced loads (sub-warp groups for narrow rows), fused with the
+//           visited AND-NOT, the [k_min,k_max] accumulation and the popcounts
+//           (dedup_and_update_visit_and_count, bitmap.cpp:1054-1096, and
+//           merge_to_MT's union, vexpand.cpp:298-354, folded into the hop).
+//           Vertices above the hub threshold get a whole CTA.
+//   PUSH    active rows OR-ed into their out-neighbours with 64-bit atomics,
+//           followed by a fused dedup/accumulate pass over the touched rows.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "expand_internal.cuh"
+#include "vs_internal.cuh"
+
+namespace vs {
+namespace ex {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Placeholder until the learned picker is loaded: no opinion.
+__device__ int picker_choose(const DecideArgs &a, const HopCtr &prev) {
+  (void)a;
+  (void)prev;
+  return 0;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+template <typename T> __device__ __forceinline__ T warp_sum(T v) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+
+// Block-wide sum of per-thread counters, one atomic per block.
+__device__ __forceinline__ void block_add(unsigned long long v, unsigned long long *dst) {
+  __shared__ unsigned long long part[32];
+  v = warp_sum(v);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0ull;
+    v = warp_sum(v);
+    if (threadIdx.x == 0 && v) atomicAdd(dst, v);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Run start: clear both frontier buffers (flagged rows only) and the counters.
+__global__ void k_clear_flagged(uint4 *__restrict__ buf, uint32_t *__restrict__ flag, uint32_t V,
+                                uint32_t Q, const Ctr *ctr, int h, int mode) {
+  // mode 0: unconditional; mode 1: only when hop h runs SPARSE or PUSH, or a
+  // multi-slice PULL (those write with atomics / partially and need clean rows)
+  if (mode == 1) {
+    int s = ctr->hop[h].strategy;
+    if (!(s == ST_SPARSE || s == ST_PUSH || (s == ST_PULL && ctr->multislice))) return;
+  }
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < V;
+       base += warps * 32) {
+    uint32_t v = base + lane;
+    uint32_t f = v < V ? flag[v] : 0u;
+    unsigned m = __ballot_sync(FULL, f != 0);
+    if (f) flag[v] = 0;
+    while (m) {
+      int b = __ffs(m) - 1;
+      m &= m - 1;
+      uint4 *row = buf + (size_t)(base + b) * Q;
+      for (uint32_t q = lane; q < Q; q += 32) row[q] = make_uint4(0, 0, 0, 0);
+    }
+  }
+}
+
+// Layer 0 (ExpandStatus::init_first_m_layer, expand_impl.hh:252-277).
+__global__ void k_seed(SeedArgs a) {
+  unsigned long long pe = 0, nv = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.S; i += gridDim.x * blockDim.x) {
+    uint32_t v = a.sources[i];
+    if (v >= a.V) {  // reported as VS_ERR_ARG; the pair stays in range
+      a.ctr->error = 1;
+      a.pairs0[i] = make_uint2(0, i);
+      continue;
+    }
+    size_t idx = (size_t)v * a.W + (i >> 6);
+    unsigned long long bit = 1ull << (i & 63);
+    atomicOr((unsigned long long *)&a.buf0[idx], bit);
+    if (atomicOr(&a.flag0[v], 1u) == 0) nv++;
+    if (a.vis) atomicOr((unsigned long long *)&a.vis[idx], bit);
+    if (a.acc) atomicOr((unsigned long long *)&a.acc[idx], bit);
+    a.pairs0[i] = make_uint2(v, i);
+    _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.out.n) pe += (unsigned long long)(a.out.off[l][v + 1] - a.out.off[l][v]);
+  }
+  block_add(pe, &a.ctr->hop[0].pair_edges);
+  block_add(nv, &a.ctr->hop[0].active_vertices);
+}
+
+// FindShortest bookkeeping before hop 1 (VExpand::before_execution, vexpand.cpp:179-195).
+__global__ void k_dist_init(const uint32_t *__restrict__ src, const uint32_t *__restrict__ tgt,
+                            int32_t *__restrict__ dist, uint32_t S, uint32_t V, Ctr *ctr) {
+  unsigned long long f = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < S; i += gridDim.x * blockDim.x) {
+    if (tgt[i] >= V) ctr->error = 1;
+    bool eq = src[i] == tgt[i];
+    dist[i] = eq ? 0 : -1;
+    f += eq;
+  }
+  block_add(f, &ctr->found);
+}
+
+// One block: early-stop checks of hop h-1 (VExpand::after_child,
+// vexpand.cpp:222-284) and the strategy of hop h.
+__global__ void k_decide(DecideArgs a) {
+  if (threadIdx.x != 0) return;
+  Ctr *c = a.ctr;
+  HopCtr &prev = c->hop[a.h - 1];
+  HopCtr &cur = c->hop[a.h];
+  if (!c->done && a.h >= 2) {
+    if (a.path != VS_PATH_ANY && prev.new_bits == 0) c->done = 1;
+    if (a.path == VS_PATH_FIND_SHORTEST && c->found >= a.S) c->done = 1;
+  }
+  if (c->done) {
+    cur.strategy = 0;
+    return;
+  }
+  c->hops_run = a.h;
+  const bool pairs_ok = (a.h == 1) || (prev.strategy == ST_SPARSE && !prev.overflow &&
+                                       prev.pairs <= a.pair_cap);
+  int s = a.forced;
+  if (s == ST_SPARSE && !pairs_ok) s = ST_PULL;
+  if (s == 0) {
+    // fixed planner: pair lists while their edge work is a small fraction of
+    // a dense pass, then push while few rows are active, then pull
+    const double E = (double)a.E;
+    const double pe = (double)prev.pair_edges;
+    if (pairs_ok && pe < E * a.sparse_frac)
+      s = ST_SPARSE;
+    else if ((double)prev.active_vertices < (double)a.V * a.push_frac && prev.strategy != 0)
+      s = ST_PUSH;
+    else
+      s = ST_PULL;
+    if (a.picker && a.picker_on) {
+      int p = picker_choose(a, prev);
+      if (p == ST_SPARSE && !pairs_ok) p = s;
+      if (p > 0) s = p;
+    }
+  }
+  cur.strategy = s;
+}
+
+// Exact E_active of hop h: out-degrees of the non-zero rows of layer h-1.
+__global__ void k_active_edges(const uint32_t *__restrict__ flagF, Lists out, uint32_t V, Ctr *ctr,
+                               int h) {
+  if (ctr->hop[h].strategy == 0) return;
+  unsigned long long s = 0;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
+    if (flagF[v])
+      _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < out.n) s += (unsigned long long)(out.off[l][v + 1] - out.off[l][v]);
+  block_add(s, &ctr->hop[h].active_edges);
+}
+
+// SPARSE: (vertex u, source i) pairs of layer h-1; every out-neighbour v gets
+// bit i.  Shortest dedups through the visited bit (atomicOr returns the old
+// word), Any through the next-layer bit.  New pairs form layer h's list.
+__global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
+  Ctr *c = a.ctr;
+  if (c->hop[a.h].strategy != ST_SPARSE) return;
+  const unsigned long long np_raw = c->hop[a.h - 1].pairs;
+  const uint64_t np = np_raw < a.cap ? np_raw : a.cap;
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  unsigned long long nb = 0, nv = 0, pe = 0, work = 0;
+  for (uint64_t p = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < np;
+       p += warps) {
+    const uint2 pr = a.pin[p];
+    const uint32_t u = pr.x, i = pr.y;
+    const uint32_t wi = i >> 6;
+    const unsigned long long bit = 1ull << (i & 63);
+    _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.out.n) {
+      const int64_t beg = a.out.off[l][u], end = a.out.off[l][u + 1];
+      if (lane == 0) work += (unsigned long long)(end - beg);
+      for (int64_t j0 = beg; j0 < end; j0 += 32) {
+        const int64_t j = j0 + lane;
+        bool fresh = false;
+        uint32_t v = 0;
+        if (j < end) {
+          v = a.out.adj[l][j];
+          const size_t idx = (size_t)v * a.W + wi;
+          if (a.shortest) {
+            unsigned long long old = atomicOr(&a.vis[idx], bit);
+            if (!(old & bit)) {
+              atomicOr(&a.N[idx], bit);
+              fresh = true;
+            }
+          } else {
+            unsigned long long old = atomicOr(&a.N[idx], bit);
+            fresh = !(old & bit);
+          }
+          if (fresh) {
+            if (a.acc_on) atomicOr(&a.acc[idx], bit);
+            if (atomicOr(&a.flagN[v], 1u) == 0) nv++;
+            nb++;
+            _Pragma("unroll") for (int l2 = 0; l2 < 2; l2++) if (l2 < a.out.n)
+              pe += (unsigned long long)(a.out.off[l2][v + 1] - a.out.off[l2][v]);
+          }
+        }
+        // warp-aggregated append of the new pairs
+        const unsigned m = __ballot_sync(FULL, fresh);
+        if (m) {
+          unsigned long long base = 0;
+          if (lane == 0) base = atomicAdd(&c->hop[a.h].pairs, (unsigned long long)__popc(m));
+          base = __shfl_sync(FULL, base, 0);
+          if (fresh) {
+            unsigned long long slot = base + __popc(m & lanemask_lt());
+            if (slot < a.cap)
+              a.pout[slot] = make_uint2(v, i);
+            else
+              c->hop[a.h].overflow = 1;
+          }
+        }
+      }
+    }
+  }
+  block_add(nb, &c->hop[a.h].new_bits);
+  block_add(nv, &c->hop[a.h].active_vertices);
+  block_add(pe, &c->hop[a.h].pair_edges);
+  block_add(work, &c->hop[a.h].work_edges);
+}
+
+// ---------------------------------------------------------------------------
+// PULL.  A warp owns one target vertex; its lanes form G = 32/L groups of L
+// lanes, each group ORs one whole active in-neighbour row (Q uint4 = L * UPL
+// per lane at most) at a time.  In-neighbour ids are read 32 at a time,
+// filtered by the frontier flags with a ballot and compacted through shared
+// memory, so inactive rows cost one flag load and no gather.
+template <int L, int UPL>
+__device__ __forceinline__ void gather_rows(const PullArgs &a, uint32_t *s_u, const uint32_t q0,
+                                            const uint32_t qn, uint4 (&acc)[UPL],
+                                            const uint32_t *adj, int64_t beg, int64_t end,
+                                            int64_t step_start, int64_t step) {
+  constexpr int G = 32 / L;
+  const int lane = threadIdx.x & 31, g = lane / L, gl = lane % L;
+  for (int64_t base = beg + step_start; base < end; base += step) {
+    const int64_t j = base + lane;
+    uint32_t u = 0;
+    bool act = false;
+    if (j < end) {
+      u = __ldg(adj + j);
+      act = __ldg(a.flagF + u) != 0;
+    }
+    const unsigned m = __ballot_sync(FULL, act);
+    if (!m) continue;
+    if (act) s_u[__popc(m & lanemask_lt())] = u;
+    __syncwarp();
+    const int n = __popc(m);
+    int t = g;
+    for (; t + 3 * G < n; t += 4 * G) {
+      const uint4 *r0 = a.F + (size_t)s_u[t] * a.Q + q0;
+      const uint4 *r1 = a.F + (size_t)s_u[t + G] * a.Q + q0;
+      const uint4 *r2 = a.F + (size_t)s_u[t + 2 * G] * a.Q + q0;
+      const uint4 *r3 = a.F + (size_t)s_u[t + 3 * G] * a.Q + q0;
+#pragma unroll
+      for (int k = 0; k < UPL; k++) {
+        const uint32_t q = gl + k * L;
+        if (q < qn) {
+          uint4 x0 = ldg4(r0 + q), x1 = ldg4(r1 + q), x2 = ldg4(r2 + q), x3 = ldg4(r3 + q);
+          acc[k] = or4(acc[k], or4(or4(x0, x1), or4(x2, x3)));
+        }
+      }
+    }
+    for (; t < n; t += G) {
+      const uint4 *r0 = a.F + (size_t)s_u[t] * a.Q + q0;
+#pragma unroll
+      for (int k = 0; k < UPL; k++) {
+        const uint32_t q = gl + k * L;
+        if (q < qn) acc[k] = or4(acc[k], ldg4(r0 + q));
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Fused epilogue for the row of v held by lanes 0..L-1 after the group reduction:
+// visited AND-NOT + update, accumulator OR, next-layer write, flag, counters.
+template <int L, int UPL>
+__device__ __forceinline__ void pull_epilogue(const PullArgs &a, uint32_t v, const uint32_t q0,
+                                              const uint32_t qn, uint4 (&acc)[UPL],
+                                              unsigned long long &nb, unsigned long long &nv) {
+  const int lane = threadIdx.x & 31;
+  const bool leader_group = lane < L;
+  bool any = false;
+  if (leader_group) {
+#pragma unroll
+    for (int k = 0; k < UPL; k++) {
+      const uint32_t q = lane + k * L;
+      if (q < qn) {
+        const size_t idx = (size_t)v * a.Q + q0 + q;
+        uint4 x = acc[k];
+        if (a.shortest && nz4(x)) {
+          const uint4 vv = a.vis[idx];
+          x = andnot4(x, vv);
+          if (nz4(x)) a.vis[idx] = or4(vv, x);
+        }
+        if (nz4(x)) {
+          any = true;
+          nb += popc4(x);
+          if (a.acc_on) a.acc[idx] = or4(a.acc[idx], x);
+        }
+        acc[k] = x;
+      }
+    }
+  }
+  const bool rownz = __any_sync(FULL, any);
+  if (!a.multislice) {
+    const uint32_t oldf = a.flagN[v];
+    if (leader_group && (rownz || oldf)) {
+#pragma unroll
+      for (int k = 0; k < UPL; k++) {
+        const uint32_t q = lane + k * L;
+        if (q < qn) a.N[(size_t)v * a.Q + q0 + q] = acc[k];
+      }
+    }
+    if (lane == 0) {
+      if ((rownz ? 1u : 0u) != oldf) a.flagN[v] = rownz ? 1u : 0u;
+      if (rownz) nv++;
+    }
+  } else if (rownz) {
+    if (leader_group) {
+#pragma unroll
+      for (int k = 0; k < UPL; k++) {
+        const uint32_t q = lane + k * L;
+        if (q < qn && nz4(acc[k])) a.N[(size_t)v * a.Q + q0 + q] = acc[k];
+      }
+    }
+    if (lane == 0 && atomicOr(&a.flagN[v], 1u) == 0) nv++;
+  }
+}
+
+template <int L, int UPL>
+__global__ void __launch_bounds__(256) k_pull(PullArgs a) {
+  if (a.ctr->hop[a.h].strategy != ST_PULL) return;
+  __shared__ uint32_t s_u[8][32];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const uint32_t q0 = blockIdx.y * a.qslice;
+  const uint32_t qn = min(a.qslice, a.Q - q0);
+  unsigned long long nb = 0, nv = 0;
+  for (uint32_t v = blockIdx.x * 8 + wib; v < a.V; v += gridDim.x * 8) {
+    if (a.hub_threshold) {
+      int64_t d = 0;
+      _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n) d += a.in.off[l][v + 1] - a.in.off[l][v];
+      if (d > (int64_t)a.hub_threshold) continue;  // handled by k_pull_hub
+    }
+    uint4 acc[UPL];
+#pragma unroll
+    for (int k = 0; k < UPL; k++) acc[k] = make_uint4(0, 0, 0, 0);
+    _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n)
+      gather_rows<L, UPL>(a, s_u[wib], q0, qn, acc, a.in.adj[l], a.in.off[l][v],
+                          a.in.off[l][v + 1], 0, 32);
+#pragma unroll
+    for (int o = L; o < 32; o <<= 1)
+#pragma unroll
+      for (int k = 0; k < UPL; k++) acc[k] = or4(acc[k], shfl_xor4(acc[k], o));
+    pull_epilogue<L, UPL>(a, v, q0, qn, acc, nb, nv);
+  }
+  (void)lane;
+  block_add(nb, &a.ctr->hop[a.h].new_bits);
+  block_add(nv, &a.ctr->hop[a.h].active_vertices);
+}
+
+// Hub vertices (in-degree above the threshold): one 512-thread CTA per vertex,
+// warps stride over the in-list, rows reduced through shared memory.
+template <int L, int UPL>
+__global__ void __launch_bounds__(512) k_pull_hub(PullArgs a) {
+  if (a.ctr->hop[a.h].strategy != ST_PULL || a.nhubs == 0) return;
+  extern __shared__ uint4 s_red[];  // [16 warps][32 lanes][UPL]
+  __shared__ uint32_t s_u[16][32];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const uint32_t q0 = blockIdx.y * a.qslice;
+  const uint32_t qn = min(a.qslice, a.Q - q0);
+  unsigned long long nb = 0, nv = 0;
+  for (uint32_t hi = blockIdx.x; hi < a.nhubs; hi += gridDim.x) {
+    const uint32_t v = a.hubs[hi];
+    uint4 acc[UPL];
+#pragma unroll
+    for (int k = 0; k < UPL; k++) acc[k] = make_uint4(0, 0, 0, 0);
+    _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n)
+      gather_rows<L, UPL>(a, s_u[wib], q0, qn, acc, a.in.adj[l], a.in.off[l][v],
+                          a.in.off[l][v + 1], (int64_t)wib * 32, (int64_t)nw * 32);
+#pragma unroll
+    for (int o = L; o < 32; o <<= 1)
+#pragma unroll
+      for (int k = 0; k < UPL; k++) acc[k] = or4(acc[k], shfl_xor4(acc[k], o));
+    if (lane < L)
+#pragma unroll
+      for (int k = 0; k < UPL; k++) s_red[(wib * 32 + lane) * UPL + k] = acc[k];
+    __syncthreads();
+    if (wib == 0) {
+      if (lane < L) {
+        for (int w = 1; w < nw; w++)
+#pragma unroll
+          for (int k = 0; k < UPL; k++) acc[k] = or4(acc[k], s_red[(w * 32 + lane) * UPL + k]);
+      }
+      pull_epilogue<L, UPL>(a, v, q0, qn, acc, nb, nv);
+    }
+    __syncthreads();
+  }
+  block_add(nb, &a.ctr->hop[a.h].new_bits);
+  block_add(nv, &a.ctr->hop[a.h].active_vertices);
+}
+
+// ---------------------------------------------------------------------------
+// PUSH.  Active rows of layer h-1 (flag set) are compacted into a list; a warp
+// per active vertex ORs its row into each out-neighbour's next-layer row with
+// 64-bit atomics and records first touches; a second pass over the touched
+// list applies the visited AND-NOT and the accumulator (Shortest/Any rules).
+__global__ void k_push_compact(const uint32_t *__restrict__ flagF, uint32_t V, uint32_t *list,
+                               Ctr *ctr, int h) {
+  if (ctr->hop[h].strategy != ST_PUSH) return;
+  const int lane = threadIdx.x & 31;
+  for (uint32_t v0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; v0 < V;
+       v0 += gridDim.x * blockDim.x) {
+    const uint32_t v = v0 + lane;
+    const bool f = v < V && flagF[v];
+    const unsigned m = __ballot_sync(FULL, f);
+    if (!m) continue;
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(&ctr->push_active, (unsigned)__popc(m));
+    base = __shfl_sync(FULL, base, 0);
+    if (f) list[base + __popc(m & lanemask_lt())] = v;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_push(PushArgs a) {
+  Ctr *c = a.ctr;
+  if (c->hop[a.h].strategy != ST_PUSH) return;
+  const uint32_t n = c->push_active;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < n; t += warps) {
+    const uint32_t u = a.active[t];
+    const unsigned long long *row = a.F + (size_t)u * a.W;
+    _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.out.n) {
+      const int64_t beg = a.out.off[l][u], end = a.out.off[l][u + 1];
+      for (int64_t j = beg; j < end; j++) {
+        const uint32_t v = __ldg(a.out.adj[l] + j);
+        unsigned long long *dst = a.N + (size_t)v * a.W;
+        for (uint32_t w = lane; w < a.W; w += 32) {
+          const unsigned long long x = row[w];
+          if (x) atomicOr(dst + w, x);
+        }
+        if (lane == 0 && atomicOr(&a.flagN[v], 1u) == 0) {
+          unsigned s = atomicAdd(&c->push_touched, 1u);
+          a.touched[s] = v;
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_push_epilogue(PushArgs a) {
+  Ctr *c = a.ctr;
+  if (c->hop[a.h].strategy != ST_PUSH) return;
+  const uint32_t n = c->push_touched;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  unsigned long long nb = 0, nv = 0;
+  for (uint32_t t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < n; t += warps) {
+    const uint32_t v = a.touched[t];
+    bool any = false;
+    for (uint32_t w = lane; w < a.W; w += 32) {
+      const size_t idx = (size_t)v * a.W + w;
+      unsigned long long x = a.N[idx];
+      if (a.shortest && x) {
+        const unsigned long long vv = a.vis[idx];
+        const unsigned long long y = x & ~vv;
+        if (y != x) a.N[idx] = y;
+        if (y) a.vis[idx] = vv | y;
+        x = y;
+      }
+      if (x) {
+        any = true;
+        nb += __popcll(x);
+        if (a.acc_on) a.acc[idx] |= x;
+      }
+    }
+    const bool rownz = __any_sync(FULL, any);
+    if (lane == 0) {
+      if (!rownz)
+        a.flagN[v] = 0;  // row is all zero again
+      else
+        nv++;
+    }
+  }
+  block_add(nb, &c->hop[a.h].new_bits);
+  block_add(nv, &c->hop[a.h].active_vertices);
+}
+
+__global__ void k_push_reset(Ctr *c) {
+  c->push_active = 0;
+  c->push_touched = 0;
+}
+
+// FindShortest target check of hop h (vexpand.cpp:237-271).
+__global__ void k_find_check(const uint64_t *__restrict__ N, const uint32_t *__restrict__ tgt,
+                             int32_t *__restrict__ dist, uint32_t S, uint32_t W, uint32_t V,
+                             Ctr *ctr, int h) {
+  if (ctr->hop[h].strategy == 0) return;
+  unsigned long long f = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < S; i += gridDim.x * blockDim.x) {
+    if (tgt[i] < V && dist[i] == -1 && ((N[(size_t)tgt[i] * W + (i >> 6)] >> (i & 63)) & 1ull)) {
+      dist[i] = h;
+      f++;
+    }
+  }
+  block_add(f, &ctr->found);
+}
+
+// Shortest with k_min == 1: the result is visited minus layer 0, i.e. the
+// source bits (i, s_i) cleared (a source is never re-reached once visited).
+__global__ void k_clear_diag(uint64_t *__restrict__ vis, const uint32_t *__restrict__ src,
+                             uint32_t S, uint32_t W, uint32_t V) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < S; i += gridDim.x * blockDim.x)
+    if (src[i] < V) atomicAnd((unsigned long long *)&vis[(size_t)src[i] * W + (i >> 6)], ~(1ull << (i & 63)));
+}
+
+// Hub list of a direction set (degree above the threshold).
+__global__ void k_hubs(Lists in, uint32_t V, uint32_t thr, uint32_t *list, unsigned *n) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    int64_t d = 0;
+    _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < in.n) d += in.off[l][v + 1] - in.off[l][v];
+    if (d > (int64_t)thr) list[atomicAdd(n, 1u)] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+Lists pull_lists(const vs_graph *g, int dir) {
+  Lists L;
+  L.n = 0;
+  const bool fwd = !g->directed || dir == VS_DIR_FORWARD || dir == VS_DIR_BOTH;
+  const bool bwd = g->directed && (dir == VS_DIR_BACKWARD || dir == VS_DIR_BOTH);
+  if (fwd) {  // in-lists of the target: reverse CSR
+    L.off[L.n] = g->rev_off;
+    L.adj[L.n] = g->rev_src;
+    L.n++;
+  }
+  if (bwd) {
+    L.off[L.n] = g->fwd_off;
+    L.adj[L.n] = g->fwd_dst;
+    L.n++;
+  }
+  return L;
+}
+
+Lists push_lists(const vs_graph *g, int dir) {
+  Lists L;
+  L.n = 0;
+  const bool fwd = !g->directed || dir == VS_DIR_FORWARD || dir == VS_DIR_BOTH;
+  const bool bwd = g->directed && (dir == VS_DIR_BACKWARD || dir == VS_DIR_BOTH);
+  if (fwd) {
+    L.off[L.n] = g->fwd_off;
+    L.adj[L.n] = g->fwd_dst;
+    L.n++;
+  }
+  if (bwd) {
+    L.off[L.n] = g->rev_off;
+    L.adj[L.n] = g->rev_src;
+    L.n++;
+  }
+  return L;
+}
+
+using PullFn = void (*)(PullArgs);
+
+struct PullVariant {
+  int L, UPL;
+  PullFn pull, hub;
+};
+
+const PullVariant kVariants[] = {
+    {1, 1, k_pull<1, 1>, k_pull_hub<1, 1>},     {2, 1, k_pull<2, 1>, k_pull_hub<2, 1>},
+    {4, 1, k_pull<4, 1>, k_pull_hub<4, 1>},     {8, 1, k_pull<8, 1>, k_pull_hub<8, 1>},
+    {16, 1, k_pull<16, 1>, k_pull_hub<16, 1>},  {32, 1, k_pull<32, 1>, k_pull_hub<32, 1>},
+    {32, 2, k_pull<32, 2>, k_pull_hub<32, 2>},  {32, 4, k_pull<32, 4>, k_pull_hub<32, 4>},
+    {32, 8, k_pull<32, 8>, k_pull_hub<32, 8>},
+};
+
+const PullVariant &pick_variant(uint32_t qslice) {
+  for (const auto &v : kVariants)
+    if ((uint32_t)(v.L * v.UPL) >= qslice) return v;
+  return kVariants[sizeof(kVariants) / sizeof(kVariants[0]) - 1];
+}
+
+}  // namespace ex
+}  // namespace vs
+
+using namespace vs;
+using namespace vs::ex;
+
+struct vs_expand_plan {
+  vs_graph *g = nullptr;
+  vs_expand_params p{};
+  uint32_t S = 0, W = 0, Q = 0, qslice = 0, nslices = 1;
+  uint64_t *buf[2] = {nullptr, nullptr};
+  uint32_t *flag[2] = {nullptr, nullptr};
+  uint64_t *vis = nullptr, *acc = nullptr;
+  uint2 *pairs[2] = {nullptr, nullptr};
+  uint64_t pair_cap = 0;
+  uint32_t *push_list = nullptr, *touched = nullptr;
+  uint32_t *d_src = nullptr, *d_tgt = nullptr;
+  int32_t *d_dist = nullptr;
+  Ctr *ctr = nullptr;
+  uint32_t *hubs = nullptr;
+  uint32_t nhubs = 0, hub_threshold = 0;
+  bool use_vis = false, use_acc = false, clear_diag = false;
+  bool collect_stats = false;
+  int grid_pull = 0, grid_hub = 0, grid_sparse = 0, grid_v = 0, grid_push = 0;
+  vs_bitmat result{};
+  bool has_result = false;
+  // tuning knobs of the fixed planner
+  double sparse_frac = 0.02, push_frac = 0.0;
+  const float *picker = nullptr;
+};
+
+namespace vs {
+namespace ex {
+
+int plan_free(vs_expand_plan *pl) {
+  if (!pl) return VS_OK;
+  void *ptrs[] = {pl->buf[0], pl->buf[1], pl->flag[0], pl->flag[1], pl->vis, pl->acc,
+                  pl->pairs[0], pl->pairs[1], pl->push_list, pl->touched, pl->d_src,
+                  pl->d_tgt, pl->d_dist, pl->ctr, pl->hubs};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  delete pl;
+  return VS_OK;
+}
+
+template <typename K> int occupancy_grid(K kernel, int threads, size_t smem, int cap_per_sm) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  if (per_sm <= 0) per_sm = 1;
+  if (cap_per_sm > 0 && per_sm > cap_per_sm) per_sm = cap_per_sm;
+  return per_sm * sm_count();
+}
+
+}  // namespace ex
+}  // namespace vs
+
+extern "C" {
+
+int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
+                          vs_expand_plan **out) {
+  if (!g || !p || !out) return fail(VS_ERR_ARG, "vs_expand_plan_create: null argument");
+  if (p->k_min > p->k_max) return fail(VS_ERR_ARG, "k_min %u > k_max %u", p->k_min, p->k_max);
+  if (p->k_max > VS_MAX_HOPS) return fail(VS_ERR_ARG, "k_max %u exceeds %d", p->k_max, VS_MAX_HOPS);
+  if (p->path_type < VS_PATH_ANY || p->path_type > VS_PATH_FIND_SHORTEST)
+    return fail(VS_ERR_ARG, "unknown path type %d", p->path_type);
+  if (p->direction < VS_DIR_FORWARD || p->direction > VS_DIR_BOTH)
+    return fail(VS_ERR_ARG, "unknown direction %d", p->direction);
+  if (p->strategy < VS_STRAT_AUTO || p->strategy > VS_STRAT_SPARSE)
+    return fail(VS_ERR_ARG, "unknown strategy %d", p->strategy);
+  if (S == 0) return fail(VS_ERR_ARG, "no start vertex for VExpand");
+  cudaStream_t st = 0;
+  vs_expand_plan *pl = new vs_expand_plan();
+  pl->g = g;
+  pl->p = *p;
+  pl->S = S;
+  pl->W = words_per_col(S);
+  pl->Q = pl->W / 2;
+  uint32_t qs = p->slice_words ? (p->slice_words + 1) / 2 : pl->Q;
+  qs = std::min(qs, (uint32_t)256);
+  if (qs == 0) qs = 1;
+  pl->qslice = qs;
+  pl->nslices = (pl->Q + qs - 1) / qs;
+  const bool shortest = p->path_type != VS_PATH_ANY;
+  pl->use_vis = shortest;
+  pl->use_acc = (p->path_type == VS_PATH_ANY) || (p->path_type == VS_PATH_SHORTEST && p->k_min >= 2);
+  pl->clear_diag = p->path_type == VS_PATH_SHORTEST && p->k_min == 1;
+  const uint32_t V = g->V;
+  const size_t rowwords = (size_t)V * pl->W;
+  pl->pair_cap = p->pair_capacity ? p->pair_capacity
+                                  : std::max<uint64_t>(1u << 20, std::min<uint64_t>((uint64_t)S * V / 8, 1ull << 25));
+  pl->pair_cap = std::max<uint64_t>(pl->pair_cap, S);
+  int rc = VS_OK;
+#define PL_ALLOC(ptr, n)                                          \
+  if ((rc = dalloc_n(&(ptr), (n), st)) != VS_OK) {                \
+    plan_free(pl);                                                \
+    return rc;                                                    \
+  }
+  PL_ALLOC(pl->buf[0], rowwords);
+  PL_ALLOC(pl->buf[1], rowwords);
+  PL_ALLOC(pl->flag[0], V);
+  PL_ALLOC(pl->flag[1], V);
+  if (pl->use_vis) PL_ALLOC(pl->vis, rowwords);
+  if (pl->use_acc) PL_ALLOC(pl->acc, rowwords);
+  PL_ALLOC(pl->pairs[0], pl->pair_cap);
+  PL_ALLOC(pl->pairs[1], pl->pair_cap);
+  PL_ALLOC(pl->push_list, V);
+  PL_ALLOC(pl->touched, V);
+  PL_ALLOC(pl->d_src, S);
+  if (p->path_type == VS_PATH_FIND_SHORTEST) {
+    PL_ALLOC(pl->d_tgt, S);
+    PL_ALLOC(pl->d_dist, S);
+  }
+  PL_ALLOC(pl->ctr, 1);
+#undef PL_ALLOC
+  cudaError_t e = cudaSuccess;
+  if ((e = cudaMemsetAsync(pl->buf[0], 0, rowwords * 8, st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(pl->buf[1], 0, rowwords * 8, st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(pl->flag[0], 0, 4ull * V, st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(pl->flag[1], 0, 4ull * V, st)) != cudaSuccess) {
+    plan_free(pl);
+    return cuda_fail(e, "cudaMemsetAsync", __FILE__, __LINE__);
+  }
+  // hub list for the pull direction set
+  pl->hub_threshold = p->hub_threshold ? p->hub_threshold : 2048;
+  {
+    Lists in = pull_lists(g, p->direction);
+    unsigned *dn = nullptr;
+    if ((rc = dalloc_n(&pl->hubs, V, st)) != VS_OK || (rc = dalloc_n(&dn, 1, st)) != VS_OK) {
+      plan_free(pl);
+      return rc;
+    }
+    cudaMemsetAsync(dn, 0, sizeof(unsigned), st);
+    k_hubs<<<sm_count() * 4, 256, 0, st>>>(in, V, pl->hub_threshold, pl->hubs, dn);
+    unsigned hn = 0;
+    cudaMemcpyAsync(&hn, dn, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    e = cudaStreamSynchronize(st);
+    dfree(dn, st);
+    if (e != cudaSuccess) {
+      plan_free(pl);
+      return cuda_fail(e, "hub list", __FILE__, __LINE__);
+    }
+    pl->nhubs = hn;
+  }
+  const PullVariant &var = pick_variant(pl->qslice);
+  if (var.UPL * 16 * 32 * 16 > 48 * 1024)
+    cudaFuncSetAttribute(var.hub, cudaFuncAttributeMaxDynamicSharedMemorySize, 16 * 32 * 16 * var.UPL);
+  pl->grid_pull = occupancy_grid(var.pull, 256, 0, 8);
+  pl->grid_hub = std::max(1, std::min((int)pl->nhubs, occupancy_grid(var.hub, 512, 16 * 32 * 16 * var.UPL, 2)));
+  pl->grid_sparse = occupancy_grid(k_sparse, 256, 0, 8);
+  pl->grid_push = occupancy_grid(k_push, 256, 0, 8);
+  pl->grid_v = sm_count() * 8;
+  *out = pl;
+  return VS_OK;
+}
+
+int vs_expand_plan_free(vs_expand_plan *plan) {
+  if (plan) cudaDeviceSynchronize();
+  return plan_free(plan);
+}
+
+int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32_t *targets,
+                       int32_t *distances, vs_stream_t stream) {
+  if (!pl || !sources) return fail(VS_ERR_ARG, "vs_expand_plan_run: null argument");
+  const vs_expand_params &p = pl->p;
+  if (p.path_type == VS_PATH_FIND_SHORTEST && (!targets || !distances))
+    return fail(VS_ERR_ARG, "FindShortest needs targets and distances");
+  cudaStream_t st = S(stream);
+  const vs_graph *g = pl->g;
+  const uint32_t V = g->V, S_ = pl->S, W = pl->W, Q = pl->Q;
+  const size_t rowbytes = (size_t)V * W * 8;
+  VS_TRY(copy_in(pl->d_src, sources, S_, st));
+  if (pl->d_tgt) VS_TRY(copy_in(pl->d_tgt, targets, S_, st));
+  // run start: clean frontier buffers, zero visited/accumulator/counters
+  for (int b = 0; b < 2; b++)
+    k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[b]), pl->flag[b],
+                                                V, Q, pl->ctr, 0, 0);
+  if (pl->vis) VS_CK(cudaMemsetAsync(pl->vis, 0, rowbytes, st));
+  if (pl->acc) VS_CK(cudaMemsetAsync(pl->acc, 0, rowbytes, st));
+  VS_CK(cudaMemsetAsync(pl->ctr, 0, sizeof(Ctr), st));
+  if (pl->nslices > 1) {
+    int one = 1;
+    VS_CK(cudaMemcpyAsync(&pl->ctr->multislice, &one, sizeof(int), cudaMemcpyHostToDevice, st));
+  }
+  const Lists in = pull_lists(g, p.direction), outl = push_lists(g, p.direction);
+  SeedArgs sa;
+  sa.sources = pl->d_src;
+  sa.S = S_;
+  sa.W = W;
+  sa.buf0 = pl->buf[0];
+  sa.flag0 = pl->flag[0];
+  sa.vis = pl->vis;
+  sa.acc = (pl->use_acc && p.k_min == 0) ? pl->acc : nullptr;
+  sa.pairs0 = pl->pairs[0];
+  sa.out = outl;
+  sa.ctr = pl->ctr;
+  sa.V = V;
+  k_seed<<<std::max(1u, std::min((S_ + 255) / 256, (uint32_t)sm_count() * 4)), 256, 0, st>>>(sa);
+  VS_CK(cudaGetLastError());
+  // layer 0 pair count
+  {
+    unsigned long long s64 = S_;
+    VS_CK(cudaMemcpyAsync(&pl->ctr->hop[0].pairs, &s64, sizeof(s64), cudaMemcpyHostToDevice, st));
+    VS_CK(cudaMemcpyAsync(&pl->ctr->hop[0].new_bits, &s64, sizeof(s64), cudaMemcpyHostToDevice, st));
+  }
+  if (p.path_type == VS_PATH_FIND_SHORTEST)
+    k_dist_init<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(pl->d_src, pl->d_tgt,
+                                                                              pl->d_dist, S_, V, pl->ctr);
+  const PullVariant &var = pick_variant(pl->qslice);
+  const int forced = p.strategy == VS_STRAT_PULL ? ST_PULL
+                     : p.strategy == VS_STRAT_PUSH ? ST_PUSH
+                     : p.strategy == VS_STRAT_SPARSE ? ST_SPARSE
+                                                     : 0;
+  for (uint32_t h = 1; h <= p.k_max; h++) {
+    const int fb = (h - 1) & 1, nbuf = h & 1;
+    DecideArgs da;
+    da.ctr = pl->ctr;
+    da.h = h;
+    da.path = p.path_type;
+    da.S = S_;
+    da.V = V;
+    da.E = g->E;
+    da.forced = forced;
+    da.pair_cap = pl->pair_cap;
+    da.sparse_frac = pl->sparse_frac;
+    da.push_frac = pl->push_frac;
+    da.picker = pl->picker;
+    da.picker_on = p.use_picker;
+    da.W = W;
+    da.k_min = p.k_min;
+    da.k_max = p.k_max;
+    k_decide<<<1, 32, 0, st>>>(da);
+    if (pl->collect_stats)
+      k_active_edges<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], outl, V, pl->ctr, h);
+    k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[nbuf]),
+                                                pl->flag[nbuf], V, Q, pl->ctr, h, 1);
+    const bool acc_on = pl->use_acc && h >= p.k_min && h <= p.k_max;
+    SparseArgs sp;
+    sp.ctr = pl->ctr;
+    sp.h = h;
+    sp.pin = pl->pairs[fb];
+    sp.pout = pl->pairs[nbuf];
+    sp.cap = pl->pair_cap;
+    sp.out = outl;
+    sp.W = W;
+    sp.N = reinterpret_cast<unsigned long long *>(pl->buf[nbuf]);
+    sp.vis = reinterpret_cast<unsigned long long *>(pl->vis);
+    sp.acc = reinterpret_cast<unsigned long long *>(pl->acc);
+    sp.flagN = pl->flag[nbuf];
+    sp.shortest = pl->use_vis;
+    sp.acc_on = acc_on;
+    k_sparse<<<pl->grid_sparse, 256, 0, st>>>(sp);
+    PushArgs pa;
+    pa.ctr = pl->ctr;
+    pa.h = h;
+    pa.out = outl;
+    pa.F = reinterpret_cast<const unsigned long long *>(pl->buf[fb]);
+    pa.N = reinterpret_cast<unsigned long long *>(pl->buf[nbuf]);
+    pa.vis = reinterpret_cast<unsigned long long *>(pl->vis);
+    pa.acc = reinterpret_cast<unsigned long long *>(pl->acc);
+    pa.flagN = pl->flag[nbuf];
+    pa.active = pl->push_list;
+    pa.touched = pl->touched;
+    pa.W = W;
+    pa.shortest = pl->use_vis;
+    pa.acc_on = acc_on;
+    k_push_reset<<<1, 1, 0, st>>>(pl->ctr);
+    k_push_compact<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], V, pl->push_list, pl->ctr, h);
+    k_push<<<pl->grid_push, 256, 0, st>>>(pa);
+    k_push_epilogue<<<pl->grid_push, 256, 0, st>>>(pa);
+    PullArgs a;
+    a.in = in;
+    a.F = reinterpret_cast<const uint4 *>(pl->buf[fb]);
+    a.N = reinterpret_cast<uint4 *>(pl->buf[nbuf]);
+    a.vis = reinterpret_cast<uint4 *>(pl->vis);
+    a.acc = reinterpret_cast<uint4 *>(pl->acc);
+    a.flagF = pl->flag[fb];
+    a.flagN = pl->flag[nbuf];
+    a.V = V;
+    a.Q = Q;
+    a.qslice = pl->qslice;
+    a.multislice = pl->nslices > 1;
+    a.shortest = pl->use_vis;
+    a.acc_on = acc_on;
+    a.hub_threshold = pl->nhubs ? pl->hub_threshold : 0;
+    a.hubs = pl->hubs;
+    a.nhubs = pl->nhubs;
+    a.ctr = pl->ctr;
+    a.h = h;
+    var.pull<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a);
+    if (pl->nhubs)
+      var.hub<<<dim3(pl->grid_hub, pl->nslices), 512, 16 * 32 * 16 * var.UPL, st>>>(a);
+    if (p.path_type == VS_PATH_FIND_SHORTEST)
+      k_find_check<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(
+          pl->buf[nbuf], pl->d_tgt, pl->d_dist, S_, W, V, pl->ctr, h);
+    VS_CK(cudaGetLastError());
+  }
+  if (pl->clear_diag)
+    k_clear_diag<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(pl->vis, pl->d_src,
+                                                                                S_, W, V);
+  if (p.path_type == VS_PATH_FIND_SHORTEST)
+    VS_TRY(copy_in(distances, (const int32_t *)pl->d_dist, S_, st));
+  VS_CK(cudaGetLastError());
+  // result view
+  vs_bitmat &r = pl->result;
+  r = vs_bitmat{};
+  r.rows = S_;
+  r.cols = V;
+  r.wpc = W;
+  r.kind = VS_KIND_VARROW;
+  r.words = pl->use_acc ? pl->acc : pl->vis;
+  r.row_map = pl->d_src;
+  r.col_map = nullptr;
+  r.owns_words = false;
+  r.view = true;
+  pl->has_result = p.path_type != VS_PATH_FIND_SHORTEST;
+  return VS_OK;
+}
+
+int vs_expand_plan_result(vs_expand_plan *pl, vs_bitmat **view) {
+  if (!pl || !view) return fail(VS_ERR_ARG, "null argument");
+  if (!pl->has_result) return fail(VS_ERR_ARG, "plan has no matrix result");
+  vs_bitmat *m = new vs_bitmat(pl->result);
+  m->view = true;
+  *view = m;
+  return VS_OK;
+}
+
+int vs_expand_plan_stats(vs_expand_plan *pl, vs_expand_stats *stats, vs_stream_t stream) {
+  if (!pl || !stats) return fail(VS_ERR_ARG, "null argument");
+  Ctr h;
+  VS_CK(cudaMemcpyAsync(&h, pl->ctr, sizeof(Ctr), cudaMemcpyDeviceToHost, S(stream)));
+  VS_CK(cudaStreamSynchronize(S(stream)));
+  std::memset(stats, 0, sizeof(*stats));
+  if (h.error) return fail(VS_ERR_ARG, "a source or target vertex id is >= V (%u)", pl->g->V);
+  stats->hops_run = (uint32_t)h.hops_run;
+  stats->found = (uint32_t)h.found;
+  uint64_t vc = pl->S;
+  for (int i = 0; i <= VS_MAX_HOPS; i++) {
+    stats->new_bits[i] = h.hop[i].new_bits;
+    stats->active_vertices[i] = h.hop[i].active_vertices;
+    stats->active_edges[i] = h.hop[i].active_edges;
+    stats->pairs[i] = h.hop[i].pairs;
+    stats->strategy[i] = h.hop[i].strategy;
+    if (i >= 1 && i <= h.hops_run) vc += h.hop[i].new_bits;
+  }
+  stats->visit_count = pl->use_vis ? vc : 0;
+  return VS_OK;
+}
+
+int vs_expand_plan_set_tuning(vs_expand_plan *pl, double sparse_frac, double push_frac,
+                              int collect_stats) {
+  if (!pl) return fail(VS_ERR_ARG, "null plan");
+  if (sparse_frac >= 0) pl->sparse_frac = sparse_frac;
+  if (push_frac >= 0) pl->push_frac = push_frac;
+  pl->collect_stats = collect_stats != 0;
+  return VS_OK;
+}
+
+int vs_expand_plan_set_picker(vs_expand_plan *pl, const float *device_weights) {
+  if (!pl) return fail(VS_ERR_ARG, "null plan");
+  pl->picker = device_weights;
+  return VS_OK;
+}
+
+int vs_expand(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_params *p,
+              const uint32_t *targets, int32_t *distances, vs_bitmat **out, vs_expand_stats *stats,
+              vs_stream_t stream) {
+  if (!g || !p) return fail(VS_ERR_ARG, "vs_expand: null argument");
+  if (S == 0) {
+    // VExpand::before_execution returns false on an empty start list: empty result
+    if (out && p->path_type != VS_PATH_FIND_SHORTEST)
+      return bitmat_alloc(0, g->V, VS_KIND_VARROW, vs::S(stream), out);
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return VS_OK;
+  }
+  vs_expand_plan *pl = nullptr;
+  VS_TRY(vs_expand_plan_create(g, S, p, &pl));
+  pl->collect_stats = stats != nullptr;
+  int rc = vs_expand_plan_run(pl, sources, targets, distances, stream);
+  if (rc == VS_OK && stats) rc = vs_expand_plan_stats(pl, stats, stream);
+  if (rc == VS_OK && !stats) {
+    int err = 0;
+    cudaError_t e = cudaMemcpyAsync(&err, &pl->ctr->error, sizeof(int), cudaMemcpyDeviceToHost,
+                                    vs::S(stream));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(vs::S(stream));
+    if (e != cudaSuccess)
+      rc = cuda_fail(e, "vs_expand", __FILE__, __LINE__);
+    else if (err)
+      rc = fail(VS_ERR_ARG, "a source or target vertex id is >= V (%u)", g->V);
+  }
+  if (rc == VS_OK && out && p->path_type != VS_PATH_FIND_SHORTEST) {
+    cudaStream_t st = vs::S(stream);
+    vs_bitmat *m = new vs_bitmat();
+    m->rows = S;
+    m->cols = g->V;
+    m->wpc = pl->W;
+    m->kind = VS_KIND_VARROW;
+    m->owns_words = true;
+    // hand the result buffer over instead of copying it
+    if (pl->use_acc) {
+      m->words = pl->acc;
+      pl->acc = nullptr;
+    } else {
+      m->words = pl->vis;
+      pl->vis = nullptr;
+    }
+    m->row_map = pl->d_src;
+    pl->d_src = nullptr;
+    *out = m;
+    (void)st;
+  }
+  if (rc == VS_OK) {
+    cudaError_t e = cudaStreamSynchronize(vs::S(stream));
+    if (e != cudaSuccess) rc = cuda_fail(e, "vs_expand", __FILE__, __LINE__);
+  }
+  plan_free(pl);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,106 @@
+// Argument blocks and counters of the expand kernels.
+#pragma once
+#include <stdint.h>
+
+#include "vs_internal.cuh"
+
+namespace vs {
+namespace ex {
+
+enum { ST_NONE = 0, ST_PULL = 1, ST_PUSH = 2, ST_SPARSE = 3 };
+
+// Per-hop device counters (hop 0 describes the seeded layer 0).
+struct HopCtr {
+  unsigned long long new_bits;         // bits set in layer h (Shortest: newly visited)
+  unsigned long long active_vertices;  // non-zero rows of layer h
+  unsigned long long active_edges;     // edges leaving non-zero rows of layer h-1 (stats pass)
+  unsigned long long pairs;            // SPARSE: (vertex, source) pairs of layer h
+  unsigned long long pair_edges;       // SPARSE: sum of out-degrees over those pairs
+  unsigned long long work_edges;       // SPARSE: edges scanned by the hop
+  int overflow;                        // SPARSE: pair list overflowed
+  int strategy;                        // strategy run at hop h (0 = not run)
+};
+
+struct Ctr {
+  HopCtr hop[VS_MAX_HOPS + 1];
+  unsigned long long found;  // FindShortest
+  int done;                  // early stop reached: later hops are no-ops
+  int hops_run;              // k_actual_max
+  int multislice;            // PULL runs in several source slices
+  unsigned push_active, push_touched;
+  int error;  // a source or target id was >= V (the offending entry was skipped)
+};
+
+// Up to two adjacency lists (Direction::Both uses both CSRs).
+struct Lists {
+  const int64_t *off[2];
+  const uint32_t *adj[2];
+  int n;
+};
+
+struct SeedArgs {
+  const uint32_t *sources;
+  uint32_t S, W, V;
+  uint64_t *buf0;
+  uint32_t *flag0;
+  uint64_t *vis, *acc;
+  uint2 *pairs0;
+  Lists out;
+  Ctr *ctr;
+};
+
+struct DecideArgs {
+  Ctr *ctr;
+  int h, path, forced, picker_on;
+  uint32_t S, V, W, k_min, k_max;
+  uint64_t E, pair_cap;
+  double sparse_frac, push_frac;
+  const float *picker;
+};
+
+struct SparseArgs {
+  Ctr *ctr;
+  int h;
+  const uint2 *pin;
+  uint2 *pout;
+  uint64_t cap;
+  Lists out;
+  uint32_t W;
+  unsigned long long *N, *vis, *acc;
+  uint32_t *flagN;
+  int shortest, acc_on;
+};
+
+struct PushArgs {
+  Ctr *ctr;
+  int h;
+  Lists out;
+  const unsigned long long *F;
+  unsigned long long *N, *vis, *acc;
+  uint32_t *flagN;
+  const uint32_t *active;
+  uint32_t *touched;
+  uint32_t W;
+  int shortest, acc_on;
+};
+
+struct PullArgs {
+  Lists in;
+  const uint4 *F;
+  uint4 *N, *vis, *acc;
+  const uint32_t *flagF;
+  uint32_t *flagN;
+  uint32_t V, Q, qslice;
+  int multislice, shortest, acc_on;
+  uint32_t hub_threshold;
+  const uint32_t *hubs;
+  uint32_t nhubs;
+  Ctr *ctr;
+  int h;
+};
+
+// Learned strategy picker evaluated inside the decide kernel (picker.cuh).
+__device__ int picker_choose(const DecideArgs &a, const HopCtr &prev);
+
+}  // namespace ex
+}  // namespace vs

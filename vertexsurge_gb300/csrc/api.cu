@@ -152,6 +152,108 @@ int popcount_words(const uint64_t *w, size_t n, uint64_t *count, cudaStream_t st
   return VS_OK;
 }
 
+// Exclusive prefix sum over n uint64 values: out[0..n] with out[n] = total.
+// Three passes: per-block scans of 1024 values, a one-block scan of the block
+// totals, then the block offsets added back.
+__global__ void k_scan_block(const unsigned long long *__restrict__ in,
+                             unsigned long long *__restrict__ out, size_t n,
+                             unsigned long long *__restrict__ sums) {
+  __shared__ unsigned long long warp_tot[32];
+  const size_t base = (size_t)blockIdx.x * 1024;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  unsigned long long v[4], run = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    size_t i = base + (size_t)t * 4 + k;
+    v[k] = i < n ? in[i] : 0ull;
+    run += v[k];
+  }
+  unsigned long long incl = run;
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    unsigned long long x = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0ull, xi = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long y = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += y;
+    }
+    warp_tot[lane] = xi - x;
+    if (lane == 31) sums[blockIdx.x] = xi;
+  }
+  __syncthreads();
+  unsigned long long pre = warp_tot[w] + incl - run;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    size_t i = base + (size_t)t * 4 + k;
+    if (i < n) out[i] = pre;
+    pre += v[k];
+  }
+}
+
+__global__ void k_scan_sums(unsigned long long *sums, size_t nb, unsigned long long *total) {
+  __shared__ unsigned long long carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ unsigned long long wt[32];
+  for (size_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+    size_t i = b0 + threadIdx.x;
+    unsigned long long x = i < nb ? sums[i] : 0ull, xi = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long y = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += y;
+    }
+    if (lane == 31) wt[w] = xi;
+    __syncthreads();
+    if (w == 0) {
+      unsigned long long a = lane < (int)(blockDim.x >> 5) ? wt[lane] : 0ull, ai = a;
+      for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, ai, o);
+        if (lane >= o) ai += y;
+      }
+      wt[lane] = ai - a;
+    }
+    __syncthreads();
+    const unsigned long long c = carry;
+    if (i < nb) sums[i] = c + wt[w] + xi - x;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = c + wt[w] + xi;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(unsigned long long *__restrict__ out, size_t n,
+                           const unsigned long long *__restrict__ sums,
+                           const unsigned long long *__restrict__ total) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] += sums[i / 1024];
+  if (i == 0) out[n] = *total;
+}
+
+int exclusive_scan_u64(const unsigned long long *in, unsigned long long *out, size_t n,
+                       cudaStream_t st) {
+  const size_t nb = (n + 1023) / 1024;
+  unsigned long long *sums, *total;
+  VS_TRY(dalloc_n(&sums, nb ? nb : 1, st));
+  VS_TRY(dalloc_n(&total, 1, st));
+  if (n) {
+    k_scan_block<<<(unsigned)nb, 256, 0, st>>>(in, out, n, sums);
+    k_scan_sums<<<1, 1024, 0, st>>>(sums, nb, total);
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, sums, total);
+  } else {
+    VS_CK(cudaMemsetAsync(out, 0, sizeof(unsigned long long), st));
+  }
+  dfree(sums, st);
+  dfree(total, st);
+  VS_CK(cudaGetLastError());
+  return VS_OK;
+}
+
 }  // namespace vs
 
 using namespace vs;

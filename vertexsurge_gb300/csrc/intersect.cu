@@ -1,10 +1,427 @@
-// Multi-way intersection (placeholder, replaced below).
+// Multi-way intersection: Mintersect (src/objects/operator/mintersect.cpp:14-345)
+// re-designed for sm_103a.
+//
+// A warp owns one base tuple.  Each dependency yields, for the vertex u the
+// tuple holds in that dependency's base column, a set of new vertices:
+//   matrix     column u of a ColMain matrix (rows = new vertices); when every
+//              dependency is a matrix the warp ANDs the columns word by word,
+//              popcounts and extracts the bits (the reference's and_col_from +
+//              count_bits_in_col + BitmapIterator, mintersect.cpp:244-333);
+//   adjacency  u's sorted out-list in the graph CSR;
+//   flat       the (u, new) pairs of a flat edge table, grouped by u on the
+//              device (counting sort) and de-duplicated through a pair hash set.
+// With a list dependency the warp walks the shortest list (32 candidates per
+// step) and tests each candidate against the others: binary search in sorted
+// adjacency, pair-hash lookup for flat tables, one bit load for matrices.
+// Counting and emitting are two passes over the same code; a prefix sum of
+// the per-tuple counts places every tuple's output.
+#include <algorithm>
+#include <cstring>
+
+#include "dev_util.cuh"
+#include "hash.cuh"
 #include "vs_internal.cuh"
-using namespace vs;
-extern "C" int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
-                             uint32_t new_vertex_count, int only_count, uint64_t max_rows,
-                             vs_flat **out, uint64_t *count, vs_stream_t stream) {
-  (void)base; (void)deps; (void)ndeps; (void)new_vertex_count; (void)only_count; (void)max_rows;
-  (void)out; (void)count; (void)stream;
-  return fail(VS_ERR_UNSUPPORTED, "vs_mintersect not built yet");
+
+namespace vs {
+namespace is {
+
+enum { DEP_MAT = 0, DEP_SORTED = 1, DEP_HASHED = 2 };
+constexpr int MAX_DEPS = 8;
+
+struct Dep {
+  int kind;
+  const uint32_t *base_u;  // base column holding u
+  // matrix
+  const uint64_t *words;
+  uint32_t wpc, rows, cols;
+  int has_cmap;
+  HashTable cmap;  // col value -> first column (val)
+  // lists
+  const int64_t *off;
+  const uint32_t *adj;
+  uint64_t n_u;
+  HashTable pairs;  // DEP_HASHED: (u << 32 | new) membership
+};
+
+struct OutCol {
+  void *dst;
+  const void *src;
+  int type;
+};
+
+struct Args {
+  Dep dep[MAX_DEPS];
+  int ndeps, all_mat, emit;
+  uint64_t nbase;
+  uint32_t cache_rows;
+  const uint32_t *target_row_map;
+  unsigned long long *tcnt, *total;
+  const unsigned long long *toff;
+  uint64_t max_rows;
+  OutCol col[16];
+  int nbcols;
+  uint32_t *out_new;
+};
+
+__device__ __forceinline__ bool in_sorted(const uint32_t *a, int64_t lo, int64_t hi, uint32_t x) {
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    const uint32_t v = a[mid];
+    if (v == x) return true;
+    if (v < x)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return false;
 }
+
+__device__ __forceinline__ void emit_row(const Args &a, uint64_t t, uint64_t pos, uint32_t x) {
+  if (pos >= a.max_rows) return;
+  for (int c = 0; c < a.nbcols; c++) {
+    const OutCol &oc = a.col[c];
+    if (oc.type == VS_T_I64)
+      ((long long *)oc.dst)[pos] = ((const long long *)oc.src)[t];
+    else
+      ((uint32_t *)oc.dst)[pos] = ((const uint32_t *)oc.src)[t];
+  }
+  a.out_new[pos] = a.target_row_map ? a.target_row_map[x] : x;
+}
+
+__global__ void __launch_bounds__(256) k_isect(Args a) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  unsigned long long tot = 0;
+  for (uint64_t t = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < a.nbase;
+       t += warps) {
+    uint32_t col[MAX_DEPS];
+    int64_t lo[MAX_DEPS], hi[MAX_DEPS];
+    uint32_t uu[MAX_DEPS];
+    bool empty = false;
+    int best = -1;
+    int64_t best_len = 0;
+#pragma unroll
+    for (int i = 0; i < MAX_DEPS; i++) {
+      if (i >= a.ndeps) break;
+      const Dep &d = a.dep[i];
+      const uint32_t u = d.base_u[t];
+      uu[i] = u;
+      col[i] = 0;
+      lo[i] = hi[i] = 0;
+      if (d.kind == DEP_MAT) {
+        if (d.has_cmap) {
+          const uint64_t s = ht_find(d.cmap, u);
+          if (s == ~0ull)
+            empty = true;
+          else
+            col[i] = d.cmap.val[s];
+        } else if (u < d.cols) {
+          col[i] = u;
+        } else {
+          empty = true;
+        }
+      } else {
+        if (u < d.n_u) {
+          lo[i] = d.off[u];
+          hi[i] = d.off[u + 1];
+        }
+        if (lo[i] == hi[i]) empty = true;
+        if (best < 0 || hi[i] - lo[i] < best_len) {
+          best = i;
+          best_len = hi[i] - lo[i];
+        }
+      }
+    }
+    unsigned long long count = 0;
+    const unsigned long long base_pos = a.emit ? a.toff[t] : 0ull;
+    if (!empty && a.all_mat) {
+      const uint32_t lw = (a.cache_rows + 63) / 64;
+      for (uint32_t q0 = 0; q0 < lw; q0 += 32) {
+        const uint32_t q = q0 + lane;
+        uint64_t w = 0;
+        if (q < lw) {
+          w = ~0ull;
+          for (int i = 0; i < a.ndeps; i++) w &= a.dep[i].words[(size_t)col[i] * a.dep[i].wpc + q];
+          if (q == lw - 1 && (a.cache_rows & 63)) w &= (1ull << (a.cache_rows & 63)) - 1;
+        }
+        const unsigned n = __popcll(w);
+        unsigned incl = n;
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned y = __shfl_up_sync(FULLMASK, incl, o);
+          if (lane >= o) incl += y;
+        }
+        if (a.emit) {
+          uint64_t pos = base_pos + count + incl - n;
+          while (w) {
+            const uint32_t x = q * 64 + (__ffsll((long long)w) - 1);
+            w &= w - 1;
+            emit_row(a, t, pos++, x);
+          }
+        }
+        count += __shfl_sync(FULLMASK, incl, 31);
+      }
+    } else if (!empty) {
+      const Dep &L = a.dep[best];
+      for (int64_t j0 = lo[best]; j0 < hi[best]; j0 += 32) {
+        const int64_t j = j0 + lane;
+        bool keep = false;
+        uint32_t x = 0;
+        if (j < hi[best]) {
+          x = L.adj[j];
+          keep = x < a.cache_rows;
+          for (int i = 0; i < a.ndeps && keep; i++) {
+            if (i == best) continue;
+            const Dep &d = a.dep[i];
+            if (d.kind == DEP_MAT) {
+              keep = x < d.rows &&
+                     ((d.words[(size_t)col[i] * d.wpc + (x >> 6)] >> (x & 63)) & 1ull);
+            } else if (d.kind == DEP_SORTED) {
+              keep = in_sorted(d.adj, lo[i], hi[i], x);
+            } else {
+              keep = ht_find(d.pairs, ((unsigned long long)uu[i] << 32) | x) != ~0ull;
+            }
+          }
+        }
+        const unsigned m = __ballot_sync(FULLMASK, keep);
+        if (a.emit && keep) emit_row(a, t, base_pos + count + __popc(m & lanemask_lt()), x);
+        count += __popc(m);
+      }
+    }
+    if (!a.emit && lane == 0) {
+      if (a.tcnt) a.tcnt[t] = count;
+      tot += count;
+    }
+  }
+  if (!a.emit) block_add(tot, a.total);
+}
+
+// Flat dependency -> CSR over u with duplicate pairs removed.
+__global__ void k_max_u(const uint32_t *u, uint64_t n, unsigned *mx) {
+  unsigned m = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    m = max(m, u[i]);
+  for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(FULLMASK, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+}
+
+__global__ void k_flat_dedup(HashTable pairs, const uint32_t *u, const uint32_t *nv, uint64_t n,
+                             unsigned long long *cnt_u, uint8_t *isnew) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t s = ht_insert(pairs, ((unsigned long long)u[i] << 32) | nv[i]);
+    const bool first = atomicCAS(&pairs.val[s], 0xffffffffu, 0u) == 0xffffffffu;
+    isnew[i] = first;
+    if (first) atomicAdd(&cnt_u[u[i]], 1ull);
+  }
+}
+
+__global__ void k_flat_scatter(const uint32_t *u, const uint32_t *nv, uint64_t n,
+                               const uint8_t *isnew, const unsigned long long *off,
+                               unsigned long long *cur, uint32_t *adj) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    if (isnew[i]) adj[off[u[i]] + atomicAdd(&cur[u[i]], 1ull)] = nv[i];
+}
+
+__global__ void k_build_cols(HashTable t, const uint32_t *col_map, uint32_t cols) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
+    const uint64_t s = ht_insert(t, col_map[c]);
+    atomicMin(&t.val[s], c);
+  }
+}
+
+struct Scratch {
+  cudaStream_t st;
+  void *p[64] = {};
+  int n = 0;
+  template <typename T> int get(T **out, size_t count) {
+    int rc = dalloc_n(out, count, st);
+    if (rc == VS_OK) p[n++] = *out;
+    return rc;
+  }
+  ~Scratch() {
+    for (int i = 0; i < n; i++) dfree(p[i], st);
+  }
+};
+
+int grid_for(uint64_t n, int per_block = 256) {
+  return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + per_block - 1) / per_block,
+                                                       (uint64_t)sm_count() * 16));
+}
+
+int hash_alloc(Scratch &sc, uint64_t n, HashTable *t) {
+  t->cap = ht_capacity(std::max<uint64_t>(n, 1));
+  VS_TRY(sc.get(&t->keys, t->cap + 1));
+  VS_TRY(sc.get(&t->val, t->cap + 1));
+  VS_CK(cudaMemsetAsync(t->keys, 0xff, 8 * (t->cap + 1), sc.st));
+  VS_CK(cudaMemsetAsync(t->val, 0xff, 4 * (t->cap + 1), sc.st));
+  t->cnt = t->off = t->cur = nullptr;
+  return VS_OK;
+}
+
+int prepare_flat_dep(Scratch &sc, const vs_flat *f, uint32_t ucol, uint32_t nvcol, Dep *d) {
+  if (ucol >= f->ncols || nvcol >= f->ncols || ucol == nvcol)
+    return fail(VS_ERR_ARG, "flat dependency columns out of range");
+  if (f->types[ucol] != VS_T_VID || f->types[nvcol] != VS_T_VID)
+    return fail(VS_ERR_ARG, "Mintersect dependency columns must be VIDs (mintersect.cpp:22-27)");
+  cudaStream_t st = sc.st;
+  const uint32_t *u = (const uint32_t *)f->cols[ucol], *nv = (const uint32_t *)f->cols[nvcol];
+  const uint64_t n = f->nrows;
+  unsigned *dmx;
+  VS_TRY(sc.get(&dmx, 1));
+  VS_CK(cudaMemsetAsync(dmx, 0, 4, st));
+  if (n) k_max_u<<<grid_for(n), 256, 0, st>>>(u, n, dmx);
+  unsigned mx = 0;
+  VS_CK(cudaMemcpyAsync(&mx, dmx, 4, cudaMemcpyDeviceToHost, st));
+  VS_CK(cudaStreamSynchronize(st));
+  const uint64_t n_u = n ? (uint64_t)mx + 1 : 0;
+  if (n_u > (1ull << 31)) return fail(VS_ERR_UNSUPPORTED, "flat dependency vertex ids above 2^31");
+  d->kind = DEP_HASHED;
+  d->n_u = n_u;
+  VS_TRY(hash_alloc(sc, n, &d->pairs));
+  unsigned long long *cnt, *off, *cur;
+  uint8_t *isnew;
+  uint32_t *adj;
+  VS_TRY(sc.get(&cnt, n_u + 1));
+  VS_TRY(sc.get(&off, n_u + 2));
+  VS_TRY(sc.get(&cur, n_u + 1));
+  VS_TRY(sc.get(&isnew, n));
+  VS_TRY(sc.get(&adj, n));
+  VS_CK(cudaMemsetAsync(cnt, 0, 8 * (n_u + 1), st));
+  VS_CK(cudaMemsetAsync(cur, 0, 8 * (n_u + 1), st));
+  if (n) k_flat_dedup<<<grid_for(n), 256, 0, st>>>(d->pairs, u, nv, n, cnt, isnew);
+  VS_TRY(exclusive_scan_u64(cnt, off, n_u, st));
+  if (n) k_flat_scatter<<<grid_for(n), 256, 0, st>>>(u, nv, n, isnew, off, cur, adj);
+  // offsets are read as int64 by the kernel
+  d->off = reinterpret_cast<const int64_t *>(off);
+  d->adj = adj;
+  VS_CK(cudaGetLastError());
+  return VS_OK;
+}
+
+}  // namespace is
+}  // namespace vs
+
+using namespace vs;
+using namespace vs::is;
+
+extern "C" {
+
+int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
+                  uint32_t new_vertex_count, int only_count, uint64_t max_rows, vs_flat **out,
+                  uint64_t *count, vs_stream_t stream) {
+  if (!count || (!only_count && !out)) return fail(VS_ERR_ARG, "vs_mintersect: null output");
+  if (!base.flat == !base.mat) return fail(VS_ERR_ARG, "base is exactly one of a flat table or a matrix");
+  if (ndeps == 0 || ndeps > (uint32_t)MAX_DEPS || !deps)
+    return fail(VS_ERR_ARG, "Mintersect takes 1..%d dependencies", MAX_DEPS);
+  cudaStream_t st = S(stream);
+  *count = 0;
+  if (out) *out = nullptr;
+  Scratch sc{st};
+  // base tuples as a flat table
+  vs_flat *bf_owned = nullptr;
+  const vs_flat *bf = base.flat;
+  if (base.mat) {
+    VS_TRY(bitmat_to_flat(base.mat, st, &bf_owned));
+    bf = bf_owned;
+  }
+  struct Owned {
+    vs_flat *f;
+    ~Owned() { vs_flat_free(f); }
+  } owned{bf_owned};
+  Args a{};
+  a.ndeps = (int)ndeps;
+  a.nbase = bf->nrows;
+  uint32_t nmat = 0, mat_rows = 0;
+  for (uint32_t i = 0; i < ndeps; i++) {
+    const vs_isect_dep &d = deps[i];
+    Dep &D = a.dep[i];
+    const int nkinds = (d.mat != nullptr) + (d.flat != nullptr) + (d.graph != nullptr);
+    if (nkinds != 1) return fail(VS_ERR_ARG, "dependency %u must name exactly one source", i);
+    if (d.base_col >= bf->ncols) return fail(VS_ERR_ARG, "dependency %u base column out of range", i);
+    if (bf->types[d.base_col] != VS_T_VID)
+      return fail(VS_ERR_ARG, "base column of dependency %u is not a VID", i);
+    D.base_u = (const uint32_t *)bf->cols[d.base_col];
+    if (d.mat) {
+      const vs_bitmat *m = d.mat;
+      if (nmat && m->rows != mat_rows)
+        return fail(VS_ERR_ARG, "matrix dependencies differ in row count (mintersect.cpp:69-76)");
+      if (!nmat) a.target_row_map = m->row_map;
+      mat_rows = m->rows;
+      nmat++;
+      D.kind = DEP_MAT;
+      D.words = m->words;
+      D.wpc = m->wpc;
+      D.rows = m->rows;
+      D.cols = m->cols;
+      D.has_cmap = m->col_map != nullptr;
+      if (D.has_cmap) {
+        VS_TRY(hash_alloc(sc, m->cols, &D.cmap));
+        if (m->cols) k_build_cols<<<grid_for(m->cols), 256, 0, st>>>(D.cmap, m->col_map, m->cols);
+      }
+    } else if (d.graph) {
+      const vs_graph *g = d.graph;
+      if (d.direction == VS_DIR_BOTH && g->directed)
+        return fail(VS_ERR_UNSUPPORTED, "adjacency dependency needs one direction");
+      const bool fwd = !g->directed || d.direction == VS_DIR_FORWARD;
+      D.kind = DEP_SORTED;
+      D.off = fwd ? g->fwd_off : g->rev_off;
+      D.adj = fwd ? g->fwd_dst : g->rev_src;
+      D.n_u = g->V;
+    } else {
+      VS_TRY(prepare_flat_dep(sc, d.flat, d.u_col, d.nv_col, &D));
+    }
+  }
+  a.all_mat = nmat == ndeps;
+  a.cache_rows = a.all_mat ? mat_rows : new_vertex_count;
+  unsigned long long *d_total, *tcnt = nullptr, *toff = nullptr;
+  VS_TRY(sc.get(&d_total, 1));
+  VS_CK(cudaMemsetAsync(d_total, 0, 8, st));
+  if (!only_count) {
+    VS_TRY(sc.get(&tcnt, a.nbase));
+    VS_TRY(sc.get(&toff, a.nbase + 1));
+  }
+  a.tcnt = tcnt;
+  a.total = d_total;
+  a.emit = 0;
+  const int grid = grid_for(a.nbase * 32);
+  if (a.nbase) k_isect<<<grid, 256, 0, st>>>(a);
+  VS_CK(cudaGetLastError());
+  unsigned long long total = 0;
+  VS_CK(cudaMemcpyAsync(&total, d_total, 8, cudaMemcpyDeviceToHost, st));
+  VS_CK(cudaStreamSynchronize(st));
+  *count = total;
+  if (only_count) return VS_OK;
+  VS_TRY(exclusive_scan_u64(tcnt, toff, a.nbase, st));
+  const uint64_t rows = std::min<uint64_t>(total, max_rows);
+  int32_t types[16];
+  if (bf->ncols + 1 > 16) return fail(VS_ERR_UNSUPPORTED, "result wider than 16 columns");
+  for (uint32_t c = 0; c < bf->ncols; c++) types[c] = bf->types[c];
+  types[bf->ncols] = VS_T_VID;
+  vs_flat *f = nullptr;
+  VS_TRY(flat_alloc(bf->ncols + 1, types, rows, st, &f));
+  a.nbcols = (int)bf->ncols;
+  for (uint32_t c = 0; c < bf->ncols; c++) {
+    a.col[c].dst = f->cols[c];
+    a.col[c].src = bf->cols[c];
+    a.col[c].type = bf->types[c];
+  }
+  a.out_new = (uint32_t *)f->cols[bf->ncols];
+  a.toff = toff;
+  a.max_rows = rows;
+  a.emit = 1;
+  if (a.nbase && rows) k_isect<<<grid, 256, 0, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    vs_flat_free(f);
+    return cuda_fail(e, "mintersect", __FILE__, __LINE__);
+  }
+  *out = f;
+  return total > max_rows ? fail(VS_ERR_CAPACITY, "intersection produced %llu rows, bound %llu",
+                                 (unsigned long long)total, (unsigned long long)max_rows)
+                          : VS_OK;
+}
+
+}  // extern "C"

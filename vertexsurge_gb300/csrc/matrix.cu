@@ -102,8 +102,6 @@ __global__ void k_to_flat(const uint64_t *__restrict__ w, uint32_t rows, uint32_
 
 }  // namespace mx
 
-int popcount_words(const uint64_t *w, size_t n, uint64_t *count, cudaStream_t st);
-
 int validate_ids(const uint32_t *d_ids, uint32_t n, uint32_t bound, cudaStream_t st, bool *ok) {
   unsigned *bad;
   VS_TRY(dalloc_n(&bad, 1, st));

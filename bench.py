@@ -1,0 +1,354 @@
+#!/usr/bin/env python3
+"""Benchmark: the power-law pattern query on one GB300.
+
+Workload (default "zipf10M_pattern"): a power-law graph with 10M vertices and
+~300M directed edges (out-degree ~ Zipf(2.1) capped at 50k, uniform targets,
+uint32 CSR).  One step is the whole pattern query:
+  A  = VExpand(4,096 sources, Shortest, hops [1,4], Forward)
+  B  = VExpand(4,096 other sources, Shortest, hops [1,2], Forward)
+  J  = HashJoin(A, B) on the vertex id, exact count
+  P  = VExpand(the A sources, Any, hops [1,1])  (edges a -> b)
+  T  = Mintersect(P; out-list of a, out-list of b): triangles a->b, a->c, b->c, count
+The metric is multi-source expand throughput, Gsrc-edges/s =
+sum over the three expands and their hops of S * E_active(h), divided by the
+whole step's time (join and intersection included).
+
+value   : device-resident inputs (sources in HBM, reusable expand plans),
+          CUDA events on the launching stream around exactly --steps steps.
+e2e     : the same query through the one-shot C-ABI calls with the source
+          lists in pinned host memory (host->device copies and the device->host
+          result reads inside the timed region).
+--impl reference : the CPU restatement of the reference's operators (the
+          oracle, OpenMP over every host core) on a bounded sample of the same
+          workload: VExpand(1,024 of the A sources, Shortest, [1,4]).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+WORKLOADS = {
+    "zipf10M_pattern": dict(kind="zipf", V=10_000_000, E=300_000_000, alpha=2.1, cap=50_000, seed=3,
+                            S_a=4096, hops_a=(1, 4), S_b=4096, hops_b=(1, 2), cpu_S=1024),
+    # smaller instances of the same query (for profiling runs)
+    "zipf1M_pattern": dict(kind="zipf", V=1_000_000, E=30_000_000, alpha=2.1, cap=50_000, seed=3,
+                           S_a=4096, hops_a=(1, 4), S_b=4096, hops_b=(1, 2), cpu_S=1024),
+    "rmat16_pattern": dict(kind="rmat", scale=16, ef=16, seed=1, S_a=512, hops_a=(1, 3), S_b=512,
+                           hops_b=(1, 2), cpu_S=512),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def make_graph(w):
+    from vertexsurge_gb300 import graphgen
+    if w["kind"] == "zipf":
+        return graphgen.zipf(w["V"], w["E"], w["alpha"], w["cap"], seed=w["seed"])
+    return graphgen.rmat(w["scale"], w["ef"], 0.57, 0.19, 0.19, seed=w["seed"])
+
+
+def sources(g, w):
+    from vertexsurge_gb300 import graphgen
+    sa = graphgen.sample_sources(g.V, w["S_a"], seed=101)
+    sb = graphgen.sample_sources(g.V, w["S_b"], seed=102)
+    return sa, sb
+
+
+def peaks():
+    try:
+        p = json.loads(PEAKS_FILE.read_text())
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        for line in Path(self.f.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()),
+                                   default=None)}
+
+
+def expand_bytes(V, W, e_act, shortest, acc):
+    """Algorithmic bytes of one hop: CSR offsets + targets, one row gather per
+    active edge (32-byte sector minimum) and P streaming passes over the V x S
+    matrices (P = 4 for the frontier/next pair plus visited or accumulator
+    read+write each)."""
+    P = 2 + (2 if shortest else 0) + (2 if acc else 0)
+    return 8 * (V + 1) + 4 * e_act + e_act * max(32, 8 * W) + P * 8 * W * V
+
+
+def cpu_baseline(g, w, sa):
+    """Oracle VExpand on the host cores: the bounded sample and its throughput."""
+    from oracle import pyoracle as O
+    S = w["cpu_S"]
+    src = sa[:S]
+    k0, k1 = w["hops_a"]
+    _, _, st = O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False, hop_stats=True)
+    src_edges = S * sum(st["active_edges"][1:])
+    t = time.perf_counter()
+    O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False)
+    dt = time.perf_counter() - t
+    return {"value": src_edges / dt / 1e9, "unit": "Gsrc-edges/s", "cores": O.lib().oracle_get_threads(),
+            "kind": "port",
+            "sample": f"VExpand(Shortest, [{k0},{k1}], Forward) from the first {S} A sources on the full "
+                      f"graph, one run of {dt:.1f} s ({src_edges / 1e9:.2f} Gsrc-edges)"}, dt
+
+
+def run_reference(args, w, rank, world):
+    """--impl reference: the oracle (CPU restatement of the reference) on host cores."""
+    if rank != 0:
+        return
+    from vertexsurge_gb300 import build as b
+    b.build_gen()
+    b.build_oracle()
+    from oracle import pyoracle as O
+    t0 = time.time()
+    g = make_graph(w)
+    sa, _ = sources(g, w)
+    log(f"graph {g.V} vertices {g.E} edges in {time.time() - t0:.1f}s")
+    S = w["cpu_S"]
+    src = sa[:S]
+    k0, k1 = w["hops_a"]
+    _, _, st = O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False, hop_stats=True)
+    src_edges = S * sum(st["active_edges"][1:])
+    for _ in range(min(args.warmup, 1)):
+        O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False)
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    value = src_edges * args.steps / total / 1e9
+    cores = O.lib().oracle_get_threads()
+    sample = (f"VExpand(Shortest, [{k0},{k1}], Forward) from {S} of the A sources on the full graph "
+              f"per step ({src_edges / 1e9:.2f} Gsrc-edges)")
+    line = {"impl": "reference", "metric": "multi-source expand Gsrc-edges/s", "value": value,
+            "unit": "Gsrc-edges/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": min(args.warmup, 1),
+            "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded power-law graph, uniform sources)",
+            "config": {"workload": args.workload, "V": g.V, "E": g.E, "S": S, "hops": [k0, k1]},
+            "cpu_baseline": {"value": value, "unit": "Gsrc-edges/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "Gsrc-edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, w, rank, world, local_rank):
+    import torch
+    import vertexsurge_gb300 as vs
+    from vertexsurge_gb300 import build as b
+    b.build_all()
+    torch.cuda.set_device(local_rank)
+    vs.init(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    t0 = time.time()
+    g = make_graph(w)
+    sa, sb = sources(g, w)
+    log(f"[rank {rank}] graph {g.V} vertices {g.E} edges in {time.time() - t0:.1f}s")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dg = vs.DeviceGraph.from_host(g, stream=stream)
+    ka, kb = w["hops_a"], w["hops_b"]
+    Sa, Sb = len(sa), len(sb)
+    pA = vs.ExpandPlan(dg, Sa, vs.make_params(ka[0], ka[1], "shortest", "forward"))
+    pB = vs.ExpandPlan(dg, Sb, vs.make_params(kb[0], kb[1], "shortest", "forward"))
+    pP = vs.ExpandPlan(dg, Sa, vs.make_params(1, 1, "any", "forward"))
+    dA = torch.from_numpy(sa.view(np.int32)).to("cuda")
+    dB = torch.from_numpy(sb.view(np.int32)).to("cuda")
+    adj = [dict(graph=dg, direction="forward", base_col=0), dict(graph=dg, direction="forward", base_col=1)]
+
+    def step(timing=False):
+        pA.run(dA, stream=stream)
+        pB.run(dB, stream=stream)
+        A, B = pA.result(), pB.result()
+        _, jc, _ = vs.hash_join(A, B, 1, 1, only_count=True, stream=stream)
+        pP.run(dA, stream=stream)
+        _, tc, _ = vs.mintersect(pP.result(), adj, g.V, only_count=True, stream=stream)
+        return jc, tc
+
+    # exact E_active of every hop (stats pass, untimed)
+    for p in (pA, pB, pP):
+        p.set_tuning(collect_stats=True)
+    jc, tc = step()
+    stA, stB, stP = pA.stats(stream), pB.stats(stream), pP.stats(stream)
+    src_edges = (Sa * sum(stA["active_edges"][1:]) + Sb * sum(stB["active_edges"][1:])
+                 + Sa * sum(stP["active_edges"][1:]))
+    log(f"[rank {rank}] A hops {stA['hops_run']} strat {stA['strategy'][1:]} e_act {stA['active_edges'][1:]}")
+    log(f"[rank {rank}] B strat {stB['strategy'][1:]} e_act {stB['active_edges'][1:]} join={jc} tri={tc}")
+    for p in (pA, pB, pP):
+        p.set_tuning(collect_stats=False)
+    pA.set_tuning(timing=True)  # per-hop CUDA events around the dominant pull kernel
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local_rank)
+    launches0 = vs.kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pull_ms, pull_bytes = 0.0, 0.0
+    W = (Sa + 63) // 64
+    W += W & 1
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+        st = pA.stats(stream)
+        for h in range(1, st["hops_run"] + 1):
+            if st["strategy"][h] == vs.STRAT_PULL:
+                pull_ms += st["pull_ms"][h]
+                pull_bytes += expand_bytes(g.V, W, stA["active_edges"][h], True, False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = vs.kernel_launches() - launches0
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * src_edges * args.steps / (ms / 1e3) / 1e9
+
+    # e2e: one-shot C-ABI calls, sources from pinned host memory, counts read back
+    pA.set_tuning(timing=False)
+    hA = torch.from_numpy(sa.view(np.int32)).pin_memory()
+    hB = torch.from_numpy(sb.view(np.int32)).pin_memory()
+
+    def step_e2e():
+        A, _, _ = vs.expand(dg, hA, ka[0], ka[1], "shortest", "forward", stream=stream)
+        B, _, _ = vs.expand(dg, hB, kb[0], kb[1], "shortest", "forward", stream=stream)
+        _, jc2, _ = vs.hash_join(A, B, 1, 1, only_count=True, stream=stream)
+        A.free()
+        B.free()
+        P, _, _ = vs.expand(dg, hA, 1, 1, "any", "forward", stream=stream)
+        _, tc2, _ = vs.mintersect(P, adj, g.V, only_count=True, stream=stream)
+        P.free()
+        return jc2, tc2
+
+    for _ in range(max(1, min(args.warmup, 3))):
+        step_e2e()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        jc2, tc2 = step_e2e()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1)
+    assert (jc2, tc2) == (jc, tc), "e2e results differ from the plan path"
+    e2e = {"value": world * src_edges * args.steps / (ms_e2e / 1e3) / 1e9, "unit": "Gsrc-edges/s",
+           "h2d_bytes_per_step": int(4 * (2 * Sa + Sb)), "d2h_bytes_per_step": 16,
+           "ms_per_step": ms_e2e / args.steps}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peak, peak_kind = peaks()
+    achieved = pull_bytes / (pull_ms / 1e3) / 1e9 if pull_ms else None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None, "traffic": None,
+                "kernel": "k_pull (expand A, pull hops)", "peak_source": peak_kind,
+                "per_launch_ms": pull_ms / max(1, args.steps * sum(1 for s in stA["strategy"][1:] if s == 1))}
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        cpu, _ = cpu_baseline(g, w, sa)
+    line = {"metric": "multi-source expand Gsrc-edges/s", "value": value, "unit": "Gsrc-edges/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded power-law graph, uniform sources)",
+            "config": {"workload": args.workload, "V": g.V, "E": g.E, "S_a": Sa, "hops_a": list(ka),
+                       "S_b": Sb, "hops_b": list(kb), "join": "A x B on vertex id, exact count",
+                       "intersect": "triangle closing over out-lists, exact count",
+                       "l2": "inputs larger than L2 (CSR 2.5 GB, 5.1 GB per bit matrix)",
+                       "parallelism": f"replicas{world}"},
+            "queries_per_s": 1000.0 / ms_per_step,
+            "results": {"join_count": jc, "triangles": tc, "visited_a": stA["visit_count"],
+                        "hops_run_a": stA["hops_run"], "strategies_a": stA["strategy"][1:],
+                        "src_edges_per_step": src_edges},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="zipf10M_pattern")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, w, rank, world)
+    else:
+        run_gpu(args, w, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

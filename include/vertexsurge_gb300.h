@@ -78,6 +78,9 @@ const char *vs_last_error(void);
  * allocator pool. */
 int vs_init(int device);
 const char *vs_version(void);
+/* Number of CUDA kernels this library has launched since it was loaded
+ * (diagnostics; no counterpart in the reference). */
+uint64_t vs_kernel_launches(void);
 
 /* ---- graph (replaces Graph::load + Graph::get_edges_refs CSR requests,
  *      src/objects/storage/graph_store.cpp:48-73, :75-110, :142-189) ------
@@ -162,6 +165,8 @@ typedef struct vs_expand_stats {
   uint64_t active_edges[VS_MAX_HOPS + 1];   /* edges leaving non-zero columns of layer h-1 */
   uint64_t pairs[VS_MAX_HOPS + 1];          /* sparse hops: pairs produced */
   int32_t strategy[VS_MAX_HOPS + 1];        /* strategy run at hop h */
+  float hop_ms[VS_MAX_HOPS + 1];            /* device time of hop h (plans with timing on) */
+  float pull_ms[VS_MAX_HOPS + 1];           /* device time of hop h's pull kernels */
 } vs_expand_stats;
 
 /* A plan owns the frontier, next, visited and accumulator matrices for S
@@ -177,6 +182,11 @@ int vs_expand_plan_run(vs_expand_plan *plan, const uint32_t *sources, const uint
 int vs_expand_plan_result(vs_expand_plan *plan, vs_bitmat **view);
 int vs_expand_plan_stats(vs_expand_plan *plan, vs_expand_stats *stats, vs_stream_t stream);
 int vs_expand_plan_free(vs_expand_plan *plan);
+/* Planner knobs: fraction of E below which pair lists (SPARSE) run, fraction
+ * of V below which PUSH runs (negative = keep), per-hop E_active statistics
+ * (an extra pass per hop) and per-hop CUDA-event timing (not for capture). */
+int vs_expand_plan_set_tuning(vs_expand_plan *plan, double sparse_frac, double push_frac,
+                              int collect_stats, int timing);
 
 /* One-shot expand: plan, run, hand the result matrix to the caller.
  * FindShortest: targets[i] is the target of source i, distances[i] receives

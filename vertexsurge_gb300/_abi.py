@@ -46,14 +46,17 @@ class ExpandStats(C.Structure):
                 ("active_vertices", C.c_uint64 * (MAX_HOPS + 1)),
                 ("active_edges", C.c_uint64 * (MAX_HOPS + 1)),
                 ("pairs", C.c_uint64 * (MAX_HOPS + 1)),
-                ("strategy", C.c_int32 * (MAX_HOPS + 1))]
+                ("strategy", C.c_int32 * (MAX_HOPS + 1)),
+                ("hop_ms", C.c_float * (MAX_HOPS + 1)),
+                ("pull_ms", C.c_float * (MAX_HOPS + 1))]
 
     def as_dict(self) -> dict:
         n = self.hops_run + 1
         return {"hops_run": self.hops_run, "found": self.found, "visit_count": self.visit_count,
                 "new_bits": list(self.new_bits[:n]), "active_vertices": list(self.active_vertices[:n]),
                 "active_edges": list(self.active_edges[:n]), "pairs": list(self.pairs[:n]),
-                "strategy": list(self.strategy[:n])}
+                "strategy": list(self.strategy[:n]), "hop_ms": list(self.hop_ms[:n]),
+                "pull_ms": list(self.pull_ms[:n])}
 
 
 class BitmatInfo(C.Structure):
@@ -77,6 +80,8 @@ _lib = None
 _SIGS = [
     ("vs_last_error", C.c_char_p, []),
     ("vs_version", C.c_char_p, []),
+    ("vs_kernel_launches", C.c_uint64, []),
+    ("vs_expand_plan_set_tuning", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_int]),
     ("vs_init", C.c_int, [C.c_int]),
     ("vs_graph_upload", C.c_int, [C.c_uint32, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
@@ -115,7 +120,6 @@ _SIGS = [
 
 # entry points beyond the header's operator set (tuning and learned picker)
 _EXTRA_SIGS = [
-    ("vs_expand_plan_set_tuning", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int]),
     ("vs_expand_plan_set_picker", C.c_int, [C.c_void_p, C.c_void_p]),
 ]
 
@@ -148,6 +152,10 @@ def check(rc: int) -> int:
 
 def init(device: int = 0) -> None:
     check(lib().vs_init(device))
+
+
+def kernel_launches() -> int:
+    return int(lib().vs_kernel_launches())
 
 
 def _ptr(a) -> C.c_void_p:
@@ -362,8 +370,9 @@ class ExpandPlan:
         self.S = S
         self.params = params
 
-    def set_tuning(self, sparse_frac=-1.0, push_frac=-1.0, collect_stats=False):
-        check(lib().vs_expand_plan_set_tuning(self.h, sparse_frac, push_frac, 1 if collect_stats else 0))
+    def set_tuning(self, sparse_frac=-1.0, push_frac=-1.0, collect_stats=False, timing=False):
+        check(lib().vs_expand_plan_set_tuning(self.h, sparse_frac, push_frac, 1 if collect_stats else 0,
+                                              1 if timing else 0))
 
     def run(self, sources, targets=None, distances=None, stream=None):
         check(lib().vs_expand_plan_run(self.h, _ptr(sources), _ptr(targets), _ptr(distances),
@@ -393,10 +402,15 @@ class ExpandPlan:
 
 def expand(graph: DeviceGraph, sources, k_min, k_max, path="any", direction="forward",
            strategy="auto", targets=None, stream=None, stats=False, **kw):
-    """One-shot VExpand. Returns (BitMatrix or None, distances or None, stats dict or None)."""
-    src = np.ascontiguousarray(sources, dtype=np.uint32)
+    """One-shot VExpand. Returns (BitMatrix or None, distances or None, stats dict or None).
+    sources: numpy array, or a torch tensor (host, pinned or device) of 32-bit ids."""
+    if hasattr(sources, "data_ptr"):
+        src = sources
+        S = int(sources.numel())
+    else:
+        src = np.ascontiguousarray(sources, dtype=np.uint32)
+        S = len(src)
     p = make_params(k_min, k_max, path, direction, strategy, **kw)
-    S = len(src)
     dist = None
     tg = None
     if p.path_type == PATH_FIND_SHORTEST:

@@ -8,6 +8,7 @@
 namespace vs {
 
 static thread_local std::string g_last_error;
+std::atomic<unsigned long long> g_launches{0};
 
 void set_error(const char *fmt, ...) {
   char buf[1024];
@@ -141,7 +142,7 @@ int popcount_words(const uint64_t *w, size_t n, uint64_t *count, cudaStream_t st
   VS_CK(cudaMemsetAsync(d, 0, sizeof(*d), st));
   if (n) {
     int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)sm_count() * 8);
-    popcount_kernel<<<blocks, 256, 0, st>>>(w, n, d);
+    { popcount_kernel<<<blocks, 256, 0, st>>>(w, n, d); vs::note_launch(); }
     VS_CK(cudaGetLastError());
   }
   unsigned long long h = 0;
@@ -242,9 +243,9 @@ int exclusive_scan_u64(const unsigned long long *in, unsigned long long *out, si
   VS_TRY(dalloc_n(&sums, nb ? nb : 1, st));
   VS_TRY(dalloc_n(&total, 1, st));
   if (n) {
-    k_scan_block<<<(unsigned)nb, 256, 0, st>>>(in, out, n, sums);
-    k_scan_sums<<<1, 1024, 0, st>>>(sums, nb, total);
-    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, sums, total);
+    { k_scan_block<<<(unsigned)nb, 256, 0, st>>>(in, out, n, sums); vs::note_launch(); }
+    { k_scan_sums<<<1, 1024, 0, st>>>(sums, nb, total); vs::note_launch(); }
+    { k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, sums, total); vs::note_launch(); }
   } else {
     VS_CK(cudaMemsetAsync(out, 0, sizeof(unsigned long long), st));
   }
@@ -263,6 +264,8 @@ extern "C" {
 const char *vs_last_error(void) { return g_last_error.c_str(); }
 
 const char *vs_version(void) { return "vertexsurge_gb300 0.1 sm_103a"; }
+
+uint64_t vs_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int vs_init(int device) {
   VS_CK(cudaSetDevice(device));
@@ -338,8 +341,8 @@ int vs_bitmat_upload(vs_bitmat *m, const uint64_t *logical_words, vs_stream_t st
                             cudaMemcpyDefault, st));
     if (m->rows % 64) {  // bits past the last row must stay zero
       const uint64_t mask = (1ull << (m->rows % 64)) - 1;
-      mask_last_word_kernel<<<std::max(1u, std::min((m->cols + 255) / 256, 4096u)), 256, 0, st>>>(
-          m->words, m->cols, m->wpc, (uint32_t)(lw - 1), mask);
+      { mask_last_word_kernel<<<std::max(1u, std::min((m->cols + 255) / 256, 4096u)), 256, 0, st>>>(
+          m->words, m->cols, m->wpc, (uint32_t)(lw - 1), mask); vs::note_launch(); }
       VS_CK(cudaGetLastError());
     }
   }

@@ -648,6 +648,9 @@ struct vs_expand_plan {
   // tuning knobs of the fixed planner
   double sparse_frac = 0.02, push_frac = 0.0;
   const float *picker = nullptr;
+  bool timing = false;
+  uint32_t timed_hops = 0;
+  cudaEvent_t ev[3 * (VS_MAX_HOPS + 1)] = {};
 };
 
 namespace vs {
@@ -660,6 +663,8 @@ int plan_free(vs_expand_plan *pl) {
                   pl->d_tgt, pl->d_dist, pl->ctr, pl->hubs};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  for (cudaEvent_t e : pl->ev)
+    if (e) cudaEventDestroy(e);
   delete pl;
   return VS_OK;
 }
@@ -751,7 +756,7 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
       return rc;
     }
     cudaMemsetAsync(dn, 0, sizeof(unsigned), st);
-    k_hubs<<<sm_count() * 4, 256, 0, st>>>(in, V, pl->hub_threshold, pl->hubs, dn);
+    { k_hubs<<<sm_count() * 4, 256, 0, st>>>(in, V, pl->hub_threshold, pl->hubs, dn); vs::note_launch(); }
     unsigned hn = 0;
     cudaMemcpyAsync(&hn, dn, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
     e = cudaStreamSynchronize(st);
@@ -793,8 +798,8 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   if (pl->d_tgt) VS_TRY(copy_in(pl->d_tgt, targets, S_, st));
   // run start: clean frontier buffers, zero visited/accumulator/counters
   for (int b = 0; b < 2; b++)
-    k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[b]), pl->flag[b],
-                                                V, Q, pl->ctr, 0, 0);
+    { k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[b]), pl->flag[b],
+                                                V, Q, pl->ctr, 0, 0); vs::note_launch(); }
   if (pl->vis) VS_CK(cudaMemsetAsync(pl->vis, 0, rowbytes, st));
   if (pl->acc) VS_CK(cudaMemsetAsync(pl->acc, 0, rowbytes, st));
   VS_CK(cudaMemsetAsync(pl->ctr, 0, sizeof(Ctr), st));
@@ -815,7 +820,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   sa.out = outl;
   sa.ctr = pl->ctr;
   sa.V = V;
-  k_seed<<<std::max(1u, std::min((S_ + 255) / 256, (uint32_t)sm_count() * 4)), 256, 0, st>>>(sa);
+  { k_seed<<<std::max(1u, std::min((S_ + 255) / 256, (uint32_t)sm_count() * 4)), 256, 0, st>>>(sa); vs::note_launch(); }
   VS_CK(cudaGetLastError());
   // layer 0 pair count
   {
@@ -824,8 +829,8 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     VS_CK(cudaMemcpyAsync(&pl->ctr->hop[0].new_bits, &s64, sizeof(s64), cudaMemcpyHostToDevice, st));
   }
   if (p.path_type == VS_PATH_FIND_SHORTEST)
-    k_dist_init<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(pl->d_src, pl->d_tgt,
-                                                                              pl->d_dist, S_, V, pl->ctr);
+    { k_dist_init<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(pl->d_src, pl->d_tgt,
+                                                                              pl->d_dist, S_, V, pl->ctr); vs::note_launch(); }
   const PullVariant &var = pick_variant(pl->qslice);
   const int forced = p.strategy == VS_STRAT_PULL ? ST_PULL
                      : p.strategy == VS_STRAT_PUSH ? ST_PUSH
@@ -849,11 +854,12 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     da.W = W;
     da.k_min = p.k_min;
     da.k_max = p.k_max;
-    k_decide<<<1, 32, 0, st>>>(da);
+    if (pl->timing) cudaEventRecord(pl->ev[3 * h], st);
+    { k_decide<<<1, 32, 0, st>>>(da); vs::note_launch(); }
     if (pl->collect_stats)
-      k_active_edges<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], outl, V, pl->ctr, h);
-    k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[nbuf]),
-                                                pl->flag[nbuf], V, Q, pl->ctr, h, 1);
+      { k_active_edges<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], outl, V, pl->ctr, h); vs::note_launch(); }
+    { k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[nbuf]),
+                                                pl->flag[nbuf], V, Q, pl->ctr, h, 1); vs::note_launch(); }
     const bool acc_on = pl->use_acc && h >= p.k_min && h <= p.k_max;
     SparseArgs sp;
     sp.ctr = pl->ctr;
@@ -869,7 +875,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     sp.flagN = pl->flag[nbuf];
     sp.shortest = pl->use_vis;
     sp.acc_on = acc_on;
-    k_sparse<<<pl->grid_sparse, 256, 0, st>>>(sp);
+    { k_sparse<<<pl->grid_sparse, 256, 0, st>>>(sp); vs::note_launch(); }
     PushArgs pa;
     pa.ctr = pl->ctr;
     pa.h = h;
@@ -884,10 +890,10 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     pa.W = W;
     pa.shortest = pl->use_vis;
     pa.acc_on = acc_on;
-    k_push_reset<<<1, 1, 0, st>>>(pl->ctr);
-    k_push_compact<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], V, pl->push_list, pl->ctr, h);
-    k_push<<<pl->grid_push, 256, 0, st>>>(pa);
-    k_push_epilogue<<<pl->grid_push, 256, 0, st>>>(pa);
+    { k_push_reset<<<1, 1, 0, st>>>(pl->ctr); vs::note_launch(); }
+    { k_push_compact<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], V, pl->push_list, pl->ctr, h); vs::note_launch(); }
+    { k_push<<<pl->grid_push, 256, 0, st>>>(pa); vs::note_launch(); }
+    { k_push_epilogue<<<pl->grid_push, 256, 0, st>>>(pa); vs::note_launch(); }
     PullArgs a;
     a.in = in;
     a.F = reinterpret_cast<const uint4 *>(pl->buf[fb]);
@@ -907,17 +913,20 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.nhubs = pl->nhubs;
     a.ctr = pl->ctr;
     a.h = h;
-    var.pull<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a);
+    if (pl->timing) cudaEventRecord(pl->ev[3 * h + 1], st);
+    { var.pull<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a); vs::note_launch(); }
     if (pl->nhubs)
-      var.hub<<<dim3(pl->grid_hub, pl->nslices), 512, 16 * 32 * 16 * var.UPL, st>>>(a);
+      { var.hub<<<dim3(pl->grid_hub, pl->nslices), 512, 16 * 32 * 16 * var.UPL, st>>>(a); vs::note_launch(); }
     if (p.path_type == VS_PATH_FIND_SHORTEST)
-      k_find_check<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(
-          pl->buf[nbuf], pl->d_tgt, pl->d_dist, S_, W, V, pl->ctr, h);
+      { k_find_check<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(
+          pl->buf[nbuf], pl->d_tgt, pl->d_dist, S_, W, V, pl->ctr, h); vs::note_launch(); }
+    if (pl->timing) cudaEventRecord(pl->ev[3 * h + 2], st);
     VS_CK(cudaGetLastError());
   }
+  pl->timed_hops = pl->timing ? p.k_max : 0;
   if (pl->clear_diag)
-    k_clear_diag<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(pl->vis, pl->d_src,
-                                                                                S_, W, V);
+    { k_clear_diag<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(pl->vis, pl->d_src,
+                                                                                S_, W, V); vs::note_launch(); }
   if (p.path_type == VS_PATH_FIND_SHORTEST)
     VS_TRY(copy_in(distances, (const int32_t *)pl->d_dist, S_, st));
   VS_CK(cudaGetLastError());
@@ -964,16 +973,26 @@ int vs_expand_plan_stats(vs_expand_plan *pl, vs_expand_stats *stats, vs_stream_t
     stats->strategy[i] = h.hop[i].strategy;
     if (i >= 1 && i <= h.hops_run) vc += h.hop[i].new_bits;
   }
+  for (uint32_t i = 1; i <= pl->timed_hops && i <= VS_MAX_HOPS; i++) {
+    float a = 0, b = 0;
+    if (cudaEventElapsedTime(&a, pl->ev[3 * i], pl->ev[3 * i + 2]) == cudaSuccess) stats->hop_ms[i] = a;
+    if (cudaEventElapsedTime(&b, pl->ev[3 * i + 1], pl->ev[3 * i + 2]) == cudaSuccess) stats->pull_ms[i] = b;
+  }
   stats->visit_count = pl->use_vis ? vc : 0;
   return VS_OK;
 }
 
 int vs_expand_plan_set_tuning(vs_expand_plan *pl, double sparse_frac, double push_frac,
-                              int collect_stats) {
+                              int collect_stats, int timing) {
   if (!pl) return fail(VS_ERR_ARG, "null plan");
   if (sparse_frac >= 0) pl->sparse_frac = sparse_frac;
   if (push_frac >= 0) pl->push_frac = push_frac;
   pl->collect_stats = collect_stats != 0;
+  if (timing && !pl->timing) {
+    for (cudaEvent_t &e : pl->ev)
+      if (!e) VS_CK(cudaEventCreate(&e));
+  }
+  pl->timing = timing != 0;
   return VS_OK;
 }
 

@@ -271,7 +271,7 @@ int prepare_flat_dep(Scratch &sc, const vs_flat *f, uint32_t ucol, uint32_t nvco
   unsigned *dmx;
   VS_TRY(sc.get(&dmx, 1));
   VS_CK(cudaMemsetAsync(dmx, 0, 4, st));
-  if (n) k_max_u<<<grid_for(n), 256, 0, st>>>(u, n, dmx);
+  if (n) { k_max_u<<<grid_for(n), 256, 0, st>>>(u, n, dmx); vs::note_launch(); }
   unsigned mx = 0;
   VS_CK(cudaMemcpyAsync(&mx, dmx, 4, cudaMemcpyDeviceToHost, st));
   VS_CK(cudaStreamSynchronize(st));
@@ -290,9 +290,9 @@ int prepare_flat_dep(Scratch &sc, const vs_flat *f, uint32_t ucol, uint32_t nvco
   VS_TRY(sc.get(&adj, n));
   VS_CK(cudaMemsetAsync(cnt, 0, 8 * (n_u + 1), st));
   VS_CK(cudaMemsetAsync(cur, 0, 8 * (n_u + 1), st));
-  if (n) k_flat_dedup<<<grid_for(n), 256, 0, st>>>(d->pairs, u, nv, n, cnt, isnew);
+  if (n) { k_flat_dedup<<<grid_for(n), 256, 0, st>>>(d->pairs, u, nv, n, cnt, isnew); vs::note_launch(); }
   VS_TRY(exclusive_scan_u64(cnt, off, n_u, st));
-  if (n) k_flat_scatter<<<grid_for(n), 256, 0, st>>>(u, nv, n, isnew, off, cur, adj);
+  if (n) { k_flat_scatter<<<grid_for(n), 256, 0, st>>>(u, nv, n, isnew, off, cur, adj); vs::note_launch(); }
   // offsets are read as int64 by the kernel
   d->off = reinterpret_cast<const int64_t *>(off);
   d->adj = adj;
@@ -358,7 +358,7 @@ int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
       D.has_cmap = m->col_map != nullptr;
       if (D.has_cmap) {
         VS_TRY(hash_alloc(sc, m->cols, &D.cmap));
-        if (m->cols) k_build_cols<<<grid_for(m->cols), 256, 0, st>>>(D.cmap, m->col_map, m->cols);
+        if (m->cols) { k_build_cols<<<grid_for(m->cols), 256, 0, st>>>(D.cmap, m->col_map, m->cols); vs::note_launch(); }
       }
     } else if (d.graph) {
       const vs_graph *g = d.graph;
@@ -386,7 +386,7 @@ int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
   a.total = d_total;
   a.emit = 0;
   const int grid = grid_for(a.nbase * 32);
-  if (a.nbase) k_isect<<<grid, 256, 0, st>>>(a);
+  if (a.nbase) { k_isect<<<grid, 256, 0, st>>>(a); vs::note_launch(); }
   VS_CK(cudaGetLastError());
   unsigned long long total = 0;
   VS_CK(cudaMemcpyAsync(&total, d_total, 8, cudaMemcpyDeviceToHost, st));
@@ -411,7 +411,7 @@ int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
   a.toff = toff;
   a.max_rows = rows;
   a.emit = 1;
-  if (a.nbase && rows) k_isect<<<grid, 256, 0, st>>>(a);
+  if (a.nbase && rows) { k_isect<<<grid, 256, 0, st>>>(a); vs::note_launch(); }
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {

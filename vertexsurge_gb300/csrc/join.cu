@@ -275,15 +275,15 @@ int join_flat_flat(FlatSide a, FlatSide b, bool only_count, uint64_t max_rows, v
   uint32_t *slot_of = nullptr;
   if (!only_count) VS_TRY(sc.get(&slot_of, bd.f->nrows));
   if (bd.f->nrows)
-    k_build<<<grid_for(bd.f->nrows), 256, 0, st>>>(t, bd.f->cols[bd.key], bd.f->types[bd.key],
-                                                   bd.f->nrows, slot_of);
+    { k_build<<<grid_for(bd.f->nrows), 256, 0, st>>>(t, bd.f->cols[bd.key], bd.f->types[bd.key],
+                                                   bd.f->nrows, slot_of); vs::note_launch(); }
   unsigned long long *d_total;
   VS_TRY(sc.get(&d_total, 1));
   VS_CK(cudaMemsetAsync(d_total, 0, 8, st));
   if (only_count) {
     if (pr.f->nrows)
-      k_probe<<<grid_for(pr.f->nrows), 256, 0, st>>>(t, pr.f->cols[pr.key], pr.f->types[pr.key],
-                                                     pr.f->nrows, nullptr, nullptr, d_total);
+      { k_probe<<<grid_for(pr.f->nrows), 256, 0, st>>>(t, pr.f->cols[pr.key], pr.f->types[pr.key],
+                                                     pr.f->nrows, nullptr, nullptr, d_total); vs::note_launch(); }
     VS_CK(cudaGetLastError());
     return read_total(d_total, count, st);
   }
@@ -291,15 +291,15 @@ int join_flat_flat(FlatSide a, FlatSide b, bool only_count, uint64_t max_rows, v
   VS_TRY(exclusive_scan_u64(t.cnt, t.off, t.cap + 1, st));
   uint32_t *rows_by_key;
   VS_TRY(sc.get(&rows_by_key, bd.f->nrows));
-  if (bd.f->nrows) k_scatter<<<grid_for(bd.f->nrows), 256, 0, st>>>(t, slot_of, bd.f->nrows, rows_by_key);
+  if (bd.f->nrows) { k_scatter<<<grid_for(bd.f->nrows), 256, 0, st>>>(t, slot_of, bd.f->nrows, rows_by_key); vs::note_launch(); }
   unsigned long long *pcnt, *poff;
   uint32_t *pslot;
   VS_TRY(sc.get(&pcnt, pr.f->nrows));
   VS_TRY(sc.get(&poff, pr.f->nrows + 1));
   VS_TRY(sc.get(&pslot, pr.f->nrows));
   if (pr.f->nrows)
-    k_probe<<<grid_for(pr.f->nrows), 256, 0, st>>>(t, pr.f->cols[pr.key], pr.f->types[pr.key],
-                                                   pr.f->nrows, pcnt, pslot, d_total);
+    { k_probe<<<grid_for(pr.f->nrows), 256, 0, st>>>(t, pr.f->cols[pr.key], pr.f->types[pr.key],
+                                                   pr.f->nrows, pcnt, pslot, d_total); vs::note_launch(); }
   VS_TRY(exclusive_scan_u64(pcnt, poff, pr.f->nrows, st));
   uint64_t total = 0;
   VS_TRY(read_total(d_total, &total, st));
@@ -335,7 +335,7 @@ int join_flat_flat(FlatSide a, FlatSide b, bool only_count, uint64_t max_rows, v
   ea.t = t;
   ea.n_probe = pr.f->nrows;
   ea.out_rows = rows;
-  if (rows) k_emit<<<(unsigned)((rows + EMIT_ROWS - 1) / EMIT_ROWS), 256, 0, st>>>(ea);
+  if (rows) { k_emit<<<(unsigned)((rows + EMIT_ROWS - 1) / EMIT_ROWS), 256, 0, st>>>(ea); vs::note_launch(); }
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
@@ -355,13 +355,13 @@ int count_flat_mat(FlatSide f, const vs_bitmat *m, uint64_t *count, cudaStream_t
   Table t;
   VS_TRY(table_alloc(sc, f.f->nrows, false, false, &t));
   if (f.f->nrows)
-    k_build<<<grid_for(f.f->nrows), 256, 0, st>>>(t, f.f->cols[f.key], VS_T_VID, f.f->nrows, nullptr);
+    { k_build<<<grid_for(f.f->nrows), 256, 0, st>>>(t, f.f->cols[f.key], VS_T_VID, f.f->nrows, nullptr); vs::note_launch(); }
   unsigned long long *d_total;
   VS_TRY(sc.get(&d_total, 1));
   VS_CK(cudaMemsetAsync(d_total, 0, 8, st));
   if (m->cols)
-    k_count_mat<<<grid_for((uint64_t)m->cols * 32), 256, 0, st>>>(t, m->words, m->cols, m->wpc,
-                                                                 m->col_map, d_total);
+    { k_count_mat<<<grid_for((uint64_t)m->cols * 32), 256, 0, st>>>(t, m->words, m->cols, m->wpc,
+                                                                 m->col_map, d_total); vs::note_launch(); }
   VS_CK(cudaGetLastError());
   return read_total(d_total, count, st);
 }
@@ -372,14 +372,14 @@ int count_mat_mat(const vs_bitmat *a, const vs_bitmat *b, uint64_t *count, cudaS
   const bool direct = !a->col_map && !b->col_map;
   if (!direct) {
     VS_TRY(table_alloc(sc, a->cols, true, false, &t));
-    if (a->cols) k_build_cols<<<grid_for(a->cols), 256, 0, st>>>(t, a->col_map, a->cols);
+    if (a->cols) { k_build_cols<<<grid_for(a->cols), 256, 0, st>>>(t, a->col_map, a->cols); vs::note_launch(); }
   }
   unsigned long long *d_total;
   VS_TRY(sc.get(&d_total, 1));
   VS_CK(cudaMemsetAsync(d_total, 0, 8, st));
   if (b->cols)
-    k_count_mat_mat<<<grid_for((uint64_t)b->cols * 32), 256, 0, st>>>(
-        t, a->words, a->cols, a->wpc, b->words, b->cols, b->wpc, b->col_map, direct ? 1 : 0, d_total);
+    { k_count_mat_mat<<<grid_for((uint64_t)b->cols * 32), 256, 0, st>>>(
+        t, a->words, a->cols, a->wpc, b->words, b->cols, b->wpc, b->col_map, direct ? 1 : 0, d_total); vs::note_launch(); }
   VS_CK(cudaGetLastError());
   return read_total(d_total, count, st);
 }

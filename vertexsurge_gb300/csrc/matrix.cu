@@ -106,7 +106,7 @@ int validate_ids(const uint32_t *d_ids, uint32_t n, uint32_t bound, cudaStream_t
   unsigned *bad;
   VS_TRY(dalloc_n(&bad, 1, st));
   VS_CK(cudaMemsetAsync(bad, 0, sizeof(unsigned), st));
-  if (n) mx::k_count_invalid<<<std::max(1u, std::min((n + 255) / 256, 4096u)), 256, 0, st>>>(d_ids, n, bound, bad);
+  if (n) { mx::k_count_invalid<<<std::max(1u, std::min((n + 255) / 256, 4096u)), 256, 0, st>>>(d_ids, n, bound, bad); vs::note_launch(); }
   unsigned h = 0;
   VS_CK(cudaMemcpyAsync(&h, bad, sizeof(h), cudaMemcpyDeviceToHost, st));
   dfree(bad, st);
@@ -130,8 +130,8 @@ int bitmat_to_flat(const vs_bitmat *m, cudaStream_t st, vs_flat **out) {
   cudaMemsetAsync(cur, 0, sizeof(*cur), st);
   if (total && m->cols) {
     int blocks = std::max(1, std::min((int)((m->cols + 7) / 8), sm_count() * 8));
-    mx::k_to_flat<<<blocks, 256, 0, st>>>(m->words, m->rows, m->cols, m->wpc, m->row_map, m->col_map,
-                                          (uint32_t *)f->cols[0], (uint32_t *)f->cols[1], cur, total);
+    { mx::k_to_flat<<<blocks, 256, 0, st>>>(m->words, m->rows, m->cols, m->wpc, m->row_map, m->col_map,
+                                          (uint32_t *)f->cols[0], (uint32_t *)f->cols[1], cur, total); vs::note_launch(); }
   }
   dfree(cur, st);
   cudaError_t e = cudaGetLastError();
@@ -173,8 +173,8 @@ int vs_matrix_select(const vs_bitmat *m, const uint32_t *targets, uint32_t T, vs
       return fail(VS_ERR_ARG, "MatrixTableSelect target outside [0, %u)", m->cols);
     }
     int blocks = std::max(1, std::min((int)((T + 7) / 8), sm_count() * 8));
-    mx::k_select<<<blocks, 256, 0, st>>>(reinterpret_cast<const uint4 *>(m->words),
-                                         reinterpret_cast<uint4 *>(r->words), r->col_map, T, m->wpc / 2);
+    { mx::k_select<<<blocks, 256, 0, st>>>(reinterpret_cast<const uint4 *>(m->words),
+                                         reinterpret_cast<uint4 *>(r->words), r->col_map, T, m->wpc / 2); vs::note_launch(); }
   }
   if (m->row_map) {
     if ((rc = dalloc_n(&r->row_map, m->rows, st)) != VS_OK) {
@@ -206,8 +206,8 @@ int vs_table_convert(const vs_bitmat *m, int transpose, vs_bitmat **out, vs_stre
     const uint32_t tiles_r = (m->rows + 63) / 64, tiles_c = (m->cols + 63) / 64;
     uint64_t tiles = (uint64_t)tiles_r * tiles_c;
     int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((tiles + 7) / 8, (uint64_t)sm_count() * 16));
-    mx::k_transpose<<<blocks, 256, 0, st>>>(m->words, r->words, m->rows, m->cols, m->wpc, r->wpc,
-                                            tiles_r, tiles_c);
+    { mx::k_transpose<<<blocks, 256, 0, st>>>(m->words, r->words, m->rows, m->cols, m->wpc, r->wpc,
+                                            tiles_r, tiles_c); vs::note_launch(); }
   }
   const uint32_t *rm = transpose ? m->col_map : m->row_map;
   const uint32_t *cm = transpose ? m->row_map : m->col_map;

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <string>
@@ -10,6 +11,10 @@
 #include "../../include/vertexsurge_gb300.h"
 
 namespace vs {
+
+// Kernels launched by this library since load (vs_kernel_launches).
+extern std::atomic<unsigned long long> g_launches;
+inline void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_error(const char *fmt, ...);
 int fail(int code, const char *fmt, ...);

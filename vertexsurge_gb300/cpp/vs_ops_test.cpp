@@ -1,0 +1,339 @@
+// Operator-level tests through the C++ operator API on the GPU, restating the
+// reference's own unit tests:
+//   HashJoin{FlatFlat,FlatMat,MatFlat,MatMat}[CountOnly] == 18   (join.cpp:451-920)
+//   Mintersect{FlatFlatFlat,FlatMatMat} == 3                     (mintersect.cpp:347-511)
+//   TableConvertVRtoCM / _T exactness                            (big_operators2.cpp:215-296)
+// and plan shapes of the query drivers (e1-self-ring, p3-tri3-1, p4-exp4-1)
+// on a small generated graph, checked against host-side breadth-first search.
+// Exit status 0 = every test passed.
+#include <cstdio>
+#include <cstdlib>
+#include <functional>
+#include <map>
+#include <queue>
+#include <random>
+#include <set>
+#include <vector>
+
+#include "../cpp/vs_operators.hh"
+
+using namespace vsgb;
+using std::make_shared;
+using std::shared_ptr;
+using std::vector;
+
+static int g_fail = 0, g_pass = 0;
+#define EXPECT_EQ(a, b)                                                                    \
+  do {                                                                                     \
+    auto _a = (a);                                                                         \
+    auto _b = (b);                                                                         \
+    if (!(_a == _b)) {                                                                     \
+      std::fprintf(stderr, "  %s:%d: %s != %s (%lld vs %lld)\n", __FILE__, __LINE__, #a, #b, \
+                   (long long)_a, (long long)_b);                                          \
+      ok = false;                                                                          \
+    }                                                                                      \
+  } while (0)
+
+static void run_test(const char *name, const std::function<bool()> &f) {
+  bool ok = false;
+  try {
+    ok = f();
+  } catch (const std::exception &e) {
+    std::fprintf(stderr, "  exception: %s\n", e.what());
+    ok = false;
+  }
+  std::printf("[%s] %s\n", ok ? "PASS" : "FAIL", name);
+  (ok ? g_pass : g_fail)++;
+}
+
+static const vector<uint64_t> A8 = {1, 2, 3, 4, 5, 6, 7, 8};
+static const vector<uint64_t> K8 = {1, 1, 1, 2, 2, 3, 3, 4};
+
+static shared_ptr<BigOperator> inlined_flat(TableSchema s, vector<vector<uint64_t>> cols) {
+  auto d = make_shared<InlinedData>();
+  d->results_schema = s;
+  auto t = make_shared<FlatTable>(s);
+  t->set_columns(cols);
+  d->results = t;
+  return d;
+}
+
+// ColMain (rows x cols): set(row_vals[i], k_map[keys[i]]), col_map = distinct keys
+// (extra columns get keys that match nothing).
+static shared_ptr<BigOperator> inlined_colmain(TableSchema s, size_t rows, size_t cols,
+                                               const vector<uint64_t> &row_vals,
+                                               const vector<uint64_t> &keys) {
+  std::map<uint64_t, size_t> k_map;
+  vector<uint32_t> k_mapv;
+  for (auto k : keys)
+    if (!k_map.count(k)) {
+      k_map[k] = k_map.size();
+      k_mapv.push_back((uint32_t)k);
+    }
+  for (size_t i = k_mapv.size(); i < cols; i++) k_mapv.push_back(1000 + (uint32_t)i);
+  const size_t wpc = (rows + 63) / 64;
+  vector<uint64_t> w(wpc * cols, 0);
+  for (size_t i = 0; i < row_vals.size(); i++) {
+    size_t r = row_vals[i], c = k_map[keys[i]];
+    w[c * wpc + r / 64] |= 1ull << (r % 64);
+  }
+  vs_bitmat *m = nullptr;
+  check(vs_bitmat_create((uint32_t)rows, (uint32_t)cols, VS_KIND_COLMAIN, nullptr, &m));
+  check(vs_bitmat_upload(m, w.data(), nullptr));
+  check(vs_bitmat_set_maps(m, nullptr, k_mapv.data(), nullptr));
+  auto d = make_shared<InlinedData>();
+  d->results_schema = s;
+  auto t = make_shared<ColMainMatrixTable>(s);
+  t->set_matrix(m);
+  d->results = t;
+  return d;
+}
+
+static bool join_case(bool a_mat, bool b_mat, size_t ncols_b, bool only_count, Type key_type) {
+  bool ok = true;
+  auto op = make_shared<HashJoin>("k", only_count);
+  if (a_mat)
+    op->addDependency(inlined_colmain({{{"a", Type::VID}, {"k", Type::VID}}}, 10, 4, A8, K8));
+  else
+    op->addDependency(inlined_flat({{{"a", Type::VID}, {"k", key_type}}}, {A8, K8}));
+  if (b_mat)
+    op->addDependency(inlined_colmain({{{"b", Type::VID}, {"k", Type::VID}}}, 10, ncols_b, A8, K8));
+  else
+    op->addDependency(inlined_flat({{{"b", Type::VID}, {"k", key_type}}}, {A8, K8}));
+  op->finishAddingDependency();
+  op->run();
+  if (only_count) {
+    EXPECT_EQ(op->results->tuple_count(), (size_t)1);
+    EXPECT_EQ(single_count(op->results.get()), (int64_t)18);
+  } else {
+    EXPECT_EQ(op->results->tuple_count(), (size_t)18);
+    EXPECT_EQ(op->results_schema.columns.size(), (size_t)3);
+    // every tuple joins equal keys: (a, k, b) with K8[a-1] == k == K8[b-1]
+    auto *f = op->results->down_to_flat_table();
+    auto ca = f->column(0), ck = f->column(1), cb = f->column(2);
+    std::multiset<std::tuple<uint64_t, uint64_t, uint64_t>> got, exp;
+    for (size_t i = 0; i < ca.size(); i++) got.insert({ca[i], ck[i], cb[i]});
+    for (size_t i = 0; i < 8; i++)
+      for (size_t j = 0; j < 8; j++)
+        if (K8[i] == K8[j]) exp.insert({A8[i], K8[i], A8[j]});
+    EXPECT_EQ(got == exp, true);
+  }
+  return ok;
+}
+
+static bool mintersect_case(bool mats, bool only_count) {
+  bool ok = true;
+  auto op = make_shared<Mintersect>("c", "Person", only_count);
+  op->addDependency(inlined_flat({{{"a", Type::VID}, {"b", Type::VID}}}, {A8, K8}));
+  if (!mats) {
+    op->addDependency(inlined_flat({{{"a", Type::VID}, {"c", Type::VID}}}, {A8, K8}));
+    op->addDependency(inlined_flat({{{"b", Type::VID}, {"c", Type::VID}}}, {A8, K8}));
+  } else {
+    op->addDependency(inlined_colmain({{{"c", Type::VID}, {"a", Type::VID}}}, 10, 10, K8, A8));
+    op->addDependency(inlined_colmain({{{"c", Type::VID}, {"b", Type::VID}}}, 10, 10, K8, A8));
+  }
+  op->finishAddingDependency();
+  op->run();
+  if (only_count)
+    EXPECT_EQ(single_count(op->results.get()), (int64_t)3);
+  else
+    EXPECT_EQ(op->results->tuple_count(), (size_t)3);
+  return ok;
+}
+
+static bool table_convert_case(bool transpose) {
+  bool ok = true;
+  std::mt19937 gen(123);
+  const size_t rows = 1000, cols = 10000, wpc = (rows + 63) / 64;
+  vector<uint64_t> w(wpc * cols);
+  for (auto &x : w) x = ((uint64_t)gen() << 32) | gen();
+  for (size_t c = 0; c < cols; c++) w[c * wpc + wpc - 1] &= (1ull << (rows % 64)) - 1;
+  vs_bitmat *m = nullptr;
+  check(vs_bitmat_create(rows, cols, VS_KIND_VARROW, nullptr, &m));
+  check(vs_bitmat_upload(m, w.data(), nullptr));
+  auto d = make_shared<InlinedData>();
+  d->results_schema = {{{"b", Type::VID}, {"k", Type::VID}}};
+  auto t = make_shared<VarRowMatrixTable>(d->results_schema);
+  t->set_matrix(m);
+  d->results = t;
+  auto op = make_shared<TableConvert>(TableType::ColMainMatrix, transpose);
+  op->addLastDependency(d);
+  op->run();
+  auto *r = op->results->down_to_matrix_table();
+  auto rw = r->logical_words();
+  const size_t rwpc = ((transpose ? cols : rows) + 63) / 64;
+  size_t bad = 0;
+  for (size_t i = 0; i < rows; i++)
+    for (size_t j = 0; j < cols; j++) {
+      bool a = (w[j * wpc + i / 64] >> (i % 64)) & 1;
+      bool b = transpose ? (rw[i * rwpc + j / 64] >> (j % 64)) & 1 : (rw[j * rwpc + i / 64] >> (i % 64)) & 1;
+      bad += a != b;
+    }
+  EXPECT_EQ(bad, (size_t)0);
+  EXPECT_EQ(op->results_schema.columns[0].name == std::string(transpose ? "k" : "b"), true);
+  return ok;
+}
+
+// A small undirected graph (R-MAT style, generated here) and host BFS.
+struct HostGraph {
+  uint32_t V;
+  vector<int64_t> off;
+  vector<uint32_t> adj;
+};
+
+static HostGraph small_graph() {
+  std::mt19937_64 gen(7);
+  const uint32_t V = 1500;
+  std::set<std::pair<uint32_t, uint32_t>> es;
+  for (int i = 0; i < 6000; i++) {
+    uint32_t u = gen() % V, v = (uint32_t)((gen() % V) * (gen() % 3 == 0 ? 1 : 0) + (gen() % 40));
+    v %= V;
+    if (u == v) continue;
+    es.insert({u, v});
+    es.insert({v, u});
+  }
+  HostGraph g{V, vector<int64_t>(V + 1, 0), {}};
+  for (auto [u, v] : es) g.off[u + 1]++;
+  for (uint32_t i = 0; i < V; i++) g.off[i + 1] += g.off[i];
+  for (auto [u, v] : es) g.adj.push_back(v);
+  return g;
+}
+
+static vector<int> bfs(const HostGraph &g, uint32_t s) {
+  vector<int> d(g.V, -1);
+  std::queue<uint32_t> q;
+  d[s] = 0;
+  q.push(s);
+  while (!q.empty()) {
+    uint32_t u = q.front();
+    q.pop();
+    for (int64_t j = g.off[u]; j < g.off[u + 1]; j++)
+      if (d[g.adj[j]] < 0) {
+        d[g.adj[j]] = d[u] + 1;
+        q.push(g.adj[j]);
+      }
+  }
+  return d;
+}
+
+static shared_ptr<BigOperator> ids(const std::string &name, const vector<uint64_t> &v) {
+  return inlined_flat({{{name, Type::VID}}}, {v});
+}
+
+static bool plans_case(const HostGraph &hg) {
+  bool ok = true;
+  vector<uint64_t> sa, sb, sc;
+  for (uint64_t i = 0; i < 120; i++) sa.push_back((i * 37) % hg.V);
+  for (uint64_t i = 0; i < 90; i++) sb.push_back((i * 53 + 5) % hg.V);
+  for (uint64_t i = 0; i < 100; i++) sc.push_back((i * 71 + 11) % hg.V);
+  auto A = ids("a.id", sa), B = ids("b.id", sb), Cn = ids("c.id", sc);
+  auto vexp = [&](shared_ptr<BigOperator> s, shared_ptr<BigOperator> t, std::string sn, std::string tn, size_t k0,
+                  size_t k1) {
+    auto ve = make_shared<VExpand>("Person", "Person", "knows", Direction::Both, k0, k1, ExpandPathType::Shortest,
+                                   ExpandStrategy::Dense, sn, tn);
+    ve->addLastDependency(s);
+    auto sel = make_shared<MatrixTableSelect>(tn);
+    sel->addDependency(ve);
+    sel->addLastDependency(t);
+    return sel;
+  };
+  vector<vector<int>> da, db;
+  for (auto s : sa) da.push_back(bfs(hg, (uint32_t)s));
+  for (auto s : sb) db.push_back(bfs(hg, (uint32_t)s));
+  auto within = [](int d, int k0, int k1) { return d >= k0 && d <= k1; };
+  // e1-self-ring: Count(Select(VExpand(a, [0,3]), targets = a))
+  {
+    auto B2 = ids("b.id", sa);
+    auto cnt = make_shared<Count>();
+    cnt->addLastDependency(vexp(A, B2, "a.id", "b.id", 0, 3));
+    cnt->run();
+    int64_t exp = 0;
+    for (size_t i = 0; i < sa.size(); i++)
+      for (size_t j = 0; j < sa.size(); j++) exp += within(da[i][sa[j]], 0, 3);
+    EXPECT_EQ(single_count(cnt->results.get()), exp);
+  }
+  // p3-tri3-1: Mintersect(p12, T(p13), T(p23)) with hops [1,2]
+  {
+    auto p12 = vexp(A, B, "a.id", "b.id", 1, 2), p13 = vexp(A, Cn, "a.id", "c.id", 1, 2),
+         p23 = vexp(B, Cn, "b.id", "c.id", 1, 2);
+    auto t13 = make_shared<TableConvert>(TableType::ColMainMatrix, true);
+    t13->addLastDependency(p13);
+    auto t23 = make_shared<TableConvert>(TableType::ColMainMatrix, true);
+    t23->addLastDependency(p23);
+    auto mi = make_shared<Mintersect>("c.id", "Person", true);
+    mi->addDependency(p12);
+    mi->addDependency(t13);
+    mi->addLastDependency(t23);
+    mi->run();
+    int64_t exp = 0;
+    for (size_t i = 0; i < sa.size(); i++)
+      for (size_t j = 0; j < sb.size(); j++) {
+        if (!within(da[i][sb[j]], 1, 2)) continue;
+        for (size_t k = 0; k < sc.size(); k++) exp += within(da[i][sc[k]], 1, 2) && within(db[j][sc[k]], 1, 2);
+      }
+    EXPECT_EQ(single_count(mi->results.get()), exp);
+  }
+  // p4-exp4-1 first join: HashJoin("b.id") over ColMain(p12) and ColMain^T(p23)
+  {
+    auto p12 = vexp(A, B, "a.id", "b.id", 1, 2), p23 = vexp(B, Cn, "b.id", "c.id", 1, 2);
+    auto c12 = make_shared<TableConvert>(TableType::ColMainMatrix, false);
+    c12->addLastDependency(p12);
+    auto c23 = make_shared<TableConvert>(TableType::ColMainMatrix, true);
+    c23->addLastDependency(p23);
+    for (bool oc : {true, false}) {
+      auto j = make_shared<HashJoin>("b.id", oc);
+      j->addDependency(c12);
+      j->addLastDependency(c23);
+      j->run();
+      int64_t exp = 0;
+      for (size_t i = 0; i < sa.size(); i++)
+        for (size_t jj = 0; jj < sb.size(); jj++) {
+          if (!within(da[i][sb[jj]], 1, 2)) continue;
+          for (size_t k = 0; k < sc.size(); k++) exp += within(db[jj][sc[k]], 1, 2);
+        }
+      if (oc)
+        EXPECT_EQ(single_count(j->results.get()), exp);
+      else
+        EXPECT_EQ((int64_t)j->results->tuple_count(), exp);
+    }
+  }
+  // FindShortest over (start, target) pairs
+  {
+    vector<uint64_t> tg;
+    for (size_t i = 0; i < sa.size(); i++) tg.push_back(sb[i % sb.size()]);
+    auto data = inlined_flat({{{"a.id", Type::VID}, {"b.id", Type::VID}}}, {sa, tg});
+    auto fs = make_shared<VExpand>("Person", "Person", "knows", Direction::Both, VExpandPathParameters::FindShortest(),
+                                   ExpandStrategy::Dense, "a.id", "b.id");
+    fs->addLastDependency(data);
+    fs->run();
+    auto dist = fs->results->down_to_flat_table()->column(2);
+    size_t bad = 0;
+    for (size_t i = 0; i < sa.size(); i++) bad += (int64_t)dist[i] != (int64_t)da[i][tg[i]];
+    EXPECT_EQ(bad, (size_t)0);
+  }
+  return ok;
+}
+
+int main() {
+  check(vs_init(0));
+  for (bool oc : {false, true}) {
+    std::string s = oc ? "CountOnly" : "";
+    run_test(("HashJoinFlatFlat" + s).c_str(), [=] { return join_case(false, false, 0, oc, Type::Int64); });
+    run_test(("HashJoinFlatMat" + s).c_str(), [=] { return join_case(false, true, 4, oc, Type::VID); });
+    run_test(("HashJoinMatFlat" + s).c_str(), [=] { return join_case(false, true, 10, oc, Type::VID); });
+    run_test(("HashJoinMatMat" + s).c_str(), [=] { return join_case(true, true, 4, oc, Type::VID); });
+    run_test(("MintersectFlatFlatFlat" + s).c_str(), [=] { return mintersect_case(false, oc); });
+    run_test(("MintersectFlatMatMat" + s).c_str(), [=] { return mintersect_case(true, oc); });
+  }
+  run_test("TableConvertVRtoCM", [] { return table_convert_case(false); });
+  run_test("TableConvertVRtoCM_T", [] { return table_convert_case(true); });
+  HostGraph hg = small_graph();
+  Graph g;
+  g.add_vertex_type("Person", hg.V);
+  g.add_edge_type("Person", "knows", "Person", false, hg.V, hg.adj.size(), hg.off.data(), hg.adj.data(),
+                  hg.off.data(), hg.adj.data());
+  g.load();
+  run_test("PlanShapes(e1,p3-tri3-1,p4-exp4-1,FindShortest)", [&] { return plans_case(hg); });
+  std::printf("%d passed, %d failed\n", g_pass, g_fail);
+  return g_fail ? 1 : 0;
+}

@@ -82,10 +82,10 @@ __global__ void k_to_flat(const uint64_t *__restrict__ w, uint32_t rows, uint32_
         unsigned y = __shfl_up_sync(FULL, incl, o);
         if (lane >= o) incl += y;
       }
-      const unsigned total = __shfl_sync(FULL, incl, 31);
-      if (!total) continue;
+      const unsigned wtot = __shfl_sync(FULL, incl, 31);
+      if (!wtot) continue;
       unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(cursor, (unsigned long long)total);
+      if (lane == 0) base = atomicAdd(cursor, (unsigned long long)wtot);
       base = __shfl_sync(FULL, base, 0);
       unsigned long long pos = base + incl - n;
       while (x) {

@@ -237,6 +237,34 @@ int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
                   uint32_t new_vertex_count, int only_count, uint64_t max_rows, vs_flat **out,
                   uint64_t *count, vs_stream_t stream);
 
+/* ---- learned per-hop strategy picker (no counterpart in the reference; it
+ *      replaces the fixed Adaptive coverage thresholds of expand.cpp:346-414)
+ * A 32-64-64-3 ReLU network, bf16 weights, fp32 accumulation, trained with
+ * softmax cross-entropy and Adam by this library's own CUDA kernels.  Input:
+ * the 32 features the expand logs per hop (vs_expand_plan_features); output
+ * class 0 = PULL, 1 = PUSH, 2 = SPARSE.  Feature rows X are n x 32 floats,
+ * labels y are n int32 classes; pointers may be host or device memory. */
+typedef struct vs_picker vs_picker;
+int vs_picker_create(uint64_t seed, vs_picker **out);
+int vs_picker_free(vs_picker *p);
+int vs_picker_num_params(void);
+int vs_picker_set_params(vs_picker *p, const float *params);
+int vs_picker_get_params(const vs_picker *p, float *params);
+int vs_picker_forward(const vs_picker *p, const float *X, uint64_t n, float *logits, vs_stream_t stream);
+int vs_picker_backward(const vs_picker *p, const float *X, const int32_t *y, uint64_t n, float *grads,
+                       float *loss, vs_stream_t stream);
+int vs_picker_train(vs_picker *p, const float *X, const int32_t *y, uint64_t n, uint32_t epochs,
+                    uint32_t batch, float lr, uint64_t seed, float *final_loss, vs_stream_t stream);
+int vs_picker_predict(const vs_picker *p, const float *X, uint64_t n, int32_t *cls, vs_stream_t stream);
+/* Let a plan's AUTO hops be chosen by the picker (NULL restores the fixed planner). */
+int vs_expand_plan_set_picker(vs_expand_plan *plan, const vs_picker *p);
+/* Per-hop overrides: strategies[h] (h = 1..k_max) forces hop h; 0 = planner's choice. */
+int vs_expand_plan_set_hop_strategies(vs_expand_plan *plan, const int32_t *strategies, uint32_t n);
+/* Feature logging: when on, every run records the 32 features of each hop;
+ * vs_expand_plan_features copies (VS_MAX_HOPS + 1) x 32 floats (row h = hop h). */
+int vs_expand_plan_log_features(vs_expand_plan *plan, int on);
+int vs_expand_plan_features(vs_expand_plan *plan, float *features, vs_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,88 @@
+"""The learned strategy picker: CUDA forward/backward against the CPU
+restatement (oracle/mlp_ref.py), training on the GPU, inference inside the
+expand's decide kernel, per-hop overrides and feature logging."""
+import numpy as np
+import pytest
+
+from oracle import mlp_ref as M
+from oracle import pyoracle as O
+from tests import graphs as G
+from vertexsurge_gb300 import graphgen
+
+pytestmark = pytest.mark.gpu
+
+
+def test_forward_and_gradient_match_cpu(vs):
+    pk = vs.Picker(seed=3)
+    rng = np.random.default_rng(1)
+    p = rng.normal(0, 0.2, M.NPARAM).astype(np.float32)
+    pk.set_params(p)
+    assert np.array_equal(pk.params(), p)
+    X = rng.normal(0, 1, (300, M.NF)).astype(np.float32)
+    y = rng.integers(0, 3, 300).astype(np.int32)
+    z_gpu = pk.forward(X)
+    z_cpu, _ = M.forward(p, X)
+    assert np.allclose(z_gpu, z_cpu, rtol=1e-4, atol=1e-4)
+    g_gpu, loss_gpu = pk.backward(X, y)
+    loss_cpu, g_cpu = M.loss_and_grad(p, X, y)
+    assert abs(loss_gpu - loss_cpu) < 1e-4 * max(1.0, abs(loss_cpu))
+    # float32 sums in different orders: 1e-4 relative plus a small absolute floor
+    assert np.allclose(g_gpu, g_cpu, rtol=1e-3, atol=2e-6), np.abs(g_gpu - g_cpu).max()
+
+
+def test_training_learns_a_separable_rule(vs):
+    rng = np.random.default_rng(2)
+    X = rng.random((20000, M.NF)).astype(np.float32)
+    y = np.where(X[:, 0] > 0.6, 0, np.where(X[:, 1] > 0.5, 1, 2)).astype(np.int32)
+    pk = vs.Picker(seed=5)
+    _, l0 = pk.backward(X, y)
+    l1 = pk.train(X, y, epochs=25, batch=512, lr=3e-3)
+    assert l1 < l0 * 0.5
+    acc = (pk.predict(X) == y).mean()
+    assert acc > 0.9, acc
+
+
+def constant_picker(vs, cls):
+    p = np.zeros(M.NPARAM, dtype=np.float32)
+    off = M.NPARAM - 3
+    p[off + cls] = 10.0  # b3: always this class
+    pk = vs.Picker()
+    pk.set_params(p)
+    return pk
+
+
+@pytest.mark.parametrize("cls,strategy", [(0, 1), (1, 2), (2, 3)])
+def test_picker_drives_the_planner_and_results_stay_exact(vs, cls, strategy):
+    g = graphgen.rmat(12, 16, seed=4)
+    dg = vs.DeviceGraph.from_host(g)
+    src = graphgen.sample_sources(g.V, 300, seed=8)
+    for path in ("any", "shortest"):
+        plan = vs.ExpandPlan(dg, len(src), vs.make_params(1, 4, path, "forward", use_picker=True))
+        plan.set_picker(constant_picker(vs, cls))
+        plan.run(src)
+        st = plan.stats()
+        exp, _, _ = O.vexpand(g, src, 1, 4, path, "forward")
+        assert np.array_equal(plan.result().download(), exp)
+        got = st["strategy"][1:]
+        if strategy == 3:  # sparse runs while its pair list is valid, then falls back
+            assert got[0] == 3
+        else:
+            assert all(s == strategy for s in got), got
+
+
+def test_hop_overrides_and_feature_logging(vs):
+    g = graphgen.rmat(12, 16, seed=4)
+    dg = vs.DeviceGraph.from_host(g)
+    src = graphgen.sample_sources(g.V, 200, seed=9)
+    plan = vs.ExpandPlan(dg, len(src), vs.make_params(1, 4, "shortest", "forward"))
+    plan.set_hop_strategies([0, "sparse", "push", "pull", "push"])
+    plan.log_features(True)
+    plan.run(src)
+    st = plan.stats()
+    n = st["hops_run"]
+    assert n >= 3 and st["strategy"][1:] == [3, 2, 1, 2][:n]
+    exp, _, _ = O.vexpand(g, src, 1, 4, "shortest", "forward")
+    assert np.array_equal(plan.result().download(), exp)
+    f = plan.features()[1:n + 1]
+    assert np.all(np.isfinite(f)) and f.max() <= 4.0 and f.min() >= 0.0
+    assert np.allclose(f[:, 16:].sum(axis=1), 1.0, atol=1e-5)  # degree histogram normalised

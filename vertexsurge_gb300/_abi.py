@@ -118,10 +118,26 @@ _SIGS = [
                                 C.c_uint64, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_void_p]),
 ]
 
-# entry points beyond the header's operator set (tuning and learned picker)
-_EXTRA_SIGS = [
+_SIGS += [
+    ("vs_picker_create", C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
+    ("vs_picker_free", C.c_int, [C.c_void_p]),
+    ("vs_picker_num_params", C.c_int, []),
+    ("vs_picker_set_params", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("vs_picker_get_params", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("vs_picker_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
+    ("vs_picker_backward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
+                                     C.POINTER(C.c_float), C.c_void_p]),
+    ("vs_picker_train", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32,
+                                  C.c_float, C.c_uint64, C.POINTER(C.c_float), C.c_void_p]),
+    ("vs_picker_predict", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
     ("vs_expand_plan_set_picker", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("vs_expand_plan_set_hop_strategies", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    ("vs_expand_plan_log_features", C.c_int, [C.c_void_p, C.c_int]),
+    ("vs_expand_plan_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
 ]
+
+# internal entry points (not part of the header)
+_EXTRA_SIGS = []
 
 HEADER_SYMBOLS = [s[0] for s in _SIGS]
 
@@ -383,6 +399,28 @@ class ExpandPlan:
         check(lib().vs_expand_plan_result(self.h, C.byref(h)))
         return BitMatrix(h, owner=self)
 
+    def set_picker(self, picker):
+        check(lib().vs_expand_plan_set_picker(self.h, picker.h if picker is not None else None))
+        self._picker = picker
+
+    def set_hop_strategies(self, strategies):
+        """strategies[h] for h = 1..k_max ('auto'/'pull'/'push'/'sparse' or codes); None clears."""
+        if strategies is None:
+            check(lib().vs_expand_plan_set_hop_strategies(self.h, None, 0))
+            return
+        arr = np.zeros(len(strategies), dtype=np.int32)
+        for i, x in enumerate(strategies):
+            arr[i] = _STRATS[x] if isinstance(x, str) else int(x)
+        check(lib().vs_expand_plan_set_hop_strategies(self.h, _ptr(arr), len(arr)))
+
+    def log_features(self, on=True):
+        check(lib().vs_expand_plan_log_features(self.h, 1 if on else 0))
+
+    def features(self, stream=None) -> np.ndarray:
+        out = np.zeros((MAX_HOPS + 1, 32), dtype=np.float32)
+        check(lib().vs_expand_plan_features(self.h, _ptr(out), _stream(stream)))
+        return out
+
     def stats(self, stream=None) -> dict:
         s = ExpandStats()
         check(lib().vs_expand_plan_stats(self.h, C.byref(s), _stream(stream)))
@@ -470,3 +508,63 @@ def mintersect(base, deps, new_vertex_count=0, only_count=False, max_rows=1 << 6
     if not truncated:
         check(rc)
     return (FlatTable(out) if out.value else None), int(cnt.value), truncated
+
+
+class Picker:
+    """The learned per-hop strategy picker (vs_picker): 32-64-64-3 MLP,
+    bf16 weights, trained by the library's CUDA kernels."""
+
+    def __init__(self, seed: int = 1):
+        h = C.c_void_p()
+        check(lib().vs_picker_create(seed, C.byref(h)))
+        self.h = h
+        self.nparam = int(lib().vs_picker_num_params())
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.nparam, dtype=np.float32)
+        check(lib().vs_picker_get_params(self.h, _ptr(out)))
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.nparam
+        check(lib().vs_picker_set_params(self.h, _ptr(p)))
+
+    def forward(self, X: np.ndarray) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        out = np.zeros((X.shape[0], 3), dtype=np.float32)
+        check(lib().vs_picker_forward(self.h, _ptr(X), X.shape[0], _ptr(out), None))
+        return out
+
+    def backward(self, X: np.ndarray, y: np.ndarray):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.int32)
+        g = np.zeros(self.nparam, dtype=np.float32)
+        loss = C.c_float()
+        check(lib().vs_picker_backward(self.h, _ptr(X), _ptr(y), X.shape[0], _ptr(g), C.byref(loss), None))
+        return g, float(loss.value)
+
+    def train(self, X, y, epochs=30, batch=512, lr=3e-3, seed=7) -> float:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.int32)
+        loss = C.c_float()
+        check(lib().vs_picker_train(self.h, _ptr(X), _ptr(y), X.shape[0], epochs, batch, lr, seed,
+                                    C.byref(loss), None))
+        return float(loss.value)
+
+    def predict(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        out = np.zeros(X.shape[0], dtype=np.int32)
+        check(lib().vs_picker_predict(self.h, _ptr(X), X.shape[0], _ptr(out), None))
+        return out
+
+    def free(self):
+        if self.h:
+            lib().vs_picker_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

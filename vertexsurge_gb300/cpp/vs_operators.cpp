@@ -335,8 +335,14 @@ void HashJoin::run_internal() {
 }
 
 // ---- Mintersect -----------------------------------------------------------------
+// The vertex type is resolved against the loaded graph at construction, as
+// the reference does (mintersect.cpp:11).
 Mintersect::Mintersect(VariableName nv, TypeName t, bool only_count)
-    : new_vertex_var_name(std::move(nv)), new_vertex_type(std::move(t)), only_count(only_count) {}
+    : new_vertex_var_name(std::move(nv)), new_vertex_type(std::move(t)), only_count(only_count) {
+  if (!graph_store || !graph_store->vertex_count.count(new_vertex_type))
+    throw Error(VS_ERR_ARG, "vertex type " + new_vertex_type + " is not in the loaded graph");
+  new_vertex_count = graph_store->vertex_count.at(new_vertex_type);
+}
 
 // Mintersect::finishAddingDependency (mintersect.cpp:14-46)
 void Mintersect::finishAddingDependency() {
@@ -383,9 +389,7 @@ void Mintersect::run_internal() {
     }
     ds.push_back(d);
   }
-  const uint32_t nvc = graph_store && graph_store->vertex_count.count(new_vertex_type)
-                           ? (uint32_t)graph_store->vertex_count.at(new_vertex_type)
-                           : 0;
+  const uint32_t nvc = (uint32_t)new_vertex_count;
   vs_flat *out = nullptr;
   uint64_t count = 0;
   check(vs_mintersect(base, ds.data(), (uint32_t)ds.size(), nvc, only_count ? 1 : 0, max_rows,

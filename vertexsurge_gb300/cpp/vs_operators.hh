@@ -199,6 +199,7 @@ class Mintersect : public BigOperator {
   VariableName new_vertex_var_name;
   TypeName new_vertex_type;
   bool only_count;
+  size_t new_vertex_count = 0;
   void run_internal() override;
 
  public:

@@ -316,6 +316,13 @@ static bool plans_case(const HostGraph &hg) {
 
 int main() {
   check(vs_init(0));
+  // like the reference's tests, load a graph first: operators resolve vertex types against it
+  HostGraph hg = small_graph();
+  Graph g;
+  g.add_vertex_type("Person", hg.V);
+  g.add_edge_type("Person", "knows", "Person", false, hg.V, hg.adj.size(), hg.off.data(), hg.adj.data(),
+                  hg.off.data(), hg.adj.data());
+  g.load();
   for (bool oc : {false, true}) {
     std::string s = oc ? "CountOnly" : "";
     run_test(("HashJoinFlatFlat" + s).c_str(), [=] { return join_case(false, false, 0, oc, Type::Int64); });
@@ -327,12 +334,6 @@ int main() {
   }
   run_test("TableConvertVRtoCM", [] { return table_convert_case(false); });
   run_test("TableConvertVRtoCM_T", [] { return table_convert_case(true); });
-  HostGraph hg = small_graph();
-  Graph g;
-  g.add_vertex_type("Person", hg.V);
-  g.add_edge_type("Person", "knows", "Person", false, hg.V, hg.adj.size(), hg.off.data(), hg.adj.data(),
-                  hg.off.data(), hg.adj.data());
-  g.load();
   run_test("PlanShapes(e1,p3-tri3-1,p4-exp4-1,FindShortest)", [&] { return plans_case(hg); });
   std::printf("%d passed, %d failed\n", g_pass, g_fail);
   return g_fail ? 1 : 0;

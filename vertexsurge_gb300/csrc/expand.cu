@@ -33,19 +33,13 @@
 #include <vector>
 
 #include "expand_internal.cuh"
+#include "picker.cuh"
 #include "vs_internal.cuh"
 
 namespace vs {
 namespace ex {
 
 constexpr unsigned FULL = 0xffffffffu;
-
-// Placeholder until the learned picker is loaded: no opinion.
-__device__ int picker_choose(const DecideArgs &a, const HopCtr &prev) {
-  (void)a;
-  (void)prev;
-  return 0;
-}
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
@@ -135,54 +129,130 @@ __global__ void k_dist_init(const uint32_t *__restrict__ src, const uint32_t *__
   block_add(f, &ctr->found);
 }
 
-// One block: early-stop checks of hop h-1 (VExpand::after_child,
-// vexpand.cpp:222-284) and the strategy of hop h.
-__global__ void k_decide(DecideArgs a) {
-  if (threadIdx.x != 0) return;
+// One block of 64 threads: early-stop checks of hop h-1 (VExpand::after_child,
+// vexpand.cpp:222-284), the fixed planner's choice for hop h, and — when a
+// picker is loaded or features are logged — the feature vector of hop h and
+// the picker network's choice.
+__global__ void __launch_bounds__(64) k_decide(DecideArgs a) {
+  __shared__ float f[pk::NF], h1[pk::H1], h2[pk::H2], out[pk::NO];
+  __shared__ int s_run, s_choice, s_pairs_ok;
+  const int t = threadIdx.x;
   Ctr *c = a.ctr;
   HopCtr &prev = c->hop[a.h - 1];
   HopCtr &cur = c->hop[a.h];
-  if (!c->done && a.h >= 2) {
-    if (a.path != VS_PATH_ANY && prev.new_bits == 0) c->done = 1;
-    if (a.path == VS_PATH_FIND_SHORTEST && c->found >= a.S) c->done = 1;
-  }
-  if (c->done) {
-    cur.strategy = 0;
-    return;
-  }
-  c->hops_run = a.h;
-  const bool pairs_ok = (a.h == 1) || (prev.strategy == ST_SPARSE && !prev.overflow &&
-                                       prev.pairs <= a.pair_cap);
-  int s = a.forced;
-  if (s == ST_SPARSE && !pairs_ok) s = ST_PULL;
-  if (s == 0) {
-    // fixed planner: pair lists while their edge work is a small fraction of
-    // a dense pass, then push while few rows are active, then pull
-    const double E = (double)a.E;
-    const double pe = (double)prev.pair_edges;
-    if (pairs_ok && pe < E * a.sparse_frac)
-      s = ST_SPARSE;
-    else if ((double)prev.active_vertices < (double)a.V * a.push_frac && prev.strategy != 0)
-      s = ST_PUSH;
-    else
-      s = ST_PULL;
-    if (a.picker && a.picker_on) {
-      int p = picker_choose(a, prev);
-      if (p == ST_SPARSE && !pairs_ok) p = s;
-      if (p > 0) s = p;
+  if (t == 0) {
+    if (!c->done && a.h >= 2) {
+      if (a.path != VS_PATH_ANY && prev.new_bits == 0) c->done = 1;
+      if (a.path == VS_PATH_FIND_SHORTEST && c->found >= a.S) c->done = 1;
+    }
+    s_run = !c->done;
+    s_choice = 0;
+    s_pairs_ok = 0;
+    if (s_run) {
+      c->hops_run = a.h;
+      const bool pairs_ok = (a.h == 1) || (prev.strategy == ST_SPARSE && !prev.overflow &&
+                                           prev.pairs <= a.pair_cap);
+      s_pairs_ok = pairs_ok;
+      int s = a.forced;
+      if (s == ST_SPARSE && !pairs_ok) s = ST_PULL;
+      if (s == 0) {
+        // fixed planner: pair lists while their edge work is a small fraction
+        // of a dense pass, then push while few rows are active, then pull
+        const double pe = (double)prev.pair_edges;
+        if (pairs_ok && pe < (double)a.E * a.sparse_frac)
+          s = ST_SPARSE;
+        else if ((double)prev.active_vertices < (double)a.V * a.push_frac && prev.strategy != 0)
+          s = ST_PUSH;
+        else
+          s = ST_PULL;
+      }
+      s_choice = s;
     }
   }
-  cur.strategy = s;
+  __syncthreads();
+  if (!s_run) {
+    if (t == 0) cur.strategy = 0;
+    return;
+  }
+  const bool use_picker = a.picker && a.picker_on && a.forced == 0;
+  if (use_picker || a.log_features) {
+    if (t == 0) {
+      pk::HopFeatIn in;
+      in.S = a.S;
+      in.V = a.V;
+      in.E = (double)a.E;
+      in.W = a.W;
+      in.h = a.h;
+      in.k_min = a.k_min;
+      in.k_max = a.k_max;
+      in.new_bits_prev = (double)prev.new_bits;
+      in.active_prev = (double)prev.active_vertices;
+      double vis = 0;
+      for (int i = 0; i < a.h; i++) vis += (double)c->hop[i].new_bits;
+      in.visited_bits = vis;
+      in.active_edges = (double)cur.active_edges;
+      in.pair_edges = s_pairs_ok ? (double)prev.pair_edges : 0.0;
+      in.pairs_ok = s_pairs_ok;
+      in.shortest = a.path != VS_PATH_ANY;
+      in.both = a.both;
+      in.hist = cur.hist;
+      pk::hop_features(in, f);
+      if (a.log_features)
+        for (int i = 0; i < pk::NF; i++) c->feat[a.h][i] = f[i];
+    }
+    __syncthreads();
+    if (use_picker) {
+      const __nv_bfloat16 *w = (const __nv_bfloat16 *)a.picker;
+      {
+        float acc = __bfloat162float(w[pk::OFF_B1 + t]);
+        for (int i = 0; i < pk::NF; i++) acc += __bfloat162float(w[pk::OFF_W1 + t * pk::NF + i]) * f[i];
+        h1[t] = acc > 0.f ? acc : 0.f;
+      }
+      __syncthreads();
+      {
+        float acc = __bfloat162float(w[pk::OFF_B2 + t]);
+        for (int i = 0; i < pk::H1; i++) acc += __bfloat162float(w[pk::OFF_W2 + t * pk::H1 + i]) * h1[i];
+        h2[t] = acc > 0.f ? acc : 0.f;
+      }
+      __syncthreads();
+      if (t < pk::NO) {
+        float acc = __bfloat162float(w[pk::OFF_B3 + t]);
+        for (int i = 0; i < pk::H2; i++) acc += __bfloat162float(w[pk::OFF_W3 + t * pk::H2 + i]) * h2[i];
+        out[t] = acc;
+      }
+      __syncthreads();
+      if (t == 0) {
+        int best = -1;
+        for (int k = 0; k < pk::NO; k++) {
+          const int st = pk::class_to_strategy(k);
+          if (st == ST_SPARSE && !s_pairs_ok) continue;  // no pair list to expand from
+          if (best < 0 || out[k] > out[best]) best = k;
+        }
+        s_choice = pk::class_to_strategy(best);
+      }
+    }
+  }
+  if (t == 0) cur.strategy = s_choice;
 }
 
-// Exact E_active of hop h: out-degrees of the non-zero rows of layer h-1.
-__global__ void k_active_edges(const uint32_t *__restrict__ flagF, Lists out, uint32_t V, Ctr *ctr,
-                               int h) {
-  if (ctr->hop[h].strategy == 0) return;
+// Per-hop frontier statistics of layer h-1: E_active (out-degrees of its
+// non-zero rows) and the log2(out-degree + 1) histogram of those rows.
+__global__ void k_hop_stats(const uint32_t *__restrict__ flagF, Lists out, uint32_t V, Ctr *ctr, int h) {
+  if (ctr->done) return;
+  __shared__ unsigned long long hist[pk::NHIST];
+  if (threadIdx.x < pk::NHIST) hist[threadIdx.x] = 0;
+  __syncthreads();
   unsigned long long s = 0;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
-    if (flagF[v])
-      _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < out.n) s += (unsigned long long)(out.off[l][v + 1] - out.off[l][v]);
+    if (flagF[v]) {
+      unsigned long long d = 0;
+      _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < out.n) d += (unsigned long long)(out.off[l][v + 1] - out.off[l][v]);
+      s += d;
+      const int b = min(pk::NHIST - 1, 63 - __clzll((long long)(d + 1)));
+      atomicAdd(&hist[b], 1ull);
+    }
+  __syncthreads();
+  if (threadIdx.x < pk::NHIST && hist[threadIdx.x]) atomicAdd(&ctr->hop[h].hist[threadIdx.x], hist[threadIdx.x]);
   block_add(s, &ctr->hop[h].active_edges);
 }
 
@@ -647,7 +717,9 @@ struct vs_expand_plan {
   bool has_result = false;
   // tuning knobs of the fixed planner
   double sparse_frac = 0.02, push_frac = 0.0;
-  const float *picker = nullptr;
+  const void *picker = nullptr;
+  bool log_features = false;
+  int hop_forced[VS_MAX_HOPS + 1] = {};
   bool timing = false;
   uint32_t timed_hops = 0;
   cudaEvent_t ev[3 * (VS_MAX_HOPS + 1)] = {};
@@ -845,7 +917,9 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     da.S = S_;
     da.V = V;
     da.E = g->E;
-    da.forced = forced;
+    da.forced = pl->hop_forced[h] ? pl->hop_forced[h] : forced;
+    da.log_features = pl->log_features;
+    da.both = p.direction == VS_DIR_BOTH && g->directed;
     da.pair_cap = pl->pair_cap;
     da.sparse_frac = pl->sparse_frac;
     da.push_frac = pl->push_frac;
@@ -855,9 +929,10 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     da.k_min = p.k_min;
     da.k_max = p.k_max;
     if (pl->timing) cudaEventRecord(pl->ev[3 * h], st);
-    { k_decide<<<1, 32, 0, st>>>(da); vs::note_launch(); }
-    if (pl->collect_stats)
-      { k_active_edges<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], outl, V, pl->ctr, h); vs::note_launch(); }
+    if (pl->collect_stats || pl->log_features || (pl->picker && p.use_picker))
+      { k_hop_stats<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], outl, V, pl->ctr, h); vs::note_launch(); }
+    { k_decide<<<1, 64, 0, st>>>(da); vs::note_launch(); }
+
     { k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[nbuf]),
                                                 pl->flag[nbuf], V, Q, pl->ctr, h, 1); vs::note_launch(); }
     const bool acc_on = pl->use_acc && h >= p.k_min && h <= p.k_max;
@@ -996,9 +1071,34 @@ int vs_expand_plan_set_tuning(vs_expand_plan *pl, double sparse_frac, double pus
   return VS_OK;
 }
 
-int vs_expand_plan_set_picker(vs_expand_plan *pl, const float *device_weights) {
+int vs_expand_plan_set_picker(vs_expand_plan *pl, const vs_picker *p) {
   if (!pl) return fail(VS_ERR_ARG, "null plan");
-  pl->picker = device_weights;
+  pl->picker = p ? vs_picker_device_weights(p) : nullptr;
+  return VS_OK;
+}
+
+int vs_expand_plan_set_hop_strategies(vs_expand_plan *pl, const int32_t *strategies, uint32_t n) {
+  if (!pl) return fail(VS_ERR_ARG, "null plan");
+  for (int h = 0; h <= VS_MAX_HOPS; h++) pl->hop_forced[h] = 0;
+  for (uint32_t h = 1; strategies && h < n && h <= VS_MAX_HOPS; h++) {
+    const int s = strategies[h];
+    if (s < VS_STRAT_AUTO || s > VS_STRAT_SPARSE) return fail(VS_ERR_ARG, "unknown strategy %d", s);
+    pl->hop_forced[h] = s == VS_STRAT_PULL ? ST_PULL : s == VS_STRAT_PUSH ? ST_PUSH : s == VS_STRAT_SPARSE ? ST_SPARSE : 0;
+  }
+  return VS_OK;
+}
+
+int vs_expand_plan_log_features(vs_expand_plan *pl, int on) {
+  if (!pl) return fail(VS_ERR_ARG, "null plan");
+  pl->log_features = on != 0;
+  return VS_OK;
+}
+
+int vs_expand_plan_features(vs_expand_plan *pl, float *features, vs_stream_t stream) {
+  if (!pl || !features) return fail(VS_ERR_ARG, "null argument");
+  VS_CK(cudaMemcpyAsync(features, pl->ctr->feat, sizeof(float) * 32 * (VS_MAX_HOPS + 1), cudaMemcpyDefault,
+                        S(stream)));
+  VS_CK(cudaStreamSynchronize(S(stream)));
   return VS_OK;
 }
 

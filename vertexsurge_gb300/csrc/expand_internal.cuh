@@ -17,6 +17,7 @@ struct HopCtr {
   unsigned long long pairs;            // SPARSE: (vertex, source) pairs of layer h
   unsigned long long pair_edges;       // SPARSE: sum of out-degrees over those pairs
   unsigned long long work_edges;       // SPARSE: edges scanned by the hop
+  unsigned long long hist[16];         // log2(out-degree + 1) histogram of layer h-1's active rows
   int overflow;                        // SPARSE: pair list overflowed
   int strategy;                        // strategy run at hop h (0 = not run)
 };
@@ -29,6 +30,7 @@ struct Ctr {
   int multislice;            // PULL runs in several source slices
   unsigned push_active, push_touched;
   int error;  // a source or target id was >= V (the offending entry was skipped)
+  float feat[VS_MAX_HOPS + 1][32];  // picker features of every hop (when logged)
 };
 
 // Up to two adjacency lists (Direction::Both uses both CSRs).
@@ -51,11 +53,11 @@ struct SeedArgs {
 
 struct DecideArgs {
   Ctr *ctr;
-  int h, path, forced, picker_on;
+  int h, path, forced, picker_on, log_features, both;
   uint32_t S, V, W, k_min, k_max;
   uint64_t E, pair_cap;
   double sparse_frac, push_frac;
-  const float *picker;
+  const void *picker;  // bf16 weights of a vs_picker (NULL = fixed planner)
 };
 
 struct SparseArgs {
@@ -99,8 +101,6 @@ struct PullArgs {
   int h;
 };
 
-// Learned strategy picker evaluated inside the decide kernel (picker.cuh).
-__device__ int picker_choose(const DecideArgs &a, const HopCtr &prev);
 
 }  // namespace ex
 }  // namespace vs

@@ -91,6 +91,7 @@ int exclusive_scan_u64(const unsigned long long *in, unsigned long long *out, si
 int popcount_words(const uint64_t *w, size_t n, uint64_t *count, cudaStream_t st);
 int bitmat_to_flat(const vs_bitmat *m, cudaStream_t st, vs_flat **out);
 int validate_ids(const uint32_t *d_ids, uint32_t n, uint32_t bound, cudaStream_t st, bool *ok);
+extern "C" const void *vs_picker_device_weights(const vs_picker *p);
 int flat_alloc(uint32_t ncols, const int32_t *types, uint64_t nrows, cudaStream_t st, vs_flat **out);
 int bitmat_alloc(uint32_t rows, uint32_t cols, int kind, cudaStream_t st, vs_bitmat **out);
 

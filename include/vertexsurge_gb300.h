@@ -214,6 +214,26 @@ typedef struct vs_table_ref {
 int vs_hash_join(vs_table_ref a, vs_table_ref b, int only_count, uint64_t max_rows,
                  vs_flat **out, uint64_t *count, vs_stream_t stream);
 
+/* Count-only join of two key columns that allocates no memory (no counterpart
+ * in the reference).  For callers that cannot call cudaMalloc: an engine or
+ * serving loop that hands all device memory to its own allocator up front,
+ * where an allocation mid-query could fail under memory pressure, take the
+ * driver's allocation lock or synchronise the device and stall other work.
+ * keys_a / keys_b are device arrays of na / nb keys (VS_T_VID = uint32,
+ * VS_T_I64 = int64); *count (host or device memory) receives
+ * sum_k multiplicity_a(k) * multiplicity_b(k), the same number as
+ * vs_hash_join(only_count = 1) on tables holding these key columns.
+ * The hash table lives in a fixed device array of this library: 2^19 slots,
+ * 8 MiB per GPU, held from the first call on that GPU until process exit.
+ * The smaller side may have at most 262,144 rows; larger inputs are rejected
+ * with VS_ERR_CAPACITY before any work is queued.  The first call on a device
+ * looks up the array's device address (make it before any stream capture).
+ * Every call reuses the same array and clears the part it needs: calls whose
+ * work overlaps on the GPU (concurrent streams, or host threads sharing a
+ * device) race on it and must be serialised by the caller. */
+int vs_hash_join_count_noalloc(const void *keys_a, uint64_t na, const void *keys_b, uint64_t nb,
+                               int key_type, uint64_t *count, vs_stream_t stream);
+
 /* ---- multi-way intersection (replaces Mintersect,
  *      src/objects/operator/mintersect.cpp:14-345) ---------------------------
  * base: flat table or VarRow matrix (columns row value, column value).

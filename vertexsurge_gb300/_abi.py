@@ -116,6 +116,8 @@ _SIGS = [
                                C.POINTER(C.c_uint64), C.c_void_p]),
     ("vs_mintersect", C.c_int, [TableRef, C.POINTER(IsectDep), C.c_uint32, C.c_uint32, C.c_int,
                                 C.c_uint64, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_void_p]),
+    ("vs_hash_join_count_noalloc", C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_int,
+                                             C.c_void_p, C.c_void_p]),
 ]
 
 _SIGS += [

@@ -19,6 +19,7 @@
 // bits to pairs (TableConvert(Flat)) and run the flat join.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "dev_util.cuh"
 #include "hash.cuh"
@@ -387,6 +388,52 @@ int count_mat_mat(const vs_bitmat *a, const vs_bitmat *b, uint64_t *count, cudaS
 }  // namespace jn
 }  // namespace vs
 
+// ---------------------------------------------------------------------------
+// Allocation-free count-only join.  Its hash table lives in this file-scope
+// device array instead of allocated memory; every GPU that loads the library
+// holds the array until the process exits.
+namespace vs {
+namespace jn {
+
+constexpr uint64_t NOALLOC_SLOTS = 1ull << 19;              // hash slots (power of two)
+constexpr uint64_t NOALLOC_MAX_BUILD = NOALLOC_SLOTS / 2;   // load factor <= 1/2
+// keys [SLOTS + 1] | counts [SLOTS + 1] | total [1]   (8 MiB + 24 B)
+constexpr uint64_t NOALLOC_WORDS = 2 * (NOALLOC_SLOTS + 1) + 1;
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[NOALLOC_WORDS];
+
+// Device address of the array, looked up once per device with that device
+// current (host code may not use the symbol itself as a device pointer).
+int noalloc_scratch(unsigned long long **out) {
+  static std::mutex mu;
+  static unsigned long long *addr[128] = {};
+  int dev = 0;
+  VS_CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return fail(VS_ERR_UNSUPPORTED, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    VS_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    addr[dev] = static_cast<unsigned long long *>(p);
+  }
+  *out = addr[dev];
+  return VS_OK;
+}
+
+// The previous call's table is still in the array: reset the slots this
+// call uses (keys to empty, counts and the total to zero).
+__global__ void k_noalloc_clear(unsigned long long *keys, unsigned long long *cnt,
+                                unsigned long long *total, uint64_t cap) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= cap;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    keys[i] = EMPTY;
+    cnt[i] = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *total = 0;
+}
+
+}  // namespace jn
+}  // namespace vs
+
 using namespace vs;
 using namespace vs::jn;
 
@@ -426,6 +473,40 @@ int vs_hash_join(vs_table_ref a, vs_table_ref b, int only_count, uint64_t max_ro
   vs_flat_free(fa);
   vs_flat_free(fb);
   return rc;
+}
+
+
+// Count-only join without allocating (see the header): the smaller key column
+// is the build side; at most NOALLOC_MAX_BUILD rows.
+int vs_hash_join_count_noalloc(const void *keys_a, uint64_t na, const void *keys_b, uint64_t nb,
+                               int key_type, uint64_t *count, vs_stream_t stream) {
+  if (!count || (na && !keys_a) || (nb && !keys_b))
+    return fail(VS_ERR_ARG, "vs_hash_join_count_noalloc: null argument");
+  if (key_type != VS_T_VID && key_type != VS_T_I64)
+    return fail(VS_ERR_ARG, "vs_hash_join_count_noalloc: unknown key type %d", key_type);
+  const bool build_a = na < nb;
+  const void *bk = build_a ? keys_a : keys_b, *pk = build_a ? keys_b : keys_a;
+  const uint64_t nbld = build_a ? na : nb, nprb = build_a ? nb : na;
+  if (nbld > NOALLOC_MAX_BUILD)
+    return fail(VS_ERR_CAPACITY,
+                "vs_hash_join_count_noalloc: the smaller side has %llu rows; the fixed table holds at most "
+                "%llu (use vs_hash_join)",
+                (unsigned long long)nbld, (unsigned long long)NOALLOC_MAX_BUILD);
+  unsigned long long *base = nullptr;
+  VS_TRY(noalloc_scratch(&base));
+  cudaStream_t st = S(stream);
+  Table t{};
+  t.cap = ht_capacity(std::max<uint64_t>(nbld, 1));
+  t.keys = base;
+  t.cnt = base + (NOALLOC_SLOTS + 1);
+  unsigned long long *total = base + 2 * (NOALLOC_SLOTS + 1);
+  { k_noalloc_clear<<<grid_for(t.cap + 1), 256, 0, st>>>(t.keys, t.cnt, total, t.cap); vs::note_launch(); }
+  if (nbld) { k_build<<<grid_for(nbld), 256, 0, st>>>(t, bk, key_type, nbld, nullptr); vs::note_launch(); }
+  if (nprb) { k_probe<<<grid_for(nprb), 256, 0, st>>>(t, pk, key_type, nprb, nullptr, nullptr, total); vs::note_launch(); }
+  VS_CK(cudaGetLastError());
+  VS_CK(cudaMemcpyAsync(count, total, sizeof(unsigned long long), cudaMemcpyDefault, st));
+  VS_CK(cudaStreamSynchronize(st));
+  return VS_OK;
 }
 
 }  // extern "C"

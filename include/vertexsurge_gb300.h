@@ -280,6 +280,12 @@ int vs_picker_predict(const vs_picker *p, const float *X, uint64_t n, int32_t *c
 int vs_expand_plan_set_picker(vs_expand_plan *plan, const vs_picker *p);
 /* Per-hop overrides: strategies[h] (h = 1..k_max) forces hop h; 0 = planner's choice. */
 int vs_expand_plan_set_hop_strategies(vs_expand_plan *plan, const int32_t *strategies, uint32_t n);
+/* Batched queries: the plan's S rows hold the sources of several queries
+ * that share path type, direction and k_min; row i stops growing after hop
+ * row_kmax[i] (<= k_max), so each query's rows equal its result when run
+ * alone.  NULL removes the limits.  (No counterpart in the reference, which
+ * runs one VExpand per query.) */
+int vs_expand_plan_set_row_limits(vs_expand_plan *plan, const uint8_t *row_kmax, uint32_t n);
 /* Feature logging: when on, every run records the 32 features of each hop;
  * vs_expand_plan_features copies (VS_MAX_HOPS + 1) x 32 floats (row h = hop h). */
 int vs_expand_plan_log_features(vs_expand_plan *plan, int on);

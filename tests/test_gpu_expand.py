@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as O
+from tests.conftest import words_to_bool
 from tests import graphs as G
 from vertexsurge_gb300 import graphgen
 
@@ -155,3 +156,24 @@ def test_expand_rejects_out_of_range_ids(vs, graphs):
     with pytest.raises(vs.VsError):
         vs.expand(dg, np.array([1, 2], np.uint32), 1, 5, "find_shortest", "forward",
                   targets=np.array([3, g.V], np.uint32))
+
+
+@pytest.mark.parametrize("path", ["any", "shortest"])
+@pytest.mark.parametrize("strategy", ["auto", "pull", "push", "sparse"])
+def test_batched_queries_equal_solo_runs(vs, graphs, path, strategy):
+    """Queries packed into one plan (row ranges, per-row hop limits) give each
+    query exactly its solo result."""
+    g, dg = graphs["rmat11_skew"]
+    sizes, kmaxs = [70, 5, 130, 64, 33], [2, 5, 3, 1, 4]
+    srcs = [graphgen.sample_sources(g.V, n, seed=100 + i) for i, n in enumerate(sizes)]
+    allsrc = np.concatenate(srcs).astype(np.uint32)
+    limits = np.concatenate([np.full(n, k, np.uint8) for n, k in zip(sizes, kmaxs)])
+    plan = vs.ExpandPlan(dg, len(allsrc), vs.make_params(1, max(kmaxs), path, "forward", strategy=strategy))
+    plan.set_row_limits(limits)
+    plan.run(allsrc)
+    got = words_to_bool(plan.result().download(), len(allsrc))
+    r0 = 0
+    for src, k in zip(srcs, kmaxs):
+        exp, _, _ = O.vexpand(g, src, 1, k, path, "forward")
+        assert np.array_equal(got[r0:r0 + len(src)], words_to_bool(exp, len(src))), (k, path, strategy)
+        r0 += len(src)

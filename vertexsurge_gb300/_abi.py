@@ -135,6 +135,7 @@ _SIGS += [
     ("vs_expand_plan_set_picker", C.c_int, [C.c_void_p, C.c_void_p]),
     ("vs_expand_plan_set_hop_strategies", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     ("vs_expand_plan_log_features", C.c_int, [C.c_void_p, C.c_int]),
+    ("vs_expand_plan_set_row_limits", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     ("vs_expand_plan_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
 ]
 
@@ -414,6 +415,14 @@ class ExpandPlan:
         for i, x in enumerate(strategies):
             arr[i] = _STRATS[x] if isinstance(x, str) else int(x)
         check(lib().vs_expand_plan_set_hop_strategies(self.h, _ptr(arr), len(arr)))
+
+    def set_row_limits(self, row_kmax):
+        """Per-row last hop (batched queries); None removes the limits."""
+        if row_kmax is None:
+            check(lib().vs_expand_plan_set_row_limits(self.h, None, 0))
+            return
+        a = np.ascontiguousarray(row_kmax, dtype=np.uint8)
+        check(lib().vs_expand_plan_set_row_limits(self.h, _ptr(a), len(a)))
 
     def log_features(self, on=True):
         check(lib().vs_expand_plan_log_features(self.h, 1 if on else 0))

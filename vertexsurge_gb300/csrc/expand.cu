@@ -101,6 +101,7 @@ __global__ void k_seed(SeedArgs a) {
     if (v >= a.V) {  // reported as VS_ERR_ARG; the pair stays in range
       a.ctr->error = 1;
       a.pairs0[i] = make_uint2(0, i);
+      a.pdeg0[i] = 0;
       continue;
     }
     size_t idx = (size_t)v * a.W + (i >> 6);
@@ -110,7 +111,10 @@ __global__ void k_seed(SeedArgs a) {
     if (a.vis) atomicOr((unsigned long long *)&a.vis[idx], bit);
     if (a.acc) atomicOr((unsigned long long *)&a.acc[idx], bit);
     a.pairs0[i] = make_uint2(v, i);
-    _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.out.n) pe += (unsigned long long)(a.out.off[l][v + 1] - a.out.off[l][v]);
+    unsigned long long d = 0;
+    _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.out.n) d += (unsigned long long)(a.out.off[l][v + 1] - a.out.off[l][v]);
+    a.pdeg0[i] = d;
+    pe += d;
   }
   block_add(pe, &a.ctr->hop[0].pair_edges);
   block_add(nv, &a.ctr->hop[0].active_vertices);
@@ -259,69 +263,187 @@ __global__ void k_hop_stats(const uint32_t *__restrict__ flagF, Lists out, uint3
 // SPARSE: (vertex u, source i) pairs of layer h-1; every out-neighbour v gets
 // bit i.  Shortest dedups through the visited bit (atomicOr returns the old
 // word), Any through the next-layer bit.  New pairs form layer h's list.
+// The work is balanced over edges, not pairs: a prefix sum of the pairs'
+// out-degrees (k_pscan*) lays all their out-lists end to end, and each warp
+// takes fixed chunks of that edge range, so a pair on a 50k-degree hub is
+// spread over many warps instead of serialising one.
+constexpr int SPARSE_CHUNK = 256;  // edges per warp task
+
+__global__ void k_pscan1(const unsigned long long *__restrict__ pdeg, unsigned long long *__restrict__ doff,
+                         unsigned long long *__restrict__ bsum, const Ctr *ctr, int h, uint64_t cap) {
+  if (ctr->hop[h].strategy != ST_SPARSE) return;
+  const unsigned long long npr = ctr->hop[h - 1].pairs;
+  const uint64_t np = npr < cap ? npr : cap;
+  __shared__ unsigned long long wt[8];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  for (uint64_t b = blockIdx.x; b * 1024 < np; b += gridDim.x) {
+    const uint64_t base = b * 1024;
+    unsigned long long v[4], run = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const uint64_t i = base + (uint64_t)t * 4 + k;
+      v[k] = i < np ? pdeg[i] : 0ull;
+      run += v[k];
+    }
+    unsigned long long incl = run;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) wt[w] = incl;
+    __syncthreads();
+    unsigned long long pre = 0;
+    for (int k = 0; k < w; k++) pre += wt[k];
+    pre += incl - run;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const uint64_t i = base + (uint64_t)t * 4 + k;
+      if (i < np) doff[i] = pre;
+      pre += v[k];
+    }
+    if (t == 255) bsum[b] = pre;  // block total (pre ends at the block's inclusive sum)
+    __syncthreads();
+  }
+}
+
+__global__ void k_pscan2(unsigned long long *__restrict__ bsum, unsigned long long *__restrict__ doff,
+                         const Ctr *ctr, int h, uint64_t cap) {
+  if (ctr->hop[h].strategy != ST_SPARSE) return;
+  const unsigned long long npr = ctr->hop[h - 1].pairs;
+  const uint64_t np = npr < cap ? npr : cap;
+  const uint64_t nb = (np + 1023) / 1024;
+  __shared__ unsigned long long carry, wt[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) carry = 0;
+  __syncthreads();
+  for (uint64_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+    const uint64_t i = b0 + t;
+    const unsigned long long x = i < nb ? bsum[i] : 0ull;
+    unsigned long long xi = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(FULL, xi, o);
+      if (lane >= o) xi += y;
+    }
+    if (lane == 31) wt[w] = xi;
+    __syncthreads();
+    unsigned long long pre = carry;
+    for (int k = 0; k < w; k++) pre += wt[k];
+    if (i < nb) bsum[i] = pre + xi - x;
+    __syncthreads();
+    if (t == blockDim.x - 1) carry = pre + xi;
+    __syncthreads();
+  }
+  if (t == 0) doff[np] = carry;
+}
+
+__global__ void k_pscan3(unsigned long long *__restrict__ doff, const unsigned long long *__restrict__ bsum,
+                         const Ctr *ctr, int h, uint64_t cap) {
+  if (ctr->hop[h].strategy != ST_SPARSE) return;
+  const unsigned long long npr = ctr->hop[h - 1].pairs;
+  const uint64_t np = npr < cap ? npr : cap;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += (uint64_t)gridDim.x * blockDim.x)
+    doff[i] += bsum[i / 1024];
+}
+
+__device__ __forceinline__ unsigned long long out_degree(const Lists &L, uint32_t v) {
+  unsigned long long d = 0;
+  _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < L.n) d += (unsigned long long)(L.off[l][v + 1] - L.off[l][v]);
+  return d;
+}
+
 __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
   Ctr *c = a.ctr;
   if (c->hop[a.h].strategy != ST_SPARSE) return;
   const unsigned long long np_raw = c->hop[a.h - 1].pairs;
   const uint64_t np = np_raw < a.cap ? np_raw : a.cap;
+  const unsigned long long T = a.doff[np];
   const int lane = threadIdx.x & 31;
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-  unsigned long long nb = 0, nv = 0, pe = 0, work = 0;
-  for (uint64_t p = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < np;
-       p += warps) {
-    const uint2 pr = a.pin[p];
-    const uint32_t u = pr.x, i = pr.y;
-    const uint32_t wi = i >> 6;
-    const unsigned long long bit = 1ull << (i & 63);
-    _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.out.n) {
-      const int64_t beg = a.out.off[l][u], end = a.out.off[l][u + 1];
-      if (lane == 0) work += (unsigned long long)(end - beg);
-      for (int64_t j0 = beg; j0 < end; j0 += 32) {
-        const int64_t j = j0 + lane;
-        bool fresh = false;
-        uint32_t v = 0;
-        if (j < end) {
-          v = a.out.adj[l][j];
+  const uint64_t nchunks = (T + SPARSE_CHUNK - 1) / SPARSE_CHUNK;
+  unsigned long long nb = 0, nv = 0, pe = 0;
+  for (uint64_t ck = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ck < nchunks; ck += warps) {
+    const unsigned long long e0 = ck * SPARSE_CHUNK;
+    const unsigned long long e1 = min(e0 + SPARSE_CHUNK, T);
+    // pairs owning the chunk's first and last edge: largest p with doff[p] <= e
+    uint64_t plo = 0, phi = np;
+    {
+      uint64_t lo = 0, hi = np;
+      while (hi - lo > 1) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (a.doff[mid] <= e0) lo = mid; else hi = mid;
+      }
+      plo = lo;
+      hi = np;
+      while (hi - lo > 1) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (a.doff[mid] <= e1 - 1) lo = mid; else hi = mid;
+      }
+      phi = lo;
+    }
+    for (unsigned long long eb = e0; eb < e1; eb += 32) {
+      const unsigned long long e = eb + lane;
+      bool fresh = false;
+      uint32_t v = 0, i = 0;
+      if (e < e1) {
+        uint64_t lo = plo, hi = phi + 1;
+        while (hi - lo > 1) {
+          const uint64_t mid = (lo + hi) >> 1;
+          if (a.doff[mid] <= e) lo = mid; else hi = mid;
+        }
+        const uint2 pr = a.pin[lo];
+        const uint32_t u = pr.x;
+        i = pr.y;
+        const uint32_t wi = i >> 6;
+        const unsigned long long bit = 1ull << (i & 63);
+        if (!a.hmask || (__ldg(a.hmask + wi) & bit)) {
+          unsigned long long j = e - a.doff[lo];
+          const int64_t b0 = a.out.off[0][u], d0 = a.out.off[0][u + 1] - b0;
+          if ((int64_t)j < d0)
+            v = a.out.adj[0][b0 + j];
+          else
+            v = a.out.adj[1][a.out.off[1][u] + (int64_t)j - d0];
           const size_t idx = (size_t)v * a.W + wi;
           if (a.shortest) {
-            unsigned long long old = atomicOr(&a.vis[idx], bit);
+            const unsigned long long old = atomicOr(&a.vis[idx], bit);
             if (!(old & bit)) {
               atomicOr(&a.N[idx], bit);
               fresh = true;
             }
           } else {
-            unsigned long long old = atomicOr(&a.N[idx], bit);
+            const unsigned long long old = atomicOr(&a.N[idx], bit);
             fresh = !(old & bit);
           }
           if (fresh) {
             if (a.acc_on) atomicOr(&a.acc[idx], bit);
             if (atomicOr(&a.flagN[v], 1u) == 0) nv++;
             nb++;
-            _Pragma("unroll") for (int l2 = 0; l2 < 2; l2++) if (l2 < a.out.n)
-              pe += (unsigned long long)(a.out.off[l2][v + 1] - a.out.off[l2][v]);
           }
         }
-        // warp-aggregated append of the new pairs
-        const unsigned m = __ballot_sync(FULL, fresh);
-        if (m) {
-          unsigned long long base = 0;
-          if (lane == 0) base = atomicAdd(&c->hop[a.h].pairs, (unsigned long long)__popc(m));
-          base = __shfl_sync(FULL, base, 0);
-          if (fresh) {
-            unsigned long long slot = base + __popc(m & lanemask_lt());
-            if (slot < a.cap)
-              a.pout[slot] = make_uint2(v, i);
-            else
-              c->hop[a.h].overflow = 1;
+      }
+      // warp-aggregated append of the new pairs (with their out-degrees)
+      const unsigned m = __ballot_sync(FULL, fresh);
+      if (m) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(&c->hop[a.h].pairs, (unsigned long long)__popc(m));
+        base = __shfl_sync(FULL, base, 0);
+        if (fresh) {
+          const unsigned long long slot = base + __popc(m & lanemask_lt());
+          const unsigned long long d = out_degree(a.out, v);
+          pe += d;
+          if (slot < a.cap) {
+            a.pout[slot] = make_uint2(v, i);
+            a.pdeg_out[slot] = d;
+          } else {
+            c->hop[a.h].overflow = 1;
           }
         }
       }
     }
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) c->hop[a.h].work_edges = T;
   block_add(nb, &c->hop[a.h].new_bits);
   block_add(nv, &c->hop[a.h].active_vertices);
   block_add(pe, &c->hop[a.h].pair_edges);
-  block_add(work, &c->hop[a.h].work_edges);
 }
 
 // ---------------------------------------------------------------------------
@@ -393,6 +515,10 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, uint32_t v, con
       if (q < qn) {
         const size_t idx = (size_t)v * a.Q + q0 + q;
         uint4 x = acc[k];
+        if (a.hmask) {
+          const uint4 m = __ldg(a.hmask + q0 + q);
+          x = make_uint4(x.x & m.x, x.y & m.y, x.z & m.z, x.w & m.w);
+        }
         if (a.shortest && nz4(x)) {
           const uint4 vv = a.vis[idx];
           x = andnot4(x, vv);
@@ -567,13 +693,14 @@ __global__ void __launch_bounds__(256) k_push_epilogue(PushArgs a) {
     for (uint32_t w = lane; w < a.W; w += 32) {
       const size_t idx = (size_t)v * a.W + w;
       unsigned long long x = a.N[idx];
+      const unsigned long long x0 = x;
+      if (a.hmask) x &= a.hmask[w];
       if (a.shortest && x) {
         const unsigned long long vv = a.vis[idx];
-        const unsigned long long y = x & ~vv;
-        if (y != x) a.N[idx] = y;
-        if (y) a.vis[idx] = vv | y;
-        x = y;
+        x &= ~vv;
+        if (x) a.vis[idx] = vv | x;
       }
+      if (x != x0) a.N[idx] = x;
       if (x) {
         any = true;
         nb += __popcll(x);
@@ -703,6 +830,7 @@ struct vs_expand_plan {
   uint32_t *flag[2] = {nullptr, nullptr};
   uint64_t *vis = nullptr, *acc = nullptr;
   uint2 *pairs[2] = {nullptr, nullptr};
+  unsigned long long *pdeg[2] = {nullptr, nullptr}, *doff = nullptr, *bsum = nullptr;
   uint64_t pair_cap = 0;
   uint32_t *push_list = nullptr, *touched = nullptr;
   uint32_t *d_src = nullptr, *d_tgt = nullptr;
@@ -719,6 +847,8 @@ struct vs_expand_plan {
   double sparse_frac = 0.02, push_frac = 0.0;
   const void *picker = nullptr;
   bool log_features = false;
+  uint64_t *hmask = nullptr;  // (k_max + 1) x W words: rows allowed to grow at hop h
+  bool use_hmask = false;
   int hop_forced[VS_MAX_HOPS + 1] = {};
   bool timing = false;
   uint32_t timed_hops = 0;
@@ -730,7 +860,7 @@ namespace ex {
 
 int plan_free(vs_expand_plan *pl) {
   if (!pl) return VS_OK;
-  void *ptrs[] = {pl->buf[0], pl->buf[1], pl->flag[0], pl->flag[1], pl->vis, pl->acc,
+  void *ptrs[] = {pl->pdeg[0], pl->pdeg[1], pl->doff, pl->bsum, pl->hmask, pl->buf[0], pl->buf[1], pl->flag[0], pl->flag[1], pl->vis, pl->acc,
                   pl->pairs[0], pl->pairs[1], pl->push_list, pl->touched, pl->d_src,
                   pl->d_tgt, pl->d_dist, pl->ctr, pl->hubs};
   for (void *p : ptrs)
@@ -801,6 +931,10 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   if (pl->use_acc) PL_ALLOC(pl->acc, rowwords);
   PL_ALLOC(pl->pairs[0], pl->pair_cap);
   PL_ALLOC(pl->pairs[1], pl->pair_cap);
+  PL_ALLOC(pl->pdeg[0], pl->pair_cap);
+  PL_ALLOC(pl->pdeg[1], pl->pair_cap);
+  PL_ALLOC(pl->doff, pl->pair_cap + 1);
+  PL_ALLOC(pl->bsum, (pl->pair_cap + 1023) / 1024 + 1);
   PL_ALLOC(pl->push_list, V);
   PL_ALLOC(pl->touched, V);
   PL_ALLOC(pl->d_src, S);
@@ -889,6 +1023,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   sa.vis = pl->vis;
   sa.acc = (pl->use_acc && p.k_min == 0) ? pl->acc : nullptr;
   sa.pairs0 = pl->pairs[0];
+  sa.pdeg0 = pl->pdeg[0];
   sa.out = outl;
   sa.ctr = pl->ctr;
   sa.V = V;
@@ -939,6 +1074,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     SparseArgs sp;
     sp.ctr = pl->ctr;
     sp.h = h;
+    sp.hmask = pl->use_hmask ? reinterpret_cast<const unsigned long long *>(pl->hmask + (size_t)h * W) : nullptr;
     sp.pin = pl->pairs[fb];
     sp.pout = pl->pairs[nbuf];
     sp.cap = pl->pair_cap;
@@ -950,10 +1086,16 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     sp.flagN = pl->flag[nbuf];
     sp.shortest = pl->use_vis;
     sp.acc_on = acc_on;
+    sp.doff = pl->doff;
+    sp.pdeg_out = pl->pdeg[nbuf];
+    { k_pscan1<<<pl->grid_v, 256, 0, st>>>(pl->pdeg[fb], pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
+    { k_pscan2<<<1, 1024, 0, st>>>(pl->bsum, pl->doff, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
+    { k_pscan3<<<pl->grid_v, 256, 0, st>>>(pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
     { k_sparse<<<pl->grid_sparse, 256, 0, st>>>(sp); vs::note_launch(); }
     PushArgs pa;
     pa.ctr = pl->ctr;
     pa.h = h;
+    pa.hmask = pl->use_hmask ? reinterpret_cast<const unsigned long long *>(pl->hmask + (size_t)h * W) : nullptr;
     pa.out = outl;
     pa.F = reinterpret_cast<const unsigned long long *>(pl->buf[fb]);
     pa.N = reinterpret_cast<unsigned long long *>(pl->buf[nbuf]);
@@ -970,6 +1112,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     { k_push<<<pl->grid_push, 256, 0, st>>>(pa); vs::note_launch(); }
     { k_push_epilogue<<<pl->grid_push, 256, 0, st>>>(pa); vs::note_launch(); }
     PullArgs a;
+    a.hmask = pl->use_hmask ? reinterpret_cast<const uint4 *>(pl->hmask + (size_t)h * W) : nullptr;
     a.in = in;
     a.F = reinterpret_cast<const uint4 *>(pl->buf[fb]);
     a.N = reinterpret_cast<uint4 *>(pl->buf[nbuf]);
@@ -1085,6 +1228,34 @@ int vs_expand_plan_set_hop_strategies(vs_expand_plan *pl, const int32_t *strateg
     if (s < VS_STRAT_AUTO || s > VS_STRAT_SPARSE) return fail(VS_ERR_ARG, "unknown strategy %d", s);
     pl->hop_forced[h] = s == VS_STRAT_PULL ? ST_PULL : s == VS_STRAT_PUSH ? ST_PUSH : s == VS_STRAT_SPARSE ? ST_SPARSE : 0;
   }
+  return VS_OK;
+}
+
+// Batched queries: row i of the plan belongs to a query whose hop range ends
+// at row_kmax[i] (<= the plan's k_max).  Rows stop growing after their own
+// last hop, so every query's rows equal the result of running it alone.
+int vs_expand_plan_set_row_limits(vs_expand_plan *pl, const uint8_t *row_kmax, uint32_t n) {
+  if (!pl) return fail(VS_ERR_ARG, "null plan");
+  if (!row_kmax) {
+    pl->use_hmask = false;
+    return VS_OK;
+  }
+  if (n != pl->S) return fail(VS_ERR_ARG, "row limits need one entry per source row (%u)", pl->S);
+  const uint32_t K = pl->p.k_max, W = pl->W;
+  std::vector<uint64_t> m((size_t)(K + 1) * W, 0);
+  bool all = true;
+  for (uint32_t i = 0; i < n; i++) {
+    if (row_kmax[i] > K) return fail(VS_ERR_ARG, "row %u hop limit %u exceeds k_max %u", i, row_kmax[i], K);
+    all &= row_kmax[i] == K;
+    for (uint32_t h = 1; h <= row_kmax[i]; h++) m[(size_t)h * W + i / 64] |= 1ull << (i % 64);
+  }
+  if (all) {
+    pl->use_hmask = false;
+    return VS_OK;
+  }
+  if (!pl->hmask) VS_TRY(dalloc_n(&pl->hmask, m.size(), 0));
+  VS_CK(cudaMemcpy(pl->hmask, m.data(), 8 * m.size(), cudaMemcpyHostToDevice));
+  pl->use_hmask = true;
   return VS_OK;
 }
 

@@ -47,6 +47,7 @@ struct SeedArgs {
   uint32_t *flag0;
   uint64_t *vis, *acc;
   uint2 *pairs0;
+  unsigned long long *pdeg0;  // out-degree of every seeded pair's vertex
   Lists out;
   Ctr *ctr;
 };
@@ -63,8 +64,11 @@ struct DecideArgs {
 struct SparseArgs {
   Ctr *ctr;
   int h;
+  const unsigned long long *hmask;  // rows that may still grow at hop h (NULL = all)
   const uint2 *pin;
   uint2 *pout;
+  const unsigned long long *doff;  // exclusive prefix of the input pairs' out-degrees (+ total)
+  unsigned long long *pdeg_out;    // out-degree of every output pair's vertex
   uint64_t cap;
   Lists out;
   uint32_t W;
@@ -76,6 +80,7 @@ struct SparseArgs {
 struct PushArgs {
   Ctr *ctr;
   int h;
+  const unsigned long long *hmask;
   Lists out;
   const unsigned long long *F;
   unsigned long long *N, *vis, *acc;
@@ -87,6 +92,7 @@ struct PushArgs {
 };
 
 struct PullArgs {
+  const uint4 *hmask;  // rows that may still grow at hop h, Q uint4 (NULL = all)
   Lists in;
   const uint4 *F;
   uint4 *N, *vis, *acc;

@@ -1,0 +1,183 @@
+"""Training data, training and evaluation of the learned per-hop strategy picker.
+
+Data comes from the method's own runs.  For every logged query the expand is
+run once per strategy family — every hop PULL, every hop PUSH, and SPARSE for
+as long as its pair list lasts — with per-hop CUDA-event timing and feature
+logging on.  All runs of a query see the same frontier at every hop (the
+strategy never changes a result), so each hop yields samples
+(features, fastest strategy):
+  * from the SPARSE run while SPARSE is still possible (features say a pair
+    list exists): label = fastest of PULL / PUSH / SPARSE at that hop;
+  * from the PULL run (features say no pair list): label = fastest of
+    PULL / PUSH.
+The network (vs_picker, CUDA training kernels) is trained on these samples.
+Evaluation on held-out queries compares, per hop, the time of the picker's
+choice with the exhaustive best and with the fixed planner's choice, using
+the logged times of the same hops.
+"""
+from __future__ import annotations
+
+import json
+import math
+import time
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+from . import _abi as vs
+from . import graphgen
+
+WEIGHTS_FILE = Path(__file__).resolve().parent / "picker_weights.npy"
+STRATS = (vs.STRAT_PULL, vs.STRAT_PUSH, vs.STRAT_SPARSE)  # class 0, 1, 2
+
+
+@dataclass
+class Samples:
+    X: list = field(default_factory=list)       # features (32,)
+    y: list = field(default_factory=list)       # fastest class
+    times: list = field(default_factory=list)   # (3,) ms per class, inf when unavailable
+    fixed: list = field(default_factory=list)   # class the fixed planner chose in the same context
+    query: list = field(default_factory=list)   # query index (for held-out splits)
+
+    def arrays(self):
+        return (np.asarray(self.X, np.float32), np.asarray(self.y, np.int32),
+                np.asarray(self.times, np.float64), np.asarray(self.fixed, np.int32),
+                np.asarray(self.query, np.int64))
+
+
+def graph_suite(scales=(16, 17, 18), skews=(0.45, 0.57, 0.65), zipf=((200_000, 4_000_000),)):
+    gs = []
+    for sc in scales:
+        for a in skews:
+            b = (1.0 - a - 0.05) / 2
+            gs.append(graphgen.rmat(sc, 16, a, b, b, seed=sc * 100 + int(a * 100)))
+    for V, E in zipf:
+        gs.append(graphgen.zipf(V, E, 2.1, min(50_000, V // 4), seed=V % 997))
+    return gs
+
+
+def _run(plan, src, forced, k_max):
+    plan.set_hop_strategies([0] + [forced] * k_max)
+    plan.run(src)
+    st = plan.stats()
+    return st, plan.features()
+
+
+def log_query(dg, g, S, k_max, path, direction, seed, out: Samples, qid: int, auto_plan_cache: dict):
+    src = graphgen.sample_sources(g.V, min(S, g.V), seed=seed)
+    key = (id(dg), len(src), k_max, path, direction)
+    plan = auto_plan_cache.get(key)
+    if plan is None:
+        plan = vs.ExpandPlan(dg, len(src), vs.make_params(1, k_max, path, direction))
+        plan.set_tuning(timing=True)
+        plan.log_features(True)
+        auto_plan_cache[key] = plan
+    runs = {}
+    for s in STRATS:
+        runs[s] = _run(plan, src, s, k_max)
+    st_auto, f_auto = _run(plan, src, vs.STRAT_AUTO, k_max)
+    hops = runs[vs.STRAT_PULL][0]["hops_run"]
+    for h in range(1, hops + 1):
+        t = {s: runs[s][0]["hop_ms"][h] if h <= runs[s][0]["hops_run"] else math.inf for s in STRATS}
+        sp_st = runs[vs.STRAT_SPARSE][0]
+        sparse_ok = h <= sp_st["hops_run"] and sp_st["strategy"][h] == vs.STRAT_SPARSE
+        fixed_class = STRATS.index(st_auto["strategy"][h]) if h <= st_auto["hops_run"] else 0
+        # context with a pair list: the SPARSE run's features
+        if sparse_ok:
+            times = [t[vs.STRAT_PULL], t[vs.STRAT_PUSH], t[vs.STRAT_SPARSE]]
+            out.X.append(runs[vs.STRAT_SPARSE][1][h])
+            out.y.append(int(np.argmin(times)))
+            out.times.append(times)
+            # the fixed planner's choice where it also had a pair list
+            fc = fixed_class if (h == 1 or st_auto["strategy"][h - 1] == vs.STRAT_SPARSE) else None
+            out.fixed.append(fc if fc is not None else int(np.argmin(times[:2])))
+            out.query.append(qid)
+        if h >= 2 or not sparse_ok:
+            times = [t[vs.STRAT_PULL], t[vs.STRAT_PUSH], math.inf]
+            out.X.append(runs[vs.STRAT_PULL][1][h])
+            out.y.append(int(np.argmin(times)))
+            out.times.append(times)
+            out.fixed.append(0 if fixed_class == 2 else fixed_class)
+            out.query.append(qid)
+
+
+def collect(n_queries: int, seed: int = 1, graphs=None, log=print) -> Samples:
+    rng = np.random.default_rng(seed)
+    graphs = graphs or graph_suite()
+    dgs = [vs.DeviceGraph.from_host(g) for g in graphs]
+    out = Samples()
+    cache: dict = {}
+    t0 = time.time()
+    for q in range(n_queries):
+        gi = int(rng.integers(len(graphs)))
+        S = int(round(math.exp(rng.uniform(math.log(64), math.log(8192)))))
+        S = max(1, min(S, graphs[gi].V))
+        k_max = int(rng.integers(2, 7))
+        path = "shortest" if rng.random() < 0.7 else "any"
+        direction = "forward" if rng.random() < 0.7 else "both"
+        if path == "any":
+            k_max = min(k_max, 4)
+        log_query(dgs[gi], graphs[gi], S, k_max, path, direction, int(rng.integers(1 << 30)), out, q, cache)
+        if log and (q + 1) % 200 == 0:
+            log(f"  {q + 1} queries, {len(out.y)} samples, {time.time() - t0:.0f}s")
+    return out
+
+
+def evaluate(pk, X, y, times, fixed):
+    """Per-hop times of the picker's, the fixed planner's and the best choices."""
+    pred = pk.predict(X)
+    # the picker never chooses an unavailable strategy (the decide kernel masks it)
+    avail = np.isfinite(times)
+    logits = pk.forward(X)
+    logits[~avail] = -np.inf
+    pred = logits.argmax(axis=1)
+    t_best = times.min(axis=1).sum()
+    t_pick = times[np.arange(len(pred)), pred].sum()
+    t_fix = times[np.arange(len(fixed)), fixed].sum()
+    return {"samples": int(len(y)), "accuracy": float((pred == y).mean()),
+            "fixed_accuracy": float((fixed == y).mean()),
+            "slowdown_vs_best": float(t_pick / t_best), "fixed_slowdown_vs_best": float(t_fix / t_best),
+            "speedup_vs_fixed": float(t_fix / t_pick)}
+
+
+def train_and_evaluate(samples: Samples, epochs=40, seed=3, holdout=0.2):
+    X, y, times, fixed, qid = samples.arrays()
+    rng = np.random.default_rng(seed)
+    queries = np.unique(qid)
+    test_q = set(rng.choice(queries, max(1, int(len(queries) * holdout)), replace=False).tolist())
+    te = np.array([q in test_q for q in qid])
+    pk = vs.Picker(seed=seed)
+    loss = pk.train(X[~te], y[~te], epochs=epochs, batch=512, lr=2e-3, seed=seed)
+    rep = evaluate(pk, X[te], y[te], times[te], fixed[te])
+    rep["train_loss"] = loss
+    rep["train_samples"] = int((~te).sum())
+    return pk, rep
+
+
+def main():
+    import argparse
+    ap = argparse.ArgumentParser(description="log, train and evaluate the strategy picker")
+    ap.add_argument("--queries", type=int, default=4000)
+    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--out", default=str(WEIGHTS_FILE))
+    ap.add_argument("--report", default="")
+    ap.add_argument("--scales", default="16,17,18")
+    args = ap.parse_args()
+    vs.init(0)
+    scales = tuple(int(x) for x in args.scales.split(","))
+    t0 = time.time()
+    samples = collect(args.queries, graphs=graph_suite(scales=scales))
+    t_log = time.time() - t0
+    pk, rep = train_and_evaluate(samples, epochs=args.epochs)
+    rep["logging_s"] = t_log
+    rep["queries"] = args.queries
+    rep["label_share"] = np.bincount(np.asarray(samples.y), minlength=3).tolist()
+    np.save(args.out, pk.params())
+    print(json.dumps(rep))
+    if args.report:
+        Path(args.report).write_text(json.dumps(rep, indent=1))
+
+
+if __name__ == "__main__":
+    main()

@@ -208,9 +208,18 @@ def run_gpu(args, w, rank, world, local_rank):
     dg = vs.DeviceGraph.from_host(g, stream=stream)
     ka, kb = w["hops_a"], w["hops_b"]
     Sa, Sb = len(sa), len(sb)
-    pA = vs.ExpandPlan(dg, Sa, vs.make_params(ka[0], ka[1], "shortest", "forward"))
-    pB = vs.ExpandPlan(dg, Sb, vs.make_params(kb[0], kb[1], "shortest", "forward"))
-    pP = vs.ExpandPlan(dg, Sa, vs.make_params(1, 1, "any", "forward"))
+    # autotuned PULL kernel shape, SPARSE threshold and hub bin per expand (untimed)
+    from vertexsurge_gb300 import autotune
+    t0 = time.time()
+    tA = autotune.tune(dg, sa, ka[0], ka[1], "shortest", "forward", stream=stream)
+    tB = autotune.tune(dg, sb, kb[0], kb[1], "shortest", "forward", stream=stream)
+    tP = autotune.tune(dg, sa, 1, 1, "any", "forward", stream=stream)
+    tuned = {k: {x: t[x] for x in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words", "ms")}
+             for k, t in (("A", tA), ("B", tB), ("P", tP))}
+    log(f"[rank {rank}] autotune {time.time() - t0:.1f}s: {tuned}")
+    pA = autotune.make_plan(dg, Sa, ka[0], ka[1], "shortest", "forward", tA)
+    pB = autotune.make_plan(dg, Sb, kb[0], kb[1], "shortest", "forward", tB)
+    pP = autotune.make_plan(dg, Sa, 1, 1, "any", "forward", tP)
     dA = torch.from_numpy(sa.view(np.int32)).to("cuda")
     dB = torch.from_numpy(sb.view(np.int32)).to("cuda")
     adj = [dict(graph=dg, direction="forward", base_col=0), dict(graph=dg, direction="forward", base_col=1)]
@@ -273,12 +282,12 @@ def run_gpu(args, w, rank, world, local_rank):
     hB = torch.from_numpy(sb.view(np.int32)).pin_memory()
 
     def step_e2e():
-        A, _, _ = vs.expand(dg, hA, ka[0], ka[1], "shortest", "forward", stream=stream)
-        B, _, _ = vs.expand(dg, hB, kb[0], kb[1], "shortest", "forward", stream=stream)
+        A, _, _ = vs.expand(dg, hA, ka[0], ka[1], "shortest", "forward", stream=stream, **autotune.params_kw(tA))
+        B, _, _ = vs.expand(dg, hB, kb[0], kb[1], "shortest", "forward", stream=stream, **autotune.params_kw(tB))
         _, jc2, _ = vs.hash_join(A, B, 1, 1, only_count=True, stream=stream)
         A.free()
         B.free()
-        P, _, _ = vs.expand(dg, hA, 1, 1, "any", "forward", stream=stream)
+        P, _, _ = vs.expand(dg, hA, 1, 1, "any", "forward", stream=stream, **autotune.params_kw(tP))
         _, tc2, _ = vs.mintersect(P, adj, g.V, only_count=True, stream=stream)
         P.free()
         return jc2, tc2
@@ -297,6 +306,41 @@ def run_gpu(args, w, rank, world, local_rank):
     e2e = {"value": world * src_edges * args.steps / (ms_e2e / 1e3) / 1e9, "unit": "Gsrc-edges/s",
            "h2d_bytes_per_step": int(4 * (2 * Sa + Sb)), "d2h_bytes_per_step": 16,
            "ms_per_step": ms_e2e / args.steps}
+
+    # learned picker: the same query with the trained network choosing each hop
+    learned = None
+    from vertexsurge_gb300 import picker_train
+    if picker_train.WEIGHTS_FILE.exists():
+        pk = vs.Picker()
+        pk.set_params(np.load(picker_train.WEIGHTS_FILE))
+        lp = [autotune.make_plan(dg, n, k0, k1, path, "forward", t, use_picker=True)
+              for n, (k0, k1), path, t in ((Sa, ka, "shortest", tA), (Sb, kb, "shortest", tB),
+                                           (Sa, (1, 1), "any", tP))]
+        for p in lp:
+            p.set_picker(pk)
+
+        def step_learned():
+            lp[0].run(dA, stream=stream)
+            lp[1].run(dB, stream=stream)
+            _, jc3, _ = vs.hash_join(lp[0].result(), lp[1].result(), 1, 1, only_count=True, stream=stream)
+            lp[2].run(dA, stream=stream)
+            _, tc3, _ = vs.mintersect(lp[2].result(), adj, g.V, only_count=True, stream=stream)
+            return jc3, tc3
+
+        for _ in range(max(1, min(args.warmup, 3))):
+            step_learned()
+        torch.cuda.synchronize()
+        l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0.record(stream)
+        for _ in range(args.steps):
+            jc3, tc3 = step_learned()
+        l1.record(stream)
+        torch.cuda.synchronize()
+        assert (jc3, tc3) == (jc, tc), "learned-picker results differ from the fixed planner"
+        ms_l = l0.elapsed_time(l1) / args.steps
+        learned = {"queries_per_s": 1000.0 / ms_l, "ms_per_step": ms_l,
+                   "value": world * src_edges / (ms_l / 1e3) / 1e9,
+                   "strategies_a": lp[0].stats(stream)["strategy"][1:]}
 
     if rank != 0:
         if dist:
@@ -320,7 +364,9 @@ def run_gpu(args, w, rank, world, local_rank):
                        "intersect": "triangle closing over out-lists, exact count",
                        "l2": "inputs larger than L2 (CSR 2.5 GB, 5.1 GB per bit matrix)",
                        "parallelism": f"replicas{world}"},
-            "queries_per_s": 1000.0 / ms_per_step,
+            "queries_per_s": {"plain": 1000.0 / ms_per_step,
+                              "learned": learned["queries_per_s"] if learned else None},
+            "learned_picker": learned, "autotune": tuned,
             "results": {"join_count": jc, "triangles": tc, "visited_a": stA["visit_count"],
                         "hops_run_a": stA["hops_run"], "strategies_a": stA["strategy"][1:],
                         "src_edges_per_step": src_edges},

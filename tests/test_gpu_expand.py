@@ -177,3 +177,19 @@ def test_batched_queries_equal_solo_runs(vs, graphs, path, strategy):
         exp, _, _ = O.vexpand(g, src, 1, k, path, "forward")
         assert np.array_equal(got[r0:r0 + len(src)], words_to_bool(exp, len(src))), (k, path, strategy)
         r0 += len(src)
+
+
+def test_autotuner_settings_keep_results(vs, graphs):
+    from vertexsurge_gb300 import autotune
+    g, dg = graphs["rmat11_skew"]
+    src = graphgen.sample_sources(g.V, 200, seed=12)
+    t = autotune.tune(dg, src, 1, 3, "shortest", "forward", repeats=1, pull_kinds=(0, 3),
+                      sparse_fracs=(0.001, 0.05), hub_thresholds=(0, 64))
+    assert len(t["table"]) == 8 and t["ms"] > 0
+    exp, _, _ = O.vexpand(g, src, 1, 3, "shortest", "forward")
+    for row in t["table"]:
+        plan = autotune.make_plan(dg, len(src), 1, 3, "shortest", "forward", row)
+        plan.run(src)
+        assert np.array_equal(plan.result().download(), exp), row
+        m, _, _ = vs.expand(dg, src, 1, 3, "shortest", "forward", **autotune.params_kw(row))
+        assert np.array_equal(m.download(), exp), row

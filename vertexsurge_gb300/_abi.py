@@ -37,7 +37,8 @@ class ExpandParams(C.Structure):
     _fields_ = [("k_min", C.c_uint32), ("k_max", C.c_uint32), ("path_type", C.c_int32),
                 ("direction", C.c_int32), ("strategy", C.c_int32), ("use_picker", C.c_int32),
                 ("hub_threshold", C.c_uint32), ("slice_words", C.c_uint32),
-                ("pair_capacity", C.c_uint64)]
+                ("pair_capacity", C.c_uint64), ("pull_kernel", C.c_int32), ("reserved", C.c_int32),
+                ("sparse_frac", C.c_double)]
 
 
 class ExpandStats(C.Structure):
@@ -136,6 +137,7 @@ _SIGS += [
     ("vs_expand_plan_set_hop_strategies", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     ("vs_expand_plan_log_features", C.c_int, [C.c_void_p, C.c_int]),
     ("vs_expand_plan_set_row_limits", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    ("vs_expand_plan_set_pull_kernel", C.c_int, [C.c_void_p, C.c_int]),
     ("vs_expand_plan_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
 ]
 
@@ -365,7 +367,7 @@ class FlatTable:
 
 
 def make_params(k_min, k_max, path="any", direction="forward", strategy="auto", use_picker=False,
-                hub_threshold=0, slice_words=0, pair_capacity=0) -> ExpandParams:
+                hub_threshold=0, slice_words=0, pair_capacity=0, pull_kernel=0, sparse_frac=0.0) -> ExpandParams:
     p = ExpandParams()
     p.k_min, p.k_max = int(k_min), int(k_max)
     p.path_type = _PATHS[path] if isinstance(path, str) else int(path)
@@ -375,6 +377,8 @@ def make_params(k_min, k_max, path="any", direction="forward", strategy="auto", 
     p.hub_threshold = int(hub_threshold)
     p.slice_words = int(slice_words)
     p.pair_capacity = int(pair_capacity)
+    p.pull_kernel = int(pull_kernel)
+    p.sparse_frac = float(sparse_frac)
     return p
 
 
@@ -415,6 +419,10 @@ class ExpandPlan:
         for i, x in enumerate(strategies):
             arr[i] = _STRATS[x] if isinstance(x, str) else int(x)
         check(lib().vs_expand_plan_set_hop_strategies(self.h, _ptr(arr), len(arr)))
+
+    def set_pull_kernel(self, kind: int):
+        """PULL kernel variant 0..3 (bit 0: 8 blocks/SM, bit 1: L2 cache policies)."""
+        check(lib().vs_expand_plan_set_pull_kernel(self.h, int(kind)))
 
     def set_row_limits(self, row_kmax):
         """Per-row last hop (batched queries); None removes the limits."""

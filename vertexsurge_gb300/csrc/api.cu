@@ -136,6 +136,55 @@ __global__ void mask_last_word_kernel(uint64_t *w, uint32_t cols, uint32_t wpc, 
     w[(size_t)c * wpc + last] &= mask;
 }
 
+// popcount of the columns whose colnz flag is set: a warp loads 32 flags at
+// once and walks only the flagged columns (16-byte loads).
+__global__ void popcount_cols_kernel(const uint4 *__restrict__ w, uint32_t cols, uint32_t q_per_col,
+                                     const uint32_t *__restrict__ colnz, unsigned long long *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  unsigned long long s = 0;
+  for (uint32_t c0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; c0 < cols; c0 += warps * 32) {
+    const uint32_t c = c0 + lane;
+    unsigned m = __ballot_sync(0xffffffffu, c < cols && colnz[c]);
+    while (m) {
+      const uint32_t cc = c0 + __ffs(m) - 1;
+      m &= m - 1;
+      for (uint32_t q = lane; q < q_per_col; q += 32) {
+        const uint4 x = __ldg(w + (size_t)cc * q_per_col + q);
+        s += __popc(x.x) + __popc(x.y) + __popc(x.z) + __popc(x.w);
+      }
+    }
+  }
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ unsigned long long part[32];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < blockDim.x / 32 ? part[threadIdx.x] : 0;
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0 && s) atomicAdd(out, s);
+  }
+}
+
+int bitmat_popcount(const vs_bitmat *m, uint64_t *count, cudaStream_t st) {
+  if (!m->colnz) return popcount_words(m->words, (size_t)m->wpc * m->cols, count, st);
+  unsigned long long *d;
+  VS_TRY(dalloc_n(&d, 1, st));
+  VS_CK(cudaMemsetAsync(d, 0, sizeof(*d), st));
+  if (m->cols) {
+    int blocks = (int)std::min<size_t>(((size_t)m->cols + 255) / 256, (size_t)sm_count() * 8);
+    { popcount_cols_kernel<<<blocks, 256, 0, st>>>(reinterpret_cast<const uint4 *>(m->words), m->cols, m->wpc / 2,
+                                                    m->colnz, d); vs::note_launch(); }
+    VS_CK(cudaGetLastError());
+  }
+  unsigned long long h = 0;
+  VS_CK(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st));
+  dfree(d, st);
+  VS_CK(cudaStreamSynchronize(st));
+  *count = h;
+  return VS_OK;
+}
+
 int popcount_words(const uint64_t *w, size_t n, uint64_t *count, cudaStream_t st) {
   unsigned long long *d;
   VS_TRY(dalloc_n(&d, 1, st));
@@ -405,6 +454,7 @@ int vs_bitmat_free(vs_bitmat *m) {
     if (m->owns_words) cudaFree(m->words);
     cudaFree(m->row_map);
     cudaFree(m->col_map);
+    cudaFree(m->colnz);
   }
   delete m;
   return VS_OK;
@@ -412,7 +462,7 @@ int vs_bitmat_free(vs_bitmat *m) {
 
 int vs_bitmat_count(const vs_bitmat *m, uint64_t *count, vs_stream_t stream) {
   if (!m || !count) return fail(VS_ERR_ARG, "null argument");
-  return popcount_words(m->words, (size_t)m->wpc * m->cols, count, S(stream));
+  return bitmat_popcount(m, count, S(stream));
 }
 
 int vs_flat_create(uint32_t ncols, const int32_t *types, uint64_t nrows, vs_flat **out) {

@@ -110,6 +110,7 @@ __global__ void k_seed(SeedArgs a) {
     if (atomicOr(&a.flag0[v], 1u) == 0) nv++;
     if (a.vis) atomicOr((unsigned long long *)&a.vis[idx], bit);
     if (a.acc) atomicOr((unsigned long long *)&a.acc[idx], bit);
+    if ((a.vis && a.res_vis) || a.acc) a.resflag[v] = 1;
     a.pairs0[i] = make_uint2(v, i);
     unsigned long long d = 0;
     _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.out.n) d += (unsigned long long)(a.out.off[l][v + 1] - a.out.off[l][v]);
@@ -415,6 +416,7 @@ __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
           }
           if (fresh) {
             if (a.acc_on) atomicOr(&a.acc[idx], bit);
+            if (a.res_vis || a.acc_on) a.resflag[v] = 1;
             if (atomicOr(&a.flagN[v], 1u) == 0) nv++;
             nb++;
           }
@@ -447,14 +449,63 @@ __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// L2 cache policies for the PULL kernels (variant H = 1): adjacency lists,
+// offsets and the visited / next-layer streams are read or written once per
+// hop and marked evict-first, so L2 keeps the frontier rows, which power-law
+// hubs make the only reused data (marked evict-last).
+template <int H> struct L2Pol {
+  uint64_t first = 0, last = 0;
+  __device__ __forceinline__ L2Pol() {
+    if (H) {
+      asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(first));
+      asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(last));
+    }
+  }
+  __device__ __forceinline__ uint32_t ld_stream(const uint32_t *p) const {
+    if (!H) return __ldg(p);
+    uint32_t r;
+    asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(first));
+    return r;
+  }
+  __device__ __forceinline__ int64_t ld_stream(const int64_t *p) const {
+    if (!H) return __ldg(p);
+    int64_t r;
+    asm("ld.global.nc.L2::cache_hint.s64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(first));
+    return r;
+  }
+  __device__ __forceinline__ uint4 ld_row(const uint4 *p) const {
+    if (!H) return __ldg(p);
+    uint4 r;
+    asm("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p), "l"(last));
+    return r;
+  }
+  __device__ __forceinline__ uint4 ld_rw(const uint4 *p) const {
+    if (!H) return *p;
+    uint4 r;
+    asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "l"(p), "l"(first) : "memory");
+    return r;
+  }
+  __device__ __forceinline__ void st(uint4 *p, uint4 v) const {
+    if (!H) {
+      *p = v;
+      return;
+    }
+    asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;"
+                 :: "l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "l"(first) : "memory");
+  }
+};
+
+// ---------------------------------------------------------------------------
 // PULL.  A warp owns one target vertex; its lanes form G = 32/L groups of L
 // lanes, each group ORs one whole active in-neighbour row (Q uint4 = L * UPL
 // per lane at most) at a time.  In-neighbour ids are read 32 at a time,
 // filtered by the frontier flags with a ballot and compacted through shared
 // memory, so inactive rows cost one flag load and no gather.
-template <int L, int UPL>
-__device__ __forceinline__ void gather_rows(const PullArgs &a, uint32_t *s_u, const uint32_t q0,
-                                            const uint32_t qn, uint4 (&acc)[UPL],
+template <int L, int UPL, int H>
+__device__ __forceinline__ void gather_rows(const PullArgs &a, const L2Pol<H> &pol, uint32_t *s_u,
+                                            const uint32_t q0, const uint32_t qn, uint4 (&acc)[UPL],
                                             const uint32_t *adj, int64_t beg, int64_t end,
                                             int64_t step_start, int64_t step) {
   constexpr int G = 32 / L;
@@ -464,7 +515,7 @@ __device__ __forceinline__ void gather_rows(const PullArgs &a, uint32_t *s_u, co
     uint32_t u = 0;
     bool act = false;
     if (j < end) {
-      u = __ldg(adj + j);
+      u = pol.ld_stream(adj + j);
       act = __ldg(a.flagF + u) != 0;
     }
     const unsigned m = __ballot_sync(FULL, act);
@@ -482,7 +533,7 @@ __device__ __forceinline__ void gather_rows(const PullArgs &a, uint32_t *s_u, co
       for (int k = 0; k < UPL; k++) {
         const uint32_t q = gl + k * L;
         if (q < qn) {
-          uint4 x0 = ldg4(r0 + q), x1 = ldg4(r1 + q), x2 = ldg4(r2 + q), x3 = ldg4(r3 + q);
+          uint4 x0 = pol.ld_row(r0 + q), x1 = pol.ld_row(r1 + q), x2 = pol.ld_row(r2 + q), x3 = pol.ld_row(r3 + q);
           acc[k] = or4(acc[k], or4(or4(x0, x1), or4(x2, x3)));
         }
       }
@@ -492,7 +543,7 @@ __device__ __forceinline__ void gather_rows(const PullArgs &a, uint32_t *s_u, co
 #pragma unroll
       for (int k = 0; k < UPL; k++) {
         const uint32_t q = gl + k * L;
-        if (q < qn) acc[k] = or4(acc[k], ldg4(r0 + q));
+        if (q < qn) acc[k] = or4(acc[k], pol.ld_row(r0 + q));
       }
     }
     __syncwarp();
@@ -501,9 +552,9 @@ __device__ __forceinline__ void gather_rows(const PullArgs &a, uint32_t *s_u, co
 
 // Fused epilogue for the row of v held by lanes 0..L-1 after the group reduction:
 // visited AND-NOT + update, accumulator OR, next-layer write, flag, counters.
-template <int L, int UPL>
-__device__ __forceinline__ void pull_epilogue(const PullArgs &a, uint32_t v, const uint32_t q0,
-                                              const uint32_t qn, uint4 (&acc)[UPL],
+template <int L, int UPL, int H>
+__device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> &pol, uint32_t v,
+                                              const uint32_t q0, const uint32_t qn, uint4 (&acc)[UPL],
                                               unsigned long long &nb, unsigned long long &nv) {
   const int lane = threadIdx.x & 31;
   const bool leader_group = lane < L;
@@ -520,9 +571,9 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, uint32_t v, con
           x = make_uint4(x.x & m.x, x.y & m.y, x.z & m.z, x.w & m.w);
         }
         if (a.shortest && nz4(x)) {
-          const uint4 vv = a.vis[idx];
+          const uint4 vv = pol.ld_rw(a.vis + idx);
           x = andnot4(x, vv);
-          if (nz4(x)) a.vis[idx] = or4(vv, x);
+          if (nz4(x)) pol.st(a.vis + idx, or4(vv, x));
         }
         if (nz4(x)) {
           any = true;
@@ -534,13 +585,14 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, uint32_t v, con
     }
   }
   const bool rownz = __any_sync(FULL, any);
+  if (lane == 0 && rownz && (a.res_vis || a.acc_on)) a.resflag[v] = 1;
   if (!a.multislice) {
     const uint32_t oldf = a.flagN[v];
     if (leader_group && (rownz || oldf)) {
 #pragma unroll
       for (int k = 0; k < UPL; k++) {
         const uint32_t q = lane + k * L;
-        if (q < qn) a.N[(size_t)v * a.Q + q0 + q] = acc[k];
+        if (q < qn) pol.st(a.N + (size_t)v * a.Q + q0 + q, acc[k]);
       }
     }
     if (lane == 0) {
@@ -559,9 +611,10 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, uint32_t v, con
   }
 }
 
-template <int L, int UPL>
-__global__ void __launch_bounds__(256) k_pull(PullArgs a) {
+template <int L, int UPL, int MINB, int H>
+__global__ void __launch_bounds__(256, MINB) k_pull(PullArgs a) {
   if (a.ctr->hop[a.h].strategy != ST_PULL) return;
+  const L2Pol<H> pol;
   __shared__ uint32_t s_u[8][32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const uint32_t q0 = blockIdx.y * a.qslice;
@@ -577,13 +630,13 @@ __global__ void __launch_bounds__(256) k_pull(PullArgs a) {
 #pragma unroll
     for (int k = 0; k < UPL; k++) acc[k] = make_uint4(0, 0, 0, 0);
     _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n)
-      gather_rows<L, UPL>(a, s_u[wib], q0, qn, acc, a.in.adj[l], a.in.off[l][v],
-                          a.in.off[l][v + 1], 0, 32);
+      gather_rows<L, UPL, H>(a, pol, s_u[wib], q0, qn, acc, a.in.adj[l], pol.ld_stream(a.in.off[l] + v),
+                             pol.ld_stream(a.in.off[l] + v + 1), 0, 32);
 #pragma unroll
     for (int o = L; o < 32; o <<= 1)
 #pragma unroll
       for (int k = 0; k < UPL; k++) acc[k] = or4(acc[k], shfl_xor4(acc[k], o));
-    pull_epilogue<L, UPL>(a, v, q0, qn, acc, nb, nv);
+    pull_epilogue<L, UPL, H>(a, pol, v, q0, qn, acc, nb, nv);
   }
   (void)lane;
   block_add(nb, &a.ctr->hop[a.h].new_bits);
@@ -596,6 +649,7 @@ template <int L, int UPL>
 __global__ void __launch_bounds__(512) k_pull_hub(PullArgs a) {
   if (a.ctr->hop[a.h].strategy != ST_PULL || a.nhubs == 0) return;
   extern __shared__ uint4 s_red[];  // [16 warps][32 lanes][UPL]
+  const L2Pol<0> pol;
   __shared__ uint32_t s_u[16][32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const uint32_t q0 = blockIdx.y * a.qslice;
@@ -607,8 +661,8 @@ __global__ void __launch_bounds__(512) k_pull_hub(PullArgs a) {
 #pragma unroll
     for (int k = 0; k < UPL; k++) acc[k] = make_uint4(0, 0, 0, 0);
     _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n)
-      gather_rows<L, UPL>(a, s_u[wib], q0, qn, acc, a.in.adj[l], a.in.off[l][v],
-                          a.in.off[l][v + 1], (int64_t)wib * 32, (int64_t)nw * 32);
+      gather_rows<L, UPL, 0>(a, pol, s_u[wib], q0, qn, acc, a.in.adj[l], a.in.off[l][v],
+                             a.in.off[l][v + 1], (int64_t)wib * 32, (int64_t)nw * 32);
 #pragma unroll
     for (int o = L; o < 32; o <<= 1)
 #pragma unroll
@@ -623,7 +677,7 @@ __global__ void __launch_bounds__(512) k_pull_hub(PullArgs a) {
 #pragma unroll
           for (int k = 0; k < UPL; k++) acc[k] = or4(acc[k], s_red[(w * 32 + lane) * UPL + k]);
       }
-      pull_epilogue<L, UPL>(a, v, q0, qn, acc, nb, nv);
+      pull_epilogue<L, UPL, 0>(a, pol, v, q0, qn, acc, nb, nv);
     }
     __syncthreads();
   }
@@ -713,6 +767,7 @@ __global__ void __launch_bounds__(256) k_push_epilogue(PushArgs a) {
         a.flagN[v] = 0;  // row is all zero again
       else
         nv++;
+      if (rownz && (a.res_vis || a.acc_on)) a.resflag[v] = 1;
     }
   }
   block_add(nb, &c->hop[a.h].new_bits);
@@ -799,16 +854,18 @@ using PullFn = void (*)(PullArgs);
 
 struct PullVariant {
   int L, UPL;
-  PullFn pull, hub;
+  PullFn pull[4], hub;  // pull[k]: bit 0 = 8 blocks per SM, bit 1 = L2 cache policies
 };
 
+#define VS_PULLS(L, U) {k_pull<L, U, 1, 0>, k_pull<L, U, 8, 0>, k_pull<L, U, 1, 1>, k_pull<L, U, 8, 1>}
 const PullVariant kVariants[] = {
-    {1, 1, k_pull<1, 1>, k_pull_hub<1, 1>},     {2, 1, k_pull<2, 1>, k_pull_hub<2, 1>},
-    {4, 1, k_pull<4, 1>, k_pull_hub<4, 1>},     {8, 1, k_pull<8, 1>, k_pull_hub<8, 1>},
-    {16, 1, k_pull<16, 1>, k_pull_hub<16, 1>},  {32, 1, k_pull<32, 1>, k_pull_hub<32, 1>},
-    {32, 2, k_pull<32, 2>, k_pull_hub<32, 2>},  {32, 4, k_pull<32, 4>, k_pull_hub<32, 4>},
-    {32, 8, k_pull<32, 8>, k_pull_hub<32, 8>},
+    {1, 1, VS_PULLS(1, 1), k_pull_hub<1, 1>},     {2, 1, VS_PULLS(2, 1), k_pull_hub<2, 1>},
+    {4, 1, VS_PULLS(4, 1), k_pull_hub<4, 1>},     {8, 1, VS_PULLS(8, 1), k_pull_hub<8, 1>},
+    {16, 1, VS_PULLS(16, 1), k_pull_hub<16, 1>},  {32, 1, VS_PULLS(32, 1), k_pull_hub<32, 1>},
+    {32, 2, VS_PULLS(32, 2), k_pull_hub<32, 2>},  {32, 4, VS_PULLS(32, 4), k_pull_hub<32, 4>},
+    {32, 8, VS_PULLS(32, 8), k_pull_hub<32, 8>},
 };
+#undef VS_PULLS
 
 const PullVariant &pick_variant(uint32_t qslice) {
   for (const auto &v : kVariants)
@@ -833,6 +890,7 @@ struct vs_expand_plan {
   unsigned long long *pdeg[2] = {nullptr, nullptr}, *doff = nullptr, *bsum = nullptr;
   uint64_t pair_cap = 0;
   uint32_t *push_list = nullptr, *touched = nullptr;
+  uint32_t *resflag = nullptr;  // per vertex: result column may be non-zero
   uint32_t *d_src = nullptr, *d_tgt = nullptr;
   int32_t *d_dist = nullptr;
   Ctr *ctr = nullptr;
@@ -847,6 +905,7 @@ struct vs_expand_plan {
   double sparse_frac = 0.02, push_frac = 0.0;
   const void *picker = nullptr;
   bool log_features = false;
+  int pull_kind = 0;  // PULL kernel variant (bit 0: 8 blocks/SM bound, bit 1: L2 policies)
   uint64_t *hmask = nullptr;  // (k_max + 1) x W words: rows allowed to grow at hop h
   bool use_hmask = false;
   int hop_forced[VS_MAX_HOPS + 1] = {};
@@ -860,7 +919,7 @@ namespace ex {
 
 int plan_free(vs_expand_plan *pl) {
   if (!pl) return VS_OK;
-  void *ptrs[] = {pl->pdeg[0], pl->pdeg[1], pl->doff, pl->bsum, pl->hmask, pl->buf[0], pl->buf[1], pl->flag[0], pl->flag[1], pl->vis, pl->acc,
+  void *ptrs[] = {pl->resflag, pl->pdeg[0], pl->pdeg[1], pl->doff, pl->bsum, pl->hmask, pl->buf[0], pl->buf[1], pl->flag[0], pl->flag[1], pl->vis, pl->acc,
                   pl->pairs[0], pl->pairs[1], pl->push_list, pl->touched, pl->d_src,
                   pl->d_tgt, pl->d_dist, pl->ctr, pl->hubs};
   for (void *p : ptrs)
@@ -895,6 +954,8 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
     return fail(VS_ERR_ARG, "unknown direction %d", p->direction);
   if (p->strategy < VS_STRAT_AUTO || p->strategy > VS_STRAT_SPARSE)
     return fail(VS_ERR_ARG, "unknown strategy %d", p->strategy);
+  if (p->pull_kernel < 0 || p->pull_kernel > 3) return fail(VS_ERR_ARG, "pull kernel variant must be 0..3");
+  if (p->sparse_frac < 0) return fail(VS_ERR_ARG, "sparse_frac must be >= 0");
   if (S == 0) return fail(VS_ERR_ARG, "no start vertex for VExpand");
   cudaStream_t st = 0;
   vs_expand_plan *pl = new vs_expand_plan();
@@ -936,6 +997,7 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   PL_ALLOC(pl->doff, pl->pair_cap + 1);
   PL_ALLOC(pl->bsum, (pl->pair_cap + 1023) / 1024 + 1);
   PL_ALLOC(pl->push_list, V);
+  PL_ALLOC(pl->resflag, V);
   PL_ALLOC(pl->touched, V);
   PL_ALLOC(pl->d_src, S);
   if (p->path_type == VS_PATH_FIND_SHORTEST) {
@@ -973,10 +1035,12 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
     }
     pl->nhubs = hn;
   }
+  pl->pull_kind = p->pull_kernel;
+  if (p->sparse_frac > 0) pl->sparse_frac = p->sparse_frac;
   const PullVariant &var = pick_variant(pl->qslice);
   if (var.UPL * 16 * 32 * 16 > 48 * 1024)
     cudaFuncSetAttribute(var.hub, cudaFuncAttributeMaxDynamicSharedMemorySize, 16 * 32 * 16 * var.UPL);
-  pl->grid_pull = occupancy_grid(var.pull, 256, 0, 8);
+  pl->grid_pull = occupancy_grid(var.pull[pl->pull_kind], 256, 0, 8);
   pl->grid_hub = std::max(1, std::min((int)pl->nhubs, occupancy_grid(var.hub, 512, 16 * 32 * 16 * var.UPL, 2)));
   pl->grid_sparse = occupancy_grid(k_sparse, 256, 0, 8);
   pl->grid_push = occupancy_grid(k_push, 256, 0, 8);
@@ -1006,6 +1070,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   for (int b = 0; b < 2; b++)
     { k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[b]), pl->flag[b],
                                                 V, Q, pl->ctr, 0, 0); vs::note_launch(); }
+  VS_CK(cudaMemsetAsync(pl->resflag, 0, 4ull * V, st));
   if (pl->vis) VS_CK(cudaMemsetAsync(pl->vis, 0, rowbytes, st));
   if (pl->acc) VS_CK(cudaMemsetAsync(pl->acc, 0, rowbytes, st));
   VS_CK(cudaMemsetAsync(pl->ctr, 0, sizeof(Ctr), st));
@@ -1024,6 +1089,8 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   sa.acc = (pl->use_acc && p.k_min == 0) ? pl->acc : nullptr;
   sa.pairs0 = pl->pairs[0];
   sa.pdeg0 = pl->pdeg[0];
+  sa.resflag = pl->resflag;
+  sa.res_vis = !pl->use_acc;
   sa.out = outl;
   sa.ctr = pl->ctr;
   sa.V = V;
@@ -1074,6 +1141,8 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     SparseArgs sp;
     sp.ctr = pl->ctr;
     sp.h = h;
+    sp.resflag = pl->resflag;
+    sp.res_vis = !pl->use_acc;
     sp.hmask = pl->use_hmask ? reinterpret_cast<const unsigned long long *>(pl->hmask + (size_t)h * W) : nullptr;
     sp.pin = pl->pairs[fb];
     sp.pout = pl->pairs[nbuf];
@@ -1095,6 +1164,8 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     PushArgs pa;
     pa.ctr = pl->ctr;
     pa.h = h;
+    pa.resflag = pl->resflag;
+    pa.res_vis = !pl->use_acc;
     pa.hmask = pl->use_hmask ? reinterpret_cast<const unsigned long long *>(pl->hmask + (size_t)h * W) : nullptr;
     pa.out = outl;
     pa.F = reinterpret_cast<const unsigned long long *>(pl->buf[fb]);
@@ -1112,6 +1183,8 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     { k_push<<<pl->grid_push, 256, 0, st>>>(pa); vs::note_launch(); }
     { k_push_epilogue<<<pl->grid_push, 256, 0, st>>>(pa); vs::note_launch(); }
     PullArgs a;
+    a.resflag = pl->resflag;
+    a.res_vis = !pl->use_acc;
     a.hmask = pl->use_hmask ? reinterpret_cast<const uint4 *>(pl->hmask + (size_t)h * W) : nullptr;
     a.in = in;
     a.F = reinterpret_cast<const uint4 *>(pl->buf[fb]);
@@ -1132,7 +1205,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.ctr = pl->ctr;
     a.h = h;
     if (pl->timing) cudaEventRecord(pl->ev[3 * h + 1], st);
-    { var.pull<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a); vs::note_launch(); }
+    { var.pull[pl->pull_kind]<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a); vs::note_launch(); }
     if (pl->nhubs)
       { var.hub<<<dim3(pl->grid_hub, pl->nslices), 512, 16 * 32 * 16 * var.UPL, st>>>(a); vs::note_launch(); }
     if (p.path_type == VS_PATH_FIND_SHORTEST)
@@ -1158,6 +1231,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   r.words = pl->use_acc ? pl->acc : pl->vis;
   r.row_map = pl->d_src;
   r.col_map = nullptr;
+  r.colnz = pl->resflag;
   r.owns_words = false;
   r.view = true;
   pl->has_result = p.path_type != VS_PATH_FIND_SHORTEST;
@@ -1259,6 +1333,17 @@ int vs_expand_plan_set_row_limits(vs_expand_plan *pl, const uint8_t *row_kmax, u
   return VS_OK;
 }
 
+// Kernel shape of the PULL hops (chosen by the autotuner): bit 0 asks for 8
+// resident 256-thread blocks per SM (32 registers), bit 1 adds L2 cache
+// policies (streams evict-first, frontier rows evict-last).
+int vs_expand_plan_set_pull_kernel(vs_expand_plan *pl, int kind) {
+  if (!pl || kind < 0 || kind > 3) return fail(VS_ERR_ARG, "pull kernel variant must be 0..3");
+  pl->pull_kind = kind;
+  const PullVariant &var = pick_variant(pl->qslice);
+  pl->grid_pull = occupancy_grid(var.pull[kind], 256, 0, 8);
+  return VS_OK;
+}
+
 int vs_expand_plan_log_features(vs_expand_plan *pl, int on) {
   if (!pl) return fail(VS_ERR_ARG, "null plan");
   pl->log_features = on != 0;
@@ -1317,6 +1402,8 @@ int vs_expand(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_
     }
     m->row_map = pl->d_src;
     pl->d_src = nullptr;
+    m->colnz = pl->resflag;
+    pl->resflag = nullptr;
     *out = m;
     (void)st;
   }

@@ -41,6 +41,8 @@ struct Lists {
 };
 
 struct SeedArgs {
+  uint32_t *resflag;  // result column may be non-zero (colnz of the result view)
+  int res_vis;        // the result is the visited matrix (else the accumulator)
   const uint32_t *sources;
   uint32_t S, W, V;
   uint64_t *buf0;
@@ -62,6 +64,8 @@ struct DecideArgs {
 };
 
 struct SparseArgs {
+  uint32_t *resflag;  // result column may be non-zero (colnz of the result view)
+  int res_vis;        // the result is the visited matrix (else the accumulator)
   Ctr *ctr;
   int h;
   const unsigned long long *hmask;  // rows that may still grow at hop h (NULL = all)
@@ -78,6 +82,8 @@ struct SparseArgs {
 };
 
 struct PushArgs {
+  uint32_t *resflag;  // result column may be non-zero (colnz of the result view)
+  int res_vis;        // the result is the visited matrix (else the accumulator)
   Ctr *ctr;
   int h;
   const unsigned long long *hmask;
@@ -92,6 +98,8 @@ struct PushArgs {
 };
 
 struct PullArgs {
+  uint32_t *resflag;  // result column may be non-zero (colnz of the result view)
+  int res_vis;        // the result is the visited matrix (else the accumulator)
   const uint4 *hmask;  // rows that may still grow at hop h, Q uint4 (NULL = all)
   Lists in;
   const uint4 *F;

@@ -145,6 +145,41 @@ __global__ void k_count_mat_mat(Table ta, const uint64_t *__restrict__ wa, uint3
   block_add(s, total);
 }
 
+// Mat x Mat count when neither operand has a column map (key = column index):
+// a warp takes 32 columns, keeps those that may be non-zero in both, and
+// popcounts each pair of columns with 16-byte loads and one warp reduction.
+__global__ void __launch_bounds__(256) k_count_direct(const uint4 *__restrict__ wa, uint32_t qa,
+                                                      const uint4 *__restrict__ wb, uint32_t qb, uint32_t cols,
+                                                      const uint32_t *__restrict__ nza,
+                                                      const uint32_t *__restrict__ nzb,
+                                                      unsigned long long *total) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  unsigned long long s = 0;
+  for (uint32_t c0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; c0 < cols; c0 += warps * 32) {
+    const uint32_t cl = c0 + lane;
+    unsigned m = __ballot_sync(FULL, cl < cols && (!nza || nza[cl]) && (!nzb || nzb[cl]));
+    while (m) {
+      const uint32_t c = c0 + __ffs(m) - 1;
+      m &= m - 1;
+      unsigned pa = 0, pb = 0;
+      for (uint32_t q = lane; q < qa; q += 32) {
+        const uint4 x = __ldg(wa + (size_t)c * qa + q);
+        pa += __popc(x.x) + __popc(x.y) + __popc(x.z) + __popc(x.w);
+      }
+      for (uint32_t q = lane; q < qb; q += 32) {
+        const uint4 x = __ldg(wb + (size_t)c * qb + q);
+        pb += __popc(x.x) + __popc(x.y) + __popc(x.z) + __popc(x.w);
+      }
+      pa = __reduce_add_sync(FULL, pa);
+      pb = __reduce_add_sync(FULL, pb);
+      s += (unsigned long long)pa * pb;
+    }
+  }
+  if (lane != 0) s = 0;
+  block_add(s, total);
+}
+
 struct OutCol {
   void *dst;
   const void *src;
@@ -371,7 +406,19 @@ int count_mat_mat(const vs_bitmat *a, const vs_bitmat *b, uint64_t *count, cudaS
   Scratch sc{st};
   Table t{};
   const bool direct = !a->col_map && !b->col_map;
-  if (!direct) {
+  if (direct) {
+    unsigned long long *d_total;
+    VS_TRY(sc.get(&d_total, 1));
+    VS_CK(cudaMemsetAsync(d_total, 0, 8, st));
+    const uint32_t cols = std::min(a->cols, b->cols);
+    if (cols)
+      { k_count_direct<<<grid_for(cols), 256, 0, st>>>(reinterpret_cast<const uint4 *>(a->words), a->wpc / 2,
+                                                      reinterpret_cast<const uint4 *>(b->words), b->wpc / 2, cols,
+                                                      a->colnz, b->colnz, d_total); vs::note_launch(); }
+    VS_CK(cudaGetLastError());
+    return read_total(d_total, count, st);
+  }
+  {
     VS_TRY(table_alloc(sc, a->cols, true, false, &t));
     if (a->cols) { k_build_cols<<<grid_for(a->cols), 256, 0, st>>>(t, a->col_map, a->cols); vs::note_launch(); }
   }

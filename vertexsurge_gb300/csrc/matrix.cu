@@ -67,11 +67,16 @@ __global__ void k_to_flat(const uint64_t *__restrict__ w, uint32_t rows, uint32_
                           uint32_t wpc, const uint32_t *__restrict__ row_map,
                           const uint32_t *__restrict__ col_map, uint32_t *__restrict__ out_r,
                           uint32_t *__restrict__ out_c, unsigned long long *__restrict__ cursor,
-                          unsigned long long total) {
+                          unsigned long long total, const uint32_t *__restrict__ colnz) {
   const int lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   const uint32_t lw = (rows + 63) / 64;
-  for (uint32_t c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < cols; c += warps) {
+  // a warp takes 32 columns at a time and walks the ones that may hold bits
+  for (uint32_t c0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; c0 < cols; c0 += warps * 32) {
+   unsigned cm = __ballot_sync(FULL, c0 + lane < cols && (!colnz || colnz[c0 + lane]));
+   while (cm) {
+    const uint32_t c = c0 + __ffs(cm) - 1;
+    cm &= cm - 1;
     const uint32_t cv = col_map ? col_map[c] : c;
     for (uint32_t w0 = 0; w0 < lw; w0 += 32) {
       const uint32_t wi = w0 + lane;
@@ -97,6 +102,7 @@ __global__ void k_to_flat(const uint64_t *__restrict__ w, uint32_t rows, uint32_
         pos++;
       }
     }
+   }
   }
 }
 
@@ -117,7 +123,7 @@ int validate_ids(const uint32_t *d_ids, uint32_t n, uint32_t bound, cudaStream_t
 
 int bitmat_to_flat(const vs_bitmat *m, cudaStream_t st, vs_flat **out) {
   uint64_t total = 0;
-  VS_TRY(popcount_words(m->words, (size_t)m->wpc * m->cols, &total, st));
+  VS_TRY(bitmat_popcount(m, &total, st));
   const int32_t types[2] = {VS_T_VID, VS_T_VID};
   vs_flat *f = nullptr;
   VS_TRY(flat_alloc(2, types, total, st, &f));
@@ -129,9 +135,9 @@ int bitmat_to_flat(const vs_bitmat *m, cudaStream_t st, vs_flat **out) {
   }
   cudaMemsetAsync(cur, 0, sizeof(*cur), st);
   if (total && m->cols) {
-    int blocks = std::max(1, std::min((int)((m->cols + 7) / 8), sm_count() * 8));
+    int blocks = std::max(1, std::min((int)((m->cols + 255) / 256), sm_count() * 8));
     { mx::k_to_flat<<<blocks, 256, 0, st>>>(m->words, m->rows, m->cols, m->wpc, m->row_map, m->col_map,
-                                          (uint32_t *)f->cols[0], (uint32_t *)f->cols[1], cur, total); vs::note_launch(); }
+                                          (uint32_t *)f->cols[0], (uint32_t *)f->cols[1], cur, total, m->colnz); vs::note_launch(); }
   }
   dfree(cur, st);
   cudaError_t e = cudaGetLastError();

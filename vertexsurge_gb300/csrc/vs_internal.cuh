@@ -73,6 +73,7 @@ struct vs_bitmat {
   int kind;
   uint64_t *words;
   uint32_t *row_map, *col_map;
+  uint32_t *colnz;  // optional: colnz[c] == 0 => column c is all zero (expand results)
   bool owns_words;
   bool view;  // borrowed view: vs_bitmat_free only releases the struct
 };
@@ -89,6 +90,7 @@ inline size_t type_size(int t) { return t == VS_T_I64 ? 8 : 4; }
 int exclusive_scan_u64(const unsigned long long *in, unsigned long long *out, size_t n,
                        cudaStream_t st);
 int popcount_words(const uint64_t *w, size_t n, uint64_t *count, cudaStream_t st);
+int bitmat_popcount(const vs_bitmat *m, uint64_t *count, cudaStream_t st);
 int bitmat_to_flat(const vs_bitmat *m, cudaStream_t st, vs_flat **out);
 int validate_ids(const uint32_t *d_ids, uint32_t n, uint32_t bound, cudaStream_t st, bool *ok);
 extern "C" const void *vs_picker_device_weights(const vs_picker *p);

@@ -64,15 +64,18 @@ def _run(plan, src, forced, k_max):
     return st, plan.features()
 
 
-def log_query(dg, g, S, k_max, path, direction, seed, out: Samples, qid: int, auto_plan_cache: dict):
+def log_query(dg, g, S, k_max, path, direction, seed, out: Samples, qid: int):
     src = graphgen.sample_sources(g.V, min(S, g.V), seed=seed)
-    key = (id(dg), len(src), k_max, path, direction)
-    plan = auto_plan_cache.get(key)
-    if plan is None:
-        plan = vs.ExpandPlan(dg, len(src), vs.make_params(1, k_max, path, direction))
-        plan.set_tuning(timing=True)
-        plan.log_features(True)
-        auto_plan_cache[key] = plan
+    plan = vs.ExpandPlan(dg, len(src), vs.make_params(1, k_max, path, direction))
+    plan.set_tuning(timing=True)
+    plan.log_features(True)
+    try:
+        _log_runs(plan, src, k_max, out, qid)
+    finally:
+        plan.free()
+
+
+def _log_runs(plan, src, k_max, out: Samples, qid: int):
     runs = {}
     for s in STRATS:
         runs[s] = _run(plan, src, s, k_max)
@@ -107,7 +110,6 @@ def collect(n_queries: int, seed: int = 1, graphs=None, log=print) -> Samples:
     graphs = graphs or graph_suite()
     dgs = [vs.DeviceGraph.from_host(g) for g in graphs]
     out = Samples()
-    cache: dict = {}
     t0 = time.time()
     for q in range(n_queries):
         gi = int(rng.integers(len(graphs)))
@@ -118,7 +120,7 @@ def collect(n_queries: int, seed: int = 1, graphs=None, log=print) -> Samples:
         direction = "forward" if rng.random() < 0.7 else "both"
         if path == "any":
             k_max = min(k_max, 4)
-        log_query(dgs[gi], graphs[gi], S, k_max, path, direction, int(rng.integers(1 << 30)), out, q, cache)
+        log_query(dgs[gi], graphs[gi], S, k_max, path, direction, int(rng.integers(1 << 30)), out, q)
         if log and (q + 1) % 200 == 0:
             log(f"  {q + 1} queries, {len(out.y)} samples, {time.time() - t0:.0f}s")
     return out

@@ -217,6 +217,9 @@ def run_gpu(args, w, rank, world, local_rank):
     tuned = {k: {x: t[x] for x in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words", "ms")}
              for k, t in (("A", tA), ("B", tB), ("P", tP))}
     log(f"[rank {rank}] autotune {time.time() - t0:.1f}s: {tuned}")
+    for name, t in (("A", tA), ("B", tB), ("P", tP)):
+        for row in sorted(t["table"], key=lambda r: r["ms"])[:6]:
+            log(f"[rank {rank}]   tune {name}: {row}")
     pA = autotune.make_plan(dg, Sa, ka[0], ka[1], "shortest", "forward", tA)
     pB = autotune.make_plan(dg, Sb, kb[0], kb[1], "shortest", "forward", tB)
     pP = autotune.make_plan(dg, Sa, 1, 1, "any", "forward", tP)

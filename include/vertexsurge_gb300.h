@@ -185,6 +185,9 @@ int vs_expand_plan_run(vs_expand_plan *plan, const uint32_t *sources, const uint
 int vs_expand_plan_result(vs_expand_plan *plan, vs_bitmat **view);
 int vs_expand_plan_stats(vs_expand_plan *plan, vs_expand_stats *stats, vs_stream_t stream);
 int vs_expand_plan_free(vs_expand_plan *plan);
+/* Device bytes a plan for S sources with these parameters allocates
+ * (admission control of the serving loop; no counterpart in the reference). */
+int vs_expand_plan_footprint(const vs_graph *g, uint32_t S, const vs_expand_params *p, uint64_t *bytes);
 /* Planner knobs: fraction of E below which pair lists (SPARSE) run, fraction
  * of V below which PUSH runs (negative = keep), per-hop E_active statistics
  * (an extra pass per hop) and per-hop CUDA-event timing (not for capture). */

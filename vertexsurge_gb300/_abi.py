@@ -111,6 +111,8 @@ _SIGS = [
     ("vs_expand_plan_result", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     ("vs_expand_plan_stats", C.c_int, [C.c_void_p, C.POINTER(ExpandStats), C.c_void_p]),
     ("vs_expand_plan_free", C.c_int, [C.c_void_p]),
+    ("vs_expand_plan_footprint", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(ExpandParams),
+                                           C.POINTER(C.c_uint64)]),
     ("vs_expand", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(ExpandParams), C.c_void_p,
                             C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(ExpandStats), C.c_void_p]),
     ("vs_hash_join", C.c_int, [TableRef, TableRef, C.c_int, C.c_uint64, C.POINTER(C.c_void_p),
@@ -380,6 +382,13 @@ def make_params(k_min, k_max, path="any", direction="forward", strategy="auto", 
     p.pull_kernel = int(pull_kernel)
     p.sparse_frac = float(sparse_frac)
     return p
+
+
+def plan_footprint(graph: "DeviceGraph", S: int, params: ExpandParams) -> int:
+    """Device bytes an expand plan for S sources allocates."""
+    b = C.c_uint64()
+    check(lib().vs_expand_plan_footprint(graph.h, S, C.byref(params), C.byref(b)))
+    return int(b.value)
 
 
 class ExpandPlan:

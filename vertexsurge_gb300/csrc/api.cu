@@ -70,6 +70,7 @@ int flat_alloc(uint32_t ncols, const int32_t *types, uint64_t nrows, cudaStream_
   vs_flat *f = new vs_flat();
   f->ncols = ncols;
   f->nrows = nrows;
+  f->st = st;
   for (uint32_t i = 0; i < ncols; i++) {
     if (types[i] != VS_T_VID && types[i] != VS_T_I64) {
       delete f;
@@ -96,6 +97,7 @@ int bitmat_alloc(uint32_t rows, uint32_t cols, int kind, cudaStream_t st, vs_bit
   m->wpc = words_per_col(rows);
   m->kind = kind;
   m->owns_words = true;
+  m->st = st;
   size_t n = (size_t)m->wpc * cols;
   int rc = dalloc_n(&m->words, n, st);
   if (rc != VS_OK) {
@@ -383,6 +385,10 @@ int vs_bitmat_create(uint32_t rows, uint32_t cols, int kind, vs_stream_t stream,
 int vs_bitmat_upload(vs_bitmat *m, const uint64_t *logical_words, vs_stream_t stream) {
   if (!m || (!logical_words && m->rows && m->cols)) return fail(VS_ERR_ARG, "null argument");
   cudaStream_t st = S(stream);
+  if (st != m->st) {  // the matrix was allocated in another stream's order
+    VS_CK(cudaStreamSynchronize(m->st));
+    m->st = st;
+  }
   const size_t lw = (m->rows + 63) / 64;
   VS_CK(cudaMemsetAsync(m->words, 0, sizeof(uint64_t) * (size_t)m->wpc * m->cols, st));
   if (lw && m->cols) {
@@ -450,11 +456,11 @@ int vs_bitmat_get_info(const vs_bitmat *m, vs_bitmat_info *info) {
 
 int vs_bitmat_free(vs_bitmat *m) {
   if (!m) return VS_OK;
-  if (!m->view) {
-    if (m->owns_words) cudaFree(m->words);
-    cudaFree(m->row_map);
-    cudaFree(m->col_map);
-    cudaFree(m->colnz);
+  if (!m->view) {  // stream-ordered after the handle's last work, no device-wide wait
+    if (m->owns_words) dfree(m->words, m->st);
+    dfree(m->row_map, m->st);
+    dfree(m->col_map, m->st);
+    dfree(m->colnz, m->st);
   }
   delete m;
   return VS_OK;
@@ -467,11 +473,15 @@ int vs_bitmat_count(const vs_bitmat *m, uint64_t *count, vs_stream_t stream) {
 
 int vs_flat_create(uint32_t ncols, const int32_t *types, uint64_t nrows, vs_flat **out) {
   if (!out || !types) return fail(VS_ERR_ARG, "null argument");
-  return flat_alloc(ncols, types, nrows, 0, out);
+  VS_TRY(flat_alloc(ncols, types, nrows, 0, out));
+  // allocated in legacy-stream order: make it usable from any stream
+  VS_CK(cudaStreamSynchronize(0));
+  return VS_OK;
 }
 
 int vs_flat_upload(vs_flat *f, uint32_t col, const void *data, vs_stream_t stream) {
   if (!f || col >= f->ncols || (!data && f->nrows)) return fail(VS_ERR_ARG, "bad column");
+  f->st = S(stream);
   if (f->nrows)
     VS_CK(cudaMemcpyAsync(f->cols[col], data, type_size(f->types[col]) * f->nrows,
                           cudaMemcpyDefault, S(stream)));
@@ -498,7 +508,7 @@ int vs_flat_info(const vs_flat *f, uint32_t *ncols, uint64_t *nrows, int32_t *ty
 
 int vs_flat_free(vs_flat *f) {
   if (!f) return VS_OK;
-  for (uint32_t i = 0; i < f->ncols; i++) cudaFree(f->cols[i]);
+  for (uint32_t i = 0; i < f->ncols; i++) dfree(f->cols[i], f->st);
   delete f;
   return VS_OK;
 }

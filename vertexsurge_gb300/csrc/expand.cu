@@ -911,6 +911,7 @@ struct vs_expand_plan {
   int hop_forced[VS_MAX_HOPS + 1] = {};
   bool timing = false;
   uint32_t timed_hops = 0;
+  cudaStream_t last_stream = 0;  // frees are ordered after the last run on it
   cudaEvent_t ev[3 * (VS_MAX_HOPS + 1)] = {};
 };
 
@@ -919,11 +920,12 @@ namespace ex {
 
 int plan_free(vs_expand_plan *pl) {
   if (!pl) return VS_OK;
+  const cudaStream_t st = pl->last_stream;
   void *ptrs[] = {pl->resflag, pl->pdeg[0], pl->pdeg[1], pl->doff, pl->bsum, pl->hmask, pl->buf[0], pl->buf[1], pl->flag[0], pl->flag[1], pl->vis, pl->acc,
                   pl->pairs[0], pl->pairs[1], pl->push_list, pl->touched, pl->d_src,
                   pl->d_tgt, pl->d_dist, pl->ctr, pl->hubs};
-  for (void *p : ptrs)
-    if (p) cudaFree(p);
+  for (void *p : ptrs)  // stream-ordered after the plan's last run
+    if (p) dfree(p, st);
   for (cudaEvent_t e : pl->ev)
     if (e) cudaEventDestroy(e);
   delete pl;
@@ -1049,10 +1051,25 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   return VS_OK;
 }
 
-int vs_expand_plan_free(vs_expand_plan *plan) {
-  if (plan) cudaDeviceSynchronize();
-  return plan_free(plan);
+// Device bytes vs_expand_plan_create allocates for these arguments (the
+// serving loop admits queries by this number).
+int vs_expand_plan_footprint(const vs_graph *g, uint32_t S, const vs_expand_params *p, uint64_t *bytes) {
+  if (!g || !p || !bytes) return fail(VS_ERR_ARG, "null argument");
+  const uint64_t V = g->V, W = words_per_col(S);
+  const bool use_vis = p->path_type != VS_PATH_ANY;
+  const bool use_acc = (p->path_type == VS_PATH_ANY) || (p->path_type == VS_PATH_SHORTEST && p->k_min >= 2);
+  uint64_t cap = p->pair_capacity ? p->pair_capacity
+                                  : std::max<uint64_t>(1u << 20, std::min<uint64_t>((uint64_t)S * V / 8, 1ull << 25));
+  cap = std::max<uint64_t>(cap, S);
+  uint64_t b = (2 + use_vis + use_acc) * V * W * 8;             // frontier pair, visited, accumulator
+  b += 6 * V * 4;                                                 // flags x2, resflag, push list, touched, hubs
+  b += cap * (2 * 8 + 2 * 8 + 8) + ((cap + 1023) / 1024 + 1) * 8;  // pair lists, degrees, offsets, block sums
+  b += (uint64_t)S * 4 * 3 + sizeof(Ctr) + (uint64_t)(p->k_max + 1) * W * 8;
+  *bytes = b;
+  return VS_OK;
 }
+
+int vs_expand_plan_free(vs_expand_plan *plan) { return plan_free(plan); }
 
 int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32_t *targets,
                        int32_t *distances, vs_stream_t stream) {
@@ -1061,6 +1078,10 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   if (p.path_type == VS_PATH_FIND_SHORTEST && (!targets || !distances))
     return fail(VS_ERR_ARG, "FindShortest needs targets and distances");
   cudaStream_t st = S(stream);
+  if (st != pl->last_stream) {  // earlier work on the plan ran in another stream's order
+    VS_CK(cudaStreamSynchronize(pl->last_stream));
+    pl->last_stream = st;
+  }
   const vs_graph *g = pl->g;
   const uint32_t V = g->V, S_ = pl->S, W = pl->W, Q = pl->Q;
   const size_t rowbytes = (size_t)V * W * 8;
@@ -1404,6 +1425,7 @@ int vs_expand(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_
     pl->d_src = nullptr;
     m->colnz = pl->resflag;
     pl->resflag = nullptr;
+    m->st = st;
     *out = m;
     (void)st;
   }

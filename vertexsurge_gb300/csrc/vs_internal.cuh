@@ -74,6 +74,7 @@ struct vs_bitmat {
   uint64_t *words;
   uint32_t *row_map, *col_map;
   uint32_t *colnz;  // optional: colnz[c] == 0 => column c is all zero (expand results)
+  cudaStream_t st;  // stream of the last work on the handle; frees are ordered on it
   bool owns_words;
   bool view;  // borrowed view: vs_bitmat_free only releases the struct
 };
@@ -83,6 +84,7 @@ struct vs_flat {
   uint64_t nrows;
   int32_t types[16];
   void *cols[16];
+  cudaStream_t st;  // stream of the last work on the handle; frees are ordered on it
 };
 
 namespace vs {

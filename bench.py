@@ -50,6 +50,16 @@ WORKLOADS = {
                            S_a=4096, hops_a=(1, 4), S_b=4096, hops_b=(1, 2), cpu_S=1024),
     "rmat16_pattern": dict(kind="rmat", scale=16, ef=16, seed=1, S_a=512, hops_a=(1, 3), S_b=512,
                            hops_b=(1, 2), cpu_S=512),
+    # 256 queries (sources log-uniform in 64..8192, hops [1,l], l in 2..6, a join of
+    # 1e5..1e7 vertex-id keys each) on the 10M-vertex graph, one CUDA-graph launch per batch
+    "zipf10M_batched256": dict(kind="zipf", V=10_000_000, E=300_000_000, alpha=2.1, cap=50_000, seed=3,
+                               batched=dict(n=256, s_range=(64, 8192), l_range=(2, 6),
+                                            join_rows=(100_000, 10_000_000), waves=(16384, 32768),
+                                            cpu_queries=3, check=6)),
+    "zipf1M_batched64": dict(kind="zipf", V=1_000_000, E=30_000_000, alpha=2.1, cap=50_000, seed=3,
+                             batched=dict(n=64, s_range=(64, 8192), l_range=(2, 6),
+                                          join_rows=(100_000, 1_000_000), waves=(16384, 32768),
+                                          cpu_queries=3, check=6)),
 }
 
 
@@ -148,6 +158,200 @@ def cpu_baseline(g, w, sa):
                       f"graph, one run of {dt:.1f} s ({src_edges / 1e9:.2f} Gsrc-edges)"}, dt
 
 
+def batched_queries(g, w):
+    from vertexsurge_gb300 import batch
+    bw = w["batched"]
+    return batch.make_queries(g, bw["n"], bw["s_range"], bw["l_range"], bw["join_rows"], seed=9)
+
+
+def cpu_batched(g, w, queries):
+    """Oracle VExpand + TableConvert + HashJoin (count) per query, one query at
+    a time as the reference runs them, on a bounded sample: the first queries
+    of the trace with at most 2,048 sources."""
+    from oracle import pyoracle as O
+    sample = [q for q in queries if len(q.sources) <= 2048][: w["batched"]["cpu_queries"]]
+    t = time.perf_counter()
+    counts = []
+    for q in sample:
+        words, _, _ = O.vexpand(g, q.sources, 1, q.k_max, "shortest", "forward")
+        # the reference's HashJoin takes ColMain matrices: TableConvert first
+        cm = O.table_convert(words, len(q.sources), g.V, False)
+        a = O.Table(O.COLMAIN, [0, 1], words=cm, mrows=len(q.sources), mcols=g.V, row_map=q.sources)
+        k = O.Table(O.FLAT, [1], cols=[q.keys])
+        counts.append(O.hash_join(k, a, 1, only_count=True)[2])
+        del words, cm, a
+    dt = time.perf_counter() - t
+    return sample, counts, dt
+
+
+def run_reference_batched(args, w):
+    from oracle import pyoracle as O
+    t0 = time.time()
+    g = make_graph(w)
+    queries = batched_queries(g, w)
+    log(f"graph {g.V} vertices {g.E} edges, {len(queries)} queries in {time.time() - t0:.1f}s")
+    times, n = [], 0
+    for i in range(args.steps + min(args.warmup, 1)):
+        sample, _, dt = cpu_batched(g, w, queries)
+        if i >= min(args.warmup, 1):
+            times.append(dt)
+            n += len(sample)
+    value = n / sum(times)
+    cores = O.lib().oracle_get_threads()
+    desc = (f"{len(sample)} queries per step, one at a time (the first with <= 2048 sources: "
+            f"VExpand(Shortest, [1,l]) then HashJoin count with the key table)")
+    line = {"impl": "reference", "metric": "batched queries/s", "value": value, "unit": "queries/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": min(args.warmup, 1),
+            "ms_per_step": 1000 * sum(times) / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded power-law graph, uniform sources)",
+            "config": {"workload": args.workload, "V": g.V, "E": g.E, "queries": len(queries)},
+            "cpu_baseline": {"value": value, "unit": "queries/s", "cores": cores, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu_batched(args, w, rank, world, local_rank):
+    """Batched queries: the whole batch as one CUDA-graph launch per step."""
+    import torch
+    import vertexsurge_gb300 as vs
+    from vertexsurge_gb300 import autotune, batch, picker_train
+    from vertexsurge_gb300 import build as b
+    b.build_all()
+    torch.cuda.set_device(local_rank)
+    vs.init(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    bw = w["batched"]
+    t0 = time.time()
+    g = make_graph(w)
+    queries = batched_queries(g, w)
+    nq = len(queries)
+    key_rows = sum(len(q.keys) for q in queries)
+    src_rows = sum(len(q.sources) for q in queries)
+    log(f"[rank {rank}] graph {g.V} vertices {g.E} edges, {nq} queries ({src_rows} sources, "
+        f"{key_rows} key rows) in {time.time() - t0:.1f}s")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dg = vs.DeviceGraph.from_host(g, stream=stream)
+    # autotune: planner knobs on a wave-sized sample, then the wave width (untimed)
+    t0 = time.time()
+    from vertexsurge_gb300 import graphgen
+    tsrc = graphgen.sample_sources(g.V, min(bw["waves"]), seed=77)
+    setting = autotune.tune(dg, tsrc, 1, 4, "shortest", "forward", stream=stream, repeats=1,
+                            pull_kinds=(0,), sparse_fracs=(0.002, 0.02), hub_thresholds=(0, 256))
+    setting = {k: setting[k] for k in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words", "ms")}
+    waves = batch.tune_wave_rows(dg, queries, stream, candidates=bw["waves"], setting=setting)
+    log(f"[rank {rank}] autotune {time.time() - t0:.1f}s: {setting} waves {waves}")
+    bt = batch.Batch(dg, queries, waves["wave_rows"], stream, setting=setting)
+    cg = bt.capture()
+    for _ in range(args.warmup):
+        bt.launch()
+    counts = bt.counts()
+    # bit-exact against running queries alone (a bounded subset)
+    chk = sorted(range(nq), key=lambda i: len(queries[i].sources))[: bw["check"] // 2] + \
+        list(range(nq))[: bw["check"] - bw["check"] // 2]
+    solo = batch.solo_counts(dg, [queries[i] for i in chk], stream=stream)
+    assert np.array_equal(counts[chk], solo), "batched counts differ from solo runs"
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local_rank)
+    launches0 = vs.kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        bt.launch()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    launches = vs.kernel_launches() - launches0
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * nq * args.steps / (ms / 1e3)
+    assert np.array_equal(bt.counts(), counts)
+    # e2e: every step copies the batch's inputs (sources, limits, keys) from pinned
+    # host memory into the batch's device buffers, replays the graph and reads the counts
+    h_src, h_lim, h_keys = (bt.d_src.cpu().pin_memory(), bt.d_lim.cpu().pin_memory(),
+                            bt.d_keys.cpu().pin_memory())
+    h_cnt = torch.zeros_like(bt.d_counts, device="cpu").pin_memory()
+
+    def step_e2e():
+        bt.d_src.copy_(h_src, non_blocking=True)
+        bt.d_lim.copy_(h_lim, non_blocking=True)
+        bt.d_keys.copy_(h_keys, non_blocking=True)
+        bt.launch()
+        h_cnt.copy_(bt.d_counts, non_blocking=True)
+
+    step_e2e()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_e2e()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1)
+    assert np.array_equal(h_cnt.numpy()[bt.slot].astype(np.uint64), counts)
+    e2e = {"value": world * nq * args.steps / (ms_e2e / 1e3), "unit": "queries/s",
+           "h2d_bytes_per_step": int(bt.h2d_bytes()), "d2h_bytes_per_step": int(8 * nq),
+           "ms_per_step": ms_e2e / args.steps}
+    kernels = cg.kernels
+    bt.free()
+    # learned picker: the same batch with the trained network choosing each hop
+    learned = None
+    if picker_train.WEIGHTS_FILE.exists():
+        pk = vs.Picker()
+        pk.set_params(np.load(picker_train.WEIGHTS_FILE))
+        bl = batch.Batch(dg, queries, waves["wave_rows"], stream, setting=setting, picker=pk)
+        bl.capture()
+        for _ in range(max(1, min(args.warmup, 3))):
+            bl.launch()
+        l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0.record(stream)
+        for _ in range(args.steps):
+            bl.launch()
+        l1.record(stream)
+        torch.cuda.synchronize()
+        assert np.array_equal(bl.counts(), counts), "learned-picker counts differ"
+        ms_l = l0.elapsed_time(l1) / args.steps
+        learned = {"queries_per_s": world * nq / (ms_l / 1e3), "ms_per_step": ms_l}
+        bl.free()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        sample, ccounts, dt = cpu_batched(g, w, queries)
+        idx = [queries.index(q) for q in sample]
+        assert [int(counts[i]) for i in idx] == ccounts, "oracle counts differ from the batch"
+        from oracle import pyoracle as O
+        cpu = {"value": len(sample) / dt, "unit": "queries/s", "cores": O.lib().oracle_get_threads(),
+               "kind": "port", "sample": f"{len(sample)} queries with <= 2048 sources, one at a time, {dt:.1f} s"}
+    line = {"metric": "batched queries/s", "value": value, "unit": "queries/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded power-law graph, uniform sources and keys)",
+            "config": {"workload": args.workload, "V": g.V, "E": g.E, "queries": nq, "sources": src_rows,
+                       "key_rows": key_rows, "wave_rows": waves["wave_rows"], "waves": len(bt.waves),
+                       "graph_kernels": kernels, "l2": "inputs larger than L2",
+                       "parallelism": f"replicas{world}"},
+            "queries_per_s": {"plain": value, "learned": learned["queries_per_s"] if learned else None},
+            "learned_picker": learned, "autotune": {"planner": setting, "waves": waves},
+            "results": {"count_sum": int(counts.sum()), "checked_against_solo": len(chk)},
+            "roofline": None, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def run_reference(args, w, rank, world):
     """--impl reference: the oracle (CPU restatement of the reference) on host cores."""
     if rank != 0:
@@ -155,6 +359,8 @@ def run_reference(args, w, rank, world):
     from vertexsurge_gb300 import build as b
     b.build_gen()
     b.build_oracle()
+    if "batched" in w:
+        return run_reference_batched(args, w)
     from oracle import pyoracle as O
     t0 = time.time()
     g = make_graph(w)
@@ -395,6 +601,8 @@ def main():
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, w, rank, world)
+    elif "batched" in w:
+        run_gpu_batched(args, w, rank, world, local_rank)
     else:
         run_gpu(args, w, rank, world, local_rank)
 

@@ -82,6 +82,23 @@ const char *vs_version(void);
  * (diagnostics; no counterpart in the reference). */
 uint64_t vs_kernel_launches(void);
 
+/* CUDA-graph capture (no counterpart in the reference): the calls made on
+ * `stream` between vs_capture_begin and vs_capture_end are recorded, not run,
+ * and vs_captured_launch replays them as one graph launch.  Capturable calls:
+ * vs_expand_plan_run with device sources (the plan's host-side settings —
+ * row limits set from the host, tuning, picker, forced strategies — are fixed
+ * at capture), vs_expand_plan_set_row_limits_device and
+ * vs_hash_join_count_row_blocks.  Run a plan once on `stream` before
+ * capturing it.  The stream must not be the legacy default stream.
+ * vs_kernel_launches counts a captured kernel once per replay. */
+typedef struct vs_captured vs_captured;
+int vs_capture_begin(vs_stream_t stream);
+int vs_capture_end(vs_stream_t stream, vs_captured **out);
+int vs_captured_launch(vs_captured *g, vs_stream_t stream);
+/* Kernel nodes of the captured graph. */
+uint64_t vs_captured_kernels(const vs_captured *g);
+int vs_captured_free(vs_captured *g);
+
 /* ---- graph (replaces Graph::load + Graph::get_edges_refs CSR requests,
  *      src/objects/storage/graph_store.cpp:48-73, :75-110, :142-189) ------
  * fwd: out-lists (u -> v), rev: in-lists (v <- u), both int64 offsets [V+1]
@@ -240,6 +257,24 @@ int vs_hash_join(vs_table_ref a, vs_table_ref b, int only_count, uint64_t max_ro
 int vs_hash_join_count_noalloc(const void *keys_a, uint64_t na, const void *keys_b, uint64_t nb,
                                int key_type, uint64_t *count, vs_stream_t stream);
 
+/* Batched join counts (no counterpart in the reference, which joins one
+ * query's result at a time).  The VarRow matrix m (a batched expand result,
+ * columns = vertex ids) holds several queries in row blocks; block q covers
+ * rows [row_begin, row_end) and is joined on the vertex id with the vertex-id
+ * keys[key_begin, key_end), count only:
+ *   counts[q] = sum over those keys k < V of popcount(column k, rows of q),
+ * the count HashJoin gives for (query q's matrix) x (a flat table with that
+ * key column).  keys and counts are device memory; counts (nblocks uint64)
+ * are overwritten in stream order without a host sync (capturable).  At most
+ * VS_MAX_ROW_BLOCKS blocks per call. */
+#define VS_MAX_ROW_BLOCKS 512
+typedef struct vs_row_block {
+  uint32_t row_begin, row_end;
+  uint64_t key_begin, key_end;
+} vs_row_block;
+int vs_hash_join_count_row_blocks(const vs_bitmat *m, const uint32_t *keys, const vs_row_block *blocks,
+                                  uint32_t nblocks, uint64_t *counts, vs_stream_t stream);
+
 /* ---- multi-way intersection (replaces Mintersect,
  *      src/objects/operator/mintersect.cpp:14-345) ---------------------------
  * base: flat table or VarRow matrix (columns row value, column value).
@@ -292,6 +327,12 @@ int vs_expand_plan_set_hop_strategies(vs_expand_plan *plan, const int32_t *strat
  * alone.  NULL removes the limits.  (No counterpart in the reference, which
  * runs one VExpand per query.) */
 int vs_expand_plan_set_row_limits(vs_expand_plan *plan, const uint8_t *row_kmax, uint32_t n);
+/* The same from a device array of n <= S limits, stream-ordered and
+ * capturable (rows n..S-1 get limit 0 and never grow; a limit above k_max
+ * makes the next run fail with VS_ERR_ARG).  Runs stop after the largest
+ * row limit. */
+int vs_expand_plan_set_row_limits_device(vs_expand_plan *plan, const uint8_t *row_kmax, uint32_t n,
+                                         vs_stream_t stream);
 /* Kernel shape of PULL hops (the autotuner's knob): kind 0..3, bit 0 = eight
  * resident 256-thread blocks per SM, bit 1 = L2 cache policies that keep
  * frontier rows and stream everything else.  Results never depend on it. */

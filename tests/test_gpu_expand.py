@@ -193,3 +193,78 @@ def test_autotuner_settings_keep_results(vs, graphs):
         assert np.array_equal(plan.result().download(), exp), row
         m, _, _ = vs.expand(dg, src, 1, 3, "shortest", "forward", **autotune.params_kw(row))
         assert np.array_equal(m.download(), exp), row
+
+
+def test_captured_graph_equals_direct_run(vs, graphs):
+    import torch
+    g, dg = graphs["zipf3000"]
+    src = graphgen.sample_sources(g.V, 300, seed=14)
+    dsrc = torch.from_numpy(src.view(np.int32)).cuda()
+    stream = torch.cuda.Stream()
+    for path in ("any", "shortest"):
+        plan = vs.ExpandPlan(dg, len(src), vs.make_params(1, 4, path, "forward"))
+        plan.run(dsrc, stream=stream)  # first run on the stream, outside the capture
+        stream.synchronize()
+        with vs.Captured(stream, keep=(plan, dsrc)) as cg:
+            plan.run(dsrc, stream=stream)
+        assert cg.kernels > 0
+        exp, _, _ = O.vexpand(g, src, 1, 4, path, "forward")
+        for _ in range(2):
+            n0 = vs.kernel_launches()
+            cg.launch(stream)
+            stream.synchronize()
+            assert vs.kernel_launches() - n0 == cg.kernels
+            assert np.array_equal(plan.result().download(stream), exp)
+        # the replay reads the sources buffer at every launch
+        src2 = graphgen.sample_sources(g.V, 300, seed=15)
+        dsrc.copy_(torch.from_numpy(src2.view(np.int32)))
+        cg.launch(stream)
+        stream.synchronize()
+        exp2, _, _ = O.vexpand(g, src2, 1, 4, path, "forward")
+        assert np.array_equal(plan.result().download(stream), exp2)
+        dsrc.copy_(torch.from_numpy(src.view(np.int32)))
+        cg.free()
+        plan.free()
+
+
+@pytest.mark.parametrize("path", ["any", "shortest"])
+def test_device_row_limits_equal_solo(vs, graphs, path):
+    """Row limits set from a device array: each query's rows equal its solo
+    result; rows past n never grow; the run stops after the largest limit."""
+    import torch
+    g, dg = graphs["rmat11_skew"]
+    sizes, kmaxs = [40, 70, 25, 90], [1, 3, 2, 2]
+    srcs = [graphgen.sample_sources(g.V, n, seed=30 + i) for i, n in enumerate(sizes)]
+    allsrc = np.concatenate(srcs).astype(np.uint32)
+    S = len(allsrc) + 20  # 20 trailing rows without a limit entry
+    padded = np.concatenate([allsrc, np.zeros(20, np.uint32)])
+    limits = np.concatenate([np.full(n, k, np.uint8) for n, k in zip(sizes, kmaxs)])
+    plan = vs.ExpandPlan(dg, S, vs.make_params(1, 5, path, "forward"))
+    plan.set_tuning(collect_stats=True)
+    dl = torch.from_numpy(limits).cuda()
+    plan.set_row_limits_device(dl, len(limits))
+    plan.run(padded)
+    st = plan.stats()
+    assert st["hops_run"] <= max(kmaxs)
+    got = words_to_bool(plan.result().download(), S)
+    r0 = 0
+    for src, k in zip(srcs, kmaxs):
+        exp, _, _ = O.vexpand(g, src, 1, k, path, "forward")
+        assert np.array_equal(got[r0:r0 + len(src)], words_to_bool(exp, len(src))), (k, path)
+        r0 += len(src)
+    # rows without a limit keep at most their seed (no hop may grow them)
+    assert got[r0:].sum(axis=1).max() <= 1
+    plan.free()
+
+
+def test_device_row_limit_above_kmax_is_an_error(vs, graphs):
+    import torch
+    g, dg = graphs["rmat11_skew"]
+    src = graphgen.sample_sources(g.V, 64, seed=3)
+    plan = vs.ExpandPlan(dg, 64, vs.make_params(1, 2, "shortest", "forward"))
+    plan.set_row_limits_device(torch.full((64,), 3, dtype=torch.uint8, device="cuda"), 64)
+    plan.set_tuning(collect_stats=True)
+    plan.run(src)
+    with pytest.raises(vs.VsError):
+        plan.stats()
+    plan.free()

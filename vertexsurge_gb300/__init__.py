@@ -4,7 +4,8 @@ expand, vertex-id hash join and multi-way intersection, behind a C ABI
 (include/vertexsurge_gb300.h).  This package is the Python view of that ABI
 plus the synthetic graph generators used by tests and benchmarks."""
 from ._abi import (  # noqa: F401
-    BitMatrix, DeviceGraph, ExpandPlan, FlatTable, Picker, VsError, check, expand, hash_join, init, kernel_launches, lib,
+    BitMatrix, Captured, DeviceGraph, ExpandPlan, FlatTable, Picker, RowBlock, VsError, check, expand, hash_join, init,
+    join_count_row_blocks, kernel_launches, lib,
     make_params, mintersect, DIR_BACKWARD, DIR_BOTH, DIR_FORWARD, KIND_COLMAIN, KIND_VARROW,
     PATH_ANY, PATH_FIND_SHORTEST, PATH_SHORTEST, STRAT_AUTO, STRAT_PULL, STRAT_PUSH, STRAT_SPARSE,
     T_I64, T_VID,

@@ -140,6 +140,14 @@ _SIGS += [
     ("vs_expand_plan_log_features", C.c_int, [C.c_void_p, C.c_int]),
     ("vs_expand_plan_set_row_limits", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     ("vs_expand_plan_set_pull_kernel", C.c_int, [C.c_void_p, C.c_int]),
+    ("vs_expand_plan_set_row_limits_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    ("vs_capture_begin", C.c_int, [C.c_void_p]),
+    ("vs_capture_end", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("vs_captured_launch", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("vs_captured_kernels", C.c_uint64, [C.c_void_p]),
+    ("vs_captured_free", C.c_int, [C.c_void_p]),
+    ("vs_hash_join_count_row_blocks", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                                C.c_void_p]),
     ("vs_expand_plan_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
 ]
 
@@ -384,6 +392,72 @@ def make_params(k_min, k_max, path="any", direction="forward", strategy="auto", 
     return p
 
 
+class Captured:
+    """A CUDA graph recorded from library calls on one stream (vs_capture_*).
+
+    Use as a context manager around the calls to record:
+        with vs.Captured(stream) as cg: plan.run(dsrc, stream=stream); ...
+        cg.launch(stream)
+    Objects the recorded calls use (plans, tensors) must outlive it: pass them
+    as `keep`."""
+
+    def __init__(self, stream, keep=()):
+        self.stream, self.h, self._keep = stream, None, list(keep)
+
+    def __enter__(self):
+        check(lib().vs_capture_begin(_stream(self.stream)))
+        return self
+
+    def __exit__(self, et, ev, tb):
+        h = C.c_void_p()
+        rc = lib().vs_capture_end(_stream(self.stream), C.byref(h))
+        if et is None:
+            check(rc)
+            self.h = h
+        elif rc == 0 and h.value:  # the recorded calls raised: drop the partial graph
+            lib().vs_captured_free(h)
+        return False
+
+    def keep(self, *objs):
+        self._keep.extend(objs)
+
+    @property
+    def kernels(self) -> int:
+        return int(lib().vs_captured_kernels(self.h)) if self.h else 0
+
+    def launch(self, stream=None):
+        check(lib().vs_captured_launch(self.h, _stream(stream if stream is not None else self.stream)))
+
+    def free(self):
+        if self.h:
+            lib().vs_captured_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+MAX_ROW_BLOCKS = 512  # VS_MAX_ROW_BLOCKS
+
+
+class RowBlock(C.Structure):
+    _fields_ = [("row_begin", C.c_uint32), ("row_end", C.c_uint32),
+                ("key_begin", C.c_uint64), ("key_end", C.c_uint64)]
+
+
+def join_count_row_blocks(m: "BitMatrix", keys, blocks, counts, stream=None):
+    """Per row block q: count of HashJoin(rows of q of m, keys[key_begin:key_end]) on
+    the vertex id (vs_hash_join_count_row_blocks).  keys: device int32/uint32 tensor;
+    counts: device int64 tensor of len(blocks), overwritten in stream order;
+    blocks: [(row_begin, row_end, key_begin, key_end)]."""
+    arr = (RowBlock * len(blocks))(*[RowBlock(*map(int, b)) for b in blocks])
+    check(lib().vs_hash_join_count_row_blocks(m.h, _ptr(keys), arr, len(blocks), _ptr(counts),
+                                              _stream(stream)))
+
+
 def plan_footprint(graph: "DeviceGraph", S: int, params: ExpandParams) -> int:
     """Device bytes an expand plan for S sources allocates."""
     b = C.c_uint64()
@@ -428,6 +502,10 @@ class ExpandPlan:
         for i, x in enumerate(strategies):
             arr[i] = _STRATS[x] if isinstance(x, str) else int(x)
         check(lib().vs_expand_plan_set_hop_strategies(self.h, _ptr(arr), len(arr)))
+
+    def set_row_limits_device(self, row_kmax, n: int, stream=None):
+        """Row limits from a device uint8 tensor (stream-ordered, capturable)."""
+        check(lib().vs_expand_plan_set_row_limits_device(self.h, _ptr(row_kmax), int(n), _stream(stream)))
 
     def set_pull_kernel(self, kind: int):
         """PULL kernel variant 0..3 (bit 0: 8 blocks/SM, bit 1: L2 cache policies)."""

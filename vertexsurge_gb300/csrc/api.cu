@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "vs_internal.cuh"
 
@@ -317,6 +318,68 @@ const char *vs_last_error(void) { return g_last_error.c_str(); }
 const char *vs_version(void) { return "vertexsurge_gb300 0.1 sm_103a"; }
 
 uint64_t vs_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+struct vs_captured {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t kernels = 0;
+};
+
+int vs_capture_begin(vs_stream_t stream) {
+  cudaStream_t st = vs::S(stream);
+  if (st == 0) return fail(VS_ERR_ARG, "capture needs a created stream, not the default stream");
+  // relaxed: the library's own host calls (stream syncs of a plan's previous
+  // stream) stay legal while the stream records
+  VS_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+  return VS_OK;
+}
+
+int vs_capture_end(vs_stream_t stream, vs_captured **out) {
+  if (!out) return fail(VS_ERR_ARG, "vs_capture_end: null argument");
+  cudaStream_t st = vs::S(stream);
+  cudaGraph_t graph = nullptr;
+  VS_CK(cudaStreamEndCapture(st, &graph));
+  if (!graph) return fail(VS_ERR_ARG, "vs_capture_end: nothing was captured");
+  size_t n = 0;
+  cudaError_t e = cudaGraphGetNodes(graph, nullptr, &n);
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (e == cudaSuccess && n) e = cudaGraphGetNodes(graph, nodes.data(), &n);
+  uint64_t kernels = 0;
+  for (size_t i = 0; e == cudaSuccess && i < n; i++) {
+    cudaGraphNodeType t;
+    e = cudaGraphNodeGetType(nodes[i], &t);
+    kernels += t == cudaGraphNodeTypeKernel;
+  }
+  vs_captured *g = new vs_captured();
+  g->graph = graph;
+  g->kernels = kernels;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    delete g;
+    return cuda_fail(e, "vs_capture_end", __FILE__, __LINE__);
+  }
+  g_launches.fetch_sub(kernels, std::memory_order_relaxed);  // recorded, not run
+  *out = g;
+  return VS_OK;
+}
+
+int vs_captured_launch(vs_captured *g, vs_stream_t stream) {
+  if (!g) return fail(VS_ERR_ARG, "null captured graph");
+  VS_CK(cudaGraphLaunch(g->exec, vs::S(stream)));
+  g_launches.fetch_add(g->kernels, std::memory_order_relaxed);
+  return VS_OK;
+}
+
+uint64_t vs_captured_kernels(const vs_captured *g) { return g ? g->kernels : 0; }
+
+int vs_captured_free(vs_captured *g) {
+  if (!g) return VS_OK;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+  return VS_OK;
+}
 
 int vs_init(int device) {
   VS_CK(cudaSetDevice(device));

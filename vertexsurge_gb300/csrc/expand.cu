@@ -96,6 +96,12 @@ __global__ void k_clear_flagged(uint4 *__restrict__ buf, uint32_t *__restrict__ 
 // Layer 0 (ExpandStatus::init_first_m_layer, expand_impl.hh:252-277).
 __global__ void k_seed(SeedArgs a) {
   unsigned long long pe = 0, nv = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {  // counters set on the device: the run has no host copies
+    a.ctr->multislice = a.multislice;
+    a.ctr->hop[0].pairs = a.S;
+    a.ctr->hop[0].new_bits = a.S;
+    if (a.rowk && a.rowk[1]) atomicOr(&a.ctr->error, 2);  // a device-set row limit exceeded k_max
+  }
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.S; i += gridDim.x * blockDim.x) {
     uint32_t v = a.sources[i];
     if (v >= a.V) {  // reported as VS_ERR_ARG; the pair stays in range
@@ -134,6 +140,31 @@ __global__ void k_dist_init(const uint32_t *__restrict__ src, const uint32_t *__
   block_add(f, &ctr->found);
 }
 
+// Per-hop row masks of batched queries from per-row hop limits: word w of
+// hop h has bit r set when row 64w+r may still grow at hop h.
+__global__ void k_row_mask(const uint8_t *__restrict__ lim, uint32_t n, uint32_t K, uint32_t W,
+                           uint64_t *__restrict__ hmask, uint32_t *rowk) {
+  const uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= W) return;
+  uint32_t kmax = 0, over = 0;
+  for (uint32_t r = 0; r < 64; r++) {
+    const uint32_t i = w * 64 + r;
+    const uint32_t l = i < n ? lim[i] : 0u;
+    over |= l > K;
+    kmax = max(kmax, min(l, K));
+  }
+  for (uint32_t h = 0; h <= K; h++) {
+    uint64_t m = 0;
+    for (uint32_t r = 0; h > 0 && r < 64; r++) {
+      const uint32_t i = w * 64 + r;
+      if (i < n && min((uint32_t)lim[i], K) >= h) m |= 1ull << r;
+    }
+    hmask[(size_t)h * W + w] = m;
+  }
+  if (kmax) atomicMax(&rowk[0], kmax);
+  if (over) rowk[1] = 1;
+}
+
 // One block of 64 threads: early-stop checks of hop h-1 (VExpand::after_child,
 // vexpand.cpp:222-284), the fixed planner's choice for hop h, and — when a
 // picker is loaded or features are logged — the feature vector of hop h and
@@ -146,6 +177,7 @@ __global__ void __launch_bounds__(64) k_decide(DecideArgs a) {
   HopCtr &prev = c->hop[a.h - 1];
   HopCtr &cur = c->hop[a.h];
   if (t == 0) {
+    if (!c->done && a.rowk && (uint32_t)a.h > a.rowk[0]) c->done = 1;  // every row is past its last hop
     if (!c->done && a.h >= 2) {
       if (a.path != VS_PATH_ANY && prev.new_bits == 0) c->done = 1;
       if (a.path == VS_PATH_FIND_SHORTEST && c->found >= a.S) c->done = 1;
@@ -907,6 +939,7 @@ struct vs_expand_plan {
   bool log_features = false;
   int pull_kind = 0;  // PULL kernel variant (bit 0: 8 blocks/SM bound, bit 1: L2 policies)
   uint64_t *hmask = nullptr;  // (k_max + 1) x W words: rows allowed to grow at hop h
+  uint32_t *rowk = nullptr;   // [0] largest row limit, [1] a limit exceeded k_max (device-set limits)
   bool use_hmask = false;
   int hop_forced[VS_MAX_HOPS + 1] = {};
   bool timing = false;
@@ -921,7 +954,7 @@ namespace ex {
 int plan_free(vs_expand_plan *pl) {
   if (!pl) return VS_OK;
   const cudaStream_t st = pl->last_stream;
-  void *ptrs[] = {pl->resflag, pl->pdeg[0], pl->pdeg[1], pl->doff, pl->bsum, pl->hmask, pl->buf[0], pl->buf[1], pl->flag[0], pl->flag[1], pl->vis, pl->acc,
+  void *ptrs[] = {pl->resflag, pl->pdeg[0], pl->pdeg[1], pl->doff, pl->bsum, pl->hmask, pl->rowk, pl->buf[0], pl->buf[1], pl->flag[0], pl->flag[1], pl->vis, pl->acc,
                   pl->pairs[0], pl->pairs[1], pl->push_list, pl->touched, pl->d_src,
                   pl->d_tgt, pl->d_dist, pl->ctr, pl->hubs};
   for (void *p : ptrs)  // stream-ordered after the plan's last run
@@ -1007,6 +1040,8 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
     PL_ALLOC(pl->d_dist, S);
   }
   PL_ALLOC(pl->ctr, 1);
+  PL_ALLOC(pl->hmask, (size_t)(p->k_max + 1) * pl->W);
+  PL_ALLOC(pl->rowk, 2);
 #undef PL_ALLOC
   cudaError_t e = cudaSuccess;
   if ((e = cudaMemsetAsync(pl->buf[0], 0, rowwords * 8, st)) != cudaSuccess ||
@@ -1085,6 +1120,9 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   const vs_graph *g = pl->g;
   const uint32_t V = g->V, S_ = pl->S, W = pl->W, Q = pl->Q;
   const size_t rowbytes = (size_t)V * W * 8;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  VS_CK(cudaStreamIsCapturing(st, &cap));
+  const bool timing = pl->timing && cap == cudaStreamCaptureStatusNone;  // events are not captured
   VS_TRY(copy_in(pl->d_src, sources, S_, st));
   if (pl->d_tgt) VS_TRY(copy_in(pl->d_tgt, targets, S_, st));
   // run start: clean frontier buffers, zero visited/accumulator/counters
@@ -1095,10 +1133,6 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   if (pl->vis) VS_CK(cudaMemsetAsync(pl->vis, 0, rowbytes, st));
   if (pl->acc) VS_CK(cudaMemsetAsync(pl->acc, 0, rowbytes, st));
   VS_CK(cudaMemsetAsync(pl->ctr, 0, sizeof(Ctr), st));
-  if (pl->nslices > 1) {
-    int one = 1;
-    VS_CK(cudaMemcpyAsync(&pl->ctr->multislice, &one, sizeof(int), cudaMemcpyHostToDevice, st));
-  }
   const Lists in = pull_lists(g, p.direction), outl = push_lists(g, p.direction);
   SeedArgs sa;
   sa.sources = pl->d_src;
@@ -1115,14 +1149,10 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   sa.out = outl;
   sa.ctr = pl->ctr;
   sa.V = V;
+  sa.multislice = pl->nslices > 1;
+  sa.rowk = pl->use_hmask ? pl->rowk : nullptr;
   { k_seed<<<std::max(1u, std::min((S_ + 255) / 256, (uint32_t)sm_count() * 4)), 256, 0, st>>>(sa); vs::note_launch(); }
   VS_CK(cudaGetLastError());
-  // layer 0 pair count
-  {
-    unsigned long long s64 = S_;
-    VS_CK(cudaMemcpyAsync(&pl->ctr->hop[0].pairs, &s64, sizeof(s64), cudaMemcpyHostToDevice, st));
-    VS_CK(cudaMemcpyAsync(&pl->ctr->hop[0].new_bits, &s64, sizeof(s64), cudaMemcpyHostToDevice, st));
-  }
   if (p.path_type == VS_PATH_FIND_SHORTEST)
     { k_dist_init<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(pl->d_src, pl->d_tgt,
                                                                               pl->d_dist, S_, V, pl->ctr); vs::note_launch(); }
@@ -1148,10 +1178,11 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     da.push_frac = pl->push_frac;
     da.picker = pl->picker;
     da.picker_on = p.use_picker;
+    da.rowk = pl->use_hmask ? pl->rowk : nullptr;
     da.W = W;
     da.k_min = p.k_min;
     da.k_max = p.k_max;
-    if (pl->timing) cudaEventRecord(pl->ev[3 * h], st);
+    if (timing) cudaEventRecord(pl->ev[3 * h], st);
     if (pl->collect_stats || pl->log_features || (pl->picker && p.use_picker))
       { k_hop_stats<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], outl, V, pl->ctr, h); vs::note_launch(); }
     { k_decide<<<1, 64, 0, st>>>(da); vs::note_launch(); }
@@ -1225,17 +1256,17 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.nhubs = pl->nhubs;
     a.ctr = pl->ctr;
     a.h = h;
-    if (pl->timing) cudaEventRecord(pl->ev[3 * h + 1], st);
+    if (timing) cudaEventRecord(pl->ev[3 * h + 1], st);
     { var.pull[pl->pull_kind]<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a); vs::note_launch(); }
     if (pl->nhubs)
       { var.hub<<<dim3(pl->grid_hub, pl->nslices), 512, 16 * 32 * 16 * var.UPL, st>>>(a); vs::note_launch(); }
     if (p.path_type == VS_PATH_FIND_SHORTEST)
       { k_find_check<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(
           pl->buf[nbuf], pl->d_tgt, pl->d_dist, S_, W, V, pl->ctr, h); vs::note_launch(); }
-    if (pl->timing) cudaEventRecord(pl->ev[3 * h + 2], st);
+    if (timing) cudaEventRecord(pl->ev[3 * h + 2], st);
     VS_CK(cudaGetLastError());
   }
-  pl->timed_hops = pl->timing ? p.k_max : 0;
+  pl->timed_hops = timing ? p.k_max : 0;
   if (pl->clear_diag)
     { k_clear_diag<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(pl->vis, pl->d_src,
                                                                                 S_, W, V); vs::note_launch(); }
@@ -1274,6 +1305,7 @@ int vs_expand_plan_stats(vs_expand_plan *pl, vs_expand_stats *stats, vs_stream_t
   VS_CK(cudaMemcpyAsync(&h, pl->ctr, sizeof(Ctr), cudaMemcpyDeviceToHost, S(stream)));
   VS_CK(cudaStreamSynchronize(S(stream)));
   std::memset(stats, 0, sizeof(*stats));
+  if (h.error & 2) return fail(VS_ERR_ARG, "a row hop limit set on the device exceeds k_max %u", pl->p.k_max);
   if (h.error) return fail(VS_ERR_ARG, "a source or target vertex id is >= V (%u)", pl->g->V);
   stats->hops_run = (uint32_t)h.hops_run;
   stats->found = (uint32_t)h.found;
@@ -1339,17 +1371,38 @@ int vs_expand_plan_set_row_limits(vs_expand_plan *pl, const uint8_t *row_kmax, u
   const uint32_t K = pl->p.k_max, W = pl->W;
   std::vector<uint64_t> m((size_t)(K + 1) * W, 0);
   bool all = true;
+  uint32_t rk[2] = {0, 0};
   for (uint32_t i = 0; i < n; i++) {
     if (row_kmax[i] > K) return fail(VS_ERR_ARG, "row %u hop limit %u exceeds k_max %u", i, row_kmax[i], K);
     all &= row_kmax[i] == K;
+    rk[0] = std::max<uint32_t>(rk[0], row_kmax[i]);
     for (uint32_t h = 1; h <= row_kmax[i]; h++) m[(size_t)h * W + i / 64] |= 1ull << (i % 64);
   }
-  if (all) {
-    pl->use_hmask = false;
-    return VS_OK;
-  }
-  if (!pl->hmask) VS_TRY(dalloc_n(&pl->hmask, m.size(), 0));
+  // the mask is written even when unused, so a run captured with limits stays right
+  VS_CK(cudaStreamSynchronize(pl->last_stream));  // no earlier run still reads the mask
   VS_CK(cudaMemcpy(pl->hmask, m.data(), 8 * m.size(), cudaMemcpyHostToDevice));
+  VS_CK(cudaMemcpy(pl->rowk, rk, sizeof(rk), cudaMemcpyHostToDevice));
+  pl->use_hmask = !all;
+  return VS_OK;
+}
+
+// Row limits from a device array, stream-ordered (capturable): the mask of
+// every hop is built by k_row_mask; rows at index >= n get limit 0 (they
+// never grow).  A limit above k_max is clamped and reported as VS_ERR_ARG by
+// the next run.
+int vs_expand_plan_set_row_limits_device(vs_expand_plan *pl, const uint8_t *row_kmax, uint32_t n,
+                                         vs_stream_t stream) {
+  if (!pl || !row_kmax) return fail(VS_ERR_ARG, "vs_expand_plan_set_row_limits_device: null argument");
+  if (n > pl->S) return fail(VS_ERR_ARG, "%u row limits for a plan of %u rows", n, pl->S);
+  cudaStream_t st = S(stream);
+  if (st != pl->last_stream) {
+    VS_CK(cudaStreamSynchronize(pl->last_stream));
+    pl->last_stream = st;
+  }
+  VS_CK(cudaMemsetAsync(pl->rowk, 0, 2 * sizeof(uint32_t), st));
+  const uint32_t W = pl->W;
+  { k_row_mask<<<(W + 255) / 256, 256, 0, st>>>(row_kmax, n, pl->p.k_max, W, pl->hmask, pl->rowk); vs::note_launch(); }
+  VS_CK(cudaGetLastError());
   pl->use_hmask = true;
   return VS_OK;
 }

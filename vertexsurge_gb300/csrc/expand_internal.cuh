@@ -29,7 +29,7 @@ struct Ctr {
   int hops_run;              // k_actual_max
   int multislice;            // PULL runs in several source slices
   unsigned push_active, push_touched;
-  int error;  // a source or target id was >= V (the offending entry was skipped)
+  int error;  // bit 0: a source or target id was >= V (entry skipped); bit 1: a row limit > k_max
   float feat[VS_MAX_HOPS + 1][32];  // picker features of every hop (when logged)
 };
 
@@ -52,6 +52,8 @@ struct SeedArgs {
   unsigned long long *pdeg0;  // out-degree of every seeded pair's vertex
   Lists out;
   Ctr *ctr;
+  int multislice;  // PULL runs in several source slices
+  const uint32_t *rowk;  // row-limit words of the plan (NULL: no row limits)
 };
 
 struct DecideArgs {
@@ -61,6 +63,7 @@ struct DecideArgs {
   uint64_t E, pair_cap;
   double sparse_frac, push_frac;
   const void *picker;  // bf16 weights of a vs_picker (NULL = fixed planner)
+  const uint32_t *rowk;  // [0] largest row hop limit (NULL: no row limits)
 };
 
 struct SparseArgs {

@@ -478,6 +478,52 @@ __global__ void k_noalloc_clear(unsigned long long *keys, unsigned long long *cn
   if (blockIdx.x == 0 && threadIdx.x == 0) *total = 0;
 }
 
+// ---------------------------------------------------------------------------
+// Batched join counts over the row blocks of one matrix (batched expand
+// results): blockIdx.y is the row block; its warps take chunks of RB_CHUNK
+// keys in turn.  A key's column slice of the block (nw words) is read by a
+// group of G = min(32, pow2 >= nw) lanes, so narrow blocks put several keys
+// in one warp.  The table of blocks travels as a kernel parameter.
+constexpr int RB_CHUNK = 256;
+struct RowBlocks {
+  vs_row_block b[VS_MAX_ROW_BLOCKS];
+};
+
+__global__ void __launch_bounds__(256) k_count_row_blocks(const __grid_constant__ RowBlocks tab,
+                                                          const uint32_t *__restrict__ keys,
+                                                          const uint64_t *__restrict__ w, uint32_t wpc,
+                                                          uint32_t cols, const uint32_t *__restrict__ colnz,
+                                                          unsigned long long *__restrict__ counts) {
+  const vs_row_block rb = tab.b[blockIdx.y];
+  if (rb.row_end <= rb.row_begin || rb.key_end <= rb.key_begin) return;
+  const uint32_t w0 = rb.row_begin >> 6, nw = ((rb.row_end - 1) >> 6) - w0 + 1;
+  const uint64_t m_first = ~0ull << (rb.row_begin & 63);
+  const uint64_t m_last = ~0ull >> (63 - ((rb.row_end - 1) & 63));
+  uint32_t G = 1;
+  while (G < 32 && G < nw) G <<= 1;
+  const uint32_t lane = threadIdx.x & 31, grp = lane / G, gl = lane % G, ngrp = 32 / G;
+  const uint64_t nkeys = rb.key_end - rb.key_begin;
+  const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  const uint32_t *kp = keys + rb.key_begin;
+  unsigned long long s = 0;
+  for (uint64_t base = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * RB_CHUNK;
+       base < nkeys; base += nwarps * RB_CHUNK) {
+    const uint64_t end = min(base + RB_CHUNK, nkeys);
+    for (uint64_t k = base + grp; k < end; k += ngrp) {
+      const uint32_t key = __ldg(kp + k);
+      if (key >= cols || (colnz && !__ldg(colnz + key))) continue;  // no such vertex / empty column
+      const uint64_t *col = w + (size_t)key * wpc + w0;
+      for (uint32_t j = gl; j < nw; j += G) {
+        uint64_t x = __ldg(col + j);
+        if (j == 0) x &= m_first;
+        if (j == nw - 1) x &= m_last;
+        s += __popcll(x);
+      }
+    }
+  }
+  block_add(s, counts + blockIdx.y);
+}
+
 }  // namespace jn
 }  // namespace vs
 
@@ -553,6 +599,44 @@ int vs_hash_join_count_noalloc(const void *keys_a, uint64_t na, const void *keys
   VS_CK(cudaGetLastError());
   VS_CK(cudaMemcpyAsync(count, total, sizeof(unsigned long long), cudaMemcpyDefault, st));
   VS_CK(cudaStreamSynchronize(st));
+  return VS_OK;
+}
+
+int vs_hash_join_count_row_blocks(const vs_bitmat *m, const uint32_t *keys, const vs_row_block *blocks,
+                                  uint32_t nblocks, uint64_t *counts, vs_stream_t stream) {
+  if (!m || !blocks || !counts || nblocks == 0)
+    return fail(VS_ERR_ARG, "vs_hash_join_count_row_blocks: null argument or no block");
+  if (nblocks > VS_MAX_ROW_BLOCKS)
+    return fail(VS_ERR_ARG, "%u row blocks; at most %d per call", nblocks, VS_MAX_ROW_BLOCKS);
+  if (m->kind != VS_KIND_VARROW || m->col_map)
+    return fail(VS_ERR_ARG, "row-block join counts need a VarRow matrix whose columns are vertex ids");
+  RowBlocks tab{};
+  uint64_t max_keys = 0;
+  for (uint32_t q = 0; q < nblocks; q++) {
+    const vs_row_block &b = blocks[q];
+    if (b.row_begin > b.row_end || b.row_end > m->rows || b.key_begin > b.key_end)
+      return fail(VS_ERR_ARG, "row block %u: rows [%u, %u) of %u, keys [%llu, %llu)", q, b.row_begin,
+                  b.row_end, m->rows, (unsigned long long)b.key_begin, (unsigned long long)b.key_end);
+    tab.b[q] = b;
+    max_keys = std::max<uint64_t>(max_keys, b.key_end - b.key_begin);
+  }
+  if (max_keys && !keys) return fail(VS_ERR_ARG, "vs_hash_join_count_row_blocks: null keys");
+  for (const void *p : {(const void *)keys, (const void *)counts}) {
+    if (!p) continue;
+    cudaPointerAttributes at{};
+    VS_CK(cudaPointerGetAttributes(&at, p));
+    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+      return fail(VS_ERR_ARG, "vs_hash_join_count_row_blocks: keys and counts must be device memory");
+  }
+  cudaStream_t st = S(stream);
+  VS_CK(cudaMemsetAsync(counts, 0, sizeof(uint64_t) * nblocks, st));
+  if (max_keys == 0 || m->rows == 0) return VS_OK;
+  const uint64_t warps_needed = (max_keys + RB_CHUNK - 1) / RB_CHUNK;
+  const uint32_t gx = (uint32_t)std::min<uint64_t>((warps_needed + 7) / 8, (uint64_t)sm_count() * 8);
+  { k_count_row_blocks<<<dim3(gx, nblocks), 256, 0, st>>>(tab, keys, m->words, m->wpc, m->cols, m->colnz,
+                                                          reinterpret_cast<unsigned long long *>(counts));
+    vs::note_launch(); }
+  VS_CK(cudaGetLastError());
   return VS_OK;
 }
 

@@ -54,11 +54,11 @@ WORKLOADS = {
     # 1e5..1e7 vertex-id keys each) on the 10M-vertex graph, one CUDA-graph launch per batch
     "zipf10M_batched256": dict(kind="zipf", V=10_000_000, E=300_000_000, alpha=2.1, cap=50_000, seed=3,
                                batched=dict(n=256, s_range=(64, 8192), l_range=(2, 6),
-                                            join_rows=(100_000, 10_000_000), waves=(16384, 32768),
+                                            join_rows=(100_000, 10_000_000), waves=(8192, 16384, 32768),
                                             cpu_queries=3, check=6)),
     "zipf1M_batched64": dict(kind="zipf", V=1_000_000, E=30_000_000, alpha=2.1, cap=50_000, seed=3,
                              batched=dict(n=64, s_range=(64, 8192), l_range=(2, 6),
-                                          join_rows=(100_000, 1_000_000), waves=(16384, 32768),
+                                          join_rows=(100_000, 1_000_000), waves=(8192, 16384, 32768),
                                           cpu_queries=3, check=6)),
 }
 
@@ -132,13 +132,14 @@ class ClockSampler:
                                    default=None)}
 
 
-def expand_bytes(V, W, e_act, shortest, acc):
+def expand_bytes(V, W, e_act, shortest, acc, gathers=True):
     """Algorithmic bytes of one hop: CSR offsets + targets, one row gather per
     active edge (32-byte sector minimum) and P streaming passes over the V x S
     matrices (P = 4 for the frontier/next pair plus visited or accumulator
-    read+write each)."""
+    read+write each).  gathers=False gives the compulsory bytes alone (every
+    frontier row read once instead of once per edge)."""
     P = 2 + (2 if shortest else 0) + (2 if acc else 0)
-    return 8 * (V + 1) + 4 * e_act + e_act * max(32, 8 * W) + P * 8 * W * V
+    return 8 * (V + 1) + 4 * e_act + (e_act * max(32, 8 * W) if gathers else 0) + P * 8 * W * V
 
 
 def cpu_baseline(g, w, sa):
@@ -161,7 +162,7 @@ def cpu_baseline(g, w, sa):
 def batched_queries(g, w):
     from vertexsurge_gb300 import batch
     bw = w["batched"]
-    return batch.make_queries(g, bw["n"], bw["s_range"], bw["l_range"], bw["join_rows"], seed=9)
+    return batch.make_queries(g, bw["n"], bw["s_range"], bw["l_range"], bw["join_rows"], seed=4)
 
 
 def cpu_batched(g, w, queries):
@@ -169,10 +170,10 @@ def cpu_batched(g, w, queries):
     a time as the reference runs them, on a bounded sample: the first queries
     of the trace with at most 2,048 sources."""
     from oracle import pyoracle as O
-    sample = [q for q in queries if len(q.sources) <= 2048][: w["batched"]["cpu_queries"]]
+    idx = [i for i, q in enumerate(queries) if len(q.sources) <= 2048][: w["batched"]["cpu_queries"]]
     t = time.perf_counter()
     counts = []
-    for q in sample:
+    for q in (queries[i] for i in idx):
         words, _, _ = O.vexpand(g, q.sources, 1, q.k_max, "shortest", "forward")
         # the reference's HashJoin takes ColMain matrices: TableConvert first
         cm = O.table_convert(words, len(q.sources), g.V, False)
@@ -181,7 +182,7 @@ def cpu_batched(g, w, queries):
         counts.append(O.hash_join(k, a, 1, only_count=True)[2])
         del words, cm, a
     dt = time.perf_counter() - t
-    return sample, counts, dt
+    return idx, counts, dt
 
 
 def run_reference_batched(args, w):
@@ -240,10 +241,21 @@ def run_gpu_batched(args, w, rank, world, local_rank):
     t0 = time.time()
     from vertexsurge_gb300 import graphgen
     tsrc = graphgen.sample_sources(g.V, min(bw["waves"]), seed=77)
+    tc = args.tune_cache or None
     setting = autotune.tune(dg, tsrc, 1, 4, "shortest", "forward", stream=stream, repeats=1,
-                            pull_kinds=(0,), sparse_fracs=(0.002, 0.02), hub_thresholds=(0, 256))
+                            pull_kinds=(0,), sparse_fracs=(0.002, 0.02), hub_thresholds=(0, 256),
+                            cache_file=tc)
     setting = {k: setting[k] for k in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words", "ms")}
-    waves = batch.tune_wave_rows(dg, queries, stream, candidates=bw["waves"], setting=setting)
+    wkey = f"waves|{args.workload}"
+    cached = json.loads(Path(tc).read_text()) if tc and Path(tc).exists() else {}
+    if wkey in cached:
+        waves = cached[wkey]
+    else:
+        waves = batch.tune_wave_rows(dg, queries, stream, candidates=bw["waves"], setting=setting)
+        if tc:
+            cached = json.loads(Path(tc).read_text()) if Path(tc).exists() else {}
+            cached[wkey] = waves
+            Path(tc).write_text(json.dumps(cached, indent=1))
     log(f"[rank {rank}] autotune {time.time() - t0:.1f}s: {setting} waves {waves}")
     bt = batch.Batch(dg, queries, waves["wave_rows"], stream, setting=setting)
     cg = bt.capture()
@@ -261,11 +273,13 @@ def run_gpu_batched(args, w, rank, world, local_rank):
     clocks = ClockSampler(local_rank)
     launches0 = vs.kernel_launches()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed")
     ev0.record(stream)
     for _ in range(args.steps):
         bt.launch()
     ev1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     launches = vs.kernel_launches() - launches0
     ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
@@ -330,8 +344,7 @@ def run_gpu_batched(args, w, rank, world, local_rank):
     cpu = None
     if world == 1 and not args.no_cpu:
         sample, ccounts, dt = cpu_batched(g, w, queries)
-        idx = [queries.index(q) for q in sample]
-        assert [int(counts[i]) for i in idx] == ccounts, "oracle counts differ from the batch"
+        assert [int(counts[i]) for i in sample] == ccounts, "oracle counts differ from the batch"
         from oracle import pyoracle as O
         cpu = {"value": len(sample) / dt, "unit": "queries/s", "cores": O.lib().oracle_get_threads(),
                "kind": "port", "sample": f"{len(sample)} queries with <= 2048 sources, one at a time, {dt:.1f} s"}
@@ -417,9 +430,10 @@ def run_gpu(args, w, rank, world, local_rank):
     # autotuned PULL kernel shape, SPARSE threshold and hub bin per expand (untimed)
     from vertexsurge_gb300 import autotune
     t0 = time.time()
-    tA = autotune.tune(dg, sa, ka[0], ka[1], "shortest", "forward", stream=stream)
-    tB = autotune.tune(dg, sb, kb[0], kb[1], "shortest", "forward", stream=stream)
-    tP = autotune.tune(dg, sa, 1, 1, "any", "forward", stream=stream)
+    tc = args.tune_cache or None
+    tA = autotune.tune(dg, sa, ka[0], ka[1], "shortest", "forward", stream=stream, cache_file=tc)
+    tB = autotune.tune(dg, sb, kb[0], kb[1], "shortest", "forward", stream=stream, cache_file=tc)
+    tP = autotune.tune(dg, sa, 1, 1, "any", "forward", stream=stream, cache_file=tc)
     tuned = {k: {x: t[x] for x in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words", "ms")}
              for k, t in (("A", tA), ("B", tB), ("P", tP))}
     log(f"[rank {rank}] autotune {time.time() - t0:.1f}s: {tuned}")
@@ -462,9 +476,10 @@ def run_gpu(args, w, rank, world, local_rank):
     clocks = ClockSampler(local_rank)
     launches0 = vs.kernel_launches()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    pull_ms, pull_bytes = 0.0, 0.0
+    pull_ms, pull_bytes, pull_comp = 0.0, 0.0, 0.0
     W = (Sa + 63) // 64
     W += W & 1
+    torch.cuda.nvtx.range_push("timed")
     ev0.record(stream)
     for _ in range(args.steps):
         step()
@@ -473,8 +488,10 @@ def run_gpu(args, w, rank, world, local_rank):
             if st["strategy"][h] == vs.STRAT_PULL:
                 pull_ms += st["pull_ms"][h]
                 pull_bytes += expand_bytes(g.V, W, stA["active_edges"][h], True, False)
+                pull_comp += expand_bytes(g.V, W, stA["active_edges"][h], True, False, gathers=False)
     ev1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     launches = vs.kernel_launches() - launches0
     ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
@@ -560,6 +577,7 @@ def run_gpu(args, w, rank, world, local_rank):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if achieved else None, "traffic": None,
                 "kernel": "k_pull (expand A, pull hops)", "peak_source": peak_kind,
+                "compulsory_frac": (pull_comp / (pull_ms / 1e3) / 1e9) / peak if pull_ms else None,
                 "per_launch_ms": pull_ms / max(1, args.steps * sum(1 for s in stA["strategy"][1:] if s == 1))}
     cpu = None
     if world == 1 and not args.no_cpu:
@@ -594,6 +612,8 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="zipf10M_pattern")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--tune-cache", default="", help="JSON file of autotuner results (read if present, "
+                    "written otherwise)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

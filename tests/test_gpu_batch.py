@@ -91,3 +91,20 @@ def test_batch_counts_equal_solo(vs, graphs, wave_rows):
         b.launch()
         assert np.array_equal(b.counts(), solo)
     b.free()
+
+
+def test_source_sharding_local_counts_sum_to_whole(vs, graphs):
+    """Per-rank shares of the pattern query, computed one rank after another
+    on this GPU (independent launches), sum to the unsharded counts, which
+    equal the oracle engine's."""
+    from tests.shard_oracle_engine import OracleEngine
+    from vertexsurge_gb300 import shard
+    g, dg = graphs["zipf3000"]
+    eng = shard.GpuEngine(dg, g.V)
+    sa = graphgen.sample_sources(g.V, 300, seed=21)
+    sb = graphgen.sample_sources(g.V, 120, seed=22)
+    whole = shard.local_counts(eng, sa, sb, (1, 3), (1, 2), 0, 1)
+    assert whole == shard.local_counts(OracleEngine(g), sa, sb, (1, 3), (1, 2), 0, 1)
+    for world in (2, 3, 8):
+        parts = [shard.local_counts(eng, sa, sb, (1, 3), (1, 2), r, world) for r in range(world)]
+        assert [sum(x) for x in zip(*parts)] == whole, world

@@ -39,3 +39,18 @@ def test_rmat16_512_sources_hops_1_3(vs, rmat16, path):
     d = words_to_bool(sel.download(), len(src))
     assert int(d[np.arange(len(src)), np.arange(len(src))].sum()) == ring
     m.free()
+
+
+def test_rmat16_e1_self_ring_count(vs, rmat16):
+    """e1-style count: Count(MatrixTableSelect(VExpand(S, Both, Shortest, [0,3]), T=S))
+    = #{(a, b) in S x S : dist(a, b) <= 3}, a = b included."""
+    g, dg = rmat16
+    src = graphgen.sample_sources(g.V, 512, seed=2)
+    m, _, _ = vs.expand(dg, src, 0, 3, "shortest", "both")
+    sel = m.select(src)
+    got = sel.count()
+    exp_w, _, _ = O.vexpand(g, src, 0, 3, "shortest", "both")
+    exp = O.matrix_count(O.matrix_select(exp_w, len(src), g.V, src), len(src), len(src))
+    assert got == exp >= len(src)
+    sel.free()
+    m.free()

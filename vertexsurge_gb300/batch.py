@@ -31,20 +31,31 @@ class Query:
     keys: np.ndarray      # uint32 vertex ids of the joined table
 
 
+def zipf_keys(rng, n: int, V: int, perm: np.ndarray, s: float = 1.2) -> np.ndarray:
+    """n vertex ids Zipf-skewed over V: rank r has probability ~ r^-s (Pareto
+    inverse transform, ranks folded into [0, V)), and ranks map to vertices
+    through a fixed permutation so the hot keys are spread over the graph."""
+    u = rng.random(n)
+    r = np.floor(np.power(1.0 - u, -1.0 / (s - 1.0))).astype(np.float64) - 1.0
+    r = np.mod(r, V).astype(np.int64)
+    return perm[r].astype(np.uint32)
+
+
 def make_queries(g, n: int, s_range=(64, 8192), l_range=(2, 6), join_rows=(100_000, 10_000_000),
-                 seed: int = 9) -> list:
+                 seed: int = 4, key_skew: float = 1.2) -> list:
     """Source counts log-uniform in s_range, last hop uniform in l_range, key
-    tables with log-uniform row counts in join_rows and uniform vertex ids."""
+    tables of (key, payload) pairs with row counts uniform in join_rows and
+    keys Zipf-skewed over the vertices (only the key column enters a count)."""
     rng = np.random.default_rng(seed)
+    perm = rng.permutation(g.V).astype(np.uint32)
     out = []
     for _ in range(n):
         S = int(round(math.exp(rng.uniform(math.log(s_range[0]), math.log(s_range[1])))))
         S = max(1, min(S, g.V))
         src = graphgen.sample_sources(g.V, S, seed=int(rng.integers(1 << 30)))
         l = int(rng.integers(l_range[0], l_range[1] + 1))
-        nk = int(round(math.exp(rng.uniform(math.log(join_rows[0]), math.log(join_rows[1])))))
-        keys = rng.integers(0, g.V, nk, dtype=np.uint32)
-        out.append(Query(src, l, keys))
+        nk = int(rng.integers(join_rows[0], join_rows[1] + 1))
+        out.append(Query(src, l, zipf_keys(rng, nk, g.V, perm, key_skew)))
     return out
 
 

@@ -90,7 +90,7 @@ def build_gen() -> Path:
 
 
 def build_ops() -> Path:
-    srcs = [PKG / "cpp" / "vs_operators.cpp"]
+    srcs = [PKG / "cpp" / "vs_operators.cpp", PKG / "cpp" / "graph_dir.cpp"]
     hdrs = [PKG / "cpp" / "vs_operators.hh", ROOT / "include" / "vertexsurge_gb300.h"]
     if not srcs[0].exists():
         return OPS_LIB

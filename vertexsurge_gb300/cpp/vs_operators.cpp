@@ -160,7 +160,10 @@ const Graph::EdgeType &Graph::edge(const TypeName &src, const TypeName &e, const
   return it->second;
 }
 
-void Graph::load() { BigOperator::graph_store = this; }
+void Graph::load() {
+  if (!dir.empty()) load_dir();
+  BigOperator::graph_store = this;
+}
 
 // ---- operator runtime (PhysicalOperator::run, physical_operator.cpp:62-101) ----
 void BigOperator::addDependency(SharedBigOperator d) {

@@ -16,6 +16,7 @@
 // exits; see vexpand.cpp:88-91, join.cpp:82-85).
 #pragma once
 #include <cstdint>
+#include <filesystem>
 #include <map>
 #include <memory>
 #include <optional>
@@ -126,15 +127,29 @@ class Graph {
   };
   std::map<TypeName, size_t> vertex_count;
   std::map<std::string, EdgeType> edges;
+  std::filesystem::path dir;  // the reference's graph directory (empty: types added by hand)
+  Graph() = default;
+  // Graph(dir) + load(): schema.json and the CSR DiskArray files the reference
+  // writes and reads (storage/graph_store.cpp:46-73)
+  explicit Graph(std::filesystem::path d) : dir(std::move(d)) {}
+  Graph(const Graph &) = delete;
+  Graph &operator=(const Graph &) = delete;
   ~Graph();
   void add_vertex_type(const TypeName &t, size_t count) { vertex_count[t] = count; }
   void add_edge_type(const TypeName &src, const TypeName &edge, const TypeName &dst, bool directed,
                      uint32_t V, uint64_t E, const int64_t *fwd_off, const uint32_t *fwd_dst,
                      const int64_t *rev_off, const uint32_t *rev_src);
   const EdgeType &edge(const TypeName &src, const TypeName &e, const TypeName &dst) const;
-  // Graph::load sets the global store (graph_store.cpp:48-73)
+  // Graph::load sets the global store (graph_store.cpp:48-73); with a
+  // directory it first uploads every self edge type's CSR found there
   void load();
+
+ private:
+  void load_dir();
 };
+// Variable names of an edge type's CSR files (meta/schema.cpp:36-66)
+std::string forward_edge_name(const TypeName &src, const TypeName &e, const TypeName &dst, bool directed);
+std::string backward_edge_name(const TypeName &src, const TypeName &e, const TypeName &dst, bool directed);
 
 class BigOperator;
 using SharedBigOperator = std::shared_ptr<BigOperator>;

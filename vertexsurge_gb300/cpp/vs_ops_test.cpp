@@ -314,8 +314,30 @@ static bool plans_case(const HostGraph &hg) {
   return ok;
 }
 
-int main() {
+// Reads a graph directory in the reference's layout through Graph(dir).load()
+// and prints Count(VExpand(sources i*7 mod V for i < 100, Forward, Shortest,
+// [1,3])) over its first self edge type.
+static int graph_dir_count(const char *dir) {
+  Graph g{std::filesystem::path(dir)};
+  g.load();
+  if (g.edges.empty()) throw Error(VS_ERR_ARG, "no self edge type in the graph directory");
+  const Graph::EdgeType &et = g.edges.begin()->second;
+  const uint64_t V = g.vertex_count.at(et.src);
+  vector<uint64_t> s;
+  for (uint64_t i = 0; i < std::min<uint64_t>(V, 100); i++) s.push_back((i * 7) % V);
+  auto ve = make_shared<VExpand>(et.src, et.dst, et.name, Direction::Forward, 1, 3, ExpandPathType::Shortest,
+                                 ExpandStrategy::Dense, "a.id", "b.id");
+  ve->addLastDependency(ids("a.id", s));
+  auto cnt = make_shared<Count>();
+  cnt->addLastDependency(ve);
+  cnt->run();
+  std::printf("count %lld\n", (long long)single_count(cnt->results.get()));
+  return 0;
+}
+
+int main(int argc, char **argv) {
   check(vs_init(0));
+  if (argc >= 3 && std::string(argv[1]) == "--graph-dir") return graph_dir_count(argv[2]);
   // like the reference's tests, load a graph first: operators resolve vertex types against it
   HostGraph hg = small_graph();
   Graph g;

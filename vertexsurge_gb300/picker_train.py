@@ -1,11 +1,13 @@
 """Training data, training and evaluation of the learned per-hop strategy picker.
 
 Data comes from the method's own runs.  For every logged query the expand is
-run once per strategy family — every hop PULL, every hop PUSH, and SPARSE for
-as long as its pair list lasts — with per-hop CUDA-event timing and feature
-logging on.  All runs of a query see the same frontier at every hop (the
-strategy never changes a result), so each hop yields samples
-(features, fastest strategy):
+run once per strategy family — every hop PULL; PUSH at every hop whose
+frontier holds under PUSH_CAP of the vertices (a PUSH hop over a denser
+frontier is an atomic write per edge and row, always far slower than PULL, and
+is counted as not chosen); SPARSE for as long as its pair list lasts — with
+per-hop CUDA-event timing and feature logging on.  All runs of a query see the
+same frontier at every hop (the strategy never changes a result), so each hop
+yields samples (features, fastest strategy):
   * from the SPARSE run while SPARSE is still possible (features say a pair
     list exists): label = fastest of PULL / PUSH / SPARSE at that hop;
   * from the PULL run (features say no pair list): label = fastest of
@@ -30,6 +32,7 @@ from . import graphgen
 
 WEIGHTS_FILE = Path(__file__).resolve().parent / "picker_weights.npy"
 STRATS = (vs.STRAT_PULL, vs.STRAT_PUSH, vs.STRAT_SPARSE)  # class 0, 1, 2
+PUSH_CAP = 0.05  # PUSH is timed at hops whose frontier holds fewer than this fraction of V
 
 
 @dataclass
@@ -46,19 +49,25 @@ class Samples:
                 np.asarray(self.query, np.int64))
 
 
-def graph_suite(scales=(16, 17, 18), skews=(0.45, 0.57, 0.65), zipf=((200_000, 4_000_000),)):
+def graph_suite(scales=(20, 21, 22, 23, 24), skews=(0.45, 0.57, 0.65), zipf=((10_000_000, 300_000_000),),
+                small=(16,)):
+    """R-MAT graphs at `scales` x skews a (b = c = (1 - a - 0.05) / 2), the
+    small R-MAT of the plain-method configuration and the power-law graph of
+    the pattern query."""
     gs = []
     for sc in scales:
         for a in skews:
             b = (1.0 - a - 0.05) / 2
             gs.append(graphgen.rmat(sc, 16, a, b, b, seed=sc * 100 + int(a * 100)))
+    for sc in small:
+        gs.append(graphgen.rmat(sc, 16, 0.57, 0.19, 0.19, seed=1))
     for V, E in zipf:
-        gs.append(graphgen.zipf(V, E, 2.1, min(50_000, V // 4), seed=V % 997))
+        gs.append(graphgen.zipf(V, E, 2.1, min(50_000, V // 4), seed=3))
     return gs
 
 
-def _run(plan, src, forced, k_max):
-    plan.set_hop_strategies([0] + [forced] * k_max)
+def _run(plan, src, strategies):
+    plan.set_hop_strategies([0] + list(strategies))
     plan.run(src)
     st = plan.stats()
     return st, plan.features()
@@ -70,19 +79,24 @@ def log_query(dg, g, S, k_max, path, direction, seed, out: Samples, qid: int):
     plan.set_tuning(timing=True)
     plan.log_features(True)
     try:
-        _log_runs(plan, src, k_max, out, qid)
+        _log_runs(plan, src, k_max, g.V, out, qid)
     finally:
         plan.free()
 
 
-def _log_runs(plan, src, k_max, out: Samples, qid: int):
-    runs = {}
-    for s in STRATS:
-        runs[s] = _run(plan, src, s, k_max)
-    st_auto, f_auto = _run(plan, src, vs.STRAT_AUTO, k_max)
+def _log_runs(plan, src, k_max, V, out: Samples, qid: int):
+    runs = {vs.STRAT_PULL: _run(plan, src, [vs.STRAT_PULL] * k_max)}
+    av = runs[vs.STRAT_PULL][0]["active_vertices"]
+    push_at = [h for h in range(1, k_max + 1) if h - 1 < len(av) and av[h - 1] < PUSH_CAP * V]
+    runs[vs.STRAT_PUSH] = _run(plan, src, [vs.STRAT_PUSH if h in push_at else vs.STRAT_PULL
+                                           for h in range(1, k_max + 1)])
+    runs[vs.STRAT_SPARSE] = _run(plan, src, [vs.STRAT_SPARSE] * k_max)
+    st_auto, f_auto = _run(plan, src, [vs.STRAT_AUTO] * k_max)
     hops = runs[vs.STRAT_PULL][0]["hops_run"]
     for h in range(1, hops + 1):
         t = {s: runs[s][0]["hop_ms"][h] if h <= runs[s][0]["hops_run"] else math.inf for s in STRATS}
+        if h not in push_at:
+            t[vs.STRAT_PUSH] = math.inf
         sp_st = runs[vs.STRAT_SPARSE][0]
         sparse_ok = h <= sp_st["hops_run"] and sp_st["strategy"][h] == vs.STRAT_SPARSE
         fixed_class = STRATS.index(st_auto["strategy"][h]) if h <= st_auto["hops_run"] else 0
@@ -105,14 +119,24 @@ def _log_runs(plan, src, k_max, out: Samples, qid: int):
             out.query.append(qid)
 
 
-def collect(n_queries: int, seed: int = 1, graphs=None, log=print) -> Samples:
+def collect(n_queries: int, seed: int = 1, graphs=None, log=print, minutes: float = 0.0,
+            target_samples: int = 0) -> Samples:
+    """Log up to n_queries queries (stopping early after `minutes` of logging or
+    at `target_samples` samples); graphs are drawn with weight 1/E so small and
+    large graphs contribute similar logging time."""
     rng = np.random.default_rng(seed)
     graphs = graphs or graph_suite()
     dgs = [vs.DeviceGraph.from_host(g) for g in graphs]
+    w = np.array([1.0 / max(1, g.E) for g in graphs])
+    w /= w.sum()
     out = Samples()
     t0 = time.time()
     for q in range(n_queries):
-        gi = int(rng.integers(len(graphs)))
+        if minutes and time.time() - t0 > 60 * minutes:
+            break
+        if target_samples and len(out.y) >= target_samples:
+            break
+        gi = int(rng.choice(len(graphs), p=w))
         S = int(round(math.exp(rng.uniform(math.log(64), math.log(8192)))))
         S = max(1, min(S, graphs[gi].V))
         k_max = int(rng.integers(2, 7))
@@ -160,20 +184,25 @@ def train_and_evaluate(samples: Samples, epochs=40, seed=3, holdout=0.2):
 def main():
     import argparse
     ap = argparse.ArgumentParser(description="log, train and evaluate the strategy picker")
-    ap.add_argument("--queries", type=int, default=4000)
+    ap.add_argument("--queries", type=int, default=100_000)
+    ap.add_argument("--samples", type=int, default=100_000, help="stop logging at this many samples")
+    ap.add_argument("--minutes", type=float, default=0.0, help="stop logging after this long (0: no limit)")
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--out", default=str(WEIGHTS_FILE))
     ap.add_argument("--report", default="")
-    ap.add_argument("--scales", default="16,17,18")
+    ap.add_argument("--scales", default="20,21,22,23,24")
+    ap.add_argument("--no-zipf", action="store_true", help="leave out the 10M-vertex power-law graph")
     args = ap.parse_args()
     vs.init(0)
     scales = tuple(int(x) for x in args.scales.split(","))
     t0 = time.time()
-    samples = collect(args.queries, graphs=graph_suite(scales=scales))
+    graphs = graph_suite(scales=scales, zipf=() if args.no_zipf else ((10_000_000, 300_000_000),))
+    samples = collect(args.queries, graphs=graphs, minutes=args.minutes, target_samples=args.samples)
     t_log = time.time() - t0
     pk, rep = train_and_evaluate(samples, epochs=args.epochs)
     rep["logging_s"] = t_log
-    rep["queries"] = args.queries
+    rep["queries"] = int(len(np.unique(samples.query)))
+    rep["graphs"] = [{"V": g.V, "E": g.E} for g in graphs]
     rep["label_share"] = np.bincount(np.asarray(samples.y), minlength=3).tolist()
     np.save(args.out, pk.params())
     print(json.dumps(rep))

@@ -28,7 +28,7 @@ def run_both(vs, g, dg, src, k_min, k_max, path, direction, **kw):
 
 @pytest.mark.parametrize("path", ["any", "shortest"])
 @pytest.mark.parametrize("direction", ["forward", "backward", "both"])
-@pytest.mark.parametrize("krange", [(0, 2), (1, 3), (2, 4), (1, 1)])
+@pytest.mark.parametrize("krange", [(0, 2), (1, 3), (2, 4), (1, 1), (2, 2), (0, 0)])
 def test_expand_parity_paths(vs, graphs, path, direction, krange):
     for name, (g, dg) in graphs.items():
         src = graphgen.sample_sources(g.V, 96, seed=7)
@@ -115,17 +115,24 @@ def test_expand_stats_active_edges(vs, graphs):
         assert st["active_edges"][1:] == ost["active_edges"][1:], (path, st, ost)
 
 
-def test_plan_rerun_is_clean(vs, graphs):
-    """A reused plan must give the same answer for a different source set."""
+@pytest.mark.parametrize("path,k0,k1", [("shortest", 1, 3), ("shortest", 2, 4), ("shortest", 0, 2),
+                                         ("any", 1, 3), ("any", 2, 2), ("any", 1, 1)])
+def test_plan_rerun_is_clean(vs, graphs, path, k0, k1):
+    """A reused plan gives the right answer for another source set: the rows
+    the previous run left in its result and frontier matrices are cleared,
+    and the result's column-occupancy flags (used by counts) stay exact."""
     g, dg = graphs["rmat11_skew"]
-    p = vs.make_params(1, 3, "shortest", "forward")
+    p = vs.make_params(k0, k1, path, "forward")
     plan = vs.ExpandPlan(dg, 256, p)
-    for seed in (1, 2, 1):
-        src = graphgen.sample_sources(g.V, 256, seed=seed)
+    for seed in (1, 2, 1, 3):
+        src = graphgen.sample_sources(g.V, 256 if seed != 3 else 40, seed=seed)
+        if len(src) < 256:  # fewer distinct vertices: repeat the last one (rows are independent)
+            src = np.concatenate([src, np.full(256 - len(src), src[-1], np.uint32)])
         plan.run(src)
         got = plan.result().download()
-        exp, _, _ = O.vexpand(g, src, 1, 3, "shortest", "forward")
+        exp, _, _ = O.vexpand(g, src, k0, k1, path, "forward")
         assert np.array_equal(got, exp), seed
+        assert plan.result().count() == O.matrix_count(exp, 256, g.V), seed
 
 
 def test_expand_empty_and_isolated(vs):

@@ -951,6 +951,14 @@ struct vs_expand_plan {
 namespace vs {
 namespace ex {
 
+// Any with k_min == k_max returns layer k_max itself: no accumulator (the last
+// frontier buffer is the result).  Any over a range, and Shortest with
+// k_min >= 2, union layers k_min..k_max into an accumulator.
+inline bool needs_acc(const vs_expand_params &p) {
+  return (p.path_type == VS_PATH_ANY && p.k_min != p.k_max) ||
+         (p.path_type == VS_PATH_SHORTEST && p.k_min >= 2);
+}
+
 int plan_free(vs_expand_plan *pl) {
   if (!pl) return VS_OK;
   const cudaStream_t st = pl->last_stream;
@@ -1006,7 +1014,7 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   pl->nslices = (pl->Q + qs - 1) / qs;
   const bool shortest = p->path_type != VS_PATH_ANY;
   pl->use_vis = shortest;
-  pl->use_acc = (p->path_type == VS_PATH_ANY) || (p->path_type == VS_PATH_SHORTEST && p->k_min >= 2);
+  pl->use_acc = needs_acc(*p);
   pl->clear_diag = p->path_type == VS_PATH_SHORTEST && p->k_min == 1;
   const uint32_t V = g->V;
   const size_t rowwords = (size_t)V * pl->W;
@@ -1044,10 +1052,14 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   PL_ALLOC(pl->rowk, 2);
 #undef PL_ALLOC
   cudaError_t e = cudaSuccess;
+  // every row starts zero; later runs clear only the rows their flags mark
   if ((e = cudaMemsetAsync(pl->buf[0], 0, rowwords * 8, st)) != cudaSuccess ||
       (e = cudaMemsetAsync(pl->buf[1], 0, rowwords * 8, st)) != cudaSuccess ||
       (e = cudaMemsetAsync(pl->flag[0], 0, 4ull * V, st)) != cudaSuccess ||
-      (e = cudaMemsetAsync(pl->flag[1], 0, 4ull * V, st)) != cudaSuccess) {
+      (e = cudaMemsetAsync(pl->flag[1], 0, 4ull * V, st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(pl->resflag, 0, 4ull * V, st)) != cudaSuccess ||
+      (pl->vis && (e = cudaMemsetAsync(pl->vis, 0, rowwords * 8, st)) != cudaSuccess) ||
+      (pl->acc && (e = cudaMemsetAsync(pl->acc, 0, rowwords * 8, st)) != cudaSuccess)) {
     plan_free(pl);
     return cuda_fail(e, "cudaMemsetAsync", __FILE__, __LINE__);
   }
@@ -1092,7 +1104,7 @@ int vs_expand_plan_footprint(const vs_graph *g, uint32_t S, const vs_expand_para
   if (!g || !p || !bytes) return fail(VS_ERR_ARG, "null argument");
   const uint64_t V = g->V, W = words_per_col(S);
   const bool use_vis = p->path_type != VS_PATH_ANY;
-  const bool use_acc = (p->path_type == VS_PATH_ANY) || (p->path_type == VS_PATH_SHORTEST && p->k_min >= 2);
+  const bool use_acc = needs_acc(*p);
   uint64_t cap = p->pair_capacity ? p->pair_capacity
                                   : std::max<uint64_t>(1u << 20, std::min<uint64_t>((uint64_t)S * V / 8, 1ull << 25));
   cap = std::max<uint64_t>(cap, S);
@@ -1129,9 +1141,13 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   for (int b = 0; b < 2; b++)
     { k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[b]), pl->flag[b],
                                                 V, Q, pl->ctr, 0, 0); vs::note_launch(); }
-  VS_CK(cudaMemsetAsync(pl->resflag, 0, 4ull * V, st));
-  if (pl->vis) VS_CK(cudaMemsetAsync(pl->vis, 0, rowbytes, st));
-  if (pl->acc) VS_CK(cudaMemsetAsync(pl->acc, 0, rowbytes, st));
+  // the result matrix (visited or accumulator): clear the rows the previous
+  // run marked in resflag, which also zeroes resflag; a visited matrix beside
+  // an accumulator has no row marks and is cleared whole
+  if (pl->acc || pl->vis)
+    { k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->acc ? pl->acc : pl->vis),
+                                                pl->resflag, V, Q, pl->ctr, 0, 0); vs::note_launch(); }
+  if (pl->acc && pl->vis) VS_CK(cudaMemsetAsync(pl->vis, 0, rowbytes, st));
   VS_CK(cudaMemsetAsync(pl->ctr, 0, sizeof(Ctr), st));
   const Lists in = pull_lists(g, p.direction), outl = push_lists(g, p.direction);
   SeedArgs sa;
@@ -1145,7 +1161,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   sa.pairs0 = pl->pairs[0];
   sa.pdeg0 = pl->pdeg[0];
   sa.resflag = pl->resflag;
-  sa.res_vis = !pl->use_acc;
+  sa.res_vis = pl->use_vis && !pl->use_acc;
   sa.out = outl;
   sa.ctr = pl->ctr;
   sa.V = V;
@@ -1194,7 +1210,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     sp.ctr = pl->ctr;
     sp.h = h;
     sp.resflag = pl->resflag;
-    sp.res_vis = !pl->use_acc;
+    sp.res_vis = pl->use_vis && !pl->use_acc;
     sp.hmask = pl->use_hmask ? reinterpret_cast<const unsigned long long *>(pl->hmask + (size_t)h * W) : nullptr;
     sp.pin = pl->pairs[fb];
     sp.pout = pl->pairs[nbuf];
@@ -1217,7 +1233,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     pa.ctr = pl->ctr;
     pa.h = h;
     pa.resflag = pl->resflag;
-    pa.res_vis = !pl->use_acc;
+    pa.res_vis = pl->use_vis && !pl->use_acc;
     pa.hmask = pl->use_hmask ? reinterpret_cast<const unsigned long long *>(pl->hmask + (size_t)h * W) : nullptr;
     pa.out = outl;
     pa.F = reinterpret_cast<const unsigned long long *>(pl->buf[fb]);
@@ -1236,7 +1252,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     { k_push_epilogue<<<pl->grid_push, 256, 0, st>>>(pa); vs::note_launch(); }
     PullArgs a;
     a.resflag = pl->resflag;
-    a.res_vis = !pl->use_acc;
+    a.res_vis = pl->use_vis && !pl->use_acc;
     a.hmask = pl->use_hmask ? reinterpret_cast<const uint4 *>(pl->hmask + (size_t)h * W) : nullptr;
     a.in = in;
     a.F = reinterpret_cast<const uint4 *>(pl->buf[fb]);
@@ -1280,10 +1296,11 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   r.cols = V;
   r.wpc = W;
   r.kind = VS_KIND_VARROW;
-  r.words = pl->use_acc ? pl->acc : pl->vis;
+  const int lb = p.k_max & 1;  // buffer of layer k_max (the result of Any [k, k])
+  r.words = pl->use_acc ? pl->acc : pl->use_vis ? pl->vis : pl->buf[lb];
   r.row_map = pl->d_src;
   r.col_map = nullptr;
-  r.colnz = pl->resflag;
+  r.colnz = (pl->use_acc || pl->use_vis) ? pl->resflag : pl->flag[lb];
   r.owns_words = false;
   r.view = true;
   pl->has_result = p.path_type != VS_PATH_FIND_SHORTEST;
@@ -1378,6 +1395,8 @@ int vs_expand_plan_set_row_limits(vs_expand_plan *pl, const uint8_t *row_kmax, u
     rk[0] = std::max<uint32_t>(rk[0], row_kmax[i]);
     for (uint32_t h = 1; h <= row_kmax[i]; h++) m[(size_t)h * W + i / 64] |= 1ull << (i % 64);
   }
+  if (!all && !pl->use_acc && !pl->use_vis)
+    return fail(VS_ERR_UNSUPPORTED, "row limits need an accumulating plan (Any with k_min < k_max, or Shortest)");
   // the mask is written even when unused, so a run captured with limits stays right
   VS_CK(cudaStreamSynchronize(pl->last_stream));  // no earlier run still reads the mask
   VS_CK(cudaMemcpy(pl->hmask, m.data(), 8 * m.size(), cudaMemcpyHostToDevice));
@@ -1394,6 +1413,8 @@ int vs_expand_plan_set_row_limits_device(vs_expand_plan *pl, const uint8_t *row_
                                          vs_stream_t stream) {
   if (!pl || !row_kmax) return fail(VS_ERR_ARG, "vs_expand_plan_set_row_limits_device: null argument");
   if (n > pl->S) return fail(VS_ERR_ARG, "%u row limits for a plan of %u rows", n, pl->S);
+  if (!pl->use_acc && !pl->use_vis)
+    return fail(VS_ERR_UNSUPPORTED, "row limits need an accumulating plan (Any with k_min < k_max, or Shortest)");
   cudaStream_t st = S(stream);
   if (st != pl->last_stream) {
     VS_CK(cudaStreamSynchronize(pl->last_stream));
@@ -1467,17 +1488,26 @@ int vs_expand(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_
     m->kind = VS_KIND_VARROW;
     m->owns_words = true;
     // hand the result buffer over instead of copying it
+    const int lb = p->k_max & 1;
     if (pl->use_acc) {
       m->words = pl->acc;
       pl->acc = nullptr;
-    } else {
+    } else if (pl->use_vis) {
       m->words = pl->vis;
       pl->vis = nullptr;
+    } else {  // Any [k, k]: the last layer's buffer and its row flags
+      m->words = pl->buf[lb];
+      pl->buf[lb] = nullptr;
     }
     m->row_map = pl->d_src;
     pl->d_src = nullptr;
-    m->colnz = pl->resflag;
-    pl->resflag = nullptr;
+    if (pl->use_acc || pl->use_vis) {
+      m->colnz = pl->resflag;
+      pl->resflag = nullptr;
+    } else {
+      m->colnz = pl->flag[lb];
+      pl->flag[lb] = nullptr;
+    }
     m->st = st;
     *out = m;
     (void)st;

@@ -79,31 +79,36 @@ class Server:
                               **params_kw(self.tuned.get(path)))
 
     def footprint(self, r: Request) -> int:
+        """Device bytes the query holds at its peak: its two expand plans run
+        one after the other, so the larger of the two."""
         S = len(r.sources)
-        return (vs.plan_footprint(self.dg, S, self._params(S, 1, r.k_max, "shortest"))
-                + vs.plan_footprint(self.dg, S, self._params(S, 1, 1, "any")))
+        return max(vs.plan_footprint(self.dg, S, self._params(S, 1, r.k_max, "shortest")),
+                   vs.plan_footprint(self.dg, S, self._params(S, 1, 1, "any")))
 
     def run_query(self, r: Request, stream) -> tuple:
         """The query's stages on its own stream; returns exact counts."""
         S = len(r.sources)
         pa = vs.ExpandPlan(self.dg, S, self._params(S, 1, r.k_max, "shortest"))
-        pp = vs.ExpandPlan(self.dg, S, self._params(S, 1, 1, "any"))
         try:
             if self.picker is not None:
                 pa.set_picker(self.picker)
-                pp.set_picker(self.picker)
             pa.run(r.sources, stream=stream)
             A = pa.result()
             visited = A.count(stream=stream)
             jt = vs.FlatTable.from_columns([r.payload, r.keys], stream=stream)
             _, jc, _ = vs.hash_join(jt, A, 1, 1, only_count=True, stream=stream)
-            pp.run(r.sources, stream=stream)
-            _, tc, _ = vs.mintersect(pp.result(), self.adj, self.dg.V, only_count=True, stream=stream)
             jt.free()
-            return (visited, jc, tc)
         finally:
             pa.free()
+        pp = vs.ExpandPlan(self.dg, S, self._params(S, 1, 1, "any"))
+        try:
+            if self.picker is not None:
+                pp.set_picker(self.picker)
+            pp.run(r.sources, stream=stream)
+            _, tc, _ = vs.mintersect(pp.result(), self.adj, self.dg.V, only_count=True, stream=stream)
+        finally:
             pp.free()
+        return (visited, jc, tc)
 
     def serve(self, trace: list, time_scale: float = 1.0) -> dict:
         """Replay the trace: arrivals follow the trace clock (scaled), admission is

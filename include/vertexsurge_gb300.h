@@ -292,7 +292,19 @@ typedef struct vs_isect_dep {
   int32_t direction;
   uint32_t u_col, nv_col;
   uint32_t base_col;
+  /* Membership test against a graph adjacency list (VS_ISECT_*; 0 = AUTO).
+   * Every choice gives the same result.  AUTO decides per base tuple: the
+   * adjacency bitmap when the list's vertex is a hub and its list is at least
+   * 4x the walked one, a warp-window merge when it is at most 8x, else a
+   * binary search.  Hub bitmaps (the highest-degree vertices, degree >= 1024,
+   * at most 1 GiB per graph and direction) are built on first use and kept
+   * with the graph. */
+  int32_t algo;
 } vs_isect_dep;
+#define VS_ISECT_AUTO 0
+#define VS_ISECT_BINARY 1
+#define VS_ISECT_MERGE 2
+#define VS_ISECT_BITMAP 3
 
 int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
                   uint32_t new_vertex_count, int only_count, uint64_t max_rows, vs_flat **out,

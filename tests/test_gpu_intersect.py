@@ -100,16 +100,29 @@ def test_random_flat_and_mat_deps(vs):
     assert np.array_equal(rows_of(out.columns()), rows_of(ocols))
 
 
-def test_adjacency_triangle_closing(vs):
-    """Base (a, b) edges; deps = out-lists of a and of b: triangles a->b, a->c, b->c."""
-    g = graphgen.rmat(12, 16, seed=33)
-    dg = vs.DeviceGraph.from_host(g)
+@pytest.fixture(scope="module")
+def hub_graphs(vs):
+    """An R-MAT graph and a power-law graph with many vertices of degree >= 1024
+    (adjacency bitmaps)."""
+    z = graphgen.zipf(20_000, 600_000, 1.6, 6000, seed=5)
+    zt = graphgen.HostGraph(z.V, z.E, z.rev_off, z.rev_src, z.fwd_off, z.fwd_dst, True)  # in-degree hubs
+    gs = {"rmat12": graphgen.rmat(12, 16, seed=33), "zipf20k": z, "zipf20k_t": zt}
+    return {k: (g, vs.DeviceGraph.from_host(g)) for k, g in gs.items()}
+
+
+@pytest.mark.parametrize("algo", ["auto", "binary", "merge", "bitmap"])
+@pytest.mark.parametrize("gname", ["rmat12", "zipf20k"])
+def test_adjacency_triangle_closing(vs, hub_graphs, algo, gname):
+    """Base (a, b) edges; deps = out-lists of a and of b: triangles a->b, a->c,
+    b->c, under every membership method (bitmap, window merge, binary search)."""
+    g, dg = hub_graphs[gname]
     rng = np.random.default_rng(1)
     src = np.repeat(np.arange(g.V, dtype=np.uint32), np.diff(g.fwd_off))
     pick = rng.choice(g.E, 30000, replace=False)
     a, b = src[pick], g.fwd_dst[pick]
     base = vs.FlatTable.from_columns([a, b])
-    deps = [dict(graph=dg, direction="forward", base_col=0), dict(graph=dg, direction="forward", base_col=1)]
+    deps = [dict(graph=dg, direction="forward", base_col=0, algo=algo),
+            dict(graph=dg, direction="forward", base_col=1, algo=algo)]
     out, count, _ = vs.mintersect(base, deps, g.V, False)
     _, c2, _ = vs.mintersect(base, deps, g.V, True)
     exp = []
@@ -119,13 +132,39 @@ def test_adjacency_triangle_closing(vs):
         for z in np.intersect1d(na, nb).tolist():
             exp.append((x, y, z))
     exp = np.array(sorted(exp), dtype=np.int64).reshape(-1, 3)
-    assert count == c2 == len(exp)
+    assert count == c2 == len(exp) > 0
     assert np.array_equal(rows_of(out.columns()), exp)
-    # the same through flat edge tables (oracle path: linear scans)
-    fe = vs.FlatTable.from_columns([src, g.fwd_dst])
-    deps_f = [dict(flat=fe, u_col=0, nv_col=1, base_col=0), dict(flat=fe, u_col=0, nv_col=1, base_col=1)]
-    _, c3, _ = vs.mintersect(base, deps_f, g.V, True)
-    assert c3 == count
+    if algo == "auto":
+        # the same through flat edge tables (pair-hash membership)
+        fe = vs.FlatTable.from_columns([src, g.fwd_dst])
+        deps_f = [dict(flat=fe, u_col=0, nv_col=1, base_col=0), dict(flat=fe, u_col=0, nv_col=1, base_col=1)]
+        _, c3, _ = vs.mintersect(base, deps_f, g.V, True)
+        assert c3 == count
+
+
+@pytest.mark.parametrize("algo", ["auto", "merge", "bitmap"])
+def test_adjacency_in_lists(vs, hub_graphs, algo):
+    """Backward (in-list) adjacency on a directed graph: common in-neighbours of
+    (a, b) pairs, every method against numpy."""
+    g, dg = hub_graphs["zipf20k_t"]
+    rng = np.random.default_rng(2)
+    a = rng.integers(0, g.V, 5000).astype(np.uint32)
+    b = rng.integers(0, g.V, 5000).astype(np.uint32)
+    base = vs.FlatTable.from_columns([a, b])
+    deps = [dict(graph=dg, direction="backward", base_col=0, algo=algo),
+            dict(graph=dg, direction="backward", base_col=1, algo=algo)]
+    _, count, _ = vs.mintersect(base, deps, g.V, True)
+    exp = 0
+    for x, y in zip(a.tolist(), b.tolist()):
+        exp += len(np.intersect1d(g.rev_src[g.rev_off[x]:g.rev_off[x + 1]], g.rev_src[g.rev_off[y]:g.rev_off[y + 1]]))
+    assert count == exp
+
+
+def test_unknown_intersection_method_is_rejected(vs, hub_graphs):
+    g, dg = hub_graphs["rmat12"]
+    base = vs.FlatTable.from_columns([np.zeros(4, np.uint32), np.ones(4, np.uint32)])
+    with pytest.raises(vs.VsError):
+        vs.mintersect(base, [dict(graph=dg, base_col=0, algo=7), dict(graph=dg, base_col=1)], g.V, True)
 
 
 def test_output_bound(vs):

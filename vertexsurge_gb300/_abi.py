@@ -72,7 +72,10 @@ class TableRef(C.Structure):
 class IsectDep(C.Structure):
     _fields_ = [("mat", C.c_void_p), ("flat", C.c_void_p), ("graph", C.c_void_p),
                 ("direction", C.c_int32), ("u_col", C.c_uint32), ("nv_col", C.c_uint32),
-                ("base_col", C.c_uint32)]
+                ("base_col", C.c_uint32), ("algo", C.c_int32)]
+
+
+ISECT_ALGOS = {"auto": 0, "binary": 1, "merge": 2, "bitmap": 3}
 
 
 _lib = None
@@ -590,7 +593,8 @@ def hash_join(a, b, key_a=0, key_b=0, only_count=False, max_rows=1 << 62, stream
 
 
 def mintersect(base, deps, new_vertex_count=0, only_count=False, max_rows=1 << 62, stream=None):
-    """Mintersect. deps: list of dicts with keys mat/flat/graph, direction, u_col, nv_col, base_col."""
+    """Mintersect. deps: list of dicts with keys mat/flat/graph, direction, u_col, nv_col, base_col
+    and, for graph adjacency, algo ('auto', 'binary', 'merge', 'bitmap')."""
     rb = TableRef()
     if isinstance(base, FlatTable):
         rb.flat = base.h
@@ -606,6 +610,8 @@ def mintersect(base, deps, new_vertex_count=0, only_count=False, max_rows=1 << 6
         arr[i].u_col = d.get("u_col", 0)
         arr[i].nv_col = d.get("nv_col", 1)
         arr[i].base_col = d.get("base_col", 0)
+        al = d.get("algo", "auto")
+        arr[i].algo = ISECT_ALGOS[al] if isinstance(al, str) else int(al)
     out = C.c_void_p()
     cnt = C.c_uint64()
     rc = lib().vs_mintersect(rb, arr, len(deps), new_vertex_count, 1 if only_count else 0, max_rows,

@@ -436,6 +436,10 @@ int vs_graph_free(vs_graph *g) {
   cudaFree(g->rev_off);
   cudaFree(g->fwd_dst);
   cudaFree(g->rev_src);
+  for (vs_hub_index &h : g->hub) {
+    if (h.slot) cudaFree(h.slot);
+    if (h.bm) cudaFree(h.bm);
+  }
   delete g;
   return VS_OK;
 }

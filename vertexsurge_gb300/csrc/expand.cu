@@ -618,7 +618,22 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
   }
   const bool rownz = __any_sync(FULL, any);
   if (lane == 0 && rownz && (a.res_vis || a.acc_on)) a.resflag[v] = 1;
-  if (!a.multislice) {
+  if (!a.multislice && a.last) {
+    // layer k_max is not kept: clear the rows an earlier layer left in this
+    // buffer, so the next run finds it clean
+    const uint32_t oldf = a.flagN[v];
+    if (leader_group && oldf) {
+#pragma unroll
+      for (int k = 0; k < UPL; k++) {
+        const uint32_t q = lane + k * L;
+        if (q < qn) pol.st(a.N + (size_t)v * a.Q + q0 + q, make_uint4(0, 0, 0, 0));
+      }
+    }
+    if (lane == 0) {
+      if (oldf) a.flagN[v] = 0;
+      if (rownz) nv++;
+    }
+  } else if (!a.multislice) {
     const uint32_t oldf = a.flagN[v];
     if (leader_group && (rownz || oldf)) {
 #pragma unroll
@@ -1267,6 +1282,9 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.multislice = pl->nslices > 1;
     a.shortest = pl->use_vis;
     a.acc_on = acc_on;
+    // the last hop's layer is read by nothing when the result is the visited
+    // matrix or the accumulator (FindShortest checks every layer's targets)
+    a.last = h == p.k_max && (pl->use_vis || pl->use_acc) && p.path_type != VS_PATH_FIND_SHORTEST;
     a.hub_threshold = pl->nhubs ? pl->hub_threshold : 0;
     a.hubs = pl->hubs;
     a.nhubs = pl->nhubs;

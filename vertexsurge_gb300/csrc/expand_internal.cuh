@@ -111,6 +111,7 @@ struct PullArgs {
   uint32_t *flagN;
   uint32_t V, Q, qslice;
   int multislice, shortest, acc_on;
+  int last;  // the run's last hop and nothing reads its layer: zero the buffer instead of writing it
   uint32_t hub_threshold;
   const uint32_t *hubs;
   uint32_t nhubs;

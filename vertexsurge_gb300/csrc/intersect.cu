@@ -11,8 +11,13 @@
 //   flat       the (u, new) pairs of a flat edge table, grouped by u on the
 //              device (counting sort) and de-duplicated through a pair hash set.
 // With a list dependency the warp walks the shortest list (32 candidates per
-// step) and tests each candidate against the others: binary search in sorted
-// adjacency, pair-hash lookup for flat tables, one bit load for matrices.
+// step) and tests each candidate against the others: pair-hash lookup for
+// flat tables, one bit load for matrices, and for sorted adjacency one of
+//   bitmap   one bit load in the list vertex's adjacency bitmap (hubs only),
+//   merge    a warp-wide window of 32 list entries slides forward with the
+//            candidates; each candidate finds its place by a shuffle search,
+//   binary   a binary search of the whole list,
+// chosen per base tuple from the two list lengths (or fixed by the caller).
 // Counting and emitting are two passes over the same code; a prefix sum of
 // the per-tuple counts places every tuple's output.
 #include <algorithm>
@@ -26,7 +31,10 @@ namespace vs {
 namespace is {
 
 enum { DEP_MAT = 0, DEP_SORTED = 1, DEP_HASHED = 2 };
+enum { M_OTHER = 0, M_BINARY = 1, M_MERGE = 2, M_BITMAP = 3 };
 constexpr int MAX_DEPS = 8;
+constexpr uint32_t HUB_MIN_DEG = 1024;           // adjacency bitmaps only for lists this long
+constexpr uint64_t HUB_BUDGET = 1ull << 30;      // bitmap bytes per graph and direction
 
 struct Dep {
   int kind;
@@ -41,6 +49,11 @@ struct Dep {
   const uint32_t *adj;
   uint64_t n_u;
   HashTable pairs;  // DEP_HASHED: (u << 32 | new) membership
+  // DEP_SORTED: membership method (VS_ISECT_*) and hub bitmaps
+  int algo;
+  const int32_t *hub_slot;
+  const uint64_t *hub_bm;
+  uint32_t hub_words;
 };
 
 struct OutCol {
@@ -161,20 +174,64 @@ __global__ void __launch_bounds__(256) k_isect(Args a) {
         count += __shfl_sync(FULLMASK, incl, 31);
       }
     } else if (!empty) {
+      // membership method per dependency for this tuple (warp-uniform)
+      int meth[MAX_DEPS];
+      int64_t cur[MAX_DEPS];
+      int32_t hs[MAX_DEPS];
+#pragma unroll
+      for (int i = 0; i < MAX_DEPS; i++) {
+        meth[i] = M_OTHER;
+        cur[i] = 0;
+        hs[i] = -1;
+        if (i >= a.ndeps) break;
+        const Dep &d = a.dep[i];
+        if (d.kind != DEP_SORTED || i == best) continue;
+        const int64_t len = hi[i] - lo[i];
+        const int32_t slot = d.hub_slot ? __ldg(d.hub_slot + uu[i]) : -1;
+        cur[i] = lo[i];
+        hs[i] = slot;
+        if (d.algo == VS_ISECT_BINARY)
+          meth[i] = M_BINARY;
+        else if (d.algo == VS_ISECT_MERGE)
+          meth[i] = M_MERGE;
+        else if (d.algo == VS_ISECT_BITMAP)
+          meth[i] = slot >= 0 ? M_BITMAP : M_BINARY;
+        else
+          meth[i] = (slot >= 0 && len >= 4 * best_len) ? M_BITMAP : len <= 8 * best_len ? M_MERGE : M_BINARY;
+      }
       const Dep &L = a.dep[best];
       for (int64_t j0 = lo[best]; j0 < hi[best]; j0 += 32) {
         const int64_t j = j0 + lane;
-        bool keep = false;
-        uint32_t x = 0;
-        if (j < hi[best]) {
-          x = L.adj[j];
-          keep = x < a.cache_rows;
-          for (int i = 0; i < a.ndeps && keep; i++) {
-            if (i == best) continue;
-            const Dep &d = a.dep[i];
+        const bool valid = j < hi[best];
+        const uint32_t x = valid ? L.adj[j] : 0xffffffffu;
+        bool keep = valid && x < a.cache_rows;
+        // the chunk's candidates ascend with the lane: its largest is the last valid lane's
+        const uint32_t cmax = __reduce_max_sync(FULLMASK, valid ? x : 0u);
+#pragma unroll
+        for (int i = 0; i < MAX_DEPS; i++) {
+          if (i >= a.ndeps) break;
+          if (i == best) continue;
+          const Dep &d = a.dep[i];
+          if (meth[i] == M_MERGE) {  // all lanes: windows of 32 list entries from the cursor on
+            bool found = false;
+            for (;;) {
+              const int64_t p = cur[i];
+              if (p >= hi[i]) break;
+              const uint32_t y = p + lane < hi[i] ? __ldg(d.adj + p + lane) : 0xffffffffu;
+              int pos = 0;  // first window entry >= x (31 when all are smaller)
+#pragma unroll
+              for (int step = 16; step; step >>= 1)
+                if (__shfl_sync(FULLMASK, y, pos + step - 1) < x) pos += step;
+              found |= __shfl_sync(FULLMASK, y, pos) == x;
+              if (__shfl_sync(FULLMASK, y, 31) >= cmax) break;  // later candidates start in this window
+              cur[i] = p + 32;
+            }
+            keep = keep && found;
+          } else if (keep) {
             if (d.kind == DEP_MAT) {
-              keep = x < d.rows &&
-                     ((d.words[(size_t)col[i] * d.wpc + (x >> 6)] >> (x & 63)) & 1ull);
+              keep = x < d.rows && ((d.words[(size_t)col[i] * d.wpc + (x >> 6)] >> (x & 63)) & 1ull);
+            } else if (meth[i] == M_BITMAP) {
+              keep = (__ldg(d.hub_bm + (size_t)hs[i] * d.hub_words + (x >> 6)) >> (x & 63)) & 1ull;
             } else if (d.kind == DEP_SORTED) {
               keep = in_sorted(d.adj, lo[i], hi[i], x);
             } else {
@@ -231,6 +288,46 @@ __global__ void k_build_cols(HashTable t, const uint32_t *col_map, uint32_t cols
   }
 }
 
+// Hub adjacency bitmaps: degree histogram (log2 bins), hub slots, bitmap fill.
+__global__ void k_deg_bins(const int64_t *__restrict__ off, uint32_t V, unsigned long long *bins) {
+  __shared__ unsigned long long b[64];
+  if (threadIdx.x < 64) b[threadIdx.x] = 0;
+  __syncthreads();
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const int64_t d = off[v + 1] - off[v];
+    if (d > 0) atomicAdd(&b[63 - __clzll((unsigned long long)d)], 1ull);
+  }
+  __syncthreads();
+  if (threadIdx.x < 64 && b[threadIdx.x]) atomicAdd(&bins[threadIdx.x], b[threadIdx.x]);
+}
+
+__global__ void k_hub_slots(const int64_t *__restrict__ off, uint32_t V, uint32_t min_deg, uint32_t cap,
+                            int32_t *slot, uint32_t *hubs, unsigned *count) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    int32_t s = -1;
+    if (off[v + 1] - off[v] >= (int64_t)min_deg) {
+      const unsigned k = atomicAdd(count, 1u);
+      if (k < cap) {
+        s = (int32_t)k;
+        hubs[k] = v;
+      }
+    }
+    slot[v] = s;
+  }
+}
+
+__global__ void k_hub_fill(const int64_t *__restrict__ off, const uint32_t *__restrict__ adj,
+                           const uint32_t *__restrict__ hubs, uint32_t n, uint64_t *bm, uint32_t words) {
+  for (uint32_t b = blockIdx.x; b < n; b += gridDim.x) {
+    const uint32_t v = hubs[b];
+    unsigned long long *row = reinterpret_cast<unsigned long long *>(bm + (size_t)b * words);
+    for (int64_t j = off[v] + threadIdx.x; j < off[v + 1]; j += blockDim.x) {
+      const uint32_t x = adj[j];
+      atomicOr(row + (x >> 6), 1ull << (x & 63));
+    }
+  }
+}
+
 struct Scratch {
   cudaStream_t st;
   void *p[64] = {};
@@ -248,6 +345,58 @@ struct Scratch {
 int grid_for(uint64_t n, int per_block = 256) {
   return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + per_block - 1) / per_block,
                                                        (uint64_t)sm_count() * 16));
+}
+
+// The hub bitmaps of one list direction of g, built once (the smallest
+// power-of-two degree threshold >= HUB_MIN_DEG whose hubs fit HUB_BUDGET).
+int hub_index(vs_graph *g, bool fwd, cudaStream_t st, const vs_hub_index **out) {
+  std::lock_guard<std::mutex> lock(g->hub_mu);
+  vs_hub_index &h = g->hub[fwd ? 0 : 1];
+  *out = &h;
+  if (h.built) return VS_OK;
+  const int64_t *off = fwd ? g->fwd_off : g->rev_off;
+  const uint32_t *adj = fwd ? g->fwd_dst : g->rev_src;
+  const uint32_t V = g->V;
+  h.words = (V + 63) / 64;
+  const uint64_t per = (uint64_t)h.words * 8;
+  const uint64_t cap = std::min<uint64_t>(HUB_BUDGET / std::max<uint64_t>(per, 1), 1u << 20);
+  unsigned long long *bins = nullptr;
+  VS_TRY(dalloc_n(&bins, 64, st));
+  VS_CK(cudaMemsetAsync(bins, 0, 64 * 8, st));
+  if (V) { k_deg_bins<<<grid_for(V), 256, 0, st>>>(off, V, bins); vs::note_launch(); }
+  unsigned long long hb[64];
+  VS_CK(cudaMemcpyAsync(hb, bins, sizeof(hb), cudaMemcpyDeviceToHost, st));
+  VS_CK(cudaStreamSynchronize(st));
+  dfree(bins, st);
+  // bin k holds degrees in [2^k, 2^(k+1)): hubs with degree >= 2^k number sum(hb[k..])
+  int k = 0;
+  while ((1ull << k) < HUB_MIN_DEG) k++;
+  uint64_t n = 0;
+  for (int b = k; b < 64; b++) n += hb[b];
+  while (k < 63 && n > cap) n -= hb[k++];
+  h.min_deg = (uint32_t)std::min<uint64_t>(1ull << k, 0xffffffffull);
+  h.n = (uint32_t)n;
+  h.built = true;
+  if (n == 0 || cap == 0) {
+    h.n = 0;
+    return VS_OK;
+  }
+  uint32_t *hubs = nullptr;
+  unsigned *cnt = nullptr;
+  VS_TRY(dalloc_n(&h.slot, V, st));
+  VS_TRY(dalloc_n(&h.bm, (size_t)n * h.words, st));
+  VS_TRY(dalloc_n(&hubs, n, st));
+  VS_TRY(dalloc_n(&cnt, 1, st));
+  VS_CK(cudaMemsetAsync(cnt, 0, 4, st));
+  VS_CK(cudaMemsetAsync(h.bm, 0, (size_t)n * per, st));
+  { k_hub_slots<<<grid_for(V), 256, 0, st>>>(off, V, h.min_deg, (uint32_t)n, h.slot, hubs, cnt); vs::note_launch(); }
+  { k_hub_fill<<<(unsigned)std::min<uint64_t>(n, (uint64_t)sm_count() * 8), 256, 0, st>>>(off, adj, hubs, (uint32_t)n,
+                                                                                      h.bm, h.words); vs::note_launch(); }
+  VS_CK(cudaGetLastError());
+  VS_CK(cudaStreamSynchronize(st));  // other streams may use the bitmaps next
+  dfree(hubs, st);
+  dfree(cnt, st);
+  return VS_OK;
 }
 
 int hash_alloc(Scratch &sc, uint64_t n, HashTable *t) {
@@ -365,10 +514,24 @@ int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
       if (d.direction == VS_DIR_BOTH && g->directed)
         return fail(VS_ERR_UNSUPPORTED, "adjacency dependency needs one direction");
       const bool fwd = !g->directed || d.direction == VS_DIR_FORWARD;
+      if (d.algo < VS_ISECT_AUTO || d.algo > VS_ISECT_BITMAP)
+        return fail(VS_ERR_ARG, "dependency %u: unknown intersection method %d", i, d.algo);
       D.kind = DEP_SORTED;
       D.off = fwd ? g->fwd_off : g->rev_off;
       D.adj = fwd ? g->fwd_dst : g->rev_src;
       D.n_u = g->V;
+      D.algo = d.algo;
+      D.hub_slot = nullptr;
+      D.hub_bm = nullptr;
+      if (d.algo == VS_ISECT_AUTO || d.algo == VS_ISECT_BITMAP) {
+        const vs_hub_index *hx = nullptr;
+        VS_TRY(hub_index(const_cast<vs_graph *>(g), fwd, st, &hx));
+        if (hx->n) {
+          D.hub_slot = hx->slot;
+          D.hub_bm = hx->bm;
+          D.hub_words = hx->words;
+        }
+      }
     } else {
       VS_TRY(prepare_flat_dep(sc, d.flat, d.u_col, d.nv_col, &D));
     }

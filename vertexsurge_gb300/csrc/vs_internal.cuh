@@ -6,6 +6,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "../../include/vertexsurge_gb300.h"
@@ -58,6 +59,15 @@ inline uint32_t words_per_col(uint32_t rows) {
 
 }  // namespace vs
 
+// Adjacency bitmaps of a graph's highest-degree vertices for one list
+// direction (membership tests of the intersection), built on first use.
+struct vs_hub_index {
+  int32_t *slot = nullptr;  // per vertex: bitmap index, or -1
+  uint64_t *bm = nullptr;   // n bitmaps of `words` uint64 (bit x = x is in the list)
+  uint32_t n = 0, words = 0, min_deg = 0;
+  bool built = false;
+};
+
 struct vs_graph {
   uint32_t V;
   uint64_t E;
@@ -66,6 +76,8 @@ struct vs_graph {
   uint32_t *fwd_dst;
   int64_t *rev_off;
   uint32_t *rev_src;
+  vs_hub_index hub[2];  // [0] forward lists, [1] reverse lists
+  std::mutex hub_mu;
 };
 
 struct vs_bitmat {

@@ -310,6 +310,27 @@ int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
                   uint32_t new_vertex_count, int only_count, uint64_t max_rows, vs_flat **out,
                   uint64_t *count, vs_stream_t stream);
 
+/* ---- result consumers (replace MatrixColumnCount, MatrixRowOrSum and
+ *      SemiJoin<N>, src/include/operator/big_operators2.hh,
+ *      src/objects/operator/matrix_column_count.cpp:6-87,
+ *      matrix_row_or_sum.cpp:7-54, semi_join.cpp:7-262) ------------------ */
+/* One (column value, bit count) row per column of a VarRow or ColMain matrix,
+ * zero counts included; order 0 = column order, 1 = ascending, 2 = descending
+ * by the (count, column value) pair.  Output columns: VID, I64 (the reference's
+ * count column is Int32; the values are the same). */
+int vs_matrix_column_count(const vs_bitmat *m, int order, vs_flat **out, vs_stream_t stream);
+/* The values of the columns holding any bit, in column order (one VID column). */
+int vs_matrix_row_or_sum(const vs_bitmat *m, vs_flat **out, vs_stream_t stream);
+/* SemiJoin over nkeys (1 or 2) key columns: a's rows (flat a) or bits
+ * (VarRow a, key columns 0 = row value, 1 = column value) whose key tuple
+ * occurs in b (flat or VarRow).  Two key columns must be vertex ids.  Output:
+ * a flat table with a's columns (flat a) or a matrix of a's shape and maps
+ * with the other bits cleared (VarRow a); count = rows or bits kept.  ColMain
+ * inputs are VS_ERR_UNSUPPORTED, as in the reference. */
+int vs_semi_join(vs_table_ref a, vs_table_ref b, uint32_t nkeys, const uint32_t *a_key_cols,
+                 const uint32_t *b_key_cols, int only_count, vs_flat **out_flat, vs_bitmat **out_mat,
+                 uint64_t *count, vs_stream_t stream);
+
 /* ---- learned per-hop strategy picker (no counterpart in the reference; it
  *      replaces the fixed Adaptive coverage thresholds of expand.cpp:346-414)
  * A 32-64-64-3 ReLU network, bf16 weights, fp32 accumulation, trained with

@@ -7,10 +7,12 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <array>
 #include <bit>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <set>
 #include <unordered_map>
 #include <vector>
 
@@ -797,6 +799,134 @@ int oracle_mintersect(const or_table *base, const or_table *deps, uint32_t ndeps
       for (size_t i = 0; i < row.size(); i++) res.cols[i].push_back(row[i]);
   res.finish(out);
   out->count = (int64_t)out->nrows;
+  return 0;
+}
+
+// ---- result consumers --------------------------------------------------------
+namespace {
+inline uint32_t mat_col_value(const or_table *m, size_t c) { return m->col_map ? m->col_map[c] : (uint32_t)c; }
+inline uint32_t mat_row_value(const or_table *m, size_t r) { return m->row_map ? m->row_map[r] : (uint32_t)r; }
+inline size_t mat_wpc(const or_table *m) { return ((size_t)m->mrows + 63) / 64; }
+}  // namespace
+
+// MatrixColumnCount::run_internal (matrix_column_count.cpp:19-87):
+// count_bits_in_col per column; with an order, the (count, col) pairs sorted
+// with std::less / std::greater.
+int oracle_matrix_column_count(const or_table *m, int ord, uint32_t *out_col, int64_t *out_count) {
+  if (m->kind != OR_VARROW && m->kind != OR_COLMAIN) return 1;
+  const size_t wpc = mat_wpc(m);
+  std::vector<std::pair<int64_t, uint32_t>> pairs(m->mcols);
+#pragma omp parallel for num_threads(nthreads())
+  for (size_t c = 0; c < m->mcols; c++) {
+    int64_t n = 0;
+    for (size_t w = 0; w < wpc; w++) n += std::popcount(m->words[c * wpc + w]);
+    pairs[c] = {n, mat_col_value(m, c)};
+  }
+  if (ord == 1) std::sort(pairs.begin(), pairs.end(), std::less<std::pair<int64_t, uint32_t>>());
+  if (ord == 2) std::sort(pairs.begin(), pairs.end(), std::greater<std::pair<int64_t, uint32_t>>());
+  for (size_t i = 0; i < pairs.size(); i++) {
+    out_col[i] = pairs[i].second;
+    out_count[i] = pairs[i].first;
+  }
+  return 0;
+}
+
+// MatrixRowOrSum::run_internal (matrix_row_or_sum.cpp:14-54): has_bits_in_col.
+uint64_t oracle_matrix_row_or_sum(const or_table *m, uint32_t *out_col) {
+  const size_t wpc = mat_wpc(m);
+  uint64_t n = 0;
+  for (size_t c = 0; c < m->mcols; c++) {
+    bool any = false;
+    for (size_t w = 0; w < wpc && !any; w++) any = m->words[c * wpc + w] != 0;
+    if (!any) continue;
+    if (out_col) out_col[n] = mat_col_value(m, c);
+    n++;
+  }
+  return n;
+}
+
+// SemiJoin<N>::build / probe_once / probe (semi_join.cpp:58-262).  Key
+// tuples are compared by value (TupleValue equality); std::set stands in for
+// the reference's concurrent set.
+int oracle_semi_join(const or_table *a, const or_table *b, const int32_t *key_vars, uint32_t N,
+                     int only_count, or_result *out, uint64_t *out_words) {
+  std::memset(out, 0, sizeof(*out));
+  if (N == 0 || N > 4) return 1;
+  if (a->kind == OR_COLMAIN || b->kind == OR_COLMAIN) return 1;  // assert(0) in the reference
+  Schema sa = schema_of(a), sb = schema_of(b);
+  int ai[4], bi[4];
+  for (uint32_t k = 0; k < N; k++) {
+    ai[k] = sa.index(key_vars[k]);
+    bi[k] = sb.index(key_vars[k]);
+    if (ai[k] < 0 || bi[k] < 0 || sa.type[ai[k]] != sb.type[bi[k]]) return 1;
+  }
+  using Tup = std::array<uint64_t, 4>;
+  std::set<Tup> bset;
+  const size_t bwpc = b->kind == OR_FLAT ? 0 : mat_wpc(b);
+  std::unordered_map<uint32_t, size_t> brow, bcol;  // VarRow b with N == 2: direct bit lookups
+  if (b->kind == OR_FLAT) {
+    for (uint64_t i = 0; i < b->nrows; i++) {
+      Tup t{};
+      for (uint32_t k = 0; k < N; k++) t[k] = flat_get(b, i, (uint32_t)bi[k]);
+      bset.insert(t);
+    }
+  } else if (N == 2) {
+    for (size_t r = 0; r < b->mrows; r++) brow.emplace(mat_row_value(b, r), r);
+    for (size_t c = 0; c < b->mcols; c++) bcol.emplace(mat_col_value(b, c), c);
+  } else {
+    for (size_t c = 0; c < b->mcols; c++)
+      for (size_t w = 0; w < bwpc; w++) {
+        uint64_t d = b->words[c * bwpc + w];
+        while (d) {
+          const size_t r = w * 64 + std::countr_zero(d);
+          d &= d - 1;
+          Tup t{};
+          for (uint32_t k = 0; k < N; k++) t[k] = bi[k] == 0 ? mat_row_value(b, r) : mat_col_value(b, c);
+          bset.insert(t);
+        }
+      }
+  }
+  auto member = [&](const Tup &t) -> bool {
+    if (b->kind == OR_FLAT || N != 2) return bset.count(t) != 0;
+    uint64_t r = t[0], c = t[1];
+    if (bi[0] == 1 && bi[1] == 0) std::swap(r, c);
+    auto ir = brow.find((uint32_t)r), ic = bcol.find((uint32_t)c);
+    if (ir == brow.end() || ic == bcol.end()) return false;
+    return (b->words[ic->second * bwpc + ir->second / 64] >> (ir->second % 64)) & 1;
+  };
+  int64_t count = 0;
+  if (a->kind == OR_FLAT) {
+    ResultBuilder res(sa);
+    for (uint64_t i = 0; i < a->nrows; i++) {
+      Tup t{};
+      for (uint32_t k = 0; k < N; k++) t[k] = flat_get(a, i, (uint32_t)ai[k]);
+      if (!member(t)) continue;
+      count++;
+      if (!only_count)
+        for (uint32_t c = 0; c < a->ncols; c++) res.cols[c].push_back(flat_get(a, i, c));
+    }
+    if (!only_count) res.finish(out);
+  } else {
+    const size_t wpc = mat_wpc(a);
+    for (size_t c = 0; c < a->mcols; c++)
+      for (size_t w = 0; w < wpc; w++) {
+        uint64_t d = a->words[c * wpc + w], keep = 0;
+        uint64_t dd = d;
+        while (dd) {
+          const size_t r = w * 64 + std::countr_zero(dd);
+          const uint64_t bit = dd & (~dd + 1);
+          dd &= dd - 1;
+          Tup t{};
+          for (uint32_t k = 0; k < N; k++) t[k] = ai[k] == 0 ? mat_row_value(a, r) : mat_col_value(a, c);
+          if (member(t)) {
+            keep |= bit;
+            count++;
+          }
+        }
+        if (!only_count && out_words) out_words[c * wpc + w] = keep;
+      }
+  }
+  out->count = count;
   return 0;
 }
 

@@ -113,6 +113,24 @@ uint64_t oracle_matrix_iterate(uint32_t rows, uint32_t cols, const uint64_t *wor
                                uint32_t stack_row_count, const uint32_t *row_map,
                                const uint32_t *col_map, uint32_t *out_r, uint32_t *out_c);
 
+/* MatrixColumnCount(count_name, ord) over a VarRow or ColMain matrix
+ * (matrix_column_count.cpp:6-87): one (column value, popcount of the column)
+ * row per column, zero counts included.  ord 0 = column order, 1 = ascending,
+ * 2 = descending by the (count, column value) pair.  out arrays: mcols each. */
+int oracle_matrix_column_count(const or_table *m, int ord, uint32_t *out_col, int64_t *out_count);
+
+/* MatrixRowOrSum (matrix_row_or_sum.cpp:7-54): the values of the columns
+ * holding any bit, in column order.  Returns their number (out nullable). */
+uint64_t oracle_matrix_row_or_sum(const or_table *m, uint32_t *out_col);
+
+/* SemiJoin<N>(key_vars, only_count) (semi_join.cpp:7-262): a = left input,
+ * b = right input (Flat or VarRow).  Flat a: the rows of a whose key tuple
+ * occurs in b.  VarRow a: the bits (r, c) of a whose key tuple occurs in b;
+ * with only_count == 0 the masked matrix goes to out_words (a's logical
+ * shape).  out->count is the number of kept rows or bits. */
+int oracle_semi_join(const or_table *a, const or_table *b, const int32_t *key_vars, uint32_t N,
+                     int only_count, or_result *out, uint64_t *out_words);
+
 /* Thread count used by every parallel region (0 = OpenMP default). */
 void oracle_set_threads(int n);
 int oracle_get_threads(void);

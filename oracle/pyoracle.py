@@ -57,6 +57,11 @@ def lib():
         L.oracle_matrix_iterate.argtypes = [C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
                                             C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_matrix_iterate.restype = C.c_uint64
+        L.oracle_matrix_column_count.argtypes = [C.POINTER(OrTable), C.c_int, C.c_void_p, C.c_void_p]
+        L.oracle_matrix_row_or_sum.argtypes = [C.POINTER(OrTable), C.c_void_p]
+        L.oracle_matrix_row_or_sum.restype = C.c_uint64
+        L.oracle_semi_join.argtypes = [C.POINTER(OrTable), C.POINTER(OrTable), C.c_void_p, C.c_uint32, C.c_int,
+                                       C.POINTER(OrResult), C.c_void_p]
         L.oracle_set_threads.argtypes = [C.c_int]
         L.oracle_get_threads.restype = C.c_int
         _lib = L
@@ -208,3 +213,39 @@ def matrix_iterate(words, rows, cols, row_map=None, col_map=None, stack_row_coun
     c = np.zeros(n, np.uint32)
     lib().oracle_matrix_iterate(rows, cols, _p(w), stack_row_count, _p(rm), _p(cm), _p(r), _p(c))
     return r, c
+
+
+def matrix_column_count(m: Table, order: int = 0):
+    """MatrixColumnCount: (column values, counts); order 0 none, 1 ascending, 2 descending."""
+    n = m.t.mcols
+    cols = np.zeros(n, np.uint32)
+    cnt = np.zeros(n, np.int64)
+    if lib().oracle_matrix_column_count(C.byref(m.t), order, _p(cols), _p(cnt)):
+        raise ValueError("oracle_matrix_column_count rejected its arguments")
+    return cols, cnt
+
+
+def matrix_row_or_sum(m: Table) -> np.ndarray:
+    """MatrixRowOrSum: values of the columns holding any bit, in column order."""
+    out = np.zeros(m.t.mcols, np.uint32)
+    n = lib().oracle_matrix_row_or_sum(C.byref(m.t), _p(out))
+    return out[:n]
+
+
+def semi_join(a: Table, b: Table, key_vars, only_count=False):
+    """SemiJoin<N>: (var, cols, count) for a flat a; (masked words or None, count) for a VarRow a."""
+    kv = np.ascontiguousarray(key_vars, dtype=np.int32)
+    r = OrResult()
+    words = None
+    if a.kind != FLAT and not only_count:
+        words = np.zeros_like(a.words)
+    if lib().oracle_semi_join(C.byref(a.t), C.byref(b.t), _p(kv), len(kv), 1 if only_count else 0,
+                              C.byref(r), _p(words)):
+        raise ValueError("oracle_semi_join rejected its arguments")
+    if a.kind != FLAT:
+        return words, int(r.count)
+    if only_count:
+        return None, None, int(r.count)
+    count = int(r.count)
+    var, cols, _ = _result(r)
+    return var, cols, count

@@ -151,6 +151,10 @@ _SIGS += [
     ("vs_captured_free", C.c_int, [C.c_void_p]),
     ("vs_hash_join_count_row_blocks", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                                 C.c_void_p]),
+    ("vs_matrix_column_count", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_void_p]),
+    ("vs_matrix_row_or_sum", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_void_p]),
+    ("vs_semi_join", C.c_int, [TableRef, TableRef, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int,
+                               C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_void_p]),
     ("vs_expand_plan_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
 ]
 
@@ -620,6 +624,41 @@ def mintersect(base, deps, new_vertex_count=0, only_count=False, max_rows=1 << 6
     if not truncated:
         check(rc)
     return (FlatTable(out) if out.value else None), int(cnt.value), truncated
+
+
+def matrix_column_count(m: "BitMatrix", order=0, stream=None) -> "FlatTable":
+    """MatrixColumnCount: (column value VID, count I64) per column; order 0/1/2 or
+    None/'asc'/'desc'."""
+    o = {None: 0, "asc": 1, "desc": 2}.get(order, order)
+    out = C.c_void_p()
+    check(lib().vs_matrix_column_count(m.h, int(o), C.byref(out), _stream(stream)))
+    return FlatTable(out)
+
+
+def matrix_row_or_sum(m: "BitMatrix", stream=None) -> "FlatTable":
+    """MatrixRowOrSum: the values of the columns holding any bit."""
+    out = C.c_void_p()
+    check(lib().vs_matrix_row_or_sum(m.h, C.byref(out), _stream(stream)))
+    return FlatTable(out)
+
+
+def semi_join(a, b, a_keys, b_keys, only_count=False, stream=None):
+    """SemiJoin over key columns a_keys / b_keys (matrix: 0 row, 1 column).
+    Returns (FlatTable or BitMatrix or None, count)."""
+    ra, rb = TableRef(), TableRef()
+    for r, t in ((ra, a), (rb, b)):
+        if isinstance(t, FlatTable):
+            r.flat = t.h
+        else:
+            r.mat = t.h
+    ak = np.ascontiguousarray(a_keys, dtype=np.uint32)
+    bk = np.ascontiguousarray(b_keys, dtype=np.uint32)
+    assert len(ak) == len(bk)
+    of, om, cnt = C.c_void_p(), C.c_void_p(), C.c_uint64()
+    check(lib().vs_semi_join(ra, rb, len(ak), _ptr(ak), _ptr(bk), 1 if only_count else 0, C.byref(of),
+                             C.byref(om), C.byref(cnt), _stream(stream)))
+    res = FlatTable(of) if of.value else (BitMatrix(om) if om.value else None)
+    return res, int(cnt.value)
 
 
 class Picker:

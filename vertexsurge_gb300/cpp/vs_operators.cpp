@@ -407,6 +407,90 @@ void Count::run_internal() {
   results = count_table((int64_t)dep_results[0]->tuple_count());
 }
 
+// ---- result consumers --------------------------------------------------------
+MatrixColumnCount::MatrixColumnCount(VariableName count_name, std::optional<SortOrder> ord)
+    : count_name(std::move(count_name)), ord(ord) {}
+
+// MatrixColumnCount::finishAddingDependency (matrix_column_count.cpp:10-17)
+void MatrixColumnCount::finishAddingDependency() {
+  if (deps.size() != 1 || deps[0]->results_schema.columns.size() != 2 ||
+      deps[0]->results_schema.columns[1].type != Type::VID)
+    throw Error(VS_ERR_ARG, "MatrixColumnCount takes one two-column matrix whose columns are vertices");
+  results_schema = TableSchema{{{count_name, Type::VID}, {"count", Type::Int64}}};
+}
+
+void MatrixColumnCount::run_internal() {
+  auto *m = dep_results[0]->down_to_matrix_table();
+  if (!m) throw Error(VS_ERR_ARG, "MatrixColumnCount needs a matrix input");  // matrix_column_count.cpp:20-21
+  vs_flat *f = nullptr;
+  check(vs_matrix_column_count(m->h, !ord ? 0 : *ord == SortOrder::ASC ? 1 : 2, &f, stream));
+  results = std::make_shared<FlatTable>(results_schema, f);
+}
+
+// MatrixRowOrSum::finishAddingDependency (matrix_row_or_sum.cpp:7-12)
+void MatrixRowOrSum::finishAddingDependency() {
+  if (deps.size() != 1 || deps[0]->results_schema.columns.size() != 2 ||
+      deps[0]->results_schema.columns[1].type != Type::VID)
+    throw Error(VS_ERR_ARG, "MatrixRowOrSum takes one two-column matrix whose columns are vertices");
+  results_schema = TableSchema{{deps[0]->results_schema.columns[1]}};
+}
+
+void MatrixRowOrSum::run_internal() {
+  auto *m = dep_results[0]->down_to_matrix_table();
+  if (!m) throw Error(VS_ERR_ARG, "MatrixRowOrSum needs a matrix input");
+  vs_flat *f = nullptr;
+  check(vs_matrix_row_or_sum(m->h, &f, stream));
+  results = std::make_shared<FlatTable>(results_schema, f);
+}
+
+template <size_t N>
+SemiJoin<N>::SemiJoin(std::array<VariableName, N> keys, bool only_count)
+    : key_variables(std::move(keys)), only_count(only_count) {}
+
+// SemiJoin<N>::finishAddingDependency (semi_join.cpp:22-56): both inputs hold
+// every key with the same type; the result keeps the left input's schema.
+template <size_t N> void SemiJoin<N>::finishAddingDependency() {
+  if (deps.size() != 2) throw Error(VS_ERR_ARG, "SemiJoin takes two dependencies");
+  for (const auto &k : key_variables) {
+    auto x = deps[0]->results_schema.get_schema(k), y = deps[1]->results_schema.get_schema(k);
+    if (!x || !y) throw Error(VS_ERR_ARG, "SemiJoin key " + k + " is missing from an input");
+    if (!(x->first == y->first)) throw Error(VS_ERR_ARG, "SemiJoin key " + k + " differs between the inputs");
+  }
+  results_schema = only_count ? TableSchema{{{"count", Type::Int64}}} : deps[0]->results_schema;
+}
+
+template <size_t N> void SemiJoin<N>::run_internal() {
+  vs_table_ref ra{}, rb{};
+  uint32_t ak[N], bk[N];
+  for (size_t i = 0; i < N; i++) {
+    ak[i] = (uint32_t)dep_results[0]->schema.get_schema(key_variables[i])->second;
+    bk[i] = (uint32_t)dep_results[1]->schema.get_schema(key_variables[i])->second;
+  }
+  for (auto [r, t] : {std::pair<vs_table_ref *, const std::shared_ptr<Table> *>{&ra, &dep_results[0]},
+                      {&rb, &dep_results[1]}}) {
+    if (auto *f = (*t)->down_to_flat_table())
+      r->flat = f->h;
+    else
+      r->mat = (*t)->down_to_matrix_table()->h;
+  }
+  vs_flat *of = nullptr;
+  vs_bitmat *om = nullptr;
+  uint64_t count = 0;
+  check(vs_semi_join(ra, rb, (uint32_t)N, ak, bk, only_count ? 1 : 0, &of, &om, &count, stream));
+  if (only_count) {
+    results = count_table((int64_t)count);
+  } else if (of) {
+    results = std::make_shared<FlatTable>(results_schema, of);
+  } else {
+    auto t = std::make_shared<VarRowMatrixTable>(results_schema);
+    t->set_matrix(om);
+    results = t;
+  }
+}
+
+template class SemiJoin<1>;
+template class SemiJoin<2>;
+
 TableConvert::TableConvert(TableType type, bool transpose) : convert_to(type), transpose(transpose) {}
 
 void TableConvert::finishAddingDependency() {

@@ -15,6 +15,7 @@
 // Errors from the device layer throw vsgb::Error (the reference asserts or
 // exits; see vexpand.cpp:88-91, join.cpp:82-85).
 #pragma once
+#include <array>
 #include <cstdint>
 #include <filesystem>
 #include <map>
@@ -255,6 +256,42 @@ class MatrixTableSelect : public BigOperator {
 
  public:
   explicit MatrixTableSelect(VariableName key_name);
+  void finishAddingDependency() override;
+};
+
+// Result consumers (big_operators2.hh, big_operators3.hh).
+enum class SortOrder { ASC, DESC };
+
+// (column value, bit count) per column (matrix_column_count.cpp:6-87); the
+// count column is Int64 here (Int32 in the reference).
+class MatrixColumnCount : public BigOperator {
+  VariableName count_name;
+  std::optional<SortOrder> ord;
+  void run_internal() override;
+
+ public:
+  explicit MatrixColumnCount(VariableName count_name, std::optional<SortOrder> ord = std::nullopt);
+  void finishAddingDependency() override;
+};
+
+// The column values holding any bit (matrix_row_or_sum.cpp:7-54).
+class MatrixRowOrSum : public BigOperator {
+  void run_internal() override;
+
+ public:
+  MatrixRowOrSum() = default;
+  void finishAddingDependency() override;
+};
+
+// SemiJoin<N> (semi_join.cpp:7-262): N = 1 or 2 key variables (two keys must
+// be vertex ids); flat or VarRow inputs.
+template <size_t N> class SemiJoin : public BigOperator {
+  std::array<VariableName, N> key_variables;
+  bool only_count;
+  void run_internal() override;
+
+ public:
+  SemiJoin(std::array<VariableName, N> key_variables, bool only_count);
   void finishAddingDependency() override;
 };
 

@@ -297,6 +297,59 @@ static bool plans_case(const HostGraph &hg) {
         EXPECT_EQ((int64_t)j->results->tuple_count(), exp);
     }
   }
+  // p3-tri3-2: HashJoin("b.id") of ColMain(p12) and ColMain^T(p23), then
+  // SemiJoin<2>({"a.id", "c.id"}) with p13: the triangles again
+  {
+    auto p12 = vexp(A, B, "a.id", "b.id", 1, 2), p13 = vexp(A, Cn, "a.id", "c.id", 1, 2),
+         p23 = vexp(B, Cn, "b.id", "c.id", 1, 2);
+    auto c12 = make_shared<TableConvert>(TableType::ColMainMatrix, false);
+    c12->addLastDependency(p12);
+    auto c32 = make_shared<TableConvert>(TableType::ColMainMatrix, true);
+    c32->addLastDependency(p23);
+    auto p123 = make_shared<HashJoin>("b.id", false);
+    p123->addDependency(c12);
+    p123->addLastDependency(c32);
+    int64_t exp = 0;
+    for (size_t i = 0; i < sa.size(); i++)
+      for (size_t j = 0; j < sb.size(); j++) {
+        if (!within(da[i][sb[j]], 1, 2)) continue;
+        for (size_t k = 0; k < sc.size(); k++) exp += within(da[i][sc[k]], 1, 2) && within(db[j][sc[k]], 1, 2);
+      }
+    for (bool oc : {true, false}) {
+      auto t123 = make_shared<SemiJoin<2>>(std::array<VariableName, 2>{"a.id", "c.id"}, oc);
+      t123->addDependency(p123);
+      t123->addLastDependency(p13);
+      t123->run();
+      if (oc)
+        EXPECT_EQ(single_count(t123->results.get()), exp);
+      else
+        EXPECT_EQ((int64_t)t123->results->tuple_count(), exp);
+    }
+  }
+  // MatrixColumnCount and MatrixRowOrSum over p12: per b, the a's within [1,2]
+  {
+    auto p12 = vexp(A, B, "a.id", "b.id", 1, 2);
+    auto mcc = make_shared<MatrixColumnCount>("b.id", SortOrder::DESC);
+    mcc->addLastDependency(p12);
+    mcc->run();
+    auto ids = mcc->results->down_to_flat_table()->column(0), cnt = mcc->results->down_to_flat_table()->column(1);
+    EXPECT_EQ(ids.size(), sb.size());
+    bool sorted = true, right = true;
+    for (size_t i = 0; i < ids.size(); i++) {
+      if (i && cnt[i] > cnt[i - 1]) sorted = false;
+      int64_t e = 0;
+      for (size_t a = 0; a < sa.size(); a++) e += within(da[a][ids[i]], 1, 2);
+      if ((int64_t)cnt[i] != e) right = false;
+    }
+    EXPECT_EQ(sorted, true);
+    EXPECT_EQ(right, true);
+    auto ros = make_shared<MatrixRowOrSum>();
+    ros->addLastDependency(p12);
+    ros->run();
+    size_t nz = 0;
+    for (size_t i = 0; i < ids.size(); i++) nz += cnt[i] != 0;
+    EXPECT_EQ(ros->results->tuple_count(), nz);
+  }
   // FindShortest over (start, target) pairs
   {
     vector<uint64_t> tg;
@@ -356,7 +409,7 @@ int main(int argc, char **argv) {
   }
   run_test("TableConvertVRtoCM", [] { return table_convert_case(false); });
   run_test("TableConvertVRtoCM_T", [] { return table_convert_case(true); });
-  run_test("PlanShapes(e1,p3-tri3-1,p4-exp4-1,FindShortest)", [&] { return plans_case(hg); });
+  run_test("PlanShapes(e1,p3-tri3-1,p3-tri3-2,p4-exp4-1,consumers,FindShortest)", [&] { return plans_case(hg); });
   std::printf("%d passed, %d failed\n", g_pass, g_fail);
   return g_fail ? 1 : 0;
 }

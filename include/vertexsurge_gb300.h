@@ -215,6 +215,21 @@ int vs_expand_plan_set_tuning(vs_expand_plan *plan, double sparse_frac, double p
  * FindShortest: targets[i] is the target of source i, distances[i] receives
  * the hop count (0 when source == target, -1 when not found) and *out may be
  * NULL. */
+/* VExpand with path_params.with_distance, Dense strategy (replaces
+ * VExpand::copy_to_multi_MT, vexpand.cpp:356-378, and MultipleMatrixTable,
+ * matrix_table.hh:132-149): every layer h in [k_min, k_actual] as its own
+ * VarRow matrix (rows = sources with them as row map, columns = vertices):
+ * Shortest, the vertices first reached at hop h; Any, the ends of the walks of
+ * exactly h hops.  k_actual is the last hop run (a Shortest expand stops when
+ * a hop adds no vertex).  layers: caller array of k_max - k_min + 1 handles;
+ * *nlayers = layers returned, from k_min up.  Not for FindShortest. */
+int vs_expand_layers(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_params *p,
+                     vs_bitmat **layers, uint32_t *nlayers, vs_stream_t stream);
+/* (row value, column value, distance) tuples of layer matrices, layer by layer
+ * (MultipleMatrixTable::output_to_flat, bit_matrix_table.cpp:302-340);
+ * distance column I64. */
+int vs_layers_to_flat(const vs_bitmat *const *layers, const int32_t *distances, uint32_t n, vs_flat **out,
+                      vs_stream_t stream);
 int vs_expand(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_params *p,
               const uint32_t *targets, int32_t *distances, vs_bitmat **out,
               vs_expand_stats *stats, vs_stream_t stream);

@@ -275,3 +275,30 @@ def test_device_row_limit_above_kmax_is_an_error(vs, graphs):
     with pytest.raises(vs.VsError):
         plan.stats()
     plan.free()
+
+
+@pytest.mark.parametrize("path", ["any", "shortest"])
+@pytest.mark.parametrize("krange", [(0, 3), (2, 4), (1, 1), (1, 8)])
+def test_expand_layers_with_distance(vs, graphs, path, krange):
+    """with_distance: layer h equals the expand over [h, h]; the layers stop at
+    the last hop run (a Shortest expand ends when a hop adds nothing)."""
+    g, dg = graphs["rmat11_skew"]
+    src = graphgen.sample_sources(g.V, 130, seed=8)
+    k0, k1 = krange
+    layers = vs.expand_layers(dg, src, k0, k1, path, "forward")
+    _, _, st = O.vexpand(g, src, k0, k1, path, "forward", hop_stats=True)
+    k_actual = min(st["hops_run"], k1) if path == "shortest" else k1
+    assert len(layers) == max(0, k_actual - k0 + 1)
+    total = 0
+    for h, m in layers:
+        exp, _, _ = O.vexpand(g, src, h, h, path, "forward")
+        got = m.download()
+        assert np.array_equal(got, exp), (path, krange, h)
+        total += O.matrix_count(exp, len(src), g.V)
+    if layers:
+        f = vs.layers_to_flat(layers)
+        r, c, d = f.columns()
+        assert len(r) == total
+        assert set(np.unique(d).tolist()) <= set(range(k0, k_actual + 1))
+        if path == "shortest":  # layers are disjoint: every (source, vertex) pair once
+            assert len(set(zip(r.tolist(), c.tolist()))) == total

@@ -152,6 +152,10 @@ _SIGS += [
     ("vs_hash_join_count_row_blocks", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                                 C.c_void_p]),
     ("vs_matrix_column_count", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_void_p]),
+    ("vs_expand_layers", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(ExpandParams),
+                                   C.POINTER(C.c_void_p), C.POINTER(C.c_uint32), C.c_void_p]),
+    ("vs_layers_to_flat", C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p),
+                                    C.c_void_p]),
     ("vs_matrix_row_or_sum", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_void_p]),
     ("vs_semi_join", C.c_int, [TableRef, TableRef, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int,
                                C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_void_p]),
@@ -624,6 +628,27 @@ def mintersect(base, deps, new_vertex_count=0, only_count=False, max_rows=1 << 6
     if not truncated:
         check(rc)
     return (FlatTable(out) if out.value else None), int(cnt.value), truncated
+
+
+def expand_layers(graph: "DeviceGraph", sources, k_min, k_max, path="shortest", direction="forward",
+                  stream=None, **kw) -> list:
+    """VExpand with distances (Dense): [(h, BitMatrix of layer h)] for h = k_min..k_actual."""
+    src = np.ascontiguousarray(sources, dtype=np.uint32)
+    p = make_params(k_min, k_max, path, direction, **kw)
+    n = k_max - k_min + 1
+    arr = (C.c_void_p * n)()
+    got = C.c_uint32()
+    check(lib().vs_expand_layers(graph.h, _ptr(src), len(src), C.byref(p), arr, C.byref(got), _stream(stream)))
+    return [(k_min + i, BitMatrix(C.c_void_p(arr[i]))) for i in range(got.value)]
+
+
+def layers_to_flat(layers: list, stream=None) -> "FlatTable":
+    """(row value, column value, distance) tuples of [(distance, BitMatrix)]."""
+    hs = (C.c_void_p * max(1, len(layers)))(*[m.h for _, m in layers])
+    d = np.ascontiguousarray([h for h, _ in layers], dtype=np.int32)
+    out = C.c_void_p()
+    check(lib().vs_layers_to_flat(hs, _ptr(d), len(layers), C.byref(out), _stream(stream)))
+    return FlatTable(out)
 
 
 def matrix_column_count(m: "BitMatrix", order=0, stream=None) -> "FlatTable":

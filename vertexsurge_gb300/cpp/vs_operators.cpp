@@ -52,6 +52,25 @@ VExpandPathParameters VExpandPathParameters::FindShortest() {
 
 // ---- tables -------------------------------------------------------------------
 FlatTable *Table::down_to_flat_table() { return dynamic_cast<FlatTable *>(this); }
+
+void MultipleMatrixTable::add_mat(std::shared_ptr<MatrixTable> t, int32_t d) {
+  mats.push_back(std::move(t));
+  dis.push_back(d);
+}
+
+size_t MultipleMatrixTable::tuple_count() {
+  size_t n = 0;
+  for (auto &m : mats) n += m->tuple_count();
+  return n;
+}
+
+std::shared_ptr<FlatTable> MultipleMatrixTable::output_to_flat() const {
+  std::vector<const vs_bitmat *> hs;
+  for (auto &m : mats) hs.push_back(m->h);
+  vs_flat *f = nullptr;
+  check(vs_layers_to_flat(hs.data(), dis.data(), (uint32_t)hs.size(), &f, BigOperator::stream));
+  return std::make_shared<FlatTable>(schema, f);
+}
 MatrixTable *Table::down_to_matrix_table() { return dynamic_cast<MatrixTable *>(this); }
 
 static int32_t abi_type(Type t) { return t == Type::Int64 ? VS_T_I64 : VS_T_VID; }
@@ -220,6 +239,16 @@ VExpand::VExpand(TypeName src_type, TypeName dst_type, TypeName edge_type, Direc
     throw Error(VS_ERR_ARG, "k max should be 1 when edge is not self edge");
 }
 
+VExpand::VExpand(TypeName src_type, TypeName dst_type, TypeName edge_type, Direction dir, size_t k_min,
+                 size_t k_max, VExpandPathParameters path_params, ExpandStrategy strategy,
+                 VariableName variable_name, std::optional<VariableName> target_variable_name)
+    : VExpand(std::move(src_type), std::move(dst_type), std::move(edge_type), dir, k_min, k_max,
+              path_params.path_type, strategy, std::move(variable_name), std::move(target_variable_name)) {
+  if (path_params.path_type == ExpandPathType::FindShortest)
+    throw Error(VS_ERR_ARG, "FindShortest has its own constructor");
+  this->path_params = path_params;
+}
+
 VExpand::VExpand(TypeName src_type, TypeName dst_type, TypeName edge_type, Direction dir,
                  VExpandPathParameters path_params, ExpandStrategy strategy, VariableName variable_name,
                  VariableName target_variable_name)
@@ -244,9 +273,8 @@ void VExpand::finishAddingDependency() {
     results_schema.columns.push_back({"distance", Type::Int64});
     return;
   }
-  if (path_params.with_distance)
-    throw Error(VS_ERR_UNSUPPORTED, "per-distance matrix export (copy_to_multi_MT) is not built");
   results_schema = TableSchema{{sv->first, target_vs}};
+  if (path_params.with_distance) results_schema.columns.push_back({"distance", Type::Int64});  // vexpand.cpp:120-123
 }
 
 void VExpand::run_internal() {
@@ -277,6 +305,30 @@ void VExpand::run_internal() {
     cols.push_back(d);
     out->set_columns(cols);
     results = out;
+    return;
+  }
+  if (path_params.with_distance) {
+    // copy_to_multi_MT (vexpand.cpp:356-378); the CSR strategy's flat output
+    // with distances (merge_to_Flat, :380-446) is the same layers as tuples,
+    // for Shortest (Any de-duplicates pairs across layers there: not built)
+    std::vector<vs_bitmat *> layers(k_max - k_min + 1, nullptr);
+    uint32_t n = 0;
+    check(vs_expand_layers(et.g, src.data(), (uint32_t)src.size(), &p, layers.data(), &n, stream));
+    TableSchema mat_schema = results_schema;
+    mat_schema.columns.pop_back();
+    auto multi = std::make_shared<MultipleMatrixTable>(results_schema);
+    for (uint32_t i = 0; i < n; i++) {
+      auto t = std::make_shared<VarRowMatrixTable>(mat_schema);
+      t->set_matrix(layers[i]);
+      multi->add_mat(t, (int32_t)(k_min + i));
+    }
+    if (strategy == ExpandStrategy::CSR) {
+      if (path_params.path_type == ExpandPathType::Any)
+        throw Error(VS_ERR_UNSUPPORTED, "CSR strategy with distances for Any (per-pair de-duplication)");
+      results = multi->output_to_flat();
+    } else {
+      results = multi;
+    }
     return;
   }
   vs_bitmat *m = nullptr;

@@ -42,7 +42,7 @@ struct Error : std::runtime_error {
 void check(int rc);
 
 enum class Type { VID, Int64 };
-enum class TableType { Flat, VarRowMatrix, ColMainMatrix };
+enum class TableType { Flat, VarRowMatrix, ColMainMatrix, MultipleVarRowMatrix };
 enum class Direction { Forward, Backward, Both, Undecide };
 enum class ExpandPathType { Any, Shortest, FindShortest };
 enum class ExpandStrategy { Adaptive, CSR, Dense };
@@ -68,6 +68,10 @@ struct VExpandPathParameters {
   static VExpandPathParameters Any();
   static VExpandPathParameters Shortest();
   static VExpandPathParameters FindShortest();
+  VExpandPathParameters set_with_distance() {
+    with_distance = true;
+    return *this;
+  }
 };
 
 class FlatTable;
@@ -112,6 +116,19 @@ class MatrixTable : public Table {
 class VarRowMatrixTable : public MatrixTable {
  public:
   explicit VarRowMatrixTable(TableSchema s) : MatrixTable(std::move(s), TableType::VarRowMatrix) {}
+};
+
+// One matrix per distance: VExpand with_distance, Dense (matrix_table.hh:132-149).
+// The schema ends with the distance column (Int64 here, Int32 in the reference).
+class MultipleMatrixTable : public Table {
+ public:
+  std::vector<int32_t> dis;
+  std::vector<std::shared_ptr<MatrixTable>> mats;
+  explicit MultipleMatrixTable(TableSchema s) : Table(std::move(s), TableType::MultipleVarRowMatrix) {}
+  void add_mat(std::shared_ptr<MatrixTable> t, int32_t d);
+  size_t tuple_count() override;
+  // (row value, column value, distance) tuples, layer by layer (bit_matrix_table.cpp:302-340)
+  std::shared_ptr<FlatTable> output_to_flat() const;
 };
 class ColMainMatrixTable : public MatrixTable {
  public:
@@ -197,6 +214,10 @@ class VExpand : public BigOperator {
   VExpand(TypeName src_type, TypeName dst_type, TypeName edge_type, Direction dir,
           VExpandPathParameters path_params, ExpandStrategy strategy, VariableName variable_name,
           VariableName target_variable_name);
+  // one edge type with path parameters (with_distance)
+  VExpand(TypeName src_type, TypeName dst_type, TypeName edge_type, Direction dir, size_t k_min,
+          size_t k_max, VExpandPathParameters path_params, ExpandStrategy strategy,
+          VariableName variable_name, std::optional<VariableName> target_variable_name);
   void finishAddingDependency() override;
 };
 

@@ -350,6 +350,29 @@ static bool plans_case(const HostGraph &hg) {
     for (size_t i = 0; i < ids.size(); i++) nz += cnt[i] != 0;
     EXPECT_EQ(ros->results->tuple_count(), nz);
   }
+  // VExpand with_distance (Dense): one matrix per distance; as tuples, every
+  // (a, v) at distance 1..3 once with that distance
+  {
+    auto ve = make_shared<VExpand>("Person", "Person", "knows", Direction::Both, 1, 3,
+                                   VExpandPathParameters::Shortest().set_with_distance(), ExpandStrategy::Dense,
+                                   "a.id", std::optional<VariableName>("b.id"));
+    ve->addLastDependency(A);
+    ve->run();
+    auto *multi = dynamic_cast<MultipleMatrixTable *>(ve->results.get());
+    EXPECT_EQ(multi != nullptr, true);
+    int64_t exp = 0;
+    for (size_t i = 0; i < sa.size(); i++)
+      for (size_t v = 0; v < hg.V; v++) exp += within(da[i][v], 1, 3);
+    EXPECT_EQ((int64_t)multi->tuple_count(), exp);
+    auto flat = multi->output_to_flat();
+    auto r = flat->column(0), c = flat->column(1), d = flat->column(2);
+    std::map<uint64_t, size_t> row_of;
+    for (size_t i = 0; i < sa.size(); i++) row_of.emplace(sa[i], i);
+    size_t bad = 0;
+    for (size_t t = 0; t < r.size(); t++) bad += (int64_t)d[t] != (int64_t)da[row_of.at(r[t])][c[t]];
+    EXPECT_EQ((int64_t)r.size(), exp);
+    EXPECT_EQ(bad, (size_t)0);
+  }
   // FindShortest over (start, target) pairs
   {
     vector<uint64_t> tg;

@@ -140,6 +140,25 @@ __global__ void k_dist_init(const uint32_t *__restrict__ src, const uint32_t *__
   block_add(f, &ctr->found);
 }
 
+// with_distance export: layer h (the frontier buffer just written) into its
+// own zeroed matrix, flagged rows only; a hop that did not run copies nothing.
+__global__ void k_copy_layer(const uint4 *__restrict__ buf, const uint32_t *__restrict__ flag, uint4 *__restrict__ out,
+                             uint32_t V, uint32_t Q, const Ctr *ctr, int h) {
+  if (h > 0 && ctr->hop[h].strategy == 0) return;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < V; base += warps * 32) {
+    const uint32_t v = base + lane;
+    unsigned m = __ballot_sync(FULL, v < V && flag[v]);
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      const size_t row = (size_t)(base + b) * Q;
+      for (uint32_t q = lane; q < Q; q += 32) out[row + q] = buf[row + q];
+    }
+  }
+}
+
 // Per-hop row masks of batched queries from per-row hop limits: word w of
 // hop h has bit r set when row 64w+r may still grow at hop h.
 __global__ void k_row_mask(const uint8_t *__restrict__ lim, uint32_t n, uint32_t K, uint32_t W,
@@ -955,6 +974,7 @@ struct vs_expand_plan {
   int pull_kind = 0;  // PULL kernel variant (bit 0: 8 blocks/SM bound, bit 1: L2 policies)
   uint64_t *hmask = nullptr;  // (k_max + 1) x W words: rows allowed to grow at hop h
   uint32_t *rowk = nullptr;   // [0] largest row limit, [1] a limit exceeded k_max (device-set limits)
+  uint64_t *layer_out[VS_MAX_HOPS + 1] = {};  // with_distance: layer h is copied here (zeroed, V x W words)
   bool use_hmask = false;
   int hop_forced[VS_MAX_HOPS + 1] = {};
   bool timing = false;
@@ -1184,6 +1204,9 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   sa.rowk = pl->use_hmask ? pl->rowk : nullptr;
   { k_seed<<<std::max(1u, std::min((S_ + 255) / 256, (uint32_t)sm_count() * 4)), 256, 0, st>>>(sa); vs::note_launch(); }
   VS_CK(cudaGetLastError());
+  if (pl->layer_out[0])
+    { k_copy_layer<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<const uint4 *>(pl->buf[0]), pl->flag[0],
+                                             reinterpret_cast<uint4 *>(pl->layer_out[0]), V, Q, pl->ctr, 0); vs::note_launch(); }
   if (p.path_type == VS_PATH_FIND_SHORTEST)
     { k_dist_init<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(pl->d_src, pl->d_tgt,
                                                                               pl->d_dist, S_, V, pl->ctr); vs::note_launch(); }
@@ -1284,7 +1307,8 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.acc_on = acc_on;
     // the last hop's layer is read by nothing when the result is the visited
     // matrix or the accumulator (FindShortest checks every layer's targets)
-    a.last = h == p.k_max && (pl->use_vis || pl->use_acc) && p.path_type != VS_PATH_FIND_SHORTEST;
+    a.last = h == p.k_max && (pl->use_vis || pl->use_acc) && p.path_type != VS_PATH_FIND_SHORTEST &&
+             !pl->layer_out[h];
     a.hub_threshold = pl->nhubs ? pl->hub_threshold : 0;
     a.hubs = pl->hubs;
     a.nhubs = pl->nhubs;
@@ -1297,6 +1321,9 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     if (p.path_type == VS_PATH_FIND_SHORTEST)
       { k_find_check<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(
           pl->buf[nbuf], pl->d_tgt, pl->d_dist, S_, W, V, pl->ctr, h); vs::note_launch(); }
+    if (pl->layer_out[h])
+      { k_copy_layer<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<const uint4 *>(pl->buf[nbuf]), pl->flag[nbuf],
+                                               reinterpret_cast<uint4 *>(pl->layer_out[h]), V, Q, pl->ctr, h); vs::note_launch(); }
     if (timing) cudaEventRecord(pl->ev[3 * h + 2], st);
     VS_CK(cudaGetLastError());
   }
@@ -1469,6 +1496,51 @@ int vs_expand_plan_features(vs_expand_plan *pl, float *features, vs_stream_t str
                         S(stream)));
   VS_CK(cudaStreamSynchronize(S(stream)));
   return VS_OK;
+}
+
+// VExpand with_distance, Dense strategy (copy_to_multi_MT, vexpand.cpp:356-378):
+// layers k_min..k_actual each as a VarRow matrix with the sources as row map.
+int vs_expand_layers(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_params *p,
+                     vs_bitmat **layers, uint32_t *nlayers, vs_stream_t stream) {
+  if (!g || !p || !layers || !nlayers) return fail(VS_ERR_ARG, "vs_expand_layers: null argument");
+  if (p->path_type == VS_PATH_FIND_SHORTEST)
+    return fail(VS_ERR_ARG, "FindShortest reports distances per pair, not layers");
+  if (p->k_min > p->k_max || p->k_max > VS_MAX_HOPS) return fail(VS_ERR_ARG, "bad hop range [%u, %u]", p->k_min, p->k_max);
+  const uint32_t n = p->k_max - p->k_min + 1;
+  *nlayers = 0;
+  for (uint32_t i = 0; i < n; i++) layers[i] = nullptr;
+  if (S == 0) return VS_OK;  // no start vertex: no layer (VExpand::before_execution)
+  cudaStream_t st = vs::S(stream);
+  vs_expand_plan *pl = nullptr;
+  VS_TRY(vs_expand_plan_create(g, S, p, &pl));
+  pl->collect_stats = true;
+  int rc = VS_OK;
+  for (uint32_t i = 0; i < n && rc == VS_OK; i++) {
+    rc = bitmat_alloc(S, g->V, VS_KIND_VARROW, st, &layers[i]);
+    if (rc == VS_OK) {
+      pl->layer_out[p->k_min + i] = layers[i]->words;
+      rc = vs_bitmat_set_maps(layers[i], sources, nullptr, stream);
+    }
+  }
+  if (rc == VS_OK) {
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "vs_expand_layers", __FILE__, __LINE__);
+  }
+  if (rc == VS_OK) rc = vs_expand_plan_run(pl, sources, nullptr, nullptr, stream);
+  vs_expand_stats stt{};
+  if (rc == VS_OK) rc = vs_expand_plan_stats(pl, &stt, stream);
+  plan_free(pl);
+  uint32_t keep = 0;
+  if (rc == VS_OK) {
+    const uint32_t k_actual = stt.hops_run;  // last hop run (VExpand::after_child, vexpand.cpp:223)
+    keep = k_actual >= p->k_min ? std::min(k_actual, p->k_max) - p->k_min + 1 : 0;
+  }
+  for (uint32_t i = keep; i < n; i++) {
+    vs_bitmat_free(layers[i]);
+    layers[i] = nullptr;
+  }
+  *nlayers = keep;
+  return rc;
 }
 
 int vs_expand(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_params *p,

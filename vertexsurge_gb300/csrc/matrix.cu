@@ -4,6 +4,7 @@
 // Reference: src/objects/operator/big_operators2.cpp:16-86,138-213,
 // src/objects/execution/bit_matrix_table.cpp:133-289.
 #include <algorithm>
+#include <vector>
 
 #include "vs_internal.cuh"
 
@@ -149,11 +150,64 @@ int bitmat_to_flat(const vs_bitmat *m, cudaStream_t st, vs_flat **out) {
   return VS_OK;
 }
 
+__global__ void k_fill_i64(long long *dst, uint64_t n, long long v) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = v;
+}
+
 }  // namespace vs
 
 using namespace vs;
 
 extern "C" {
+
+int vs_layers_to_flat(const vs_bitmat *const *layers, const int32_t *distances, uint32_t n, vs_flat **out,
+                      vs_stream_t stream) {
+  if (!out || (n && (!layers || !distances))) return fail(VS_ERR_ARG, "vs_layers_to_flat: null argument");
+  cudaStream_t st = S(stream);
+  std::vector<vs_flat *> parts(n, nullptr);
+  struct Free {
+    std::vector<vs_flat *> &p;
+    ~Free() {
+      for (auto *f : p) vs_flat_free(f);
+    }
+  } fr{parts};
+  uint64_t total = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    if (!layers[i]) return fail(VS_ERR_ARG, "layer %u is null", i);
+    VS_TRY(bitmat_to_flat(layers[i], st, &parts[i]));
+    total += parts[i]->nrows;
+  }
+  const int32_t types[3] = {VS_T_VID, VS_T_VID, VS_T_I64};
+  vs_flat *f = nullptr;
+  VS_TRY(flat_alloc(3, types, total, st, &f));
+  uint64_t off = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    const uint64_t k = parts[i]->nrows;
+    if (!k) continue;
+    cudaError_t e = cudaMemcpyAsync((uint32_t *)f->cols[0] + off, parts[i]->cols[0], 4 * k, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync((uint32_t *)f->cols[1] + off, parts[i]->cols[1], 4 * k, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) {
+      const int blocks = (int)std::min<uint64_t>((k + 255) / 256, (uint64_t)sm_count() * 8);
+      k_fill_i64<<<blocks, 256, 0, st>>>((long long *)f->cols[2] + off, k, distances[i]);
+      vs::note_launch();
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+      vs_flat_free(f);
+      return cuda_fail(e, "vs_layers_to_flat", __FILE__, __LINE__);
+    }
+    off += k;
+  }
+  const cudaError_t e = cudaStreamSynchronize(st);  // the parts are freed on return
+  if (e != cudaSuccess) {
+    vs_flat_free(f);
+    return cuda_fail(e, "vs_layers_to_flat", __FILE__, __LINE__);
+  }
+  *out = f;
+  return VS_OK;
+}
 
 int vs_matrix_select(const vs_bitmat *m, const uint32_t *targets, uint32_t T, vs_bitmat **out,
                      vs_stream_t stream) {

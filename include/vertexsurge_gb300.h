@@ -324,6 +324,17 @@ typedef struct vs_isect_dep {
 int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
                   uint32_t new_vertex_count, int only_count, uint64_t max_rows, vs_flat **out,
                   uint64_t *count, vs_stream_t stream);
+/* The same with the learned choice of the adjacency membership method (no
+ * counterpart in the reference): method_picker (a vs_picker trained on
+ * intersection timings; class 0 = binary search, 1 = window merge, 2 = hub
+ * bitmap) decides on the device, from 32 features sampled over up to 4096
+ * base tuples, for every graph dependency whose algo is VS_ISECT_AUTO.
+ * features (nullable, 32 floats, host or device) receives those features.
+ * Results do not depend on the choice. */
+typedef struct vs_picker vs_picker;
+int vs_mintersect_ex(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
+                     uint32_t new_vertex_count, int only_count, uint64_t max_rows, const vs_picker *method_picker,
+                     float *features, vs_flat **out, uint64_t *count, vs_stream_t stream);
 
 /* ---- result consumers (replace MatrixColumnCount, MatrixRowOrSum and
  *      SemiJoin<N>, src/include/operator/big_operators2.hh,
@@ -353,7 +364,6 @@ int vs_semi_join(vs_table_ref a, vs_table_ref b, uint32_t nkeys, const uint32_t 
  * the 32 features the expand logs per hop (vs_expand_plan_features); output
  * class 0 = PULL, 1 = PUSH, 2 = SPARSE.  Feature rows X are n x 32 floats,
  * labels y are n int32 classes; pointers may be host or device memory. */
-typedef struct vs_picker vs_picker;
 int vs_picker_create(uint64_t seed, vs_picker **out);
 int vs_picker_free(vs_picker *p);
 int vs_picker_num_params(void);

@@ -86,3 +86,36 @@ def test_hop_overrides_and_feature_logging(vs):
     f = plan.features()[1:n + 1]
     assert np.all(np.isfinite(f)) and f.max() <= 4.0 and f.min() >= 0.0
     assert np.allclose(f[:, 16:].sum(axis=1), 1.0, atol=1e-5)  # degree histogram normalised
+
+
+@pytest.mark.parametrize("cls", [0, 1, 2])
+def test_intersection_method_picker_keeps_results(vs, cls):
+    """A network choosing the adjacency membership method (binary search,
+    window merge, hub bitmap) on the device: every choice gives the count of
+    the per-tuple rule; the call's features are finite and normalised."""
+    g = graphgen.zipf(20_000, 600_000, 1.6, 6000, seed=5)
+    dg = vs.DeviceGraph.from_host(g)
+    src = graphgen.sample_sources(g.V, 500, seed=3)
+    P, _, _ = vs.expand(dg, src, 1, 1, "any", "forward")
+    deps = [dict(graph=dg, direction="forward", base_col=0), dict(graph=dg, direction="forward", base_col=1)]
+    _, exp, _ = vs.mintersect(P, deps, g.V, True)
+    out, count, _, feat = vs.mintersect(P, deps, g.V, False, method_picker=constant_picker(vs, cls), features=True)
+    assert count == exp > 0 and out.info()[1] == exp
+    assert np.all(np.isfinite(feat)) and feat.min() >= 0.0 and feat.max() <= 4.0
+    assert abs(feat[16:24].sum() - 1.0) < 1e-4  # walked-list length histogram
+    assert feat[13] == 1.0  # the graph has adjacency bitmaps (degrees >= 1024)
+
+
+def test_trained_hop_picker_beats_the_fixed_planner(vs):
+    """The committed network against the fixed planner on fresh logged hops
+    (graphs and queries it was not trained on): it picks the fastest strategy
+    more often, and its per-hop choices cost less time in total."""
+    from vertexsurge_gb300 import picker_train as T
+    pk = vs.Picker()
+    pk.set_params(np.load(T.WEIGHTS_FILE))
+    graphs = [graphgen.rmat(17, 16, 0.6, 0.175, 0.175, seed=77), graphgen.zipf(300_000, 6_000_000, 2.1, 50_000, seed=78)]
+    samples = T.collect(40, seed=99, graphs=graphs, log=None)
+    X, y, times, fixed, _ = samples.arrays()
+    rep = T.evaluate(pk, X, y, times, fixed)
+    assert rep["accuracy"] > rep["fixed_accuracy"], rep
+    assert rep["slowdown_vs_best"] <= rep["fixed_slowdown_vs_best"] * 1.02, rep

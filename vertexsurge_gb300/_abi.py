@@ -152,6 +152,9 @@ _SIGS += [
     ("vs_hash_join_count_row_blocks", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                                 C.c_void_p]),
     ("vs_matrix_column_count", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_void_p]),
+    ("vs_mintersect_ex", C.c_int, [TableRef, C.POINTER(IsectDep), C.c_uint32, C.c_uint32, C.c_int, C.c_uint64,
+                                   C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
+                                   C.c_void_p]),
     ("vs_expand_layers", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(ExpandParams),
                                    C.POINTER(C.c_void_p), C.POINTER(C.c_uint32), C.c_void_p]),
     ("vs_layers_to_flat", C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p),
@@ -600,9 +603,12 @@ def hash_join(a, b, key_a=0, key_b=0, only_count=False, max_rows=1 << 62, stream
     return (FlatTable(out) if out.value else None), int(cnt.value), truncated
 
 
-def mintersect(base, deps, new_vertex_count=0, only_count=False, max_rows=1 << 62, stream=None):
+def mintersect(base, deps, new_vertex_count=0, only_count=False, max_rows=1 << 62, stream=None,
+               method_picker=None, features=False):
     """Mintersect. deps: list of dicts with keys mat/flat/graph, direction, u_col, nv_col, base_col
-    and, for graph adjacency, algo ('auto', 'binary', 'merge', 'bitmap')."""
+    and, for graph adjacency, algo ('auto', 'binary', 'merge', 'bitmap').  method_picker: a Picker
+    trained on intersection timings that chooses the method of 'auto' adjacency deps on the device;
+    features=True appends the call's 32 features to the returned tuple."""
     rb = TableRef()
     if isinstance(base, FlatTable):
         rb.flat = base.h
@@ -622,12 +628,19 @@ def mintersect(base, deps, new_vertex_count=0, only_count=False, max_rows=1 << 6
         arr[i].algo = ISECT_ALGOS[al] if isinstance(al, str) else int(al)
     out = C.c_void_p()
     cnt = C.c_uint64()
-    rc = lib().vs_mintersect(rb, arr, len(deps), new_vertex_count, 1 if only_count else 0, max_rows,
-                             None if only_count else C.byref(out), C.byref(cnt), _stream(stream))
+    feat = np.zeros(32, np.float32) if features else None
+    if method_picker is not None or features:
+        rc = lib().vs_mintersect_ex(rb, arr, len(deps), new_vertex_count, 1 if only_count else 0, max_rows,
+                                    method_picker.h if method_picker is not None else None, _ptr(feat),
+                                    None if only_count else C.byref(out), C.byref(cnt), _stream(stream))
+    else:
+        rc = lib().vs_mintersect(rb, arr, len(deps), new_vertex_count, 1 if only_count else 0, max_rows,
+                                 None if only_count else C.byref(out), C.byref(cnt), _stream(stream))
     truncated = rc == VS_ERR_CAPACITY
     if not truncated:
         check(rc)
-    return (FlatTable(out) if out.value else None), int(cnt.value), truncated
+    res = (FlatTable(out) if out.value else None), int(cnt.value), truncated
+    return res + (feat,) if features else res
 
 
 def expand_layers(graph: "DeviceGraph", sources, k_min, k_max, path="shortest", direction="forward",

@@ -25,6 +25,7 @@
 
 #include "dev_util.cuh"
 #include "hash.cuh"
+#include "picker.cuh"
 #include "vs_internal.cuh"
 
 namespace vs {
@@ -74,6 +75,7 @@ struct Args {
   OutCol col[16];
   int nbcols;
   uint32_t *out_new;
+  const int *method;  // learned method for AUTO adjacency deps (VS_ISECT_*), or NULL
 };
 
 __device__ __forceinline__ bool in_sorted(const uint32_t *a, int64_t lo, int64_t hi, uint32_t x) {
@@ -174,6 +176,7 @@ __global__ void __launch_bounds__(256) k_isect(Args a) {
         count += __shfl_sync(FULLMASK, incl, 31);
       }
     } else if (!empty) {
+      const int learned = a.method ? *a.method : VS_ISECT_AUTO;
       // membership method per dependency for this tuple (warp-uniform)
       int meth[MAX_DEPS];
       int64_t cur[MAX_DEPS];
@@ -190,11 +193,12 @@ __global__ void __launch_bounds__(256) k_isect(Args a) {
         const int32_t slot = d.hub_slot ? __ldg(d.hub_slot + uu[i]) : -1;
         cur[i] = lo[i];
         hs[i] = slot;
-        if (d.algo == VS_ISECT_BINARY)
+        const int algo = d.algo == VS_ISECT_AUTO ? learned : d.algo;
+        if (algo == VS_ISECT_BINARY)
           meth[i] = M_BINARY;
-        else if (d.algo == VS_ISECT_MERGE)
+        else if (algo == VS_ISECT_MERGE)
           meth[i] = M_MERGE;
-        else if (d.algo == VS_ISECT_BITMAP)
+        else if (algo == VS_ISECT_BITMAP)
           meth[i] = slot >= 0 ? M_BITMAP : M_BINARY;
         else
           meth[i] = (slot >= 0 && len >= 4 * best_len) ? M_BITMAP : len <= 8 * best_len ? M_MERGE : M_BINARY;
@@ -250,6 +254,124 @@ __global__ void __launch_bounds__(256) k_isect(Args a) {
     }
   }
   if (!a.emit) block_add(tot, a.total);
+}
+
+// Features of one call for the learned membership method, from up to
+// ISECT_SAMPLE base tuples spread over the base table: list lengths of the
+// walked (shortest) list and of the other adjacency lists, their ratios and how
+// often the other list's vertex has an adjacency bitmap.  With a picker the
+// block then runs the network and stores its choice (class 0 binary search,
+// 1 window merge, 2 hub bitmap) for k_isect.
+constexpr int ISECT_SAMPLE = 4096;
+
+__global__ void __launch_bounds__(256) k_isect_decide(Args a, uint32_t V, uint64_t E, int has_hubs,
+                                                      const void *picker, float *feat_out, int *method) {
+  __shared__ float acc[32];
+  __shared__ float f[pk::NF], h1[pk::H1], h2[pk::H2], out[pk::NO];
+  if (threadIdx.x < 32) acc[threadIdx.x] = 0.f;
+  __syncthreads();
+  const uint64_t n = a.nbase < (uint64_t)ISECT_SAMPLE ? a.nbase : (uint64_t)ISECT_SAMPLE;
+  // acc: 0 samples, 1 empty, 2 sum log len_walk, 3 sum log len_other, 4 sum log ratio, 5 hub, 6 ratio<=8,
+  //      7 bitmap rule, 8 other-list count, 16..23 hist log len_walk, 24..31 hist log ratio
+  for (uint64_t k = threadIdx.x; k < n; k += blockDim.x) {
+    const uint64_t t = n == a.nbase ? k : k * a.nbase / n;
+    float lw = 0.f;
+    int64_t walk = -1;
+    bool empty = false;
+    for (int i = 0; i < a.ndeps; i++) {
+      const Dep &d = a.dep[i];
+      if (d.kind != DEP_SORTED) continue;
+      const uint32_t u = d.base_u[t];
+      const int64_t len = u < d.n_u ? d.off[u + 1] - d.off[u] : 0;
+      if (len == 0) empty = true;
+      if (walk < 0 || len < walk) walk = len;
+    }
+    atomicAdd(&acc[0], 1.f);
+    if (walk < 0) continue;
+    if (empty) {
+      atomicAdd(&acc[1], 1.f);
+      continue;
+    }
+    lw = log2f(1.f + (float)walk);
+    atomicAdd(&acc[2], lw);
+    atomicAdd(&acc[16 + min(7, (int)(lw * 0.5f))], 1.f);
+    bool walked = false;
+    for (int i = 0; i < a.ndeps; i++) {
+      const Dep &d = a.dep[i];
+      if (d.kind != DEP_SORTED) continue;
+      const uint32_t u = d.base_u[t];
+      const int64_t len = d.off[u + 1] - d.off[u];
+      if (len == walk && !walked) {
+        walked = true;
+        continue;
+      }
+      const float lo = log2f(1.f + (float)len), lr = log2f((float)len / (float)walk);
+      const bool hub = d.hub_slot && d.hub_slot[u] >= 0;
+      atomicAdd(&acc[3], lo);
+      atomicAdd(&acc[4], lr);
+      atomicAdd(&acc[8], 1.f);
+      if (hub) atomicAdd(&acc[5], 1.f);
+      if (len <= 8 * walk) atomicAdd(&acc[6], 1.f);
+      if (hub && len >= 4 * walk) atomicAdd(&acc[7], 1.f);
+      atomicAdd(&acc[24 + max(0, min(7, (int)lr))], 1.f);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const float ns = fmaxf(acc[0], 1.f), nw = fmaxf(acc[0] - acc[1], 1.f), no = fmaxf(acc[8], 1.f);
+    int nsorted = 0;
+    for (int i = 0; i < a.ndeps; i++) nsorted += a.dep[i].kind == DEP_SORTED;
+    f[0] = log2f(1.f + (float)a.nbase) / 40.f;
+    f[1] = a.ndeps / 8.f;
+    f[2] = log2f(1.f + (float)V) / 32.f;
+    f[3] = log2f(1.f + (float)E) / 40.f;
+    f[4] = (float)E / fmaxf(1.f, (float)V) / 64.f;
+    f[5] = nsorted / 8.f;
+    f[6] = acc[1] / ns;
+    f[7] = acc[2] / nw / 32.f;
+    f[8] = acc[3] / no / 32.f;
+    f[9] = acc[4] / no / 32.f;
+    f[10] = acc[5] / no;
+    f[11] = acc[6] / no;
+    f[12] = acc[7] / no;
+    f[13] = (float)has_hubs;
+    f[14] = (float)a.all_mat;
+    f[15] = 0.f;
+    for (int b = 0; b < 8; b++) {
+      f[16 + b] = acc[16 + b] / nw;
+      f[24 + b] = acc[24 + b] / no;
+    }
+    if (feat_out)
+      for (int i = 0; i < pk::NF; i++) feat_out[i] = f[i];
+  }
+  __syncthreads();
+  if (!picker || !method) return;
+  const __nv_bfloat16 *w = (const __nv_bfloat16 *)picker;
+  const int t = threadIdx.x;
+  if (t < pk::H1) {
+    float s = __bfloat162float(w[pk::OFF_B1 + t]);
+    for (int i = 0; i < pk::NF; i++) s += __bfloat162float(w[pk::OFF_W1 + t * pk::NF + i]) * f[i];
+    h1[t] = s > 0.f ? s : 0.f;
+  }
+  __syncthreads();
+  if (t < pk::H2) {
+    float s = __bfloat162float(w[pk::OFF_B2 + t]);
+    for (int i = 0; i < pk::H1; i++) s += __bfloat162float(w[pk::OFF_W2 + t * pk::H1 + i]) * h1[i];
+    h2[t] = s > 0.f ? s : 0.f;
+  }
+  __syncthreads();
+  if (t < pk::NO) {
+    float s = __bfloat162float(w[pk::OFF_B3 + t]);
+    for (int i = 0; i < pk::H2; i++) s += __bfloat162float(w[pk::OFF_W3 + t * pk::H2 + i]) * h2[i];
+    out[t] = s;
+  }
+  __syncthreads();
+  if (t == 0) {
+    int best = 0;
+    for (int k = 1; k < pk::NO; k++)
+      if (out[k] > out[best]) best = k;
+    *method = best == 0 ? VS_ISECT_BINARY : best == 1 ? VS_ISECT_MERGE : VS_ISECT_BITMAP;
+  }
 }
 
 // Flat dependency -> CSR over u with duplicate pairs removed.
@@ -460,6 +582,13 @@ extern "C" {
 int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
                   uint32_t new_vertex_count, int only_count, uint64_t max_rows, vs_flat **out,
                   uint64_t *count, vs_stream_t stream) {
+  return vs_mintersect_ex(base, deps, ndeps, new_vertex_count, only_count, max_rows, nullptr, nullptr, out,
+                          count, stream);
+}
+
+int vs_mintersect_ex(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
+                     uint32_t new_vertex_count, int only_count, uint64_t max_rows, const vs_picker *method_picker,
+                     float *features, vs_flat **out, uint64_t *count, vs_stream_t stream) {
   if (!count || (!only_count && !out)) return fail(VS_ERR_ARG, "vs_mintersect: null output");
   if (!base.flat == !base.mat) return fail(VS_ERR_ARG, "base is exactly one of a flat table or a matrix");
   if (ndeps == 0 || ndeps > (uint32_t)MAX_DEPS || !deps)
@@ -538,6 +667,28 @@ int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
   }
   a.all_mat = nmat == ndeps;
   a.cache_rows = a.all_mat ? mat_rows : new_vertex_count;
+  // learned membership method (AUTO adjacency dependencies) and/or its features
+  const vs_graph *fg = nullptr;
+  bool hubs = false;
+  for (uint32_t i = 0; i < ndeps; i++)
+    if (deps[i].graph) {
+      fg = deps[i].graph;
+      hubs |= a.dep[i].hub_slot != nullptr;
+    }
+  if ((method_picker || features) && fg && !a.all_mat) {
+    int *d_method = nullptr;
+    float *d_feat = nullptr;
+    VS_TRY(sc.get(&d_method, 1));
+    VS_TRY(sc.get(&d_feat, pk::NF));
+    VS_CK(cudaMemsetAsync(d_method, 0, sizeof(int), st));  // VS_ISECT_AUTO until the network decides
+    { k_isect_decide<<<1, 256, 0, st>>>(a, fg->V, fg->E, hubs ? 1 : 0,
+                                      method_picker ? vs_picker_device_weights(method_picker) : nullptr, d_feat,
+                                      d_method); vs::note_launch(); }
+    a.method = method_picker ? d_method : nullptr;
+    if (features) VS_CK(cudaMemcpyAsync(features, d_feat, sizeof(float) * pk::NF, cudaMemcpyDefault, st));
+  } else if (features) {
+    std::memset(features, 0, sizeof(float) * pk::NF);
+  }
   unsigned long long *d_total, *tcnt = nullptr, *toff = nullptr;
   VS_TRY(sc.get(&d_total, 1));
   VS_CK(cudaMemsetAsync(d_total, 0, 8, st));

@@ -302,3 +302,16 @@ def test_expand_layers_with_distance(vs, graphs, path, krange):
         assert set(np.unique(d).tolist()) <= set(range(k0, k_actual + 1))
         if path == "shortest":  # layers are disjoint: every (source, vertex) pair once
             assert len(set(zip(r.tolist(), c.tolist()))) == total
+
+
+def test_malformed_csr_is_rejected(vs):
+    g = graphgen.from_edges(10, [1, 2], [2, 3])
+    bad = g.fwd_dst.copy()
+    bad[0] = 10  # a target outside the vertex range
+    with pytest.raises(vs.VsError):
+        vs.DeviceGraph(g.V, g.E, g.fwd_off, bad, g.rev_off, g.rev_src)
+    off = g.fwd_off.copy()
+    off[5], off[6] = off[6] + 1, off[6]  # offsets that go down
+    with pytest.raises(vs.VsError):
+        vs.DeviceGraph(g.V, g.E, off, g.fwd_dst, g.rev_off, g.rev_src)
+    vs.DeviceGraph(g.V, g.E, g.fwd_off, g.fwd_dst, g.rev_off, g.rev_src)  # the well-formed one loads

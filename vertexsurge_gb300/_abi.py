@@ -229,6 +229,7 @@ class DeviceGraph:
     """A CSR graph resident in HBM (vs_graph)."""
 
     def __init__(self, V, E, fwd_off, fwd_dst, rev_off, rev_src, directed=True, stream=None):
+        self.h = None
         h = C.c_void_p()
         check(lib().vs_graph_upload(V, E, _ptr(fwd_off), _ptr(fwd_dst), _ptr(rev_off), _ptr(rev_src),
                                     1 if directed else 0, _stream(stream), C.byref(h)))

@@ -391,6 +391,19 @@ int vs_init(int device) {
   return VS_OK;
 }
 
+// A CSR is well formed when off[0] = 0, off[V] = E, offsets never decrease
+// and every target is a vertex id; any violation sets *bad.
+__global__ void k_check_csr(const int64_t *__restrict__ off, const uint32_t *__restrict__ adj, uint32_t V,
+                            uint64_t E, unsigned *bad) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool ok = true;
+  if (i0 == 0) ok = off[0] == 0 && off[V] == (int64_t)E;
+  for (uint64_t i = i0; i < V; i += stride) ok &= off[i] <= off[i + 1];
+  for (uint64_t i = i0; i < E; i += stride) ok &= adj[i] < V;
+  if (!ok) atomicExch(bad, 1u);
+}
+
 int vs_graph_upload(uint32_t V, uint64_t E, const int64_t *fwd_off, const uint32_t *fwd_dst,
                     const int64_t *rev_off, const uint32_t *rev_src, int directed,
                     vs_stream_t stream, vs_graph **out) {
@@ -413,10 +426,33 @@ int vs_graph_upload(uint32_t V, uint64_t E, const int64_t *fwd_off, const uint32
     vs_graph_free(g);
     return rc;
   }
-  cudaError_t e = cudaStreamSynchronize(st);
+  // every later kernel indexes rows and lists by these arrays: reject malformed input here
+  unsigned *bad = nullptr;
+  if ((rc = dalloc_n(&bad, 1, st)) != VS_OK) {
+    vs_graph_free(g);
+    return rc;
+  }
+  unsigned hbad = 0;
+  cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(unsigned), st);
+  const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((std::max<uint64_t>(V, E) + 255) / 256,
+                                                                   (uint64_t)sm_count() * 8));
+  if (e == cudaSuccess) {
+    k_check_csr<<<blocks, 256, 0, st>>>(g->fwd_off, g->fwd_dst, V, E, bad);
+    vs::note_launch();
+    k_check_csr<<<blocks, 256, 0, st>>>(g->rev_off, g->rev_src, V, E, bad);
+    vs::note_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, bad, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  dfree(bad, st);
   if (e != cudaSuccess) {
     vs_graph_free(g);
-    return cuda_fail(e, "cudaStreamSynchronize", __FILE__, __LINE__);
+    return cuda_fail(e, "vs_graph_upload", __FILE__, __LINE__);
+  }
+  if (hbad) {
+    vs_graph_free(g);
+    return fail(VS_ERR_ARG, "malformed CSR: offsets must rise from 0 to E and every target must be < V (%u)", V);
   }
   *out = g;
   return VS_OK;

@@ -71,7 +71,7 @@ def test_row_block_counts_reject_bad_blocks(vs, graphs):
     m.free()
 
 
-@pytest.mark.parametrize("wave_rows", [256, 700])
+@pytest.mark.parametrize("wave_rows", [256, 400])
 def test_batch_counts_equal_solo(vs, graphs, wave_rows):
     import torch
     from vertexsurge_gb300 import batch
@@ -80,7 +80,7 @@ def test_batch_counts_equal_solo(vs, graphs, wave_rows):
     solo = batch.solo_counts(dg, qs)
     stream = torch.cuda.Stream()
     b = batch.Batch(dg, qs, wave_rows, stream)
-    assert len(b.waves) >= 2
+    assert len(b.waves) >= 2, [len(q.sources) for q in qs]
     b.run_eager()
     assert np.array_equal(b.counts(), solo)
     b.d_counts.zero_()

@@ -544,13 +544,19 @@ def run_gpu(args, w, rank, world, local_rank):
                                            (Sa, (1, 1), "any", tP))]
         for p in lp:
             p.set_picker(pk)
+        # the intersection's membership method, chosen by its own trained network
+        from vertexsurge_gb300 import isect_train
+        ipk = None
+        if isect_train.WEIGHTS_FILE.exists():
+            ipk = vs.Picker()
+            ipk.set_params(np.load(isect_train.WEIGHTS_FILE))
 
         def step_learned():
             lp[0].run(dA, stream=stream)
             lp[1].run(dB, stream=stream)
             _, jc3, _ = vs.hash_join(lp[0].result(), lp[1].result(), 1, 1, only_count=True, stream=stream)
             lp[2].run(dA, stream=stream)
-            _, tc3, _ = vs.mintersect(lp[2].result(), adj, g.V, only_count=True, stream=stream)
+            _, tc3, _ = vs.mintersect(lp[2].result(), adj, g.V, only_count=True, stream=stream, method_picker=ipk)
             return jc3, tc3
 
         for _ in range(max(1, min(args.warmup, 3))):

@@ -156,6 +156,8 @@ int vs_flat_upload(vs_flat *f, uint32_t col, const void *data, vs_stream_t strea
 int vs_flat_download(const vs_flat *f, uint32_t col, void *data, vs_stream_t stream);
 int vs_flat_info(const vs_flat *f, uint32_t *ncols, uint64_t *nrows, int32_t *types);
 int vs_flat_free(vs_flat *f);
+/* Device address of column col (valid until the table is freed). */
+int vs_flat_column(const vs_flat *f, uint32_t col, const void **device_ptr);
 
 /* ---- expand (replaces VExpand + Expand<DenseVarStackMatrix> with
  *      ExpandStrategy::Dense: src/objects/operator/vexpand.cpp:45-483,
@@ -309,11 +311,11 @@ typedef struct vs_isect_dep {
   uint32_t base_col;
   /* Membership test against a graph adjacency list (VS_ISECT_*; 0 = AUTO).
    * Every choice gives the same result.  AUTO decides per base tuple: the
-   * adjacency bitmap when the list's vertex is a hub and its list is at least
-   * 4x the walked one, a warp-window merge when it is at most 8x, else a
-   * binary search.  Hub bitmaps (the highest-degree vertices, degree >= 1024,
-   * at most 1 GiB per graph and direction) are built on first use and kept
-   * with the graph. */
+   * adjacency bitmap when the list's vertex is a hub, a warp-window merge when
+   * the walked list has at least 512 entries and this one at most 4x that,
+   * else a binary search.  Hub bitmaps (the highest-degree vertices, degree
+   * >= 1024, at most 1 GiB per graph and direction) are built on first use
+   * and kept with the graph. */
   int32_t algo;
 } vs_isect_dep;
 #define VS_ISECT_AUTO 0
@@ -356,6 +358,14 @@ int vs_matrix_row_or_sum(const vs_bitmat *m, vs_flat **out, vs_stream_t stream);
 int vs_semi_join(vs_table_ref a, vs_table_ref b, uint32_t nkeys, const uint32_t *a_key_cols,
                  const uint32_t *b_key_cols, int only_count, vs_flat **out_flat, vs_bitmat **out_mat,
                  uint64_t *count, vs_stream_t stream);
+
+/* Scan with a range filter (replaces Scan + VariableFilter over a vertex
+ * property, big_operators.hh:21-38, scan.cpp:31-70): the vertex ids i < n with
+ * lo <= values[i] <= hi, ascending, as one VID column.  values: device array
+ * of n unsigned 1-, 2- or 4-byte or signed 8-byte properties; NULL selects
+ * every id (no filter). */
+int vs_select_ids_in_range(const void *values, int value_bytes, uint32_t n, int64_t lo, int64_t hi, vs_flat **out,
+                           vs_stream_t stream);
 
 /* ---- learned per-hop strategy picker (no counterpart in the reference; it
  *      replaces the fixed Adaptive coverage thresholds of expand.cpp:346-414)

@@ -90,8 +90,8 @@ def build_gen() -> Path:
 
 
 def build_ops() -> Path:
-    srcs = [PKG / "cpp" / "vs_operators.cpp", PKG / "cpp" / "graph_dir.cpp"]
-    hdrs = [PKG / "cpp" / "vs_operators.hh", ROOT / "include" / "vertexsurge_gb300.h"]
+    srcs = [PKG / "cpp" / "vs_operators.cpp", PKG / "cpp" / "graph_dir.cpp", PKG / "cpp" / "vql.cpp"]
+    hdrs = [PKG / "cpp" / "vs_operators.hh", PKG / "cpp" / "vql.hh", ROOT / "include" / "vertexsurge_gb300.h"]
     if not srcs[0].exists():
         return OPS_LIB
     if _stale(OPS_LIB, srcs + hdrs + [LIB]):

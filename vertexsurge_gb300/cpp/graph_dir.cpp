@@ -225,8 +225,31 @@ void Graph::load_dir() {
   ss << f.rdbuf();
   const std::string text = ss.str();
   Json schema = Parser(text).value();
-  for (const Json &v : schema.at("vertex").arr)
-    add_vertex_type(v.at("type").str, (size_t)v.at("statistics").at("count").num);
+  for (const Json &v : schema.at("vertex").arr) {
+    const TypeName vt = v.at("type").str;
+    const size_t n = (size_t)v.at("statistics").at("count").num;
+    add_vertex_type(vt, n);
+    // properties ("Type.name" DiskArray files, Graph::load's variable table, meta/schema.cpp:160-168)
+    for (const auto &kv : v.at("properties").obj) {
+      const std::string ty = kv.second.at("type").str;
+      const size_t bytes = ty == "TagValue8" ? 1 : ty == "TagValue16" ? 2 : (ty == "VID" || ty == "Int32") ? 4
+                         : ty == "Int64" ? 8 : 0;
+      if (!bytes) continue;  // strings and pairs are not vertex filters of the path
+      const std::filesystem::path f = dir / (vt + "." + kv.first);
+      if (!std::filesystem::exists(f)) continue;
+      Mapped m;
+      map_disk_array(f, bytes, m);
+      std::vector<uint64_t> vals((size_t)m.count);
+      const unsigned char *p = static_cast<const unsigned char *>(m.data());
+      for (size_t i = 0; i < vals.size(); i++) {
+        if (bytes == 1) vals[i] = p[i];
+        else if (bytes == 2) vals[i] = reinterpret_cast<const uint16_t *>(p)[i];
+        else if (bytes == 4) vals[i] = reinterpret_cast<const uint32_t *>(p)[i];
+        else vals[i] = (uint64_t)reinterpret_cast<const int64_t *>(p)[i];
+      }
+      add_vertex_property(vt + "." + kv.first, vals, bytes == 8 ? Type::Int64 : Type::VID);
+    }
+  }
   for (const Json &e : schema.at("edge").arr) {
     const TypeName src = e.at("src").str, dst = e.at("dst").str, type = e.at("type").str;
     const bool directed = e.at("directed").b;

@@ -161,6 +161,7 @@ bool MatrixTable::get(size_t r, size_t c) const {
 // ---- graph --------------------------------------------------------------------
 Graph::~Graph() {
   for (auto &kv : edges) vs_graph_free(kv.second.g);
+  for (auto &kv : properties) vs_flat_free(kv.second);
   if (BigOperator::graph_store == this) BigOperator::graph_store = nullptr;
 }
 
@@ -171,6 +172,21 @@ void Graph::add_edge_type(const TypeName &src, const TypeName &edge, const TypeN
   check(vs_graph_upload(V, E, fwd_off, fwd_dst, rev_off, rev_src, directed ? 1 : 0,
                         BigOperator::stream, &t.g));
   edges[src + "_" + edge + "_" + dst] = t;
+}
+
+void Graph::add_vertex_property(const std::string &var, const std::vector<uint64_t> &values, Type t) {
+  const int32_t ty = t == Type::Int64 ? VS_T_I64 : VS_T_VID;
+  vs_flat *f = nullptr;
+  check(vs_flat_create(1, &ty, values.size(), &f));
+  if (t == Type::Int64) {
+    check(vs_flat_upload(f, 0, values.data(), BigOperator::stream));
+  } else {
+    std::vector<uint32_t> v(values.begin(), values.end());
+    check(vs_flat_upload(f, 0, v.data(), BigOperator::stream));
+  }
+  auto it = properties.find(var);
+  if (it != properties.end()) vs_flat_free(it->second);
+  properties[var] = f;
 }
 
 const Graph::EdgeType &Graph::edge(const TypeName &src, const TypeName &e, const TypeName &dst) const {
@@ -226,6 +242,39 @@ static int abi_dir(Direction d, bool directed) {
       if (directed) throw Error(VS_ERR_ARG, "a directed self edge needs a direction");
       return VS_DIR_FORWARD;
   }
+}
+
+// ---- Scan ---------------------------------------------------------------------
+Scan::Scan(TypeName type, std::vector<VariableName> fetch, std::vector<VariableFilter> f)
+    : vertex_type(std::move(type)), filters(std::move(f)) {
+  if (fetch.size() != 1 || fetch[0] != "id")
+    throw Error(VS_ERR_UNSUPPORTED, "Scan fetches the vertex id only");
+  if (filters.size() > 1) throw Error(VS_ERR_UNSUPPORTED, "Scan takes at most one range filter");
+  results_schema = TableSchema{{{vertex_type + ".id", Type::VID}}};  // Scan::set_table_schema (scan.cpp:22-29)
+}
+
+void Scan::run_internal() {
+  if (!graph_store || !graph_store->vertex_count.count(vertex_type))
+    throw Error(VS_ERR_ARG, "vertex type " + vertex_type + " is not in the loaded graph");
+  const size_t V = graph_store->vertex_count.at(vertex_type);
+  const void *vals = nullptr;
+  int bytes = 0;
+  int64_t lo = 0, hi = 0;
+  if (!filters.empty()) {
+    auto it = graph_store->properties.find(filters[0].property);
+    if (it == graph_store->properties.end()) throw Error(VS_ERR_ARG, "no vertex property " + filters[0].property);
+    int32_t ty = 0;
+    uint64_t n = 0;
+    check(vs_flat_info(it->second, nullptr, &n, &ty));
+    if (n != V) throw Error(VS_ERR_ARG, "property " + filters[0].property + " has a value per vertex");
+    check(vs_flat_column(it->second, 0, &vals));
+    bytes = ty == VS_T_I64 ? 8 : 4;
+    lo = filters[0].lo;
+    hi = filters[0].hi;
+  }
+  vs_flat *f = nullptr;
+  check(vs_select_ids_in_range(vals, bytes, (uint32_t)V, lo, hi, &f, stream));
+  results = std::make_shared<FlatTable>(results_schema, f);
 }
 
 // ---- VExpand ------------------------------------------------------------------

@@ -145,6 +145,10 @@ class Graph {
   };
   std::map<TypeName, size_t> vertex_count;
   std::map<std::string, EdgeType> edges;
+  // vertex properties ("Type.name"), one device column each (1/2/4-byte
+  // unsigned values widened to VID, Int64 kept); read from the directory
+  std::map<std::string, vs_flat *> properties;
+  void add_vertex_property(const std::string &var, const std::vector<uint64_t> &values, Type t);
   std::filesystem::path dir;  // the reference's graph directory (empty: types added by hand)
   Graph() = default;
   // Graph(dir) + load(): schema.json and the CSR DiskArray files the reference
@@ -193,6 +197,25 @@ class BigOperator {
 
 class InlinedData : public BigOperator {
   void run_internal() override {}
+};
+
+// An inclusive range filter on a vertex property ("Person.community"),
+// VariableFilter with Range (meta/type.hh:250-310, utils/utils.hh:574-586).
+struct VariableFilter {
+  VariableName property;
+  int64_t lo, hi;
+};
+
+// Scan(vertex_type, {"id"}, filters) (big_operators.hh:21-38, scan.cpp:14-70):
+// the ids of the vertices passing the filter, as "Type.id".  Fetches only
+// the id (the plans' use); at most one filter.
+class Scan : public BigOperator {
+  TypeName vertex_type;
+  std::vector<VariableFilter> filters;
+  void run_internal() override;
+
+ public:
+  Scan(TypeName vertex_type, std::vector<VariableName> fetch_properties, std::vector<VariableFilter> filters = {});
 };
 
 class VExpand : public BigOperator {

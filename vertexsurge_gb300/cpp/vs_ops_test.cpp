@@ -15,6 +15,7 @@
 #include <set>
 #include <vector>
 
+#include "../cpp/vql.hh"
 #include "../cpp/vs_operators.hh"
 
 using namespace vsgb;
@@ -411,9 +412,46 @@ static int graph_dir_count(const char *dir) {
   return 0;
 }
 
+// Runs a VQL query over a graph directory: prints "count N" (count of) or
+// "rows N" and the rows as "r: v0 v1 ...".
+static int vql_run(const char *dir, const char *text) {
+  Graph g{std::filesystem::path(dir)};
+  g.load();
+  query::Builder b(text);
+  b.parse();
+  auto root = b.build(b.variable_apperance_order());
+  root->run();
+  if (b.only_count) {  // a two-vertex query ends at its expand: count its pairs
+    auto *ft = root->results->down_to_flat_table();
+    const bool count_table = ft && ft->schema.columns.size() == 1 && ft->schema.columns[0].name == "count";
+    std::printf("count %lld\n", count_table ? (long long)single_count(root->results.get())
+                                            : (long long)root->results->tuple_count());
+    return 0;
+  }
+  auto *f = root->results->down_to_flat_table();
+  std::vector<std::vector<uint64_t>> cols;
+  if (f) {
+    for (size_t c = 0; c < f->schema.columns.size(); c++) cols.push_back(f->column(c));
+  } else {  // a matrix: its (row value, column value) pairs
+    vs_flat *fl = nullptr;
+    check(vs_bitmat_to_flat(root->results->down_to_matrix_table()->h, &fl, nullptr));
+    FlatTable t(TableSchema{{{"r", Type::VID}, {"c", Type::VID}}}, fl);
+    cols = {t.column(0), t.column(1)};
+  }
+  const size_t n = cols.empty() ? 0 : cols[0].size();
+  std::printf("rows %zu\n", n);
+  for (size_t r = 0; r < n; r++) {
+    std::printf("r:");
+    for (auto &c : cols) std::printf(" %llu", (unsigned long long)c[r]);
+    std::printf("\n");
+  }
+  return 0;
+}
+
 int main(int argc, char **argv) {
   check(vs_init(0));
   if (argc >= 3 && std::string(argv[1]) == "--graph-dir") return graph_dir_count(argv[2]);
+  if (argc >= 4 && std::string(argv[1]) == "--vql") return vql_run(argv[2], argv[3]);
   // like the reference's tests, load a graph first: operators resolve vertex types against it
   HostGraph hg = small_graph();
   Graph g;

@@ -609,6 +609,13 @@ int vs_flat_info(const vs_flat *f, uint32_t *ncols, uint64_t *nrows, int32_t *ty
   return VS_OK;
 }
 
+int vs_flat_column(const vs_flat *f, uint32_t col, const void **device_ptr) {
+  if (!f || !device_ptr) return fail(VS_ERR_ARG, "vs_flat_column: null argument");
+  if (col >= f->ncols) return fail(VS_ERR_ARG, "column %u of %u", col, f->ncols);
+  *device_ptr = f->cols[col];
+  return VS_OK;
+}
+
 int vs_flat_free(vs_flat *f) {
   if (!f) return VS_OK;
   for (uint32_t i = 0; i < f->ncols; i++) dfree(f->cols[i], f->st);

@@ -359,6 +359,31 @@ int hash_alloc(Scratch &sc, uint64_t n, HashTable *t) {
   return VS_OK;
 }
 
+// ---- vertex selection by a property range (the Scan filter of the plans) -----
+__global__ void k_range_flags(const void *__restrict__ vals, int bytes, uint32_t n, long long lo, long long hi,
+                              unsigned long long *__restrict__ f) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    long long v = 0;
+    if (vals) {
+      if (bytes == 1)
+        v = ((const uint8_t *)vals)[i];
+      else if (bytes == 2)
+        v = ((const uint16_t *)vals)[i];
+      else if (bytes == 4)
+        v = ((const uint32_t *)vals)[i];
+      else
+        v = ((const long long *)vals)[i];
+    }
+    f[i] = !vals || (v >= lo && v <= hi);
+  }
+}
+
+__global__ void k_compact_ids(const unsigned long long *__restrict__ f, const unsigned long long *__restrict__ pos,
+                              uint32_t n, uint32_t *__restrict__ out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (f[i]) out[pos[i]] = i;
+}
+
 }  // namespace cs
 }  // namespace vs
 
@@ -433,6 +458,46 @@ int vs_matrix_row_or_sum(const vs_bitmat *m, vs_flat **out, vs_stream_t stream) 
   if (e != cudaSuccess) {
     vs_flat_free(f);
     return cuda_fail(e, "vs_matrix_row_or_sum", __FILE__, __LINE__);
+  }
+  *out = f;
+  return VS_OK;
+}
+
+int vs_select_ids_in_range(const void *values, int value_bytes, uint32_t n, int64_t lo, int64_t hi, vs_flat **out,
+                           vs_stream_t stream) {
+  if (!out) return fail(VS_ERR_ARG, "vs_select_ids_in_range: null output");
+  if (values && value_bytes != 1 && value_bytes != 2 && value_bytes != 4 && value_bytes != 8)
+    return fail(VS_ERR_ARG, "property values are 1, 2, 4 or 8 bytes wide");
+  if (values) {
+    cudaPointerAttributes at{};
+    VS_CK(cudaPointerGetAttributes(&at, values));
+    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+      return fail(VS_ERR_ARG, "vs_select_ids_in_range: values must be device memory");
+  }
+  cudaStream_t st = S(stream);
+  Scratch sc{st};
+  unsigned long long *flags, *pos;
+  VS_TRY(sc.get(&flags, n));
+  VS_TRY(sc.get(&pos, (size_t)n + 1));
+  unsigned long long cnt = 0;
+  if (n) {
+    { k_range_flags<<<grid_for(n), 256, 0, st>>>(values, value_bytes, n, lo, hi, flags); vs::note_launch(); }
+    VS_TRY(exclusive_scan_u64(flags, pos, n, st));
+    unsigned long long last[2];
+    VS_CK(cudaMemcpyAsync(&last[0], pos + n - 1, 8, cudaMemcpyDeviceToHost, st));
+    VS_CK(cudaMemcpyAsync(&last[1], flags + n - 1, 8, cudaMemcpyDeviceToHost, st));
+    VS_CK(cudaStreamSynchronize(st));
+    cnt = last[0] + last[1];
+  }
+  const int32_t types[1] = {VS_T_VID};
+  vs_flat *f = nullptr;
+  VS_TRY(flat_alloc(1, types, cnt, st, &f));
+  if (cnt) { k_compact_ids<<<grid_for(n), 256, 0, st>>>(flags, pos, n, (uint32_t *)f->cols[0]); vs::note_launch(); }
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    vs_flat_free(f);
+    return cuda_fail(e, "vs_select_ids_in_range", __FILE__, __LINE__);
   }
   *out = f;
   return VS_OK;

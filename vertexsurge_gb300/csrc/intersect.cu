@@ -17,7 +17,9 @@
 //   merge    a warp-wide window of 32 list entries slides forward with the
 //            candidates; each candidate finds its place by a shuffle search,
 //   binary   a binary search of the whole list,
-// chosen per base tuple from the two list lengths (or fixed by the caller).
+// chosen per base tuple (bitmap when the list's vertex has one, merge for two
+// long lists of similar length, else binary search), fixed by the caller, or
+// chosen per call by a trained network (k_isect_decide).
 // Counting and emitting are two passes over the same code; a prefix sum of
 // the per-tuple counts places every tuple's output.
 #include <algorithm>
@@ -200,8 +202,8 @@ __global__ void __launch_bounds__(256) k_isect(Args a) {
           meth[i] = M_MERGE;
         else if (algo == VS_ISECT_BITMAP)
           meth[i] = slot >= 0 ? M_BITMAP : M_BINARY;
-        else
-          meth[i] = (slot >= 0 && len >= 4 * best_len) ? M_BITMAP : len <= 8 * best_len ? M_MERGE : M_BINARY;
+        else  // measured on GB300: a bitmap probe wins whenever one exists; merging pays only for long lists of similar length
+          meth[i] = slot >= 0 ? M_BITMAP : (best_len >= 512 && len <= 4 * best_len) ? M_MERGE : M_BINARY;
       }
       const Dep &L = a.dep[best];
       for (int64_t j0 = lo[best]; j0 < hi[best]; j0 += 32) {
@@ -311,8 +313,8 @@ __global__ void __launch_bounds__(256) k_isect_decide(Args a, uint32_t V, uint64
       atomicAdd(&acc[4], lr);
       atomicAdd(&acc[8], 1.f);
       if (hub) atomicAdd(&acc[5], 1.f);
-      if (len <= 8 * walk) atomicAdd(&acc[6], 1.f);
-      if (hub && len >= 4 * walk) atomicAdd(&acc[7], 1.f);
+      if (walk >= 512 && len <= 4 * walk) atomicAdd(&acc[6], 1.f);
+      if (hub) atomicAdd(&acc[7], 1.f);
       atomicAdd(&acc[24 + max(0, min(7, (int)lr))], 1.f);
     }
   }

@@ -77,10 +77,23 @@ def write_disk_array(path, arr: np.ndarray) -> None:
         f.write(arr.tobytes())
 
 
-def save(dir_, g: HostGraph, vertex_type="Person", edge_type="knows", graph_name="synthetic") -> None:
-    """Write one vertex type and one self edge type (src = dst = vertex_type)."""
+PROPERTY_TYPES = {np.dtype(np.uint8): "TagValue8", np.dtype(np.uint16): "TagValue16",
+                  np.dtype(np.uint32): "VID", np.dtype(np.int32): "Int32", np.dtype(np.int64): "Int64"}
+
+
+def save(dir_, g: HostGraph, vertex_type="Person", edge_type="knows", graph_name="synthetic",
+         properties: dict | None = None) -> None:
+    """Write one vertex type (with optional properties: name -> per-vertex
+    array, stored as "Type.name") and one self edge type (src = dst)."""
     d = Path(dir_)
     d.mkdir(parents=True, exist_ok=True)
+    props = {}
+    for name, arr in (properties or {}).items():
+        arr = np.ascontiguousarray(arr)
+        if len(arr) != g.V or arr.dtype not in PROPERTY_TYPES:
+            raise ValueError(f"property {name}: one value per vertex of a supported type")
+        write_disk_array(d / f"{vertex_type}.{name}", arr)
+        props[name] = {"name": name, "type": PROPERTY_TYPES[arr.dtype]}
     names = csr_names(vertex_type, edge_type, vertex_type, g.directed)
     write_disk_array(d / names["fwd_index"], g.fwd_off.astype(np.int64))
     write_disk_array(d / names["fwd_data"], g.fwd_dst.astype(np.uint32))
@@ -89,7 +102,7 @@ def save(dir_, g: HostGraph, vertex_type="Person", edge_type="knows", graph_name
         write_disk_array(d / names["bwd_data"], g.rev_src.astype(np.uint32))
     schema = {
         "graph_name": graph_name, "graph_type": "synthetic",
-        "vertex": [{"type": vertex_type, "statistics": {"count": int(g.V)}, "properties": {}}],
+        "vertex": [{"type": vertex_type, "statistics": {"count": int(g.V)}, "properties": props}],
         "edge": [{"type": edge_type, "directed": bool(g.directed), "allow_multiple_edge": False,
                   "src": vertex_type, "dst": vertex_type, "properties": {},
                   "statistics": {"count": int(g.E)},

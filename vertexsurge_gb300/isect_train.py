@@ -41,7 +41,8 @@ class Calls:
                 np.asarray(self.rule, np.float64), np.asarray(self.call, np.int64))
 
 
-def graph_suite(scales=(18, 19, 20, 21), skews=(0.45, 0.57, 0.65), zipf=((1_000_000, 30_000_000),)):
+def graph_suite(scales=(18, 19, 20, 21, 22), skews=(0.45, 0.57, 0.65), zipf=((1_000_000, 30_000_000),
+                                                                                (10_000_000, 300_000_000))):
     gs = []
     for sc in scales:
         for a in skews:
@@ -140,12 +141,12 @@ def train_and_evaluate(calls: Calls, epochs=60, seed=3, holdout=0.25):
 def main():
     import argparse
     ap = argparse.ArgumentParser(description="log, train and evaluate the intersection-method picker")
-    ap.add_argument("--calls", type=int, default=3000)
+    ap.add_argument("--calls", type=int, default=6000)
     ap.add_argument("--minutes", type=float, default=0.0)
     ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--out", default=str(WEIGHTS_FILE))
     ap.add_argument("--report", default="")
-    ap.add_argument("--scales", default="18,19,20,21")
+    ap.add_argument("--scales", default="18,19,20,21,22")
     args = ap.parse_args()
     vs.init(0)
     graphs = graph_suite(scales=tuple(int(x) for x in args.scales.split(",")))

@@ -139,3 +139,14 @@ def test_semi_join_rejects_colmain_and_wide_keys(vs):
         vs.semi_join(f, cm, [0], [0])
     with pytest.raises(vs.VsError):
         vs.semi_join(f, f, [0, 1, 2], [0, 1, 2])
+
+
+def test_select_ids_in_range(vs):
+    import torch
+    rng = np.random.default_rng(3)
+    for dt in (torch.uint8, torch.int16, torch.int32, torch.int64):
+        v = torch.from_numpy(rng.integers(0, 50, 10_000).astype(np.int64)).to(dt).cuda()
+        got = vs.select_ids_in_range(v, 10, 20).columns()[0]
+        h = v.cpu().numpy()
+        assert np.array_equal(got, np.nonzero((h >= 10) & (h <= 20))[0].astype(np.uint32)), dt
+    assert np.array_equal(vs.select_ids_in_range(77, 0, 0).columns()[0], np.arange(77, dtype=np.uint32))

@@ -152,6 +152,9 @@ _SIGS += [
     ("vs_hash_join_count_row_blocks", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                                 C.c_void_p]),
     ("vs_matrix_column_count", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.c_void_p]),
+    ("vs_select_ids_in_range", C.c_int, [C.c_void_p, C.c_int, C.c_uint32, C.c_int64, C.c_int64,
+                                         C.POINTER(C.c_void_p), C.c_void_p]),
+    ("vs_flat_column", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p)]),
     ("vs_mintersect_ex", C.c_int, [TableRef, C.POINTER(IsectDep), C.c_uint32, C.c_uint32, C.c_int, C.c_uint64,
                                    C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
                                    C.c_void_p]),
@@ -662,6 +665,18 @@ def layers_to_flat(layers: list, stream=None) -> "FlatTable":
     d = np.ascontiguousarray([h for h, _ in layers], dtype=np.int32)
     out = C.c_void_p()
     check(lib().vs_layers_to_flat(hs, _ptr(d), len(layers), C.byref(out), _stream(stream)))
+    return FlatTable(out)
+
+
+def select_ids_in_range(values, lo, hi, stream=None) -> "FlatTable":
+    """Scan filter: ids i with lo <= values[i] <= hi; values a device torch tensor of
+    uint8/int16/int32/int64 (or None with an int n meaning every id < n)."""
+    if isinstance(values, int):
+        ptr, nbytes, n = None, 0, values
+    else:
+        ptr, nbytes, n = _ptr(values), values.element_size(), values.numel()
+    out = C.c_void_p()
+    check(lib().vs_select_ids_in_range(ptr, nbytes, n, int(lo), int(hi), C.byref(out), _stream(stream)))
     return FlatTable(out)
 
 

@@ -81,6 +81,19 @@ def sources(g, w):
     return sa, sb
 
 
+def profiled_traffic(workload: str):
+    """DRAM bytes per launch of the roofline kernel, from the committed ncu
+    summary of this workload (the line `traffic_bytes_per_launch: N`), or None."""
+    f = ROOT / "profiles" / f"k_pull_{workload}.md"
+    try:
+        for line in f.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":", 1)[1].strip())
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 def peaks():
     try:
         p = json.loads(PEAKS_FILE.read_text())
@@ -581,7 +594,9 @@ def run_gpu(args, w, rank, world, local_rank):
     peak, peak_kind = peaks()
     achieved = pull_bytes / (pull_ms / 1e3) / 1e9 if pull_ms else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if achieved else None, "traffic": None,
+                "frac": achieved / peak if achieved else None, "traffic": profiled_traffic(args.workload),
+                "traffic_source": f"profiles/k_pull_{args.workload}.md (ncu dram__bytes_read.sum + "
+                                  "dram__bytes_write.sum per working launch)",
                 "kernel": "k_pull (expand A, pull hops)", "peak_source": peak_kind,
                 "compulsory_frac": (pull_comp / (pull_ms / 1e3) / 1e9) / peak if pull_ms else None,
                 "per_launch_ms": pull_ms / max(1, args.steps * sum(1 for s in stA["strategy"][1:] if s == 1))}

@@ -328,9 +328,10 @@ int vs_mintersect(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps,
                   uint64_t *count, vs_stream_t stream);
 /* The same with the learned choice of the adjacency membership method (no
  * counterpart in the reference): method_picker (a vs_picker trained on
- * intersection timings; class 0 = binary search, 1 = window merge, 2 = hub
- * bitmap) decides on the device, from 32 features sampled over up to 4096
- * base tuples, for every graph dependency whose algo is VS_ISECT_AUTO.
+ * intersection timings; class 0 = the per-tuple rule of VS_ISECT_AUTO,
+ * 1 = binary search, 2 = hub bitmap) decides on the device, from 32 features
+ * sampled over up to 4096 base tuples, for every graph dependency whose algo
+ * is VS_ISECT_AUTO.
  * features (nullable, 32 floats, host or device) receives those features.
  * Results do not depend on the choice. */
 typedef struct vs_picker vs_picker;

@@ -78,7 +78,10 @@ struct Args {
   int nbcols;
   uint32_t *out_new;
   const int *method;  // learned method for AUTO adjacency deps (VS_ISECT_*), or NULL
+  unsigned long long *next;  // work queue head: next base tuple to hand out (zeroed per launch)
 };
+
+constexpr int ISECT_CHUNK = 4;  // base tuples a warp takes from the queue at a time
 
 __device__ __forceinline__ bool in_sorted(const uint32_t *a, int64_t lo, int64_t hi, uint32_t x) {
   while (lo < hi) {
@@ -105,12 +108,19 @@ __device__ __forceinline__ void emit_row(const Args &a, uint64_t t, uint64_t pos
   a.out_new[pos] = a.target_row_map ? a.target_row_map[x] : x;
 }
 
+// Base tuples differ by orders of magnitude in cost (hub lists), so warps
+// take small chunks from a queue instead of a fixed stride, and each warp adds
+// its count on its own (no block-wide barrier waiting for the slowest warp).
 __global__ void __launch_bounds__(256) k_isect(Args a) {
   const int lane = threadIdx.x & 31;
-  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
   unsigned long long tot = 0;
-  for (uint64_t t = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); t < a.nbase;
-       t += warps) {
+  for (;;) {
+  unsigned long long t0 = 0;
+  if (lane == 0) t0 = atomicAdd(a.next, (unsigned long long)ISECT_CHUNK);
+  t0 = __shfl_sync(FULLMASK, t0, 0);
+  if (t0 >= a.nbase) break;
+  const uint64_t t1 = t0 + ISECT_CHUNK < a.nbase ? t0 + ISECT_CHUNK : a.nbase;
+  for (uint64_t t = t0; t < t1; t++) {
     uint32_t col[MAX_DEPS];
     int64_t lo[MAX_DEPS], hi[MAX_DEPS];
     uint32_t uu[MAX_DEPS];
@@ -255,15 +265,17 @@ __global__ void __launch_bounds__(256) k_isect(Args a) {
       tot += count;
     }
   }
-  if (!a.emit) block_add(tot, a.total);
+  }
+  if (!a.emit && lane == 0 && tot) atomicAdd(a.total, tot);
 }
 
 // Features of one call for the learned membership method, from up to
 // ISECT_SAMPLE base tuples spread over the base table: list lengths of the
 // walked (shortest) list and of the other adjacency lists, their ratios and how
 // often the other list's vertex has an adjacency bitmap.  With a picker the
-// block then runs the network and stores its choice (class 0 binary search,
-// 1 window merge, 2 hub bitmap) for k_isect.
+// block then runs the network and stores its choice (class 0 the per-tuple
+// rule, 1 binary search everywhere, 2 hub bitmap wherever one exists) for
+// k_isect.
 constexpr int ISECT_SAMPLE = 4096;
 
 __global__ void __launch_bounds__(256) k_isect_decide(Args a, uint32_t V, uint64_t E, int has_hubs,
@@ -372,7 +384,7 @@ __global__ void __launch_bounds__(256) k_isect_decide(Args a, uint32_t V, uint64
     int best = 0;
     for (int k = 1; k < pk::NO; k++)
       if (out[k] > out[best]) best = k;
-    *method = best == 0 ? VS_ISECT_BINARY : best == 1 ? VS_ISECT_MERGE : VS_ISECT_BITMAP;
+    *method = best == 0 ? VS_ISECT_AUTO : best == 1 ? VS_ISECT_BINARY : VS_ISECT_BITMAP;
   }
 }
 
@@ -702,6 +714,8 @@ int vs_mintersect_ex(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps
   a.total = d_total;
   a.emit = 0;
   const int grid = grid_for(a.nbase * 32);
+  VS_TRY(sc.get(&a.next, 1));
+  VS_CK(cudaMemsetAsync(a.next, 0, 8, st));
   if (a.nbase) { k_isect<<<grid, 256, 0, st>>>(a); vs::note_launch(); }
   VS_CK(cudaGetLastError());
   unsigned long long total = 0;
@@ -727,6 +741,7 @@ int vs_mintersect_ex(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps
   a.toff = toff;
   a.max_rows = rows;
   a.emit = 1;
+  VS_CK(cudaMemsetAsync(a.next, 0, 8, st));
   if (a.nbase && rows) { k_isect<<<grid, 256, 0, st>>>(a); vs::note_launch(); }
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

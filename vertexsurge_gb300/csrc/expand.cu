@@ -258,7 +258,10 @@ __global__ void __launch_bounds__(64) k_decide(DecideArgs a) {
     }
     __syncthreads();
     if (use_picker) {
-      const __nv_bfloat16 *w = (const __nv_bfloat16 *)a.picker;
+      __shared__ __nv_bfloat16 w[pk::NPARAM];  // the network, staged with coalesced loads
+      const __nv_bfloat16 *gw = (const __nv_bfloat16 *)a.picker;
+      for (int i = t; i < pk::NPARAM; i += blockDim.x) w[i] = gw[i];
+      __syncthreads();
       {
         float acc = __bfloat162float(w[pk::OFF_B1 + t]);
         for (int i = 0; i < pk::NF; i++) acc += __bfloat162float(w[pk::OFF_W1 + t * pk::NF + i]) * f[i];
@@ -299,14 +302,19 @@ __global__ void k_hop_stats(const uint32_t *__restrict__ flagF, Lists out, uint3
   if (threadIdx.x < pk::NHIST) hist[threadIdx.x] = 0;
   __syncthreads();
   unsigned long long s = 0;
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x)
-    if (flagF[v]) {
+  // warp-uniform loop; lanes with the same bin add once through their leader
+  for (uint32_t v0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; v0 < V; v0 += gridDim.x * blockDim.x) {
+    const uint32_t v = v0 + (threadIdx.x & 31);
+    int b = -1;
+    if (v < V && flagF[v]) {
       unsigned long long d = 0;
       _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < out.n) d += (unsigned long long)(out.off[l][v + 1] - out.off[l][v]);
       s += d;
-      const int b = min(pk::NHIST - 1, 63 - __clzll((long long)(d + 1)));
-      atomicAdd(&hist[b], 1ull);
+      b = min(pk::NHIST - 1, 63 - __clzll((long long)(d + 1)));
     }
+    const unsigned peers = __match_any_sync(FULL, b);
+    if (b >= 0 && (peers & lanemask_lt()) == 0) atomicAdd(&hist[b], (unsigned long long)__popc(peers));
+  }
   __syncthreads();
   if (threadIdx.x < pk::NHIST && hist[threadIdx.x]) atomicAdd(&ctr->hop[h].hist[threadIdx.x], hist[threadIdx.x]);
   block_add(s, &ctr->hop[h].active_edges);

@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import json
 import math
+import sys
 import time
 from dataclasses import dataclass, field
 from pathlib import Path
@@ -151,7 +152,8 @@ def main():
     vs.init(0)
     graphs = graph_suite(scales=tuple(int(x) for x in args.scales.split(",")))
     t0 = time.time()
-    calls = collect(args.calls, graphs=graphs, minutes=args.minutes)
+    calls = collect(args.calls, graphs=graphs, minutes=args.minutes,
+                    log=lambda m: print(m, file=sys.stderr, flush=True))
     pk, rep = train_and_evaluate(calls, epochs=args.epochs)
     rep["logging_s"] = time.time() - t0
     rep["graphs"] = [{"V": g.V, "E": g.E} for g in graphs]

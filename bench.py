@@ -258,7 +258,8 @@ def run_gpu_batched(args, w, rank, world, local_rank):
     setting = autotune.tune(dg, tsrc, 1, 4, "shortest", "forward", stream=stream, repeats=1,
                             pull_kinds=(0,), sparse_fracs=(0.002, 0.02), hub_thresholds=(0, 256),
                             cache_file=tc)
-    setting = {k: setting[k] for k in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words", "ms")}
+    setting = {k: setting.get(k, 0.0) for k in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words",
+                                                "rowlist_bits", "ms")}
     wkey = f"waves|{args.workload}"
     cached = json.loads(Path(tc).read_text()) if tc and Path(tc).exists() else {}
     if wkey in cached:
@@ -447,7 +448,8 @@ def run_gpu(args, w, rank, world, local_rank):
     tA = autotune.tune(dg, sa, ka[0], ka[1], "shortest", "forward", stream=stream, cache_file=tc)
     tB = autotune.tune(dg, sb, kb[0], kb[1], "shortest", "forward", stream=stream, cache_file=tc)
     tP = autotune.tune(dg, sa, 1, 1, "any", "forward", stream=stream, cache_file=tc)
-    tuned = {k: {x: t[x] for x in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words", "ms")}
+    tuned = {k: {x: t.get(x, 0.0) for x in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words",
+                                           "rowlist_bits", "ms")}
              for k, t in (("A", tA), ("B", tB), ("P", tP))}
     log(f"[rank {rank}] autotune {time.time() - t0:.1f}s: {tuned}")
     for name, t in (("A", tA), ("B", tB), ("P", tP)):

@@ -175,6 +175,9 @@ typedef struct vs_expand_params {
   int32_t pull_kernel;     /* PULL kernel shape 0..3, see vs_expand_plan_set_pull_kernel */
   int32_t reserved;
   double sparse_frac;      /* fixed planner: SPARSE while pair-list edges < this x E (0 = 0.02) */
+  double rowlist_bits;     /* a PULL hop gathers the source lists of the frontier rows instead of
+                              the rows when they hold at most this x W bits on average (0 = 2.0,
+                              < 0 = never); needs S <= 65536 and whole-row passes */
 } vs_expand_params;
 
 #define VS_MAX_HOPS 64
@@ -189,6 +192,7 @@ typedef struct vs_expand_stats {
   int32_t strategy[VS_MAX_HOPS + 1];        /* strategy run at hop h */
   float hop_ms[VS_MAX_HOPS + 1];            /* device time of hop h (plans with timing on) */
   float pull_ms[VS_MAX_HOPS + 1];           /* device time of hop h's pull kernels */
+  int32_t rowlist[VS_MAX_HOPS + 1];         /* 1: the PULL of hop h gathered row lists */
 } vs_expand_stats;
 
 /* A plan owns the frontier, next, visited and accumulator matrices for S

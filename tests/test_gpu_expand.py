@@ -315,3 +315,47 @@ def test_malformed_csr_is_rejected(vs):
     with pytest.raises(vs.VsError):
         vs.DeviceGraph(g.V, g.E, off, g.fwd_dst, g.rev_off, g.rev_src)
     vs.DeviceGraph(g.V, g.E, g.fwd_off, g.fwd_dst, g.rev_off, g.rev_src)  # the well-formed one loads
+
+
+@pytest.mark.parametrize("path", ["any", "shortest"])
+@pytest.mark.parametrize("direction", ["forward", "backward", "both"])
+def test_rowlist_pull_parity(vs, graphs, path, direction):
+    """PULL over row lists (the frontier rows' source lists, OR-ed in shared
+    memory) against the oracle, forced on every PULL hop, on graphs with
+    in-degree hubs (the CTA-per-hub variant) and without; the dense PULL
+    (row lists off) gives the same."""
+    for name in ("rmat11_skew", "zipf3000", "rmat10"):
+        g, dg = graphs[name]
+        for S in (40, 300, 1000):
+            src = graphgen.sample_sources(g.V, S, seed=S + 1)
+            exp, _, _ = O.vexpand(g, src, 1, 4, path, direction)
+            for rb in (1e9, -1.0):
+                m, _, st = vs.expand(dg, src, 1, 4, path, direction, strategy="pull", stats=True,
+                                     rowlist_bits=rb, hub_threshold=64)
+                assert np.array_equal(m.download(), exp), (name, S, path, direction, rb)
+                used = [r for r, s in zip(st["rowlist"][1:], st["strategy"][1:]) if s == 1]
+                assert all(used) if rb > 0 else not any(used), (st["rowlist"], st["strategy"])
+
+
+def test_rowlist_pull_with_row_limits_and_layers(vs, graphs):
+    """Row lists under batched per-row hop limits and with per-distance layers."""
+    import torch
+    g, dg = graphs["rmat11_skew"]
+    sizes, kmaxs = [50, 90, 30], [1, 3, 2]
+    srcs = [graphgen.sample_sources(g.V, n, seed=60 + i) for i, n in enumerate(sizes)]
+    allsrc = np.concatenate(srcs).astype(np.uint32)
+    plan = vs.ExpandPlan(dg, len(allsrc), vs.make_params(1, 3, "shortest", "forward", strategy="pull",
+                                                         rowlist_bits=1e9))
+    plan.set_row_limits_device(torch.from_numpy(np.concatenate(
+        [np.full(n, k, np.uint8) for n, k in zip(sizes, kmaxs)])).cuda(), len(allsrc))
+    plan.run(allsrc)
+    got = words_to_bool(plan.result().download(), len(allsrc))
+    r0 = 0
+    for src, k in zip(srcs, kmaxs):
+        exp, _, _ = O.vexpand(g, src, 1, k, "shortest", "forward")
+        assert np.array_equal(got[r0:r0 + len(src)], words_to_bool(exp, len(src)))
+        r0 += len(src)
+    src = graphgen.sample_sources(g.V, 200, seed=4)
+    for h, m in vs.expand_layers(dg, src, 1, 4, "shortest", "forward", strategy="pull", rowlist_bits=1e9):
+        exp, _, _ = O.vexpand(g, src, h, h, "shortest", "forward")
+        assert np.array_equal(m.download(), exp), h

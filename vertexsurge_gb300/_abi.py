@@ -38,7 +38,7 @@ class ExpandParams(C.Structure):
                 ("direction", C.c_int32), ("strategy", C.c_int32), ("use_picker", C.c_int32),
                 ("hub_threshold", C.c_uint32), ("slice_words", C.c_uint32),
                 ("pair_capacity", C.c_uint64), ("pull_kernel", C.c_int32), ("reserved", C.c_int32),
-                ("sparse_frac", C.c_double)]
+                ("sparse_frac", C.c_double), ("rowlist_bits", C.c_double)]
 
 
 class ExpandStats(C.Structure):
@@ -49,7 +49,8 @@ class ExpandStats(C.Structure):
                 ("pairs", C.c_uint64 * (MAX_HOPS + 1)),
                 ("strategy", C.c_int32 * (MAX_HOPS + 1)),
                 ("hop_ms", C.c_float * (MAX_HOPS + 1)),
-                ("pull_ms", C.c_float * (MAX_HOPS + 1))]
+                ("pull_ms", C.c_float * (MAX_HOPS + 1)),
+                ("rowlist", C.c_int32 * (MAX_HOPS + 1))]
 
     def as_dict(self) -> dict:
         n = self.hops_run + 1
@@ -57,7 +58,7 @@ class ExpandStats(C.Structure):
                 "new_bits": list(self.new_bits[:n]), "active_vertices": list(self.active_vertices[:n]),
                 "active_edges": list(self.active_edges[:n]), "pairs": list(self.pairs[:n]),
                 "strategy": list(self.strategy[:n]), "hop_ms": list(self.hop_ms[:n]),
-                "pull_ms": list(self.pull_ms[:n])}
+                "pull_ms": list(self.pull_ms[:n]), "rowlist": list(self.rowlist[:n])}
 
 
 class BitmatInfo(C.Structure):
@@ -395,7 +396,8 @@ class FlatTable:
 
 
 def make_params(k_min, k_max, path="any", direction="forward", strategy="auto", use_picker=False,
-                hub_threshold=0, slice_words=0, pair_capacity=0, pull_kernel=0, sparse_frac=0.0) -> ExpandParams:
+                hub_threshold=0, slice_words=0, pair_capacity=0, pull_kernel=0, sparse_frac=0.0,
+                rowlist_bits=0.0) -> ExpandParams:
     p = ExpandParams()
     p.k_min, p.k_max = int(k_min), int(k_max)
     p.path_type = _PATHS[path] if isinstance(path, str) else int(path)
@@ -407,6 +409,7 @@ def make_params(k_min, k_max, path="any", direction="forward", strategy="auto", 
     p.pair_capacity = int(pair_capacity)
     p.pull_kernel = int(pull_kernel)
     p.sparse_frac = float(sparse_frac)
+    p.rowlist_bits = float(rowlist_bits)
     return p
 
 

@@ -7,7 +7,8 @@ times the expand under candidate settings and keeps the fastest:
   * the SPARSE threshold of the fixed planner (pair-list edge work below this
     fraction of E runs as SPARSE),
   * the hub degree bin (in-degree above which a vertex gets a whole CTA),
-  * the source-word group width (words per PULL pass) for very wide rows.
+  * the source-word group width (words per PULL pass) for very wide rows,
+  * whether PULL hops over sparse frontier rows gather the rows' source lists.
 Timing uses CUDA events around whole plan runs on the plan's stream; every
 candidate gives the same result, so only time decides.  Results are cached
 per shape in memory and, when a path is given, in a JSON file.
@@ -43,9 +44,9 @@ def _time_runs(plan, src, repeats, stream):
 
 def tune(dg, src, k_min, k_max, path="shortest", direction="forward", stream=None, repeats=3,
          pull_kinds=(0, 1, 2, 3), sparse_fracs=(0.0005, 0.002, 0.005, 0.02), hub_thresholds=(0, 256),
-         slice_words=(0,), cache_file: str | None = None) -> dict:
+         slice_words=(0,), rowlist_bits=(0.0, -1.0), cache_file: str | None = None) -> dict:
     """Time the candidates; returns {'pull_kind', 'sparse_frac', 'hub_threshold', 'slice_words',
-    'ms', 'table'} and caches it."""
+    'rowlist_bits', 'ms', 'table'} and caches it."""
     import torch
     key = _key(dg, len(src), k_min, k_max, path, direction)
     if key in _CACHE:
@@ -60,18 +61,20 @@ def tune(dg, src, k_min, k_max, path="shortest", direction="forward", stream=Non
     table = []
     for hub in hub_thresholds:
         for sw in slice_words:
-            plan = vs.ExpandPlan(dg, len(src), vs.make_params(k_min, k_max, path, direction,
-                                                              hub_threshold=hub, slice_words=sw))
-            try:
-                for pk in pull_kinds:
-                    plan.set_pull_kernel(pk)
-                    for sf in sparse_fracs:
-                        plan.set_tuning(sparse_frac=sf)
-                        ms = _time_runs(plan, dsrc, repeats, stream)
-                        table.append({"pull_kind": pk, "sparse_frac": sf, "hub_threshold": hub,
-                                      "slice_words": sw, "ms": ms})
-            finally:
-                plan.free()
+            for rb in rowlist_bits:
+                plan = vs.ExpandPlan(dg, len(src), vs.make_params(k_min, k_max, path, direction,
+                                                                  hub_threshold=hub, slice_words=sw,
+                                                                  rowlist_bits=rb))
+                try:
+                    for pk in pull_kinds:
+                        plan.set_pull_kernel(pk)
+                        for sf in sparse_fracs:
+                            plan.set_tuning(sparse_frac=sf)
+                            ms = _time_runs(plan, dsrc, repeats, stream)
+                            table.append({"pull_kind": pk, "sparse_frac": sf, "hub_threshold": hub,
+                                          "slice_words": sw, "rowlist_bits": rb, "ms": ms})
+                finally:
+                    plan.free()
     best = min(table, key=lambda r: r["ms"])
     out = dict(best)
     out["table"] = table
@@ -94,7 +97,8 @@ def params_kw(setting: dict | None) -> dict:
     """Keyword arguments of make_params / expand for a tuned setting."""
     s = setting or {}
     return {"hub_threshold": s.get("hub_threshold", 0), "slice_words": s.get("slice_words", 0),
-            "pull_kernel": s.get("pull_kind", 0), "sparse_frac": s.get("sparse_frac", 0.0)}
+            "pull_kernel": s.get("pull_kind", 0), "sparse_frac": s.get("sparse_frac", 0.0),
+            "rowlist_bits": s.get("rowlist_bits", 0.0)}
 
 
 def make_plan(dg, S, k_min, k_max, path, direction, setting: dict | None, **kw):

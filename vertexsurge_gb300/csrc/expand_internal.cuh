@@ -20,6 +20,7 @@ struct HopCtr {
   unsigned long long hist[16];         // log2(out-degree + 1) histogram of layer h-1's active rows
   int overflow;                        // SPARSE: pair list overflowed
   int strategy;                        // strategy run at hop h (0 = not run)
+  int rowlist;                         // PULL over the row lists of layer h-1
 };
 
 struct Ctr {
@@ -64,6 +65,8 @@ struct DecideArgs {
   double sparse_frac, push_frac;
   const void *picker;  // bf16 weights of a vs_picker (NULL = fixed planner)
   const uint32_t *rowk;  // [0] largest row hop limit (NULL: no row limits)
+  uint64_t rl_cap;       // row-list entries available (0: row lists off)
+  double rl_bits;        // PULL over row lists when a frontier row holds at most rl_bits * W bits on average
 };
 
 struct SparseArgs {

@@ -155,6 +155,18 @@ def expand_bytes(V, W, e_act, shortest, acc, gathers=True):
     return 8 * (V + 1) + 4 * e_act + (e_act * max(32, 8 * W) if gathers else 0) + P * 8 * W * V
 
 
+def rowlist_bytes(V, W, e_act, entries, active_prev, bits_prev, shortest, acc, gathers=True):
+    """Algorithmic bytes of a PULL hop over row lists: CSR offsets + targets,
+    per active in-edge the row's (count, offset) pair and its list entries
+    (2 bytes each), the list build (two reads of the active frontier rows,
+    counts and offsets, the ids written), and the same P passes over the
+    V x S matrices as the dense hop."""
+    P = 2 + (2 if shortest else 0) + (2 if acc else 0)
+    per_edge = (16 * e_act + 2 * entries) if gathers else 0
+    return (8 * (V + 1) + 4 * e_act + per_edge + 16 * W * active_prev + 32 * V + 2 * bits_prev
+            + P * 8 * W * V)
+
+
 def cpu_baseline(g, w, sa):
     """Oracle VExpand on the host cores: the bounded sample and its throughput."""
     from oracle import pyoracle as O
@@ -502,8 +514,14 @@ def run_gpu(args, w, rank, world, local_rank):
         for h in range(1, st["hops_run"] + 1):
             if st["strategy"][h] == vs.STRAT_PULL:
                 pull_ms += st["pull_ms"][h]
-                pull_bytes += expand_bytes(g.V, W, stA["active_edges"][h], True, False)
-                pull_comp += expand_bytes(g.V, W, stA["active_edges"][h], True, False, gathers=False)
+                if stA["rowlist"][h]:
+                    args_rl = (g.V, W, stA["active_edges"][h], stA["rowlist_entries"][h],
+                               stA["active_vertices"][h - 1], stA["new_bits"][h - 1], True, False)
+                    pull_bytes += rowlist_bytes(*args_rl)
+                    pull_comp += rowlist_bytes(*args_rl, gathers=False)
+                else:
+                    pull_bytes += expand_bytes(g.V, W, stA["active_edges"][h], True, False)
+                    pull_comp += expand_bytes(g.V, W, stA["active_edges"][h], True, False, gathers=False)
     ev1.record(stream)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
@@ -599,7 +617,8 @@ def run_gpu(args, w, rank, world, local_rank):
                 "frac": achieved / peak if achieved else None, "traffic": profiled_traffic(args.workload),
                 "traffic_source": f"profiles/k_pull_{args.workload}.md (ncu dram__bytes_read.sum + "
                                   "dram__bytes_write.sum per working launch)",
-                "kernel": "k_pull (expand A, pull hops)", "peak_source": peak_kind,
+                "kernel": ("k_pull_rl + row-list build (expand A, pull hops)" if any(stA["rowlist"][1:])
+                           else "k_pull (expand A, pull hops)"), "peak_source": peak_kind,
                 "compulsory_frac": (pull_comp / (pull_ms / 1e3) / 1e9) / peak if pull_ms else None,
                 "per_launch_ms": pull_ms / max(1, args.steps * sum(1 for s in stA["strategy"][1:] if s == 1))}
     cpu = None

@@ -193,6 +193,7 @@ typedef struct vs_expand_stats {
   float hop_ms[VS_MAX_HOPS + 1];            /* device time of hop h (plans with timing on) */
   float pull_ms[VS_MAX_HOPS + 1];           /* device time of hop h's pull kernels */
   int32_t rowlist[VS_MAX_HOPS + 1];         /* 1: the PULL of hop h gathered row lists */
+  uint64_t rowlist_entries[VS_MAX_HOPS + 1];/* list entries that PULL gathered (out-degree x row bits) */
 } vs_expand_stats;
 
 /* A plan owns the frontier, next, visited and accumulator matrices for S

@@ -50,7 +50,8 @@ class ExpandStats(C.Structure):
                 ("strategy", C.c_int32 * (MAX_HOPS + 1)),
                 ("hop_ms", C.c_float * (MAX_HOPS + 1)),
                 ("pull_ms", C.c_float * (MAX_HOPS + 1)),
-                ("rowlist", C.c_int32 * (MAX_HOPS + 1))]
+                ("rowlist", C.c_int32 * (MAX_HOPS + 1)),
+                ("rowlist_entries", C.c_uint64 * (MAX_HOPS + 1))]
 
     def as_dict(self) -> dict:
         n = self.hops_run + 1
@@ -58,7 +59,8 @@ class ExpandStats(C.Structure):
                 "new_bits": list(self.new_bits[:n]), "active_vertices": list(self.active_vertices[:n]),
                 "active_edges": list(self.active_edges[:n]), "pairs": list(self.pairs[:n]),
                 "strategy": list(self.strategy[:n]), "hop_ms": list(self.hop_ms[:n]),
-                "pull_ms": list(self.pull_ms[:n]), "rowlist": list(self.rowlist[:n])}
+                "pull_ms": list(self.pull_ms[:n]), "rowlist": list(self.rowlist[:n]),
+                "rowlist_entries": list(self.rowlist_entries[:n])}
 
 
 class BitmatInfo(C.Structure):

@@ -794,10 +794,11 @@ struct RowLists {
 
 // popcount of every flagged row of layer h-1 (zero for the others)
 __global__ void k_rl_count(const uint32_t *__restrict__ flagF, const uint4 *__restrict__ F, uint32_t V, uint32_t Q,
-                           unsigned long long *__restrict__ cnt, const Ctr *ctr, int h) {
+                           unsigned long long *__restrict__ cnt, Lists out, Ctr *ctr, int h) {
   if (!rowlist_hop(ctr, h)) return;
   const int lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  unsigned long long entries = 0;  // what the targets will gather: out-degree x row bits
   for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < V; base += warps * 32) {
     const uint32_t v = base + lane;
     const bool f = v < V && flagF[v];
@@ -810,9 +811,15 @@ __global__ void k_rl_count(const uint32_t *__restrict__ flagF, const uint4 *__re
       unsigned long long c = 0;
       for (uint32_t q = lane; q < Q; q += 32) c += popc4(row[q]);
       c = warp_sum(c);
-      if (lane == 0) cnt[base + b] = c;
+      if (lane == 0) {
+        cnt[base + b] = c;
+        unsigned long long d = 0;
+        _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < out.n) d += (unsigned long long)(out.off[l][base + b + 1] - out.off[l][base + b]);
+        entries += c * d;
+      }
     }
   }
+  block_add(entries, &ctr->hop[h].rl_entries);
 }
 
 // the set source indices of every flagged row, at its scanned offset
@@ -1568,17 +1575,17 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.nhubs = pl->nhubs;
     a.ctr = pl->ctr;
     a.h = h;
+    if (timing) cudaEventRecord(pl->ev[3 * h + 1], st);
     if (pl->rl_cap) {  // row lists of layer h-1, used when the decide kernel chose them
       RowLists rl{pl->rl_cnt, pl->rl_off, pl->rl_ids, pl->rl_cap};
       { k_rl_count<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<const uint4 *>(pl->buf[fb]), V, Q,
-                                              pl->rl_cnt, pl->ctr, h); vs::note_launch(); }
+                                              pl->rl_cnt, outl, pl->ctr, h); vs::note_launch(); }
       { k_pscan1<<<pl->grid_v, 256, 0, st>>>(pl->rl_cnt, pl->rl_off, pl->rl_bsum, pl->ctr, h, 0, V); vs::note_launch(); }
       { k_pscan2<<<1, 1024, 0, st>>>(pl->rl_bsum, pl->rl_off, pl->ctr, h, 0, V); vs::note_launch(); }
       { k_pscan3<<<pl->grid_v, 256, 0, st>>>(pl->rl_off, pl->rl_bsum, pl->ctr, h, 0, V); vs::note_launch(); }
       { k_rl_fill<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<const uint4 *>(pl->buf[fb]), V, Q, rl,
                                              pl->ctr, h); vs::note_launch(); }
     }
-    if (timing) cudaEventRecord(pl->ev[3 * h + 1], st);
     { var.pull[pl->pull_kind]<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a); vs::note_launch(); }
     if (pl->nhubs)
       { var.hub<<<dim3(pl->grid_hub, pl->nslices), 512, 16 * 32 * 16 * var.UPL, st>>>(a); vs::note_launch(); }
@@ -1648,6 +1655,7 @@ int vs_expand_plan_stats(vs_expand_plan *pl, vs_expand_stats *stats, vs_stream_t
     stats->pairs[i] = h.hop[i].pairs;
     stats->strategy[i] = h.hop[i].strategy;
     stats->rowlist[i] = h.hop[i].rowlist;
+    stats->rowlist_entries[i] = h.hop[i].rl_entries;
     if (i >= 1 && i <= h.hops_run) vc += h.hop[i].new_bits;
   }
   for (uint32_t i = 1; i <= pl->timed_hops && i <= VS_MAX_HOPS; i++) {

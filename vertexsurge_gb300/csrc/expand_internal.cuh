@@ -21,6 +21,7 @@ struct HopCtr {
   int overflow;                        // SPARSE: pair list overflowed
   int strategy;                        // strategy run at hop h (0 = not run)
   int rowlist;                         // PULL over the row lists of layer h-1
+  unsigned long long rl_entries;       // row-list entries the PULL gathers (sum of out-degree x row bits)
 };
 
 struct Ctr {

@@ -155,16 +155,16 @@ def expand_bytes(V, W, e_act, shortest, acc, gathers=True):
     return 8 * (V + 1) + 4 * e_act + (e_act * max(32, 8 * W) if gathers else 0) + P * 8 * W * V
 
 
-def rowlist_bytes(V, W, e_act, entries, active_prev, bits_prev, shortest, acc, gathers=True):
-    """Algorithmic bytes of a PULL hop over row lists: CSR offsets + targets,
-    per active in-edge the row's (count, offset) pair and its list entries
-    (2 bytes each), the list build (two reads of the active frontier rows,
-    counts and offsets, the ids written), and the same P passes over the
-    V x S matrices as the dense hop."""
+def short_bytes(V, W, e_act, e_short, active_prev, built, shortest, acc, gathers=True):
+    """Algorithmic bytes of a short-mode PULL hop: CSR offsets + targets, a
+    32-byte slot per active in-edge whose row is short and a whole-row gather
+    (at least one sector) for the others, the slot writes of the layer (32 B
+    per vertex), the slot build when SPARSE wrote the frontier (its rows read
+    once), and the same P passes over the V x S matrices as the dense hop."""
     P = 2 + (2 if shortest else 0) + (2 if acc else 0)
-    per_edge = (16 * e_act + 2 * entries) if gathers else 0
-    return (8 * (V + 1) + 4 * e_act + per_edge + 16 * W * active_prev + 32 * V + 2 * bits_prev
-            + P * 8 * W * V)
+    per_edge = (32 * e_short + max(32, 8 * W) * (e_act - e_short)) if gathers else 0
+    build = (8 * W + 32) * active_prev if built else 0
+    return 8 * (V + 1) + 4 * e_act + per_edge + 32 * V + build + P * 8 * W * V
 
 
 def cpu_baseline(g, w, sa):
@@ -271,7 +271,7 @@ def run_gpu_batched(args, w, rank, world, local_rank):
                             pull_kinds=(0,), sparse_fracs=(0.002, 0.02), hub_thresholds=(0, 256),
                             cache_file=tc)
     setting = {k: setting.get(k, 0.0) for k in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words",
-                                                "rowlist_bits", "ms")}
+                                                "short_share", "ms")}
     wkey = f"waves|{args.workload}"
     cached = json.loads(Path(tc).read_text()) if tc and Path(tc).exists() else {}
     if wkey in cached:
@@ -461,7 +461,7 @@ def run_gpu(args, w, rank, world, local_rank):
     tB = autotune.tune(dg, sb, kb[0], kb[1], "shortest", "forward", stream=stream, cache_file=tc)
     tP = autotune.tune(dg, sa, 1, 1, "any", "forward", stream=stream, cache_file=tc)
     tuned = {k: {x: t.get(x, 0.0) for x in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words",
-                                           "rowlist_bits", "ms")}
+                                           "short_share", "ms")}
              for k, t in (("A", tA), ("B", tB), ("P", tP))}
     log(f"[rank {rank}] autotune {time.time() - t0:.1f}s: {tuned}")
     for name, t in (("A", tA), ("B", tB), ("P", tP)):
@@ -514,11 +514,11 @@ def run_gpu(args, w, rank, world, local_rank):
         for h in range(1, st["hops_run"] + 1):
             if st["strategy"][h] == vs.STRAT_PULL:
                 pull_ms += st["pull_ms"][h]
-                if stA["rowlist"][h]:
-                    args_rl = (g.V, W, stA["active_edges"][h], stA["rowlist_entries"][h],
-                               stA["active_vertices"][h - 1], stA["new_bits"][h - 1], True, False)
-                    pull_bytes += rowlist_bytes(*args_rl)
-                    pull_comp += rowlist_bytes(*args_rl, gathers=False)
+                if stA["short_pull"][h]:
+                    args_sh = (g.V, W, stA["active_edges"][h], stA["short_edges"][h],
+                               stA["active_vertices"][h - 1], stA["strategy"][h - 1] != vs.STRAT_PULL, True, False)
+                    pull_bytes += short_bytes(*args_sh)
+                    pull_comp += short_bytes(*args_sh, gathers=False)
                 else:
                     pull_bytes += expand_bytes(g.V, W, stA["active_edges"][h], True, False)
                     pull_comp += expand_bytes(g.V, W, stA["active_edges"][h], True, False, gathers=False)
@@ -617,8 +617,9 @@ def run_gpu(args, w, rank, world, local_rank):
                 "frac": achieved / peak if achieved else None, "traffic": profiled_traffic(args.workload),
                 "traffic_source": f"profiles/k_pull_{args.workload}.md (ncu dram__bytes_read.sum + "
                                   "dram__bytes_write.sum per working launch)",
-                "kernel": ("k_pull_rl + row-list build (expand A, pull hops)" if any(stA["rowlist"][1:])
-                           else "k_pull (expand A, pull hops)"), "peak_source": peak_kind,
+                "kernel": ("k_pull, short mode on hops " + str([h for h in range(1, len(stA["short_pull"]))
+                                                             if stA["short_pull"][h]]) + " (expand A, pull hops)"
+                           if any(stA["short_pull"][1:]) else "k_pull (expand A, pull hops)"), "peak_source": peak_kind,
                 "compulsory_frac": (pull_comp / (pull_ms / 1e3) / 1e9) / peak if pull_ms else None,
                 "per_launch_ms": pull_ms / max(1, args.steps * sum(1 for s in stA["strategy"][1:] if s == 1))}
     cpu = None

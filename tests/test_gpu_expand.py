@@ -192,7 +192,8 @@ def test_autotuner_settings_keep_results(vs, graphs):
     src = graphgen.sample_sources(g.V, 200, seed=12)
     t = autotune.tune(dg, src, 1, 3, "shortest", "forward", repeats=1, pull_kinds=(0, 3),
                       sparse_fracs=(0.001, 0.05), hub_thresholds=(0, 64))
-    assert len(t["table"]) == 8 and t["ms"] > 0
+    assert len(t["table"]) == 16 and t["ms"] > 0  # x2: row lists on and off
+    assert {r["short_share"] for r in t["table"]} == {0.0, -1.0}
     exp, _, _ = O.vexpand(g, src, 1, 3, "shortest", "forward")
     for row in t["table"]:
         plan = autotune.make_plan(dg, len(src), 1, 3, "shortest", "forward", row)
@@ -319,41 +320,73 @@ def test_malformed_csr_is_rejected(vs):
 
 @pytest.mark.parametrize("path", ["any", "shortest"])
 @pytest.mark.parametrize("direction", ["forward", "backward", "both"])
-def test_rowlist_pull_parity(vs, graphs, path, direction):
-    """PULL over row lists (the frontier rows' source lists, OR-ed in shared
-    memory) against the oracle, forced on every PULL hop, on graphs with
-    in-degree hubs (the CTA-per-hub variant) and without; the dense PULL
-    (row lists off) gives the same."""
-    n_rowlist = 0
+def test_short_pull_parity(vs, graphs, path, direction):
+    """Short-mode PULL (rows with at most 15 bits read from their id slots,
+    longer rows gathered whole) against the oracle, forced on every PULL hop:
+    slots written by the PULL epilogue (warp and hub CTA) and by the build
+    pass after SPARSE hops or the seed; rows of 1 to 128 uint4; with
+    short mode off no hop uses it and the results are the same."""
+    n_short, n_edges = 0, 0
     for name in ("rmat11_skew", "zipf3000", "rmat10"):
         g, dg = graphs[name]
-        for S in (40, 300, 1000):
-            src = graphgen.sample_sources(g.V, S, seed=S + 1)
+        for S in (20, 40, 300, 1000, 4000) + ((16384,) if name == "rmat10" else ()):
+            src = graphgen.sample_sources(g.V, min(S, g.V), seed=S + 1)
+            if S > g.V:
+                src = np.resize(src, S).astype(np.uint32)
             exp, _, _ = O.vexpand(g, src, 1, 4, path, direction)
-            for rb in (1e9, -1.0):
-                m, _, st = vs.expand(dg, src, 1, 4, path, direction, strategy="pull", stats=True,
-                                     rowlist_bits=rb, hub_threshold=64)
-                assert np.array_equal(m.download(), exp), (name, S, path, direction, rb)
-                # row lists run on every PULL hop whose frontier fits the list
-                # buffer (at least 2^20 entries at these sizes), never when off
-                for h in range(1, st["hops_run"] + 1):
-                    if st["strategy"][h] != 1:
-                        continue
-                    want = rb > 0 and st["new_bits"][h - 1] <= (1 << 20)
-                    assert bool(st["rowlist"][h]) == want, (h, st["rowlist"], st["new_bits"])
-                    n_rowlist += want
-    assert n_rowlist > 20
+            for strategy in ("pull", "auto"):
+                for share in (2.0, -1.0):
+                    m, _, st = vs.expand(dg, src, 1, 4, path, direction, strategy=strategy, stats=True,
+                                         short_share=share, hub_threshold=64)
+                    assert np.array_equal(m.download(), exp), (name, S, path, direction, strategy, share)
+                    for h in range(1, st["hops_run"] + 1):
+                        if st["strategy"][h] == vs.STRAT_PULL:
+                            assert bool(st["short_pull"][h]) == (share > 0), (h, st["short_pull"])
+                            n_short += share > 0
+                            n_edges += st["short_edges"][h]
+                        else:
+                            assert not st["short_pull"][h]
+    assert n_short > 50 and n_edges > 0
 
 
-def test_rowlist_pull_with_row_limits_and_layers(vs, graphs):
-    """Row lists under batched per-row hop limits and with per-distance layers."""
+@pytest.mark.parametrize("path", ["any", "shortest"])
+def test_short_rows_counted(vs, graphs, path):
+    """The PULL epilogue's count of short rows (1..15 bits) in every layer it
+    writes slots for equals the count over the oracle's layer."""
+    g, dg = graphs["zipf3000"]
+    src = graphgen.sample_sources(g.V, 700, seed=8)
+    _, _, st = vs.expand(dg, src, 1, 4, path, "forward", strategy="pull", stats=True, short_share=2.0)
+    W = (len(src) + 63) // 64
+    W += W & 1
+    checked = 0
+    for h in range(1, min(st["hops_run"], 3) + 1):  # hop 4 is the last: no slots
+        layer, _, _ = O.vexpand(g, src, h, h, path, "forward")
+        bits = words_to_bool(layer, len(src)).sum(axis=0) if layer.size else np.zeros(g.V)
+        assert st["short_rows"][h] == int(((bits >= 1) & (bits <= 15)).sum()), h
+        checked += 1
+    assert checked == 3
+
+
+def test_short_pull_default_rule(vs, graphs):
+    """With the default share, frontiers that fit in half of L2 keep the
+    dense PULL (every small test graph), and the results agree."""
+    g, dg = graphs["rmat11_skew"]
+    src = graphgen.sample_sources(g.V, 500, seed=3)
+    m, _, st = vs.expand(dg, src, 1, 4, "shortest", "forward", strategy="pull", stats=True)
+    assert not any(st["short_pull"])
+    exp, _, _ = O.vexpand(g, src, 1, 4, "shortest", "forward")
+    assert np.array_equal(m.download(), exp)
+
+
+def test_short_pull_with_row_limits_and_layers(vs, graphs):
+    """Short mode under batched per-row hop limits and with per-distance layers."""
     import torch
     g, dg = graphs["rmat11_skew"]
     sizes, kmaxs = [50, 90, 30], [1, 3, 2]
     srcs = [graphgen.sample_sources(g.V, n, seed=60 + i) for i, n in enumerate(sizes)]
     allsrc = np.concatenate(srcs).astype(np.uint32)
     plan = vs.ExpandPlan(dg, len(allsrc), vs.make_params(1, 3, "shortest", "forward", strategy="pull",
-                                                         rowlist_bits=1e9))
+                                                         short_share=2.0))
     plan.set_row_limits_device(torch.from_numpy(np.concatenate(
         [np.full(n, k, np.uint8) for n, k in zip(sizes, kmaxs)])).cuda(), len(allsrc))
     plan.run(allsrc)
@@ -364,6 +397,6 @@ def test_rowlist_pull_with_row_limits_and_layers(vs, graphs):
         assert np.array_equal(got[r0:r0 + len(src)], words_to_bool(exp, len(src)))
         r0 += len(src)
     src = graphgen.sample_sources(g.V, 200, seed=4)
-    for h, m in vs.expand_layers(dg, src, 1, 4, "shortest", "forward", strategy="pull", rowlist_bits=1e9):
+    for h, m in vs.expand_layers(dg, src, 1, 4, "shortest", "forward", strategy="pull", short_share=2.0):
         exp, _, _ = O.vexpand(g, src, h, h, "shortest", "forward")
         assert np.array_equal(m.download(), exp), h

@@ -38,7 +38,7 @@ class ExpandParams(C.Structure):
                 ("direction", C.c_int32), ("strategy", C.c_int32), ("use_picker", C.c_int32),
                 ("hub_threshold", C.c_uint32), ("slice_words", C.c_uint32),
                 ("pair_capacity", C.c_uint64), ("pull_kernel", C.c_int32), ("reserved", C.c_int32),
-                ("sparse_frac", C.c_double), ("rowlist_bits", C.c_double)]
+                ("sparse_frac", C.c_double), ("short_share", C.c_double)]
 
 
 class ExpandStats(C.Structure):
@@ -50,8 +50,9 @@ class ExpandStats(C.Structure):
                 ("strategy", C.c_int32 * (MAX_HOPS + 1)),
                 ("hop_ms", C.c_float * (MAX_HOPS + 1)),
                 ("pull_ms", C.c_float * (MAX_HOPS + 1)),
-                ("rowlist", C.c_int32 * (MAX_HOPS + 1)),
-                ("rowlist_entries", C.c_uint64 * (MAX_HOPS + 1))]
+                ("short_pull", C.c_int32 * (MAX_HOPS + 1)),
+                ("short_rows", C.c_uint64 * (MAX_HOPS + 1)),
+                ("short_edges", C.c_uint64 * (MAX_HOPS + 1))]
 
     def as_dict(self) -> dict:
         n = self.hops_run + 1
@@ -59,8 +60,8 @@ class ExpandStats(C.Structure):
                 "new_bits": list(self.new_bits[:n]), "active_vertices": list(self.active_vertices[:n]),
                 "active_edges": list(self.active_edges[:n]), "pairs": list(self.pairs[:n]),
                 "strategy": list(self.strategy[:n]), "hop_ms": list(self.hop_ms[:n]),
-                "pull_ms": list(self.pull_ms[:n]), "rowlist": list(self.rowlist[:n]),
-                "rowlist_entries": list(self.rowlist_entries[:n])}
+                "pull_ms": list(self.pull_ms[:n]), "short_pull": list(self.short_pull[:n]),
+                "short_rows": list(self.short_rows[:n]), "short_edges": list(self.short_edges[:n])}
 
 
 class BitmatInfo(C.Structure):
@@ -399,7 +400,7 @@ class FlatTable:
 
 def make_params(k_min, k_max, path="any", direction="forward", strategy="auto", use_picker=False,
                 hub_threshold=0, slice_words=0, pair_capacity=0, pull_kernel=0, sparse_frac=0.0,
-                rowlist_bits=0.0) -> ExpandParams:
+                short_share=0.0) -> ExpandParams:
     p = ExpandParams()
     p.k_min, p.k_max = int(k_min), int(k_max)
     p.path_type = _PATHS[path] if isinstance(path, str) else int(path)
@@ -411,7 +412,7 @@ def make_params(k_min, k_max, path="any", direction="forward", strategy="auto", 
     p.pair_capacity = int(pair_capacity)
     p.pull_kernel = int(pull_kernel)
     p.sparse_frac = float(sparse_frac)
-    p.rowlist_bits = float(rowlist_bits)
+    p.short_share = float(short_share)
     return p
 
 

@@ -44,9 +44,9 @@ def _time_runs(plan, src, repeats, stream):
 
 def tune(dg, src, k_min, k_max, path="shortest", direction="forward", stream=None, repeats=3,
          pull_kinds=(0, 1, 2, 3), sparse_fracs=(0.0005, 0.002, 0.005, 0.02), hub_thresholds=(0, 256),
-         slice_words=(0,), rowlist_bits=(0.0, -1.0), cache_file: str | None = None) -> dict:
+         slice_words=(0,), short_shares=(0.0, -1.0), cache_file: str | None = None) -> dict:
     """Time the candidates; returns {'pull_kind', 'sparse_frac', 'hub_threshold', 'slice_words',
-    'rowlist_bits', 'ms', 'table'} and caches it."""
+    'short_share', 'ms', 'table'} and caches it."""
     import torch
     key = _key(dg, len(src), k_min, k_max, path, direction)
     if key in _CACHE:
@@ -61,10 +61,10 @@ def tune(dg, src, k_min, k_max, path="shortest", direction="forward", stream=Non
     table = []
     for hub in hub_thresholds:
         for sw in slice_words:
-            for rb in rowlist_bits:
+            for rb in short_shares:
                 plan = vs.ExpandPlan(dg, len(src), vs.make_params(k_min, k_max, path, direction,
                                                                   hub_threshold=hub, slice_words=sw,
-                                                                  rowlist_bits=rb))
+                                                                  short_share=rb))
                 try:
                     for pk in pull_kinds:
                         plan.set_pull_kernel(pk)
@@ -72,7 +72,7 @@ def tune(dg, src, k_min, k_max, path="shortest", direction="forward", stream=Non
                             plan.set_tuning(sparse_frac=sf)
                             ms = _time_runs(plan, dsrc, repeats, stream)
                             table.append({"pull_kind": pk, "sparse_frac": sf, "hub_threshold": hub,
-                                          "slice_words": sw, "rowlist_bits": rb, "ms": ms})
+                                          "slice_words": sw, "short_share": rb, "ms": ms})
                 finally:
                     plan.free()
     best = min(table, key=lambda r: r["ms"])
@@ -98,7 +98,7 @@ def params_kw(setting: dict | None) -> dict:
     s = setting or {}
     return {"hub_threshold": s.get("hub_threshold", 0), "slice_words": s.get("slice_words", 0),
             "pull_kernel": s.get("pull_kind", 0), "sparse_frac": s.get("sparse_frac", 0.0),
-            "rowlist_bits": s.get("rowlist_bits", 0.0)}
+            "short_share": s.get("short_share", 0.0)}
 
 
 def make_plan(dg, S, k_min, k_max, path, direction, setting: dict | None, **kw):

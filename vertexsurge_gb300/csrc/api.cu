@@ -65,6 +65,17 @@ int sm_count() {
   return n;
 }
 
+size_t l2_bytes() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrL2CacheSize, dev);
+    if (n <= 0) n = 1 << 20;
+  }
+  return (size_t)n;
+}
+
 int flat_alloc(uint32_t ncols, const int32_t *types, uint64_t nrows, cudaStream_t st,
                vs_flat **out) {
   if (ncols == 0 || ncols > 16) return fail(VS_ERR_ARG, "flat table needs 1..16 columns");

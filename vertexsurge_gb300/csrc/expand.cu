@@ -294,8 +294,19 @@ __global__ void __launch_bounds__(64) k_decide(DecideArgs a) {
   if (t == 0) {
     cur.strategy = s_choice;
     // sparse frontier rows: PULL gathers the rows' source lists instead of whole rows
-    cur.rowlist = s_choice == ST_PULL && a.rl_cap && !c->multislice && prev.new_bits <= a.rl_cap &&
-                  (double)prev.new_bits <= a.rl_bits * (double)a.W * (double)prev.active_vertices;
+    // short mode: enough short rows in a frontier that L2 does not already
+    // hold (a layer from a PULL hop counted them; from SPARSE or PUSH, a few
+    // bits per row on average stand in for the count)
+    bool sp = false;
+    if (s_choice == ST_PULL && a.short_min > 0 && !c->multislice) {
+      const double act = (double)prev.active_vertices;
+      if (a.short_min > 1.0)
+        sp = true;
+      else if (act * 8.0 * (double)a.W > (double)a.l2_half)
+        sp = prev.strategy == ST_PULL ? (double)prev.short_rows >= a.short_min * act
+                                      : (double)prev.new_bits <= 4.0 * act;
+    }
+    cur.short_pull = sp;
   }
 }
 
@@ -334,23 +345,16 @@ __global__ void k_hop_stats(const uint32_t *__restrict__ flagF, Lists out, uint3
 // spread over many warps instead of serialising one.
 constexpr int SPARSE_CHUNK = 256;  // edges per warp task
 
-// hop h runs PULL over the row lists of layer h-1
-__device__ __forceinline__ bool rowlist_hop(const Ctr *c, int h) {
-  return c->hop[h].strategy == ST_PULL && c->hop[h].rowlist;
-}
-
-// Entries the scan covers: the SPARSE hop's pairs (rows == 0), or the V row
-// popcounts of a row-list PULL hop (rows == V); 0 when the hop runs neither.
-__device__ __forceinline__ uint64_t scan_len(const Ctr *ctr, int h, uint64_t cap, uint64_t rows) {
-  if (rows) return rowlist_hop(ctr, h) ? rows : 0;
+// Pairs the SPARSE hop h scans (0 when the hop runs another strategy).
+__device__ __forceinline__ uint64_t scan_len(const Ctr *ctr, int h, uint64_t cap) {
   if (ctr->hop[h].strategy != ST_SPARSE) return 0;
   const unsigned long long npr = ctr->hop[h - 1].pairs;
   return npr < cap ? npr : cap;
 }
 
 __global__ void k_pscan1(const unsigned long long *__restrict__ pdeg, unsigned long long *__restrict__ doff,
-                         unsigned long long *__restrict__ bsum, const Ctr *ctr, int h, uint64_t cap, uint64_t rows) {
-  const uint64_t np = scan_len(ctr, h, cap, rows);
+                         unsigned long long *__restrict__ bsum, const Ctr *ctr, int h, uint64_t cap) {
+  const uint64_t np = scan_len(ctr, h, cap);
   if (!np) return;
   __shared__ unsigned long long wt[8];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -385,8 +389,8 @@ __global__ void k_pscan1(const unsigned long long *__restrict__ pdeg, unsigned l
 }
 
 __global__ void k_pscan2(unsigned long long *__restrict__ bsum, unsigned long long *__restrict__ doff,
-                         const Ctr *ctr, int h, uint64_t cap, uint64_t rows) {
-  const uint64_t np = scan_len(ctr, h, cap, rows);
+                         const Ctr *ctr, int h, uint64_t cap) {
+  const uint64_t np = scan_len(ctr, h, cap);
   if (!np) return;
   const uint64_t nb = (np + 1023) / 1024;
   __shared__ unsigned long long carry, wt[32];
@@ -414,8 +418,8 @@ __global__ void k_pscan2(unsigned long long *__restrict__ bsum, unsigned long lo
 }
 
 __global__ void k_pscan3(unsigned long long *__restrict__ doff, const unsigned long long *__restrict__ bsum,
-                         const Ctr *ctr, int h, uint64_t cap, uint64_t rows) {
-  const uint64_t np = scan_len(ctr, h, cap, rows);
+                         const Ctr *ctr, int h, uint64_t cap) {
+  const uint64_t np = scan_len(ctr, h, cap);
   if (!np) return;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += (uint64_t)gridDim.x * blockDim.x)
     doff[i] += bsum[i / 1024];
@@ -578,11 +582,41 @@ template <int H> struct L2Pol {
 // per lane at most) at a time.  In-neighbour ids are read 32 at a time,
 // filtered by the frontier flags with a ballot and compacted through shared
 // memory, so inactive rows cost one flag load and no gather.
-template <int L, int UPL, int H>
-__device__ __forceinline__ void gather_rows(const PullArgs &a, const L2Pol<H> &pol, uint32_t *s_u,
+//
+// Short rows.  In the later hops of a many-source expand over a power-law
+// graph most frontier rows hold a handful of sources, and a whole-row gather
+// then moves mostly zero words.  Every PULL hop with a successor therefore
+// also writes a 32-byte slot per non-zero row of its layer: the row's bit
+// count and, when that is at most SHORT_MAX, the source ids (uint16).  A later
+// PULL hop in short mode reads an active in-neighbour's slot (one sector)
+// and, for a short row, ORs the ids into a per-warp shared-memory row with
+// 32-bit atomics instead of gathering 8W bytes; longer rows are gathered
+// whole.  Layers written by SPARSE or PUSH get their slots from a build pass
+// (k_slot_build) when the next hop reads them.
+constexpr uint32_t SHORT_MAX = 15;  // a slot is 16 uint16: the count, then up to 15 ids
+
+// Bulk prefetch of `bytes` (a multiple of 16, 16-byte aligned) into L2.
+__device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
+}
+
+// OR the ids of a short slot (count in [1, SHORT_MAX]) into a shared row
+__device__ __forceinline__ void or_slot_ids(uint32_t *row32, const uint4 s0, const uint4 s1, uint32_t cnt) {
+  const uint32_t w[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+#pragma unroll
+  for (uint32_t i = 1; i <= SHORT_MAX; i++) {
+    if (i <= cnt) {
+      const uint32_t id = (w[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
+      atomicOr(row32 + (id >> 5), 1u << (id & 31));
+    }
+  }
+}
+
+template <int L, int UPL, int H, bool SHORT>
+__device__ __forceinline__ void gather_rows(const PullArgs &a, const L2Pol<H> &pol, uint32_t *s_u, uint32_t *row32,
                                             const uint32_t q0, const uint32_t qn, uint4 (&acc)[UPL],
                                             const uint32_t *adj, int64_t beg, int64_t end,
-                                            int64_t step_start, int64_t step) {
+                                            int64_t step_start, int64_t step, unsigned long long &se) {
   constexpr int G = 32 / L;
   const int lane = threadIdx.x & 31, g = lane / L, gl = lane % L;
   for (int64_t base = beg + step_start; base < end; base += step) {
@@ -592,6 +626,16 @@ __device__ __forceinline__ void gather_rows(const PullArgs &a, const L2Pol<H> &p
     if (j < end) {
       u = pol.ld_stream(adj + j);
       act = __ldg(a.flagF + u) != 0;
+    }
+    if (SHORT && act) {  // a short row: its ids from the slot, no gather
+      const uint4 *sp = a.slot_in + (size_t)u * 2;
+      const uint4 s0 = __ldg(sp), s1 = __ldg(sp + 1);
+      const uint32_t cnt = s0.x & 0xFFFFu;
+      if (cnt <= SHORT_MAX) {
+        or_slot_ids(row32, s0, s1, cnt);
+        act = false;
+        se++;
+      }
     }
     const unsigned m = __ballot_sync(FULL, act);
     if (!m) continue;
@@ -625,12 +669,58 @@ __device__ __forceinline__ void gather_rows(const PullArgs &a, const L2Pol<H> &p
   }
 }
 
+// The slot of a non-zero row held by lanes 0..L-1 (uint4 q = lane + k * L):
+// its bit count (saturated at 0xFFFF) and, for a short row, its ids in order.
+template <int L, int UPL>
+__device__ __forceinline__ void write_slot(uint16_t *slot, const uint4 (&acc)[UPL], uint32_t qn,
+                                           unsigned long long &ns) {
+  const int lane = threadIdx.x & 31;
+  uint32_t c = 0;
+  if (lane < L) {
+#pragma unroll
+    for (int k = 0; k < UPL; k++)
+      if (lane + k * L < qn) c += popc4(acc[k]);
+  }
+  uint32_t incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const uint32_t total = __shfl_sync(FULL, incl, 31);
+  if (total <= SHORT_MAX) {
+    uint32_t pos = 1 + incl - c;
+    if (c) {
+#pragma unroll
+      for (int k = 0; k < UPL; k++) {
+        const uint32_t q = lane + k * L;
+        if (q < qn) {
+          const uint32_t w[4] = {acc[k].x, acc[k].y, acc[k].z, acc[k].w};
+#pragma unroll
+          for (int wi = 0; wi < 4; wi++) {
+            uint32_t bits = w[wi];
+            while (bits) {
+              const uint32_t t = __ffs(bits) - 1;
+              bits &= bits - 1;
+              slot[pos++] = (uint16_t)(q * 128 + wi * 32 + t);
+            }
+          }
+        }
+      }
+    }
+    if (lane == 0) ns++;
+  }
+  if (lane == 0) slot[0] = (uint16_t)(total < 0xFFFFu ? total : 0xFFFFu);
+}
+
 // Fused epilogue for the row of v held by lanes 0..L-1 after the group reduction:
-// visited AND-NOT + update, accumulator OR, next-layer write, flag, counters.
+// visited AND-NOT + update, accumulator OR, next-layer write (and its slot),
+// flag, counters.
 template <int L, int UPL, int H>
 __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> &pol, uint32_t v,
                                               const uint32_t q0, const uint32_t qn, uint4 (&acc)[UPL],
-                                              unsigned long long &nb, unsigned long long &nv) {
+                                              unsigned long long &nb, unsigned long long &nv,
+                                              unsigned long long &ns) {
   const int lane = threadIdx.x & 31;
   const bool leader_group = lane < L;
   bool any = false;
@@ -685,6 +775,7 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
         if (q < qn) pol.st(a.N + (size_t)v * a.Q + q0 + q, acc[k]);
       }
     }
+    if (a.slot_out && rownz) write_slot<L, UPL>(a.slot_out + (size_t)v * 16, acc, qn, ns);
     if (lane == 0) {
       if ((rownz ? 1u : 0u) != oldf) a.flagN[v] = rownz ? 1u : 0u;
       if (rownz) nv++;
@@ -701,58 +792,108 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
   }
 }
 
-template <int L, int UPL, int MINB, int H>
-__global__ void __launch_bounds__(256, MINB) k_pull(PullArgs a) {
-  if (a.ctr->hop[a.h].strategy != ST_PULL || a.ctr->hop[a.h].rowlist) return;
+__device__ __forceinline__ void pull_counters(const PullArgs &a, unsigned long long nb, unsigned long long nv,
+                                              unsigned long long ns, unsigned long long se) {
+  block_add(nb, &a.ctr->hop[a.h].new_bits);
+  block_add(nv, &a.ctr->hop[a.h].active_vertices);
+  if (a.slot_out) block_add(ns, &a.ctr->hop[a.h].short_rows);
+  if (a.slot_in) block_add(se, &a.ctr->hop[a.h].short_edges);
+}
+
+template <int L, int UPL, int H, bool SHORT>
+__device__ __forceinline__ void pull_vertices(const PullArgs &a) {
   const L2Pol<H> pol;
   __shared__ uint32_t s_u[8][32];
+  extern __shared__ uint4 s_short[];  // SHORT: [8 warps][Q], the ids of short in-neighbour rows
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const uint32_t q0 = blockIdx.y * a.qslice;
   const uint32_t qn = min(a.qslice, a.Q - q0);
-  unsigned long long nb = 0, nv = 0;
+  uint4 *srow = s_short + (size_t)wib * a.Q;
+  if (SHORT) {
+    for (uint32_t q = lane; q < a.Q; q += 32) srow[q] = make_uint4(0, 0, 0, 0);
+    __syncwarp();
+  }
+  unsigned long long nb = 0, nv = 0, ns = 0, se = 0;
   for (uint32_t v = blockIdx.x * 8 + wib; v < a.V; v += gridDim.x * 8) {
     if (a.hub_threshold) {
       int64_t d = 0;
       _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n) d += a.in.off[l][v + 1] - a.in.off[l][v];
       if (d > (int64_t)a.hub_threshold) continue;  // handled by k_pull_hub
     }
+    if (SHORT && lane == 0) {  // the epilogue's read-modify-write rows, fetched while the gather runs
+      if (a.shortest) prefetch_l2(a.vis + (size_t)v * a.Q + q0, qn * 16);
+      if (a.acc_on) prefetch_l2(a.acc + (size_t)v * a.Q + q0, qn * 16);
+    }
     uint4 acc[UPL];
 #pragma unroll
     for (int k = 0; k < UPL; k++) acc[k] = make_uint4(0, 0, 0, 0);
     _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n)
-      gather_rows<L, UPL, H>(a, pol, s_u[wib], q0, qn, acc, a.in.adj[l], pol.ld_stream(a.in.off[l] + v),
-                             pol.ld_stream(a.in.off[l] + v + 1), 0, 32);
+      gather_rows<L, UPL, H, SHORT>(a, pol, s_u[wib], reinterpret_cast<uint32_t *>(srow), q0, qn, acc,
+                                    a.in.adj[l], pol.ld_stream(a.in.off[l] + v),
+                                    pol.ld_stream(a.in.off[l] + v + 1), 0, 32, se);
 #pragma unroll
     for (int o = L; o < 32; o <<= 1)
 #pragma unroll
       for (int k = 0; k < UPL; k++) acc[k] = or4(acc[k], shfl_xor4(acc[k], o));
-    pull_epilogue<L, UPL, H>(a, pol, v, q0, qn, acc, nb, nv);
+    if (SHORT) {  // one slice: q0 = 0, qn = Q
+      __syncwarp();
+      if (lane < L) {
+#pragma unroll
+        for (int k = 0; k < UPL; k++) {
+          const uint32_t q = lane + k * L;
+          if (q < qn) {
+            acc[k] = or4(acc[k], srow[q]);
+            srow[q] = make_uint4(0, 0, 0, 0);
+          }
+        }
+      }
+      __syncwarp();
+    }
+    pull_epilogue<L, UPL, H>(a, pol, v, q0, qn, acc, nb, nv, ns);
   }
-  (void)lane;
-  block_add(nb, &a.ctr->hop[a.h].new_bits);
-  block_add(nv, &a.ctr->hop[a.h].active_vertices);
+  pull_counters(a, nb, nv, ns, se);
+}
+
+template <int L, int UPL, int MINB, int H>
+__global__ void __launch_bounds__(256, MINB) k_pull(PullArgs a) {
+  if (a.ctr->hop[a.h].strategy != ST_PULL || a.ctr->hop[a.h].short_pull) return;
+  pull_vertices<L, UPL, H, false>(a);
+}
+
+// the same in short mode (its own kernel: the slot path's registers stay out
+// of the dense kernels' budget)
+template <int L, int UPL>
+__global__ void __launch_bounds__(256, UPL >= 4 ? 2 : 6) k_pull_short(PullArgs a) {
+  if (a.ctr->hop[a.h].strategy != ST_PULL || !a.ctr->hop[a.h].short_pull || !a.slot_in) return;
+  pull_vertices<L, UPL, 0, true>(a);
 }
 
 // Hub vertices (in-degree above the threshold): one 512-thread CTA per vertex,
-// warps stride over the in-list, rows reduced through shared memory.
-template <int L, int UPL>
-__global__ void __launch_bounds__(512) k_pull_hub(PullArgs a) {
-  if (a.ctr->hop[a.h].strategy != ST_PULL || a.ctr->hop[a.h].rowlist || a.nhubs == 0) return;
-  extern __shared__ uint4 s_red[];  // [16 warps][32 lanes][UPL]
+// warps stride over the in-list, rows reduced through shared memory (short
+// rows through one shared row of the CTA).
+template <int L, int UPL, bool SHORT>
+__device__ __forceinline__ void pull_hubs(const PullArgs &a) {
+  extern __shared__ uint4 s_red[];  // [16 warps][32 lanes][UPL], then SHORT: one row of Q
   const L2Pol<0> pol;
   __shared__ uint32_t s_u[16][32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const uint32_t q0 = blockIdx.y * a.qslice;
   const uint32_t qn = min(a.qslice, a.Q - q0);
-  unsigned long long nb = 0, nv = 0;
+  uint4 *srow = s_red + 16 * 32 * UPL;
+  if (SHORT) {
+    for (uint32_t q = threadIdx.x; q < a.Q; q += blockDim.x) srow[q] = make_uint4(0, 0, 0, 0);
+    __syncthreads();
+  }
+  unsigned long long nb = 0, nv = 0, ns = 0, se = 0;
   for (uint32_t hi = blockIdx.x; hi < a.nhubs; hi += gridDim.x) {
     const uint32_t v = a.hubs[hi];
     uint4 acc[UPL];
 #pragma unroll
     for (int k = 0; k < UPL; k++) acc[k] = make_uint4(0, 0, 0, 0);
     _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n)
-      gather_rows<L, UPL, 0>(a, pol, s_u[wib], q0, qn, acc, a.in.adj[l], a.in.off[l][v],
-                             a.in.off[l][v + 1], (int64_t)wib * 32, (int64_t)nw * 32);
+      gather_rows<L, UPL, 0, SHORT>(a, pol, s_u[wib], reinterpret_cast<uint32_t *>(srow), q0, qn, acc,
+                                    a.in.adj[l], a.in.off[l][v], a.in.off[l][v + 1], (int64_t)wib * 32,
+                                    (int64_t)nw * 32, se);
 #pragma unroll
     for (int o = L; o < 32; o <<= 1)
 #pragma unroll
@@ -766,66 +907,43 @@ __global__ void __launch_bounds__(512) k_pull_hub(PullArgs a) {
         for (int w = 1; w < nw; w++)
 #pragma unroll
           for (int k = 0; k < UPL; k++) acc[k] = or4(acc[k], s_red[(w * 32 + lane) * UPL + k]);
+        if (SHORT) {
+#pragma unroll
+          for (int k = 0; k < UPL; k++) {
+            const uint32_t q = lane + k * L;
+            if (q < qn) acc[k] = or4(acc[k], srow[q]);
+          }
+        }
       }
-      pull_epilogue<L, UPL, 0>(a, pol, v, q0, qn, acc, nb, nv);
+      pull_epilogue<L, UPL, 0>(a, pol, v, q0, qn, acc, nb, nv, ns);
     }
     __syncthreads();
-  }
-  block_add(nb, &a.ctr->hop[a.h].new_bits);
-  block_add(nv, &a.ctr->hop[a.h].active_vertices);
-}
-
-// ---------------------------------------------------------------------------
-// PULL over row lists.  When the frontier's rows are sparse in bits (a few
-// sources per vertex, as in the later hops of a many-source expand over a
-// power-law graph), gathering whole 8W-byte rows per edge moves mostly zero
-// words.  The hop then first turns every non-zero frontier row into the list
-// of its set source indices (uint16, one exclusive scan over the row
-// popcounts), and each target vertex ORs its active in-neighbours' lists into
-// a shared-memory row with 32-bit atomics; the same fused epilogue follows.
-// A warp flattens the lists of its 32 in-neighbours (warp prefix sum of their
-// lengths) and hands out entries 32 at a time, so short lists keep every
-// lane busy.
-struct RowLists {
-  const unsigned long long *cnt, *off;  // per vertex: entries, first entry
-  uint16_t *ids;
-  uint64_t cap;
-};
-
-// popcount of every flagged row of layer h-1 (zero for the others)
-__global__ void k_rl_count(const uint32_t *__restrict__ flagF, const uint4 *__restrict__ F, uint32_t V, uint32_t Q,
-                           unsigned long long *__restrict__ cnt, Lists out, Ctr *ctr, int h) {
-  if (!rowlist_hop(ctr, h)) return;
-  const int lane = threadIdx.x & 31;
-  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-  unsigned long long entries = 0;  // what the targets will gather: out-degree x row bits
-  for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < V; base += warps * 32) {
-    const uint32_t v = base + lane;
-    const bool f = v < V && flagF[v];
-    if (v < V && !f) cnt[v] = 0;
-    unsigned m = __ballot_sync(FULL, f);
-    while (m) {
-      const int b = __ffs(m) - 1;
-      m &= m - 1;
-      const uint4 *row = F + (size_t)(base + b) * Q;
-      unsigned long long c = 0;
-      for (uint32_t q = lane; q < Q; q += 32) c += popc4(row[q]);
-      c = warp_sum(c);
-      if (lane == 0) {
-        cnt[base + b] = c;
-        unsigned long long d = 0;
-        _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < out.n) d += (unsigned long long)(out.off[l][base + b + 1] - out.off[l][base + b]);
-        entries += c * d;
-      }
+    if (SHORT) {
+      for (uint32_t q = threadIdx.x; q < a.Q; q += blockDim.x) srow[q] = make_uint4(0, 0, 0, 0);
+      __syncthreads();
     }
   }
-  block_add(entries, &ctr->hop[h].rl_entries);
+  pull_counters(a, nb, nv, ns, se);
 }
 
-// the set source indices of every flagged row, at its scanned offset
-__global__ void k_rl_fill(const uint32_t *__restrict__ flagF, const uint4 *__restrict__ F, uint32_t V, uint32_t Q,
-                          RowLists rl, Ctr *ctr, int h) {
-  if (!rowlist_hop(ctr, h)) return;
+template <int L, int UPL>
+__global__ void __launch_bounds__(512) k_pull_hub(PullArgs a) {
+  if (a.ctr->hop[a.h].strategy != ST_PULL || a.ctr->hop[a.h].short_pull || a.nhubs == 0) return;
+  pull_hubs<L, UPL, false>(a);
+}
+
+template <int L, int UPL>
+__global__ void __launch_bounds__(512) k_pull_hub_short(PullArgs a) {
+  if (a.ctr->hop[a.h].strategy != ST_PULL || !a.ctr->hop[a.h].short_pull || !a.slot_in || a.nhubs == 0) return;
+  pull_hubs<L, UPL, true>(a);
+}
+
+// Slots of layer h-1 when hop h pulls in short mode and that layer was not
+// written by a PULL hop (SPARSE, PUSH or the seed): a warp per flagged row
+// counts its bits and, for a short row, writes its ids in order.
+__global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__restrict__ F, uint32_t V,
+                             uint32_t Q, uint16_t *__restrict__ slots, const Ctr *ctr, int h) {
+  if (ctr->hop[h].strategy != ST_PULL || !ctr->hop[h].short_pull || ctr->hop[h - 1].strategy == ST_PULL) return;
   const int lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < V; base += warps * 32) {
@@ -835,146 +953,39 @@ __global__ void k_rl_fill(const uint32_t *__restrict__ flagF, const uint4 *__res
       const int b = __ffs(m) - 1;
       m &= m - 1;
       const uint4 *row = F + (size_t)(base + b) * Q;
-      unsigned long long pos = rl.off[base + b];
-      for (uint32_t q0 = 0; q0 < Q; q0 += 32) {
-        const uint32_t q = q0 + lane;
-        const uint4 x = q < Q ? row[q] : make_uint4(0, 0, 0, 0);
-        const unsigned n = popc4(x);
-        unsigned incl = n;
-        for (int o = 1; o < 32; o <<= 1) {
-          const unsigned y = __shfl_up_sync(FULL, incl, o);
-          if (lane >= o) incl += y;
-        }
-        unsigned long long at = pos + incl - n;
-        const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+      uint16_t *slot = slots + (size_t)(base + b) * 16;
+      uint32_t c = 0;
+      for (uint32_t q = lane; q < Q; q += 32) c += popc4(row[q]);
+      const uint32_t total = warp_sum(c);
+      if (total <= SHORT_MAX) {
+        uint32_t pos = 1;
+        for (uint32_t q0 = 0; q0 < Q; q0 += 32) {
+          const uint32_t q = q0 + lane;
+          const uint4 x = q < Q ? row[q] : make_uint4(0, 0, 0, 0);
+          const uint32_t n = popc4(x);
+          uint32_t incl = n;
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-          uint32_t bits = w[k];
-          while (bits) {
-            const int t = __ffs(bits) - 1;
-            bits &= bits - 1;
-            if (at < rl.cap)
-              rl.ids[at] = (uint16_t)(q * 128 + k * 32 + t);
-            else
-              ctr->error |= 4;  // cannot happen: the decide kernel checked the layer's bit count
-            at++;
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
           }
+          uint32_t at = pos + incl - n;
+          const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+          for (int wi = 0; wi < 4; wi++) {
+            uint32_t bits = w[wi];
+            while (bits) {
+              const uint32_t t = __ffs(bits) - 1;
+              bits &= bits - 1;
+              slot[at++] = (uint16_t)(q * 128 + wi * 32 + t);
+            }
+          }
+          pos += __shfl_sync(FULL, incl, 31);
         }
-        pos += __shfl_sync(FULL, incl, 31);
       }
+      if (lane == 0) slot[0] = (uint16_t)(total < 0xFFFFu ? total : 0xFFFFu);
     }
   }
-}
-
-// OR the lists of the active in-neighbours of v (in [beg, end) of one list
-// set, warp-strided from start) into the shared row acc32.
-__device__ __forceinline__ void gather_lists(const PullArgs &a, const RowLists &rl, uint32_t *acc32,
-                                             const uint32_t *adj, int64_t beg, int64_t end, int64_t start,
-                                             int64_t step) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t base = beg + start; base < end; base += step) {
-    const int64_t j = base + lane;
-    unsigned long long o = 0, n = 0;
-    if (j < end) {
-      const uint32_t u = __ldg(adj + j);
-      if (__ldg(a.flagF + u)) {
-        n = rl.cnt[u];
-        o = rl.off[u];
-      }
-    }
-    unsigned long long incl = n;
-    for (int k = 1; k < 32; k <<= 1) {
-      const unsigned long long y = __shfl_up_sync(FULL, incl, k);
-      if (lane >= k) incl += y;
-    }
-    const unsigned long long total = __shfl_sync(FULL, incl, 31);
-    for (unsigned long long k0 = 0; k0 < total; k0 += 32) {
-      const unsigned long long k = k0 + lane;
-      int pos = 0;  // first lane whose inclusive count exceeds k
-#pragma unroll
-      for (int st = 16; st; st >>= 1)
-        if (__shfl_sync(FULL, incl, pos + st - 1) <= k) pos += st;
-      const unsigned long long so = __shfl_sync(FULL, o, pos);
-      const unsigned long long sn = __shfl_sync(FULL, n, pos);
-      const unsigned long long si = __shfl_sync(FULL, incl, pos);
-      const unsigned long long at = so + (k - (si - sn));
-      if (k < total && at < rl.cap) {  // entries past the capacity were never written
-        const uint32_t id = rl.ids[at];
-        if ((id >> 5) < 4 * a.Q) atomicOr(acc32 + (id >> 5), 1u << (id & 31));
-      }
-    }
-  }
-}
-
-template <int L, int UPL>
-__global__ void __launch_bounds__(256) k_pull_rl(PullArgs a, RowLists rl) {
-  if (!rowlist_hop(a.ctr, a.h)) return;
-  extern __shared__ uint4 s_rows[];  // [8 warps][Q]
-  const L2Pol<0> pol;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  uint4 *row = s_rows + (size_t)wib * a.Q;
-  uint32_t *acc32 = reinterpret_cast<uint32_t *>(row);
-  for (uint32_t q = lane; q < a.Q; q += 32) row[q] = make_uint4(0, 0, 0, 0);
-  __syncwarp();
-  unsigned long long nb = 0, nv = 0;
-  for (uint32_t v = blockIdx.x * 8 + wib; v < a.V; v += gridDim.x * 8) {
-    if (a.hub_threshold) {
-      int64_t d = 0;
-      _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n) d += a.in.off[l][v + 1] - a.in.off[l][v];
-      if (d > (int64_t)a.hub_threshold) continue;  // handled by k_pull_rl_hub
-    }
-    _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n)
-      gather_lists(a, rl, acc32, a.in.adj[l], __ldg(a.in.off[l] + v), __ldg(a.in.off[l] + v + 1), 0, 32);
-    __syncwarp();
-    uint4 acc[UPL];
-#pragma unroll
-    for (int k = 0; k < UPL; k++) {
-      const uint32_t q = lane + k * L;
-      acc[k] = make_uint4(0, 0, 0, 0);
-      if (lane < L && q < a.Q) {
-        acc[k] = row[q];
-        row[q] = make_uint4(0, 0, 0, 0);
-      }
-    }
-    __syncwarp();
-    pull_epilogue<L, UPL, 0>(a, pol, v, 0, a.Q, acc, nb, nv);
-  }
-  block_add(nb, &a.ctr->hop[a.h].new_bits);
-  block_add(nv, &a.ctr->hop[a.h].active_vertices);
-}
-
-// hub targets: one 512-thread CTA per vertex, all warps OR into one shared row
-template <int L, int UPL>
-__global__ void __launch_bounds__(512) k_pull_rl_hub(PullArgs a, RowLists rl) {
-  if (!rowlist_hop(a.ctr, a.h) || a.nhubs == 0) return;
-  extern __shared__ uint4 s_row[];  // [Q]
-  const L2Pol<0> pol;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  uint32_t *acc32 = reinterpret_cast<uint32_t *>(s_row);
-  for (uint32_t q = threadIdx.x; q < a.Q; q += blockDim.x) s_row[q] = make_uint4(0, 0, 0, 0);
-  __syncthreads();
-  unsigned long long nb = 0, nv = 0;
-  for (uint32_t hi = blockIdx.x; hi < a.nhubs; hi += gridDim.x) {
-    const uint32_t v = a.hubs[hi];
-    _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n)
-      gather_lists(a, rl, acc32, a.in.adj[l], a.in.off[l][v], a.in.off[l][v + 1], (int64_t)wib * 32,
-                   (int64_t)nw * 32);
-    __syncthreads();
-    if (wib == 0) {
-      uint4 acc[UPL];
-#pragma unroll
-      for (int k = 0; k < UPL; k++) {
-        const uint32_t q = lane + k * L;
-        acc[k] = (lane < L && q < a.Q) ? s_row[q] : make_uint4(0, 0, 0, 0);
-      }
-      pull_epilogue<L, UPL, 0>(a, pol, v, 0, a.Q, acc, nb, nv);
-    }
-    __syncthreads();
-    for (uint32_t q = threadIdx.x; q < a.Q; q += blockDim.x) s_row[q] = make_uint4(0, 0, 0, 0);
-    __syncthreads();
-  }
-  block_add(nb, &a.ctr->hop[a.h].new_bits);
-  block_add(nv, &a.ctr->hop[a.h].active_vertices);
 }
 
 // ---------------------------------------------------------------------------
@@ -1144,15 +1155,14 @@ Lists push_lists(const vs_graph *g, int dir) {
 
 using PullFn = void (*)(PullArgs);
 
-using PullRlFn = void (*)(PullArgs, RowLists);
 struct PullVariant {
   int L, UPL;
   PullFn pull[4], hub;  // pull[k]: bit 0 = 8 blocks per SM, bit 1 = L2 cache policies
-  PullRlFn pull_rl, hub_rl;
+  PullFn pull_short, hub_short;
 };
 
 #define VS_PULLS(L, U) {k_pull<L, U, 1, 0>, k_pull<L, U, 8, 0>, k_pull<L, U, 1, 1>, k_pull<L, U, 8, 1>}
-#define VS_VARIANT(L, U) {L, U, VS_PULLS(L, U), k_pull_hub<L, U>, k_pull_rl<L, U>, k_pull_rl_hub<L, U>}
+#define VS_VARIANT(L, U) {L, U, VS_PULLS(L, U), k_pull_hub<L, U>, k_pull_short<L, U>, k_pull_hub_short<L, U>}
 const PullVariant kVariants[] = {
     VS_VARIANT(1, 1),  VS_VARIANT(2, 1),  VS_VARIANT(4, 1),  VS_VARIANT(8, 1), VS_VARIANT(16, 1),
     VS_VARIANT(32, 1), VS_VARIANT(32, 2), VS_VARIANT(32, 4), VS_VARIANT(32, 8),
@@ -1191,7 +1201,7 @@ struct vs_expand_plan {
   uint32_t nhubs = 0, hub_threshold = 0;
   bool use_vis = false, use_acc = false, clear_diag = false;
   bool collect_stats = false;
-  int grid_pull = 0, grid_hub = 0, grid_sparse = 0, grid_v = 0, grid_push = 0, grid_rl = 0;
+  int grid_pull = 0, grid_hub = 0, grid_sparse = 0, grid_v = 0, grid_push = 0, grid_short = 0;
   vs_bitmat result{};
   bool has_result = false;
   // tuning knobs of the fixed planner
@@ -1203,10 +1213,8 @@ struct vs_expand_plan {
   uint32_t *rowk = nullptr;   // [0] largest row limit, [1] a limit exceeded k_max (device-set limits)
   uint64_t *layer_out[VS_MAX_HOPS + 1] = {};  // with_distance: layer h is copied here (zeroed, V x W words)
   // row lists of sparse frontier rows (PULL over lists); none when S > 65536 or multi-slice
-  unsigned long long *rl_cnt = nullptr, *rl_off = nullptr, *rl_bsum = nullptr;
-  uint16_t *rl_ids = nullptr;
-  uint64_t rl_cap = 0;
-  double rl_bits = 2.0;
+  uint16_t *slot[2] = {nullptr, nullptr};  // short-row slots of the two frontier buffers' layers
+  double short_min = 0.0;                  // share of short rows for a short-mode PULL (0: off)
   bool use_hmask = false;
   int hop_forced[VS_MAX_HOPS + 1] = {};
   bool timing = false;
@@ -1226,17 +1234,15 @@ inline bool needs_acc(const vs_expand_params &p) {
          (p.path_type == VS_PATH_SHORTEST && p.k_min >= 2);
 }
 
-// Row-list entries a plan keeps (uint16 source ids: S <= 65536, one slice):
-// a sixty-fourth of the S x V bits, between 2^20 and 2^29.
-inline uint64_t rowlist_cap(uint32_t S, uint32_t V, uint32_t nslices) {
-  if (S > 65536 || nslices != 1) return 0;
-  return std::max<uint64_t>(1ull << 20, std::min<uint64_t>((uint64_t)S * V / 64, 1ull << 29));
+// Short-row slots (uint16 ids: S <= 65536) need rows in one slice.
+inline bool short_slots_ok(uint32_t S, uint32_t nslices, double share) {
+  return share >= 0 && S <= 65536 && nslices == 1;
 }
 
 int plan_free(vs_expand_plan *pl) {
   if (!pl) return VS_OK;
   const cudaStream_t st = pl->last_stream;
-  void *ptrs[] = {pl->rl_cnt, pl->rl_off, pl->rl_bsum, pl->rl_ids, pl->resflag, pl->pdeg[0], pl->pdeg[1], pl->doff,
+  void *ptrs[] = {pl->slot[0], pl->slot[1], pl->resflag, pl->pdeg[0], pl->pdeg[1], pl->doff,
                   pl->bsum, pl->hmask, pl->rowk, pl->buf[0], pl->buf[1], pl->flag[0], pl->flag[1], pl->vis, pl->acc,
                   pl->pairs[0], pl->pairs[1], pl->push_list, pl->touched, pl->d_src,
                   pl->d_tgt, pl->d_dist, pl->ctr, pl->hubs};
@@ -1325,13 +1331,12 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   PL_ALLOC(pl->ctr, 1);
   PL_ALLOC(pl->hmask, (size_t)(p->k_max + 1) * pl->W);
   PL_ALLOC(pl->rowk, 2);
-  pl->rl_bits = p->rowlist_bits == 0 ? 2.0 : p->rowlist_bits;
-  pl->rl_cap = pl->rl_bits > 0 ? rowlist_cap(S, V, pl->nslices) : 0;
-  if (pl->rl_cap) {
-    PL_ALLOC(pl->rl_cnt, V);
-    PL_ALLOC(pl->rl_off, (size_t)V + 1);
-    PL_ALLOC(pl->rl_bsum, ((size_t)V + 1023) / 1024 + 1);
-    PL_ALLOC(pl->rl_ids, pl->rl_cap);
+  pl->short_min = p->short_share == 0 ? 0.1 : p->short_share;
+  if (short_slots_ok(S, pl->nslices, p->short_share)) {
+    PL_ALLOC(pl->slot[0], (size_t)V * 16);
+    PL_ALLOC(pl->slot[1], (size_t)V * 16);
+  } else {
+    pl->short_min = 0;
   }
 #undef PL_ALLOC
   cudaError_t e = cudaSuccess;
@@ -1370,15 +1375,14 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   pl->pull_kind = p->pull_kernel;
   if (p->sparse_frac > 0) pl->sparse_frac = p->sparse_frac;
   const PullVariant &var = pick_variant(pl->qslice);
-  if (var.UPL * 16 * 32 * 16 > 48 * 1024)
-    cudaFuncSetAttribute(var.hub, cudaFuncAttributeMaxDynamicSharedMemorySize, 16 * 32 * 16 * var.UPL);
+  const int hub_smem = 16 * 32 * 16 * var.UPL;
+  if (hub_smem > 48 * 1024) cudaFuncSetAttribute(var.hub, cudaFuncAttributeMaxDynamicSharedMemorySize, hub_smem);
   pl->grid_pull = occupancy_grid(var.pull[pl->pull_kind], 256, 0, 8);
-  pl->grid_hub = std::max(1, std::min((int)pl->nhubs, occupancy_grid(var.hub, 512, 16 * 32 * 16 * var.UPL, 2)));
-  if (pl->rl_cap) {
-    const size_t rl_smem = 8 * (size_t)pl->Q * 16;
-    if (rl_smem > 48 * 1024)
-      cudaFuncSetAttribute(var.pull_rl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rl_smem);
-    pl->grid_rl = occupancy_grid(var.pull_rl, 256, rl_smem, 8);
+  pl->grid_hub = std::max(1, std::min((int)pl->nhubs, occupancy_grid(var.hub, 512, hub_smem, 2)));
+  if (pl->slot[0]) {  // short mode: a row of Q uint4 per warp (PULL) or per CTA (hubs)
+    const int hs = hub_smem + (int)pl->Q * 16;
+    if (hs > 48 * 1024) cudaFuncSetAttribute(var.hub_short, cudaFuncAttributeMaxDynamicSharedMemorySize, hs);
+    pl->grid_short = occupancy_grid(var.pull_short, 256, 8 * (size_t)pl->Q * 16, 8);
   }
   pl->grid_sparse = occupancy_grid(k_sparse, 256, 0, 8);
   pl->grid_push = occupancy_grid(k_push, 256, 0, 8);
@@ -1404,8 +1408,7 @@ int vs_expand_plan_footprint(const vs_graph *g, uint32_t S, const vs_expand_para
   uint32_t qs = p->slice_words ? (p->slice_words + 1) / 2 : (uint32_t)(W / 2);
   qs = std::max<uint32_t>(1, std::min<uint32_t>(qs, 256));
   const uint32_t nslices = (uint32_t)((W / 2 + qs - 1) / qs);
-  const uint64_t rl = p->rowlist_bits < 0 ? 0 : rowlist_cap(S, (uint32_t)V, nslices);
-  if (rl) b += 2 * (V + 1) * 8 + ((V + 1023) / 1024 + 1) * 8 + rl * 2;  // row counts, offsets, ids
+  if (short_slots_ok(S, nslices, p->short_share)) b += 2 * V * 32;  // short-row slots of both buffers
   *bytes = b;
   return VS_OK;
 }
@@ -1492,8 +1495,8 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     da.picker = pl->picker;
     da.picker_on = p.use_picker;
     da.rowk = pl->use_hmask ? pl->rowk : nullptr;
-    da.rl_cap = pl->rl_bits > 0 ? pl->rl_cap : 0;
-    da.rl_bits = pl->rl_bits;
+    da.short_min = pl->short_min;
+    da.l2_half = l2_bytes() / 2;
     da.W = W;
     da.k_min = p.k_min;
     da.k_max = p.k_max;
@@ -1524,9 +1527,9 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     sp.acc_on = acc_on;
     sp.doff = pl->doff;
     sp.pdeg_out = pl->pdeg[nbuf];
-    { k_pscan1<<<pl->grid_v, 256, 0, st>>>(pl->pdeg[fb], pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap, 0); vs::note_launch(); }
-    { k_pscan2<<<1, 1024, 0, st>>>(pl->bsum, pl->doff, pl->ctr, h, pl->pair_cap, 0); vs::note_launch(); }
-    { k_pscan3<<<pl->grid_v, 256, 0, st>>>(pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap, 0); vs::note_launch(); }
+    { k_pscan1<<<pl->grid_v, 256, 0, st>>>(pl->pdeg[fb], pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
+    { k_pscan2<<<1, 1024, 0, st>>>(pl->bsum, pl->doff, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
+    { k_pscan3<<<pl->grid_v, 256, 0, st>>>(pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
     { k_sparse<<<pl->grid_sparse, 256, 0, st>>>(sp); vs::note_launch(); }
     PushArgs pa;
     pa.ctr = pl->ctr;
@@ -1575,24 +1578,19 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.nhubs = pl->nhubs;
     a.ctr = pl->ctr;
     a.h = h;
+    a.slot_in = pl->slot[0] ? reinterpret_cast<const uint4 *>(pl->slot[fb]) : nullptr;
+    a.slot_out = pl->slot[0] && h < p.k_max && !a.last ? pl->slot[nbuf] : nullptr;
     if (timing) cudaEventRecord(pl->ev[3 * h + 1], st);
-    if (pl->rl_cap) {  // row lists of layer h-1, used when the decide kernel chose them
-      RowLists rl{pl->rl_cnt, pl->rl_off, pl->rl_ids, pl->rl_cap};
-      { k_rl_count<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<const uint4 *>(pl->buf[fb]), V, Q,
-                                              pl->rl_cnt, outl, pl->ctr, h); vs::note_launch(); }
-      { k_pscan1<<<pl->grid_v, 256, 0, st>>>(pl->rl_cnt, pl->rl_off, pl->rl_bsum, pl->ctr, h, 0, V); vs::note_launch(); }
-      { k_pscan2<<<1, 1024, 0, st>>>(pl->rl_bsum, pl->rl_off, pl->ctr, h, 0, V); vs::note_launch(); }
-      { k_pscan3<<<pl->grid_v, 256, 0, st>>>(pl->rl_off, pl->rl_bsum, pl->ctr, h, 0, V); vs::note_launch(); }
-      { k_rl_fill<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<const uint4 *>(pl->buf[fb]), V, Q, rl,
-                                             pl->ctr, h); vs::note_launch(); }
-    }
+    if (pl->slot[0])  // slots of a layer SPARSE or PUSH wrote, when this hop reads them
+      { k_slot_build<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<const uint4 *>(pl->buf[fb]), V, Q,
+                                               pl->slot[fb], pl->ctr, h); vs::note_launch(); }
     { var.pull[pl->pull_kind]<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a); vs::note_launch(); }
     if (pl->nhubs)
       { var.hub<<<dim3(pl->grid_hub, pl->nslices), 512, 16 * 32 * 16 * var.UPL, st>>>(a); vs::note_launch(); }
-    if (pl->rl_cap) {
-      RowLists rl{pl->rl_cnt, pl->rl_off, pl->rl_ids, pl->rl_cap};
-      { var.pull_rl<<<pl->grid_rl, 256, 8 * (size_t)Q * 16, st>>>(a, rl); vs::note_launch(); }
-      if (pl->nhubs) { var.hub_rl<<<pl->grid_hub, 512, (size_t)Q * 16, st>>>(a, rl); vs::note_launch(); }
+    if (pl->slot[0]) {
+      { var.pull_short<<<pl->grid_short, 256, 8 * (size_t)Q * 16, st>>>(a); vs::note_launch(); }
+      if (pl->nhubs)
+        { var.hub_short<<<pl->grid_hub, 512, 16 * 32 * 16 * var.UPL + (size_t)Q * 16, st>>>(a); vs::note_launch(); }
     }
     if (p.path_type == VS_PATH_FIND_SHORTEST)
       { k_find_check<<<std::max(1u, std::min((S_ + 255) / 256, 1024u)), 256, 0, st>>>(
@@ -1654,8 +1652,9 @@ int vs_expand_plan_stats(vs_expand_plan *pl, vs_expand_stats *stats, vs_stream_t
     stats->active_edges[i] = h.hop[i].active_edges;
     stats->pairs[i] = h.hop[i].pairs;
     stats->strategy[i] = h.hop[i].strategy;
-    stats->rowlist[i] = h.hop[i].rowlist;
-    stats->rowlist_entries[i] = h.hop[i].rl_entries;
+    stats->short_pull[i] = h.hop[i].short_pull;
+    stats->short_rows[i] = h.hop[i].short_rows;
+    stats->short_edges[i] = h.hop[i].short_edges;
     if (i >= 1 && i <= h.hops_run) vc += h.hop[i].new_bits;
   }
   for (uint32_t i = 1; i <= pl->timed_hops && i <= VS_MAX_HOPS; i++) {

@@ -20,8 +20,9 @@ struct HopCtr {
   unsigned long long hist[16];         // log2(out-degree + 1) histogram of layer h-1's active rows
   int overflow;                        // SPARSE: pair list overflowed
   int strategy;                        // strategy run at hop h (0 = not run)
-  int rowlist;                         // PULL over the row lists of layer h-1
-  unsigned long long rl_entries;       // row-list entries the PULL gathers (sum of out-degree x row bits)
+  int short_pull;                      // PULL reads the short rows of layer h-1 through their slots
+  unsigned long long short_rows;       // rows of layer h with 1..15 bits (counted when its slots are written)
+  unsigned long long short_edges;      // active in-edges of a short-mode PULL served from a slot
 };
 
 struct Ctr {
@@ -66,8 +67,8 @@ struct DecideArgs {
   double sparse_frac, push_frac;
   const void *picker;  // bf16 weights of a vs_picker (NULL = fixed planner)
   const uint32_t *rowk;  // [0] largest row hop limit (NULL: no row limits)
-  uint64_t rl_cap;       // row-list entries available (0: row lists off)
-  double rl_bits;        // PULL over row lists when a frontier row holds at most rl_bits * W bits on average
+  double short_min;      // short-mode PULL when at least this share of the frontier's rows are short (0: off; > 1: always)
+  uint64_t l2_half;       // ... and the frontier's rows exceed this many bytes (smaller ones stay in L2)
 };
 
 struct SparseArgs {
@@ -116,6 +117,8 @@ struct PullArgs {
   uint32_t V, Q, qslice;
   int multislice, shortest, acc_on;
   int last;  // the run's last hop and nothing reads its layer: zero the buffer instead of writing it
+  const uint4 *slot_in;  // slots of layer h-1 (two uint4 per vertex; NULL: no short mode)
+  uint16_t *slot_out;    // slots of layer h, written for its non-zero rows (NULL: not kept)
   uint32_t hub_threshold;
   const uint32_t *hubs;
   uint32_t nhubs;

@@ -51,6 +51,7 @@ template <typename T> int copy_in(T *dst, const T *src, size_t n, cudaStream_t s
 }
 
 int sm_count();
+size_t l2_bytes();  // the device's L2 cache size
 
 inline uint32_t words_per_col(uint32_t rows) {
   uint32_t w = (rows + 63) / 64;

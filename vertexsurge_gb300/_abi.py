@@ -52,7 +52,8 @@ class ExpandStats(C.Structure):
                 ("pull_ms", C.c_float * (MAX_HOPS + 1)),
                 ("short_pull", C.c_int32 * (MAX_HOPS + 1)),
                 ("short_rows", C.c_uint64 * (MAX_HOPS + 1)),
-                ("short_edges", C.c_uint64 * (MAX_HOPS + 1))]
+                ("short_edges", C.c_uint64 * (MAX_HOPS + 1)),
+                ("tiny_rows", C.c_uint64 * (MAX_HOPS + 1))]
 
     def as_dict(self) -> dict:
         n = self.hops_run + 1
@@ -61,7 +62,8 @@ class ExpandStats(C.Structure):
                 "active_edges": list(self.active_edges[:n]), "pairs": list(self.pairs[:n]),
                 "strategy": list(self.strategy[:n]), "hop_ms": list(self.hop_ms[:n]),
                 "pull_ms": list(self.pull_ms[:n]), "short_pull": list(self.short_pull[:n]),
-                "short_rows": list(self.short_rows[:n]), "short_edges": list(self.short_edges[:n])}
+                "short_rows": list(self.short_rows[:n]), "short_edges": list(self.short_edges[:n]),
+                "tiny_rows": list(self.tiny_rows[:n])}
 
 
 class BitmatInfo(C.Structure):

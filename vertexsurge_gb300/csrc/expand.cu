@@ -293,7 +293,6 @@ __global__ void __launch_bounds__(64) k_decide(DecideArgs a) {
   }
   if (t == 0) {
     cur.strategy = s_choice;
-    // sparse frontier rows: PULL gathers the rows' source lists instead of whole rows
     // short mode: enough short rows in a frontier that L2 does not already
     // hold (a layer from a PULL hop counted them; from SPARSE or PUSH, a few
     // bits per row on average stand in for the count)
@@ -303,10 +302,13 @@ __global__ void __launch_bounds__(64) k_decide(DecideArgs a) {
       if (a.short_min > 1.0)
         sp = true;
       else if (act * 8.0 * (double)a.W > (double)a.l2_half)
-        sp = prev.strategy == ST_PULL ? (double)prev.short_rows >= a.short_min * act
+        sp = prev.strategy == ST_PULL ? (double)(prev.short_rows & 0xFFFFFFFFull) >= a.short_min * act
                                       : (double)prev.new_bits <= 4.0 * act;
     }
     cur.short_pull = sp;
+    // a frontier of mostly 4..15-bit rows reads slots instead of words
+    cur.short_slots = sp && prev.strategy == ST_PULL &&
+                      (double)(prev.short_rows >> 32) < 0.5 * (double)(prev.short_rows & 0xFFFFFFFFull);
   }
 }
 
@@ -586,94 +588,156 @@ template <int H> struct L2Pol {
 // Short rows.  In the later hops of a many-source expand over a power-law
 // graph most frontier rows hold a handful of sources, and a whole-row gather
 // then moves mostly zero words.  Every PULL hop with a successor therefore
-// also writes a 32-byte slot per non-zero row of its layer: the row's bit
-// count and, when that is at most SHORT_MAX, the source ids (uint16).  A later
-// PULL hop in short mode reads an active in-neighbour's slot (one sector)
-// and, for a short row, ORs the ids into a per-warp shared-memory row with
-// 32-bit atomics instead of gathering 8W bytes; longer rows are gathered
-// whole.  Layers written by SPARSE or PUSH get their slots from a build pass
-// (k_slot_build) when the next hop reads them.
-constexpr uint32_t SHORT_MAX = 15;  // a slot is 16 uint16: the count, then up to 15 ids
+// also writes, for every vertex, a tiny word (uint64: the row's bit count,
+// saturated at 0xFFFF, and up to TINY_MAX source ids as uint16) and a 32-byte
+// slot (entry 0: the count; entries 1..count: the ids, for up to SHORT_MAX
+// bits).  A later PULL hop in short mode reads, per in-neighbour, either its
+// tiny word (word mode: 8 bytes per vertex, an array L2 can hold, loaded with
+// an evict-last hint; the slot follows only for rows of more than TINY_MAX
+// bits) or its slot alone (slot mode, for frontiers of mostly longer rows):
+// count 0 is an empty row, short rows OR their ids into a per-warp
+// shared-memory row with 32-bit atomics, and only longer rows are gathered
+// whole.  Layers written by SPARSE or PUSH get their words and slots from a
+// build pass (k_slot_build) when the next hop reads them.
+constexpr uint32_t TINY_MAX = 3;    // ids in a tiny word (count + 3 x uint16)
+constexpr uint32_t SHORT_MAX = 15;  // ids in a slot (16 uint16, entry 0 = the count)
 
 // Bulk prefetch of `bytes` (a multiple of 16, 16-byte aligned) into L2.
 __device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
 }
 
-// OR the ids of a short slot (count in [1, SHORT_MAX]) into a shared row
+// Read-only 8-byte load that asks L2 to keep the line (evict-last).
+__device__ __forceinline__ uint64_t ld_keep(const uint64_t *p) {
+  uint64_t pol, r;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  asm("ld.global.nc.L2::cache_hint.b64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(pol));
+  return r;
+}
+
+// OR the ids of a tiny word (count in [1, TINY_MAX]) into a shared row
+__device__ __forceinline__ void or_tiny_ids(uint32_t *row32, uint64_t t, uint32_t cnt) {
+#pragma unroll
+  for (uint32_t i = 1; i <= TINY_MAX; i++) {
+    if (i > cnt) break;
+    const uint32_t id = (uint32_t)(t >> (16 * i)) & 0xFFFFu;
+    atomicOr(row32 + (id >> 5), 1u << (id & 31));
+  }
+}
+
+// OR the ids of a slot (count in [TINY_MAX + 1, SHORT_MAX], ids at entries
+// 1..count) into a shared row; the loop leaves at the warp's longest list
 __device__ __forceinline__ void or_slot_ids(uint32_t *row32, const uint4 s0, const uint4 s1, uint32_t cnt) {
   const uint32_t w[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
 #pragma unroll
   for (uint32_t i = 1; i <= SHORT_MAX; i++) {
-    if (i <= cnt) {
-      const uint32_t id = (w[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
-      atomicOr(row32 + (id >> 5), 1u << (id & 31));
+    if (i > cnt) break;
+    const uint32_t id = (w[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
+    atomicOr(row32 + (id >> 5), 1u << (id & 31));
+  }
+}
+
+// One chunk of up to 32 in-neighbours, u / act per lane.  Dense mode: act =
+// the row is non-zero (flag).  Short mode: act = the lane holds an
+// in-neighbour and tv is its tiny word; short rows OR their ids into row32,
+// the others are gathered whole.
+template <int L, int UPL, int H, bool SHORT>
+__device__ __forceinline__ void gather_chunk(const PullArgs &a, const L2Pol<H> &pol, uint32_t *s_u, uint32_t *row32,
+                                             const uint32_t q0, const uint32_t qn, uint4 (&acc)[UPL], uint32_t u,
+                                             bool act, uint64_t tv, bool slotmode, unsigned long long &se) {
+  constexpr int G = 32 / L;
+  const int lane = threadIdx.x & 31, g = lane / L, gl = lane % L;
+  if (SHORT && act) {
+    // slot mode (frontiers of mostly 4..15-bit rows): the slot alone, its
+    // entry 0 holds the count; word mode: the word, then the slot when the
+    // row has more ids than the word holds
+    const uint4 *sp = a.slot_in + (size_t)u * 2;
+    uint4 s0 = make_uint4(0, 0, 0, 0), s1 = s0;
+    uint32_t cnt;
+    if (slotmode) {
+      s0 = __ldg(sp);
+      s1 = __ldg(sp + 1);
+      cnt = s0.x & 0xFFFFu;
+    } else {
+      cnt = (uint32_t)tv & 0xFFFFu;
+    }
+    if (cnt == 0) {
+      act = false;
+    } else if (!slotmode && cnt <= TINY_MAX) {
+      or_tiny_ids(row32, tv, cnt);
+      act = false;
+      se++;
+    } else if (cnt <= SHORT_MAX) {
+      if (!slotmode) {
+        s0 = __ldg(sp);
+        s1 = __ldg(sp + 1);
+      }
+      or_slot_ids(row32, s0, s1, cnt);
+      act = false;
+      se++;
     }
   }
+  const unsigned m = __ballot_sync(FULL, act);
+  if (!m) return;
+  if (act) s_u[__popc(m & lanemask_lt())] = u;
+  __syncwarp();
+  const int n = __popc(m);
+  int t = g;
+  for (; t + 3 * G < n; t += 4 * G) {
+    const uint4 *r0 = a.F + (size_t)s_u[t] * a.Q + q0;
+    const uint4 *r1 = a.F + (size_t)s_u[t + G] * a.Q + q0;
+    const uint4 *r2 = a.F + (size_t)s_u[t + 2 * G] * a.Q + q0;
+    const uint4 *r3 = a.F + (size_t)s_u[t + 3 * G] * a.Q + q0;
+#pragma unroll
+    for (int k = 0; k < UPL; k++) {
+      const uint32_t q = gl + k * L;
+      if (q < qn) {
+        uint4 x0 = pol.ld_row(r0 + q), x1 = pol.ld_row(r1 + q), x2 = pol.ld_row(r2 + q), x3 = pol.ld_row(r3 + q);
+        acc[k] = or4(acc[k], or4(or4(x0, x1), or4(x2, x3)));
+      }
+    }
+  }
+  for (; t < n; t += G) {
+    const uint4 *r0 = a.F + (size_t)s_u[t] * a.Q + q0;
+#pragma unroll
+    for (int k = 0; k < UPL; k++) {
+      const uint32_t q = gl + k * L;
+      if (q < qn) acc[k] = or4(acc[k], pol.ld_row(r0 + q));
+    }
+  }
+  __syncwarp();
 }
 
 template <int L, int UPL, int H, bool SHORT>
 __device__ __forceinline__ void gather_rows(const PullArgs &a, const L2Pol<H> &pol, uint32_t *s_u, uint32_t *row32,
                                             const uint32_t q0, const uint32_t qn, uint4 (&acc)[UPL],
                                             const uint32_t *adj, int64_t beg, int64_t end,
-                                            int64_t step_start, int64_t step, unsigned long long &se) {
-  constexpr int G = 32 / L;
-  const int lane = threadIdx.x & 31, g = lane / L, gl = lane % L;
+                                            int64_t step_start, int64_t step, unsigned long long &se,
+                                            bool slotmode = false) {
+  const int lane = threadIdx.x & 31;
   for (int64_t base = beg + step_start; base < end; base += step) {
     const int64_t j = base + lane;
     uint32_t u = 0;
     bool act = false;
+    uint64_t tv = 0;
     if (j < end) {
       u = pol.ld_stream(adj + j);
-      act = __ldg(a.flagF + u) != 0;
-    }
-    if (SHORT && act) {  // a short row: its ids from the slot, no gather
-      const uint4 *sp = a.slot_in + (size_t)u * 2;
-      const uint4 s0 = __ldg(sp), s1 = __ldg(sp + 1);
-      const uint32_t cnt = s0.x & 0xFFFFu;
-      if (cnt <= SHORT_MAX) {
-        or_slot_ids(row32, s0, s1, cnt);
-        act = false;
-        se++;
+      if (SHORT) {
+        if (!slotmode) tv = ld_keep(a.tiny_in + u);
+        act = true;
+      } else {
+        act = __ldg(a.flagF + u) != 0;
       }
     }
-    const unsigned m = __ballot_sync(FULL, act);
-    if (!m) continue;
-    if (act) s_u[__popc(m & lanemask_lt())] = u;
-    __syncwarp();
-    const int n = __popc(m);
-    int t = g;
-    for (; t + 3 * G < n; t += 4 * G) {
-      const uint4 *r0 = a.F + (size_t)s_u[t] * a.Q + q0;
-      const uint4 *r1 = a.F + (size_t)s_u[t + G] * a.Q + q0;
-      const uint4 *r2 = a.F + (size_t)s_u[t + 2 * G] * a.Q + q0;
-      const uint4 *r3 = a.F + (size_t)s_u[t + 3 * G] * a.Q + q0;
-#pragma unroll
-      for (int k = 0; k < UPL; k++) {
-        const uint32_t q = gl + k * L;
-        if (q < qn) {
-          uint4 x0 = pol.ld_row(r0 + q), x1 = pol.ld_row(r1 + q), x2 = pol.ld_row(r2 + q), x3 = pol.ld_row(r3 + q);
-          acc[k] = or4(acc[k], or4(or4(x0, x1), or4(x2, x3)));
-        }
-      }
-    }
-    for (; t < n; t += G) {
-      const uint4 *r0 = a.F + (size_t)s_u[t] * a.Q + q0;
-#pragma unroll
-      for (int k = 0; k < UPL; k++) {
-        const uint32_t q = gl + k * L;
-        if (q < qn) acc[k] = or4(acc[k], pol.ld_row(r0 + q));
-      }
-    }
-    __syncwarp();
+    gather_chunk<L, UPL, H, SHORT>(a, pol, s_u, row32, q0, qn, acc, u, act, tv, slotmode, se);
   }
 }
 
-// The slot of a non-zero row held by lanes 0..L-1 (uint4 q = lane + k * L):
-// its bit count (saturated at 0xFFFF) and, for a short row, its ids in order.
+// The tiny word (and, for TINY_MAX+1..SHORT_MAX bits, the slot) of the
+// non-zero row of v held by lanes 0..L-1 (uint4 q = lane + k * L).
 template <int L, int UPL>
-__device__ __forceinline__ void write_slot(uint16_t *slot, const uint4 (&acc)[UPL], uint32_t qn,
-                                           unsigned long long &ns) {
+__device__ __forceinline__ void write_short(const PullArgs &a, uint32_t v, const uint4 (&acc)[UPL], uint32_t qn,
+                                            unsigned long long &ns) {
   const int lane = threadIdx.x & 31;
   uint32_t c = 0;
   if (lane < L) {
@@ -688,7 +752,10 @@ __device__ __forceinline__ void write_slot(uint16_t *slot, const uint4 (&acc)[UP
     if (lane >= o) incl += y;
   }
   const uint32_t total = __shfl_sync(FULL, incl, 31);
+  uint64_t tv = total < 0xFFFFu ? total : 0xFFFFu;
+  uint16_t *slot = a.slot_out + (size_t)v * 16;
   if (total <= SHORT_MAX) {
+    uint64_t part = 0;
     uint32_t pos = 1 + incl - c;
     if (c) {
 #pragma unroll
@@ -702,15 +769,27 @@ __device__ __forceinline__ void write_slot(uint16_t *slot, const uint4 (&acc)[UP
             while (bits) {
               const uint32_t t = __ffs(bits) - 1;
               bits &= bits - 1;
-              slot[pos++] = (uint16_t)(q * 128 + wi * 32 + t);
+              const uint32_t id = q * 128 + wi * 32 + t;
+              if (total <= TINY_MAX) part |= (uint64_t)id << (16 * pos);
+              slot[pos] = (uint16_t)id;
+              pos++;
             }
           }
         }
       }
     }
-    if (lane == 0) ns++;
+    if (total <= TINY_MAX) {
+#pragma unroll
+      for (int o = 16; o; o >>= 1) part |= __shfl_xor_sync(FULL, part, o);
+      tv |= part;
+    }
+    // short rows in the low half, rows of at most TINY_MAX bits in the high half
+    if (lane == 0) ns += 1ull + (total <= TINY_MAX ? 1ull << 32 : 0ull);
   }
-  if (lane == 0) slot[0] = (uint16_t)(total < 0xFFFFu ? total : 0xFFFFu);
+  if (lane == 0) {
+    a.tiny_out[v] = tv;
+    slot[0] = (uint16_t)tv;
+  }
 }
 
 // Fused epilogue for the row of v held by lanes 0..L-1 after the group reduction:
@@ -775,7 +854,14 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
         if (q < qn) pol.st(a.N + (size_t)v * a.Q + q0 + q, acc[k]);
       }
     }
-    if (a.slot_out && rownz) write_slot<L, UPL>(a.slot_out + (size_t)v * 16, acc, qn, ns);
+    if (a.tiny_out) {  // every vertex gets a tiny word: the count is 0 for an empty row
+      if (rownz)
+        write_short<L, UPL>(a, v, acc, qn, ns);
+      else if (lane == 0) {
+        a.tiny_out[v] = 0;
+        a.slot_out[(size_t)v * 16] = 0;
+      }
+    }
     if (lane == 0) {
       if ((rownz ? 1u : 0u) != oldf) a.flagN[v] = rownz ? 1u : 0u;
       if (rownz) nv++;
@@ -796,23 +882,17 @@ __device__ __forceinline__ void pull_counters(const PullArgs &a, unsigned long l
                                               unsigned long long ns, unsigned long long se) {
   block_add(nb, &a.ctr->hop[a.h].new_bits);
   block_add(nv, &a.ctr->hop[a.h].active_vertices);
-  if (a.slot_out) block_add(ns, &a.ctr->hop[a.h].short_rows);
-  if (a.slot_in) block_add(se, &a.ctr->hop[a.h].short_edges);
+  if (a.tiny_out) block_add(ns, &a.ctr->hop[a.h].short_rows);
+  if (a.tiny_in) block_add(se, &a.ctr->hop[a.h].short_edges);
 }
 
-template <int L, int UPL, int H, bool SHORT>
+template <int L, int UPL, int H>
 __device__ __forceinline__ void pull_vertices(const PullArgs &a) {
   const L2Pol<H> pol;
   __shared__ uint32_t s_u[8][32];
-  extern __shared__ uint4 s_short[];  // SHORT: [8 warps][Q], the ids of short in-neighbour rows
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int wib = threadIdx.x >> 5;
   const uint32_t q0 = blockIdx.y * a.qslice;
   const uint32_t qn = min(a.qslice, a.Q - q0);
-  uint4 *srow = s_short + (size_t)wib * a.Q;
-  if (SHORT) {
-    for (uint32_t q = lane; q < a.Q; q += 32) srow[q] = make_uint4(0, 0, 0, 0);
-    __syncwarp();
-  }
   unsigned long long nb = 0, nv = 0, ns = 0, se = 0;
   for (uint32_t v = blockIdx.x * 8 + wib; v < a.V; v += gridDim.x * 8) {
     if (a.hub_threshold) {
@@ -820,22 +900,84 @@ __device__ __forceinline__ void pull_vertices(const PullArgs &a) {
       _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n) d += a.in.off[l][v + 1] - a.in.off[l][v];
       if (d > (int64_t)a.hub_threshold) continue;  // handled by k_pull_hub
     }
-    if (SHORT && lane == 0) {  // the epilogue's read-modify-write rows, fetched while the gather runs
-      if (a.shortest) prefetch_l2(a.vis + (size_t)v * a.Q + q0, qn * 16);
-      if (a.acc_on) prefetch_l2(a.acc + (size_t)v * a.Q + q0, qn * 16);
-    }
     uint4 acc[UPL];
 #pragma unroll
     for (int k = 0; k < UPL; k++) acc[k] = make_uint4(0, 0, 0, 0);
     _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n)
-      gather_rows<L, UPL, H, SHORT>(a, pol, s_u[wib], reinterpret_cast<uint32_t *>(srow), q0, qn, acc,
-                                    a.in.adj[l], pol.ld_stream(a.in.off[l] + v),
-                                    pol.ld_stream(a.in.off[l] + v + 1), 0, 32, se);
+      gather_rows<L, UPL, H, false>(a, pol, s_u[wib], nullptr, q0, qn, acc, a.in.adj[l],
+                                    pol.ld_stream(a.in.off[l] + v), pol.ld_stream(a.in.off[l] + v + 1), 0, 32, se);
 #pragma unroll
     for (int o = L; o < 32; o <<= 1)
 #pragma unroll
       for (int k = 0; k < UPL; k++) acc[k] = or4(acc[k], shfl_xor4(acc[k], o));
-    if (SHORT) {  // one slice: q0 = 0, qn = Q
+    pull_epilogue<L, UPL, H>(a, pol, v, q0, qn, acc, nb, nv, ns);
+  }
+  pull_counters(a, nb, nv, ns, se);
+}
+
+// Short mode (one slice).  Software-pipelined over the warp's targets: while
+// target v is processed, the next target's list bounds, first 32
+// in-neighbours and their tiny words are already in flight.
+template <int L, int UPL>
+__device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
+  const L2Pol<0> pol;
+  __shared__ uint32_t s_u[8][32];
+  extern __shared__ uint4 s_short[];  // [8 warps][Q], the ids of short in-neighbour rows
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const uint32_t qn = a.Q;
+  uint4 *srow = s_short + (size_t)wib * a.Q;
+  uint32_t *row32 = reinterpret_cast<uint32_t *>(srow);
+  for (uint32_t q = lane; q < a.Q; q += 32) srow[q] = make_uint4(0, 0, 0, 0);
+  __syncwarp();
+  const bool slotmode = a.ctr->hop[a.h].short_slots;
+  const int64_t *off0 = a.in.off[0];
+  const uint32_t *adj0 = a.in.adj[0];
+  const uint32_t stride = gridDim.x * 8;
+  unsigned long long nb = 0, nv = 0, ns = 0, se = 0;
+  uint32_t v = blockIdx.x * 8 + wib;
+  int64_t beg = 0, end = 0;  // list 0 of target v
+  uint32_t pu = 0;           // this lane's in-neighbour in v's first chunk
+  uint64_t pt = 0;           // ... and its tiny word
+  bool pact = false;
+  if (v < a.V) {
+    beg = __ldg(off0 + v);
+    end = __ldg(off0 + v + 1);
+    if (beg + lane < end) {
+      pu = __ldg(adj0 + beg + lane);
+      if (!slotmode) pt = ld_keep(a.tiny_in + pu);
+      pact = true;
+    }
+  }
+  for (; v < a.V; v += stride) {
+    const uint32_t vn = v + stride;
+    int64_t nbeg = 0, nend = 0;
+    if (vn < a.V) {
+      nbeg = __ldg(off0 + vn);
+      nend = __ldg(off0 + vn + 1);
+    }
+    int64_t d = end - beg;
+    if (a.in.n > 1) d += a.in.off[1][v + 1] - a.in.off[1][v];
+    uint32_t pun = 0;
+    uint64_t ptn = 0;
+    const bool pactn = nbeg + lane < nend;
+    if (!(a.hub_threshold && d > (int64_t)a.hub_threshold)) {  // hubs: k_pull_hub_short
+      if (lane == 0) {  // the epilogue's read-modify-write rows, fetched while the gather runs
+        if (a.shortest) prefetch_l2(a.vis + (size_t)v * a.Q, qn * 16);
+        if (a.acc_on) prefetch_l2(a.acc + (size_t)v * a.Q, qn * 16);
+      }
+      uint4 acc[UPL];
+#pragma unroll
+      for (int k = 0; k < UPL; k++) acc[k] = make_uint4(0, 0, 0, 0);
+      gather_chunk<L, UPL, 0, true>(a, pol, s_u[wib], row32, 0, qn, acc, pu, pact, pt, slotmode, se);
+      if (pactn) pun = __ldg(adj0 + nbeg + lane);  // in flight during the rest of v
+      gather_rows<L, UPL, 0, true>(a, pol, s_u[wib], row32, 0, qn, acc, adj0, beg + 32, end, 0, 32, se, slotmode);
+      if (a.in.n > 1)
+        gather_rows<L, UPL, 0, true>(a, pol, s_u[wib], row32, 0, qn, acc, a.in.adj[1], a.in.off[1][v],
+                                     a.in.off[1][v + 1], 0, 32, se, slotmode);
+#pragma unroll
+      for (int o = L; o < 32; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < UPL; k++) acc[k] = or4(acc[k], shfl_xor4(acc[k], o));
       __syncwarp();
       if (lane < L) {
 #pragma unroll
@@ -848,8 +990,17 @@ __device__ __forceinline__ void pull_vertices(const PullArgs &a) {
         }
       }
       __syncwarp();
+      if (pactn && !slotmode) ptn = ld_keep(a.tiny_in + pun);  // in flight during the epilogue
+      pull_epilogue<L, UPL, 0>(a, pol, v, 0, qn, acc, nb, nv, ns);
+    } else if (pactn) {
+      pun = __ldg(adj0 + nbeg + lane);
+      if (!slotmode) ptn = ld_keep(a.tiny_in + pun);
     }
-    pull_epilogue<L, UPL, H>(a, pol, v, q0, qn, acc, nb, nv, ns);
+    beg = nbeg;
+    end = nend;
+    pu = pun;
+    pt = ptn;
+    pact = pactn;
   }
   pull_counters(a, nb, nv, ns, se);
 }
@@ -857,15 +1008,15 @@ __device__ __forceinline__ void pull_vertices(const PullArgs &a) {
 template <int L, int UPL, int MINB, int H>
 __global__ void __launch_bounds__(256, MINB) k_pull(PullArgs a) {
   if (a.ctr->hop[a.h].strategy != ST_PULL || a.ctr->hop[a.h].short_pull) return;
-  pull_vertices<L, UPL, H, false>(a);
+  pull_vertices<L, UPL, H>(a);
 }
 
 // the same in short mode (its own kernel: the slot path's registers stay out
 // of the dense kernels' budget)
 template <int L, int UPL>
-__global__ void __launch_bounds__(256, UPL >= 4 ? 2 : 6) k_pull_short(PullArgs a) {
-  if (a.ctr->hop[a.h].strategy != ST_PULL || !a.ctr->hop[a.h].short_pull || !a.slot_in) return;
-  pull_vertices<L, UPL, 0, true>(a);
+__global__ void __launch_bounds__(256, UPL >= 4 ? 2 : 5) k_pull_short(PullArgs a) {
+  if (a.ctr->hop[a.h].strategy != ST_PULL || !a.ctr->hop[a.h].short_pull || !a.tiny_in) return;
+  pull_vertices_short<L, UPL>(a);
 }
 
 // Hub vertices (in-degree above the threshold): one 512-thread CTA per vertex,
@@ -893,7 +1044,7 @@ __device__ __forceinline__ void pull_hubs(const PullArgs &a) {
     _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.in.n)
       gather_rows<L, UPL, 0, SHORT>(a, pol, s_u[wib], reinterpret_cast<uint32_t *>(srow), q0, qn, acc,
                                     a.in.adj[l], a.in.off[l][v], a.in.off[l][v + 1], (int64_t)wib * 32,
-                                    (int64_t)nw * 32, se);
+                                    (int64_t)nw * 32, se, SHORT && a.ctr->hop[a.h].short_slots);
 #pragma unroll
     for (int o = L; o < 32; o <<= 1)
 #pragma unroll
@@ -934,30 +1085,40 @@ __global__ void __launch_bounds__(512) k_pull_hub(PullArgs a) {
 
 template <int L, int UPL>
 __global__ void __launch_bounds__(512) k_pull_hub_short(PullArgs a) {
-  if (a.ctr->hop[a.h].strategy != ST_PULL || !a.ctr->hop[a.h].short_pull || !a.slot_in || a.nhubs == 0) return;
+  if (a.ctr->hop[a.h].strategy != ST_PULL || !a.ctr->hop[a.h].short_pull || !a.tiny_in || a.nhubs == 0) return;
   pull_hubs<L, UPL, true>(a);
 }
 
-// Slots of layer h-1 when hop h pulls in short mode and that layer was not
-// written by a PULL hop (SPARSE, PUSH or the seed): a warp per flagged row
-// counts its bits and, for a short row, writes its ids in order.
+// Tiny words and slots of layer h-1 when hop h pulls in short mode and that
+// layer was not written by a PULL hop (SPARSE, PUSH or the seed): a warp per
+// flagged row counts its bits and writes its word (and slot); every other
+// vertex gets the count 0.
 __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__restrict__ F, uint32_t V,
-                             uint32_t Q, uint16_t *__restrict__ slots, const Ctr *ctr, int h) {
+                             uint32_t Q, uint64_t *__restrict__ tiny, uint16_t *__restrict__ slots, const Ctr *ctr,
+                             int h) {
   if (ctr->hop[h].strategy != ST_PULL || !ctr->hop[h].short_pull || ctr->hop[h - 1].strategy == ST_PULL) return;
   const int lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < V; base += warps * 32) {
     const uint32_t v = base + lane;
-    unsigned m = __ballot_sync(FULL, v < V && flagF[v]);
+    const bool f = v < V && flagF[v];
+    if (v < V && !f) {  // empty row
+      tiny[v] = 0;
+      slots[(size_t)v * 16] = 0;
+    }
+    unsigned m = __ballot_sync(FULL, f);
     while (m) {
       const int b = __ffs(m) - 1;
       m &= m - 1;
-      const uint4 *row = F + (size_t)(base + b) * Q;
-      uint16_t *slot = slots + (size_t)(base + b) * 16;
+      const uint32_t r = base + b;
+      const uint4 *row = F + (size_t)r * Q;
       uint32_t c = 0;
       for (uint32_t q = lane; q < Q; q += 32) c += popc4(row[q]);
       const uint32_t total = warp_sum(c);
+      uint64_t tv = total < 0xFFFFu ? total : 0xFFFFu;
+      uint16_t *slot = slots + (size_t)r * 16;
       if (total <= SHORT_MAX) {
+        uint64_t part = 0;
         uint32_t pos = 1;
         for (uint32_t q0 = 0; q0 < Q; q0 += 32) {
           const uint32_t q = q0 + lane;
@@ -977,13 +1138,24 @@ __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__
             while (bits) {
               const uint32_t t = __ffs(bits) - 1;
               bits &= bits - 1;
-              slot[at++] = (uint16_t)(q * 128 + wi * 32 + t);
+              const uint32_t id = q * 128 + wi * 32 + t;
+              if (total <= TINY_MAX) part |= (uint64_t)id << (16 * at);
+              slot[at] = (uint16_t)id;
+              at++;
             }
           }
           pos += __shfl_sync(FULL, incl, 31);
         }
+        if (total <= TINY_MAX) {
+#pragma unroll
+          for (int o = 16; o; o >>= 1) part |= __shfl_xor_sync(FULL, part, o);
+          tv |= part;
+        }
       }
-      if (lane == 0) slot[0] = (uint16_t)(total < 0xFFFFu ? total : 0xFFFFu);
+      if (lane == 0) {
+        tiny[r] = tv;
+        slot[0] = (uint16_t)tv;
+      }
     }
   }
 }
@@ -1213,7 +1385,8 @@ struct vs_expand_plan {
   uint32_t *rowk = nullptr;   // [0] largest row limit, [1] a limit exceeded k_max (device-set limits)
   uint64_t *layer_out[VS_MAX_HOPS + 1] = {};  // with_distance: layer h is copied here (zeroed, V x W words)
   // row lists of sparse frontier rows (PULL over lists); none when S > 65536 or multi-slice
-  uint16_t *slot[2] = {nullptr, nullptr};  // short-row slots of the two frontier buffers' layers
+  uint64_t *tiny[2] = {nullptr, nullptr};  // short-row words of the two frontier buffers' layers
+  uint16_t *slot[2] = {nullptr, nullptr};  // ... and their slots
   double short_min = 0.0;                  // share of short rows for a short-mode PULL (0: off)
   bool use_hmask = false;
   int hop_forced[VS_MAX_HOPS + 1] = {};
@@ -1242,7 +1415,7 @@ inline bool short_slots_ok(uint32_t S, uint32_t nslices, double share) {
 int plan_free(vs_expand_plan *pl) {
   if (!pl) return VS_OK;
   const cudaStream_t st = pl->last_stream;
-  void *ptrs[] = {pl->slot[0], pl->slot[1], pl->resflag, pl->pdeg[0], pl->pdeg[1], pl->doff,
+  void *ptrs[] = {pl->tiny[0], pl->tiny[1], pl->slot[0], pl->slot[1], pl->resflag, pl->pdeg[0], pl->pdeg[1], pl->doff,
                   pl->bsum, pl->hmask, pl->rowk, pl->buf[0], pl->buf[1], pl->flag[0], pl->flag[1], pl->vis, pl->acc,
                   pl->pairs[0], pl->pairs[1], pl->push_list, pl->touched, pl->d_src,
                   pl->d_tgt, pl->d_dist, pl->ctr, pl->hubs};
@@ -1333,6 +1506,8 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   PL_ALLOC(pl->rowk, 2);
   pl->short_min = p->short_share == 0 ? 0.1 : p->short_share;
   if (short_slots_ok(S, pl->nslices, p->short_share)) {
+    PL_ALLOC(pl->tiny[0], V);
+    PL_ALLOC(pl->tiny[1], V);
     PL_ALLOC(pl->slot[0], (size_t)V * 16);
     PL_ALLOC(pl->slot[1], (size_t)V * 16);
   } else {
@@ -1408,7 +1583,7 @@ int vs_expand_plan_footprint(const vs_graph *g, uint32_t S, const vs_expand_para
   uint32_t qs = p->slice_words ? (p->slice_words + 1) / 2 : (uint32_t)(W / 2);
   qs = std::max<uint32_t>(1, std::min<uint32_t>(qs, 256));
   const uint32_t nslices = (uint32_t)((W / 2 + qs - 1) / qs);
-  if (short_slots_ok(S, nslices, p->short_share)) b += 2 * V * 32;  // short-row slots of both buffers
+  if (short_slots_ok(S, nslices, p->short_share)) b += 2 * V * 40;  // short-row words and slots of both buffers
   *bytes = b;
   return VS_OK;
 }
@@ -1578,12 +1753,15 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.nhubs = pl->nhubs;
     a.ctr = pl->ctr;
     a.h = h;
+    const bool keep_short = pl->slot[0] && h < p.k_max && !a.last;  // the next hop may read this layer's words
+    a.tiny_in = pl->slot[0] ? pl->tiny[fb] : nullptr;
     a.slot_in = pl->slot[0] ? reinterpret_cast<const uint4 *>(pl->slot[fb]) : nullptr;
-    a.slot_out = pl->slot[0] && h < p.k_max && !a.last ? pl->slot[nbuf] : nullptr;
+    a.tiny_out = keep_short ? pl->tiny[nbuf] : nullptr;
+    a.slot_out = keep_short ? pl->slot[nbuf] : nullptr;
     if (timing) cudaEventRecord(pl->ev[3 * h + 1], st);
     if (pl->slot[0])  // slots of a layer SPARSE or PUSH wrote, when this hop reads them
       { k_slot_build<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<const uint4 *>(pl->buf[fb]), V, Q,
-                                               pl->slot[fb], pl->ctr, h); vs::note_launch(); }
+                                               pl->tiny[fb], pl->slot[fb], pl->ctr, h); vs::note_launch(); }
     { var.pull[pl->pull_kind]<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a); vs::note_launch(); }
     if (pl->nhubs)
       { var.hub<<<dim3(pl->grid_hub, pl->nslices), 512, 16 * 32 * 16 * var.UPL, st>>>(a); vs::note_launch(); }
@@ -1653,7 +1831,8 @@ int vs_expand_plan_stats(vs_expand_plan *pl, vs_expand_stats *stats, vs_stream_t
     stats->pairs[i] = h.hop[i].pairs;
     stats->strategy[i] = h.hop[i].strategy;
     stats->short_pull[i] = h.hop[i].short_pull;
-    stats->short_rows[i] = h.hop[i].short_rows;
+    stats->short_rows[i] = h.hop[i].short_rows & 0xFFFFFFFFull;
+    stats->tiny_rows[i] = h.hop[i].short_rows >> 32;
     stats->short_edges[i] = h.hop[i].short_edges;
     if (i >= 1 && i <= h.hops_run) vc += h.hop[i].new_bits;
   }

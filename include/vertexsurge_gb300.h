@@ -199,7 +199,7 @@ typedef struct vs_expand_stats {
   uint64_t short_rows[VS_MAX_HOPS + 1];     /* rows of layer h with 1..15 bits (when a PULL hop wrote
                                                its slots) */
   uint64_t short_edges[VS_MAX_HOPS + 1];    /* active in-edges of hop h's PULL served from a slot */
-  uint64_t tiny_rows[VS_MAX_HOPS + 1];      /* rows of layer h with 1..3 bits (ids inline in the word) */
+  uint64_t tiny_rows[VS_MAX_HOPS + 1];      /* rows of layer h with one bit (its id inline in the word) */
 } vs_expand_stats;
 
 /* A plan owns the frontier, next, visited and accumulator matrices for S

@@ -352,7 +352,7 @@ def test_short_pull_parity(vs, graphs, path, direction):
 @pytest.mark.parametrize("path", ["any", "shortest"])
 def test_short_rows_counted(vs, graphs, path):
     """The PULL epilogue's counts of short rows (1..15 bits) and of rows with
-    their ids inline in the tiny word (1..3 bits), in every layer it writes
+    their id inline in the tiny word (one bit), in every layer it writes
     words for, equal the counts over the oracle's layer."""
     g, dg = graphs["zipf3000"]
     src = graphgen.sample_sources(g.V, 700, seed=8)
@@ -364,7 +364,7 @@ def test_short_rows_counted(vs, graphs, path):
         layer, _, _ = O.vexpand(g, src, h, h, path, "forward")
         bits = words_to_bool(layer, len(src)).sum(axis=0) if layer.size else np.zeros(g.V)
         assert st["short_rows"][h] == int(((bits >= 1) & (bits <= 15)).sum()), h
-        assert st["tiny_rows"][h] == int(((bits >= 1) & (bits <= 3)).sum()), h
+        assert st["tiny_rows"][h] == int((bits == 1).sum()), h
         checked += 1
     assert checked == 3
 

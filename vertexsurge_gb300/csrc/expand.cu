@@ -588,18 +588,19 @@ template <int H> struct L2Pol {
 // Short rows.  In the later hops of a many-source expand over a power-law
 // graph most frontier rows hold a handful of sources, and a whole-row gather
 // then moves mostly zero words.  Every PULL hop with a successor therefore
-// also writes, for every vertex, a tiny word (uint64: the row's bit count,
-// saturated at 0xFFFF, and up to TINY_MAX source ids as uint16) and a 32-byte
+// also writes, for every vertex, a tiny word (uint32: the row's bit count,
+// saturated at 0xFFFF, and for a one-bit row its source id) and a 32-byte
 // slot (entry 0: the count; entries 1..count: the ids, for up to SHORT_MAX
 // bits).  A later PULL hop in short mode reads, per in-neighbour, either its
-// tiny word (word mode: 8 bytes per vertex, an array L2 can hold, loaded with
+// tiny word (word mode: 4 bytes per vertex, an array L2 can hold, loaded with
 // an evict-last hint; the slot follows only for rows of more than TINY_MAX
 // bits) or its slot alone (slot mode, for frontiers of mostly longer rows):
 // count 0 is an empty row, short rows OR their ids into a per-warp
 // shared-memory row with 32-bit atomics, and only longer rows are gathered
 // whole.  Layers written by SPARSE or PUSH get their words and slots from a
 // build pass (k_slot_build) when the next hop reads them.
-constexpr uint32_t TINY_MAX = 3;    // ids in a tiny word (count + 3 x uint16)
+using Tiny = uint32_t;                                       // count, then ids, as uint16
+constexpr uint32_t TINY_MAX = sizeof(Tiny) / 2 - 1;          // ids in a tiny word
 constexpr uint32_t SHORT_MAX = 15;  // ids in a slot (16 uint16, entry 0 = the count)
 
 // Bulk prefetch of `bytes` (a multiple of 16, 16-byte aligned) into L2.
@@ -607,16 +608,23 @@ __device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
 }
 
-// Read-only 8-byte load that asks L2 to keep the line (evict-last).
-__device__ __forceinline__ uint64_t ld_keep(const uint64_t *p) {
-  uint64_t pol, r;
+// Read-only tiny-word load that asks L2 to keep the line (evict-last).
+__device__ __forceinline__ Tiny ld_keep(const Tiny *p) {
+  uint64_t pol;
   asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
-  asm("ld.global.nc.L2::cache_hint.b64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(pol));
-  return r;
+  if constexpr (sizeof(Tiny) == 8) {
+    uint64_t r;
+    asm("ld.global.nc.L2::cache_hint.b64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(pol));
+    return (Tiny)r;
+  } else {
+    uint32_t r;
+    asm("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+    return (Tiny)r;
+  }
 }
 
 // OR the ids of a tiny word (count in [1, TINY_MAX]) into a shared row
-__device__ __forceinline__ void or_tiny_ids(uint32_t *row32, uint64_t t, uint32_t cnt) {
+__device__ __forceinline__ void or_tiny_ids(uint32_t *row32, Tiny t, uint32_t cnt) {
 #pragma unroll
   for (uint32_t i = 1; i <= TINY_MAX; i++) {
     if (i > cnt) break;
@@ -644,7 +652,7 @@ __device__ __forceinline__ void or_slot_ids(uint32_t *row32, const uint4 s0, con
 template <int L, int UPL, int H, bool SHORT>
 __device__ __forceinline__ void gather_chunk(const PullArgs &a, const L2Pol<H> &pol, uint32_t *s_u, uint32_t *row32,
                                              const uint32_t q0, const uint32_t qn, uint4 (&acc)[UPL], uint32_t u,
-                                             bool act, uint64_t tv, bool slotmode, unsigned long long &se) {
+                                             bool act, Tiny tv, bool slotmode, unsigned long long &se) {
   constexpr int G = 32 / L;
   const int lane = threadIdx.x & 31, g = lane / L, gl = lane % L;
   if (SHORT && act) {
@@ -719,7 +727,7 @@ __device__ __forceinline__ void gather_rows(const PullArgs &a, const L2Pol<H> &p
     const int64_t j = base + lane;
     uint32_t u = 0;
     bool act = false;
-    uint64_t tv = 0;
+    Tiny tv = 0;
     if (j < end) {
       u = pol.ld_stream(adj + j);
       if (SHORT) {
@@ -752,10 +760,10 @@ __device__ __forceinline__ void write_short(const PullArgs &a, uint32_t v, const
     if (lane >= o) incl += y;
   }
   const uint32_t total = __shfl_sync(FULL, incl, 31);
-  uint64_t tv = total < 0xFFFFu ? total : 0xFFFFu;
+  Tiny tv = total < 0xFFFFu ? total : 0xFFFFu;
   uint16_t *slot = a.slot_out + (size_t)v * 16;
   if (total <= SHORT_MAX) {
-    uint64_t part = 0;
+    Tiny part = 0;
     uint32_t pos = 1 + incl - c;
     if (c) {
 #pragma unroll
@@ -770,7 +778,7 @@ __device__ __forceinline__ void write_short(const PullArgs &a, uint32_t v, const
               const uint32_t t = __ffs(bits) - 1;
               bits &= bits - 1;
               const uint32_t id = q * 128 + wi * 32 + t;
-              if (total <= TINY_MAX) part |= (uint64_t)id << (16 * pos);
+              if (total <= TINY_MAX) part |= (Tiny)id << (16 * pos);
               slot[pos] = (uint16_t)id;
               pos++;
             }
@@ -780,7 +788,7 @@ __device__ __forceinline__ void write_short(const PullArgs &a, uint32_t v, const
     }
     if (total <= TINY_MAX) {
 #pragma unroll
-      for (int o = 16; o; o >>= 1) part |= __shfl_xor_sync(FULL, part, o);
+      for (int o = 16; o; o >>= 1) part |= (Tiny)__shfl_xor_sync(FULL, part, o);
       tv |= part;
     }
     // short rows in the low half, rows of at most TINY_MAX bits in the high half
@@ -937,7 +945,7 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
   uint32_t v = blockIdx.x * 8 + wib;
   int64_t beg = 0, end = 0;  // list 0 of target v
   uint32_t pu = 0;           // this lane's in-neighbour in v's first chunk
-  uint64_t pt = 0;           // ... and its tiny word
+  Tiny pt = 0;               // ... and its tiny word
   bool pact = false;
   if (v < a.V) {
     beg = __ldg(off0 + v);
@@ -958,7 +966,7 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
     int64_t d = end - beg;
     if (a.in.n > 1) d += a.in.off[1][v + 1] - a.in.off[1][v];
     uint32_t pun = 0;
-    uint64_t ptn = 0;
+    Tiny ptn = 0;
     const bool pactn = nbeg + lane < nend;
     if (!(a.hub_threshold && d > (int64_t)a.hub_threshold)) {  // hubs: k_pull_hub_short
       if (lane == 0) {  // the epilogue's read-modify-write rows, fetched while the gather runs
@@ -1094,7 +1102,7 @@ __global__ void __launch_bounds__(512) k_pull_hub_short(PullArgs a) {
 // flagged row counts its bits and writes its word (and slot); every other
 // vertex gets the count 0.
 __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__restrict__ F, uint32_t V,
-                             uint32_t Q, uint64_t *__restrict__ tiny, uint16_t *__restrict__ slots, const Ctr *ctr,
+                             uint32_t Q, Tiny *__restrict__ tiny, uint16_t *__restrict__ slots, const Ctr *ctr,
                              int h) {
   if (ctr->hop[h].strategy != ST_PULL || !ctr->hop[h].short_pull || ctr->hop[h - 1].strategy == ST_PULL) return;
   const int lane = threadIdx.x & 31;
@@ -1115,10 +1123,10 @@ __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__
       uint32_t c = 0;
       for (uint32_t q = lane; q < Q; q += 32) c += popc4(row[q]);
       const uint32_t total = warp_sum(c);
-      uint64_t tv = total < 0xFFFFu ? total : 0xFFFFu;
+      Tiny tv = total < 0xFFFFu ? total : 0xFFFFu;
       uint16_t *slot = slots + (size_t)r * 16;
       if (total <= SHORT_MAX) {
-        uint64_t part = 0;
+        Tiny part = 0;
         uint32_t pos = 1;
         for (uint32_t q0 = 0; q0 < Q; q0 += 32) {
           const uint32_t q = q0 + lane;
@@ -1139,7 +1147,7 @@ __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__
               const uint32_t t = __ffs(bits) - 1;
               bits &= bits - 1;
               const uint32_t id = q * 128 + wi * 32 + t;
-              if (total <= TINY_MAX) part |= (uint64_t)id << (16 * at);
+              if (total <= TINY_MAX) part |= (Tiny)id << (16 * at);
               slot[at] = (uint16_t)id;
               at++;
             }
@@ -1148,7 +1156,7 @@ __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__
         }
         if (total <= TINY_MAX) {
 #pragma unroll
-          for (int o = 16; o; o >>= 1) part |= __shfl_xor_sync(FULL, part, o);
+          for (int o = 16; o; o >>= 1) part |= (Tiny)__shfl_xor_sync(FULL, part, o);
           tv |= part;
         }
       }
@@ -1385,7 +1393,7 @@ struct vs_expand_plan {
   uint32_t *rowk = nullptr;   // [0] largest row limit, [1] a limit exceeded k_max (device-set limits)
   uint64_t *layer_out[VS_MAX_HOPS + 1] = {};  // with_distance: layer h is copied here (zeroed, V x W words)
   // row lists of sparse frontier rows (PULL over lists); none when S > 65536 or multi-slice
-  uint64_t *tiny[2] = {nullptr, nullptr};  // short-row words of the two frontier buffers' layers
+  Tiny *tiny[2] = {nullptr, nullptr};      // short-row words of the two frontier buffers' layers
   uint16_t *slot[2] = {nullptr, nullptr};  // ... and their slots
   double short_min = 0.0;                  // share of short rows for a short-mode PULL (0: off)
   bool use_hmask = false;
@@ -1583,7 +1591,8 @@ int vs_expand_plan_footprint(const vs_graph *g, uint32_t S, const vs_expand_para
   uint32_t qs = p->slice_words ? (p->slice_words + 1) / 2 : (uint32_t)(W / 2);
   qs = std::max<uint32_t>(1, std::min<uint32_t>(qs, 256));
   const uint32_t nslices = (uint32_t)((W / 2 + qs - 1) / qs);
-  if (short_slots_ok(S, nslices, p->short_share)) b += 2 * V * 40;  // short-row words and slots of both buffers
+  if (short_slots_ok(S, nslices, p->short_share))
+    b += 2 * V * (32 + sizeof(Tiny));  // short-row words and slots of both buffers
   *bytes = b;
   return VS_OK;
 }

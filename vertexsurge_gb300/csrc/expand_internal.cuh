@@ -22,8 +22,8 @@ struct HopCtr {
   int strategy;                        // strategy run at hop h (0 = not run)
   int short_pull;                      // PULL reads the short rows of layer h-1 through their slots
   int short_slots;                     // ... reading slots (count in entry 0) instead of tiny words
-  unsigned long long short_rows;       // rows of layer h with 1..15 bits (low 32 bits) and with 1..3 bits
-                                       // (high 32 bits), counted when its short-row words are written
+  unsigned long long short_rows;       // rows of layer h with 1..15 bits (low 32 bits) and with at most
+                                       // TINY_MAX bits (high 32 bits), counted when its words are written
   unsigned long long short_edges;      // active in-edges of a short-mode PULL served from a slot
 };
 
@@ -119,9 +119,9 @@ struct PullArgs {
   uint32_t V, Q, qslice;
   int multislice, shortest, acc_on;
   int last;  // the run's last hop and nothing reads its layer: zero the buffer instead of writing it
-  const uint64_t *tiny_in;  // short-row words of layer h-1, one per vertex (NULL: no short mode)
+  const uint32_t *tiny_in;  // short-row words of layer h-1, one per vertex (NULL: no short mode)
   const uint4 *slot_in;     // slots of layer h-1 (two uint4 per vertex)
-  uint64_t *tiny_out;       // words of layer h, written for every vertex (NULL: not kept)
+  uint32_t *tiny_out;       // words of layer h, written for every vertex (NULL: not kept)
   uint16_t *slot_out;       // slots of layer h, written for rows of TINY_MAX+1..SHORT_MAX bits
   uint32_t hub_threshold;
   const uint32_t *hubs;

@@ -1097,6 +1097,47 @@ __global__ void __launch_bounds__(512) k_pull_hub_short(PullArgs a) {
   pull_hubs<L, UPL, true>(a);
 }
 
+// Word and slot of row r held in one chunk (Q <= 32: lane q holds uint4 q).
+__device__ __forceinline__ void short_from_chunk(uint4 x, uint32_t r, Tiny *tiny, uint16_t *slots) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t n = popc4(x);
+  uint32_t incl = n;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(FULL, incl, o);
+    if (lane >= (uint32_t)o) incl += y;
+  }
+  const uint32_t total = __shfl_sync(FULL, incl, 31);
+  Tiny tv = total < 0xFFFFu ? total : 0xFFFFu;
+  uint16_t *slot = slots + (size_t)r * 16;
+  if (total <= SHORT_MAX) {
+    Tiny part = 0;
+    uint32_t at = 1 + incl - n;
+    const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+    for (int wi = 0; wi < 4; wi++) {
+      uint32_t bits = w[wi];
+      while (bits) {
+        const uint32_t t = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const uint32_t id = lane * 128 + wi * 32 + t;
+        if (total <= TINY_MAX) part |= (Tiny)id << (16 * at);
+        slot[at] = (uint16_t)id;
+        at++;
+      }
+    }
+    if (total <= TINY_MAX) {
+#pragma unroll
+      for (int o = 16; o; o >>= 1) part |= (Tiny)__shfl_xor_sync(FULL, part, o);
+      tv |= part;
+    }
+  }
+  if (lane == 0) {
+    tiny[r] = tv;
+    slot[0] = (uint16_t)tv;
+  }
+}
+
 // Tiny words and slots of layer h-1 when hop h pulls in short mode and that
 // layer was not written by a PULL hop (SPARSE, PUSH or the seed): a warp per
 // flagged row counts its bits and writes its word (and slot); every other
@@ -1115,6 +1156,27 @@ __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__
       slots[(size_t)v * 16] = 0;
     }
     unsigned m = __ballot_sync(FULL, f);
+    if (Q <= 32) {  // one chunk per row: four rows' loads in flight at once
+      while (m) {
+        uint32_t rr[4] = {0, 0, 0, 0};
+        int n = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+          if (m) {
+            rr[k] = base + __ffs(m) - 1;
+            m &= m - 1;
+            n = k + 1;
+          }
+        uint4 x[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+          x[k] = (k < n && (uint32_t)lane < Q) ? F[(size_t)rr[k] * Q + lane] : make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+          if (k < n) short_from_chunk(x[k], rr[k], tiny, slots);
+      }
+      continue;
+    }
     while (m) {
       const int b = __ffs(m) - 1;
       m &= m - 1;

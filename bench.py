@@ -81,10 +81,11 @@ def sources(g, w):
     return sa, sb
 
 
-def profiled_traffic(workload: str):
+def profiled_traffic(workload: str, kernel: str = "k_pull"):
     """DRAM bytes per launch of the roofline kernel, from the committed ncu
-    summary of this workload (the line `traffic_bytes_per_launch: N`), or None."""
-    f = ROOT / "profiles" / f"k_pull_{workload}.md"
+    summary of this kernel and workload (the line `traffic_bytes_per_launch:
+    N`), or None."""
+    f = ROOT / "profiles" / f"{kernel}_{workload}.md"
     try:
         for line in f.read_text().splitlines():
             if line.startswith("traffic_bytes_per_launch:"):
@@ -156,15 +157,16 @@ def expand_bytes(V, W, e_act, shortest, acc, gathers=True):
 
 
 def short_bytes(V, W, e_act, e_short, active_prev, built, shortest, acc, gathers=True):
-    """Algorithmic bytes of a short-mode PULL hop: CSR offsets + targets, a
-    32-byte slot per active in-edge whose row is short and a whole-row gather
-    (at least one sector) for the others, the slot writes of the layer (32 B
-    per vertex), the slot build when SPARSE wrote the frontier (its rows read
-    once), and the same P passes over the V x S matrices as the dense hop."""
+    """Algorithmic bytes of a short-mode PULL hop: CSR offsets + targets, one
+    32-byte sector per active in-edge whose row is short (its tiny word or
+    slot) and a whole-row gather (at least one sector) for the others, the
+    layer's tiny words and slots (36 B per vertex), the build of the
+    frontier's words and slots when SPARSE wrote it (its rows read once), and
+    the same P passes over the V x S matrices as the dense hop."""
     P = 2 + (2 if shortest else 0) + (2 if acc else 0)
     per_edge = (32 * e_short + max(32, 8 * W) * (e_act - e_short)) if gathers else 0
-    build = (8 * W + 32) * active_prev if built else 0
-    return 8 * (V + 1) + 4 * e_act + per_edge + 32 * V + build + P * 8 * W * V
+    build = (8 * W + 36) * active_prev if built else 0
+    return 8 * (V + 1) + 4 * e_act + per_edge + 36 * V + build + P * 8 * W * V
 
 
 def cpu_baseline(g, w, sa):
@@ -282,6 +284,7 @@ def run_gpu_batched(args, w, rank, world, local_rank):
             cached = json.loads(Path(tc).read_text()) if Path(tc).exists() else {}
             cached[wkey] = waves
             Path(tc).write_text(json.dumps(cached, indent=1))
+    setting["short_share"] = waves.get("short_share", setting["short_share"])
     log(f"[rank {rank}] autotune {time.time() - t0:.1f}s: {setting} waves {waves}")
     bt = batch.Batch(dg, queries, waves["wave_rows"], stream, setting=setting)
     cg = bt.capture()
@@ -613,9 +616,10 @@ def run_gpu(args, w, rank, world, local_rank):
         return
     peak, peak_kind = peaks()
     achieved = pull_bytes / (pull_ms / 1e3) / 1e9 if pull_ms else None
+    rl_kernel = "k_pull_short" if any(stA["short_pull"][1:]) else "k_pull"
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if achieved else None, "traffic": profiled_traffic(args.workload),
-                "traffic_source": f"profiles/k_pull_{args.workload}.md (ncu dram__bytes_read.sum + "
+                "frac": achieved / peak if achieved else None, "traffic": profiled_traffic(args.workload, rl_kernel),
+                "traffic_source": f"profiles/{rl_kernel}_{args.workload}.md (ncu dram__bytes_read.sum + "
                                   "dram__bytes_write.sum per working launch)",
                 "kernel": ("k_pull, short mode on hops " + str([h for h in range(1, len(stA["short_pull"]))
                                                              if stA["short_pull"][h]]) + " (expand A, pull hops)"

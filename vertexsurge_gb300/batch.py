@@ -179,27 +179,33 @@ def solo_counts(dg, queries: list, path="shortest", direction="forward", stream=
 
 
 def tune_wave_rows(dg, queries, stream, candidates=(16384, 32768), setting=None, repeats=1,
-                   picker=None) -> dict:
-    """Time one captured batch per wave width; returns {'wave_rows', 'ms', 'table'}."""
+                   picker=None, short_shares=(0.0, -1.0)) -> dict:
+    """Time one captured batch per wave width and short-mode setting (the
+    waves' hop limits and mixed sizes decide whether short-row PULL pays, so
+    it is tuned here on the batch itself); returns {'wave_rows',
+    'short_share', 'ms', 'table'}."""
     import torch
     table = []
     for wr in candidates:
         if wr < max(len(q.sources) for q in queries):
             continue
-        b = Batch(dg, queries, wr, stream, setting=setting, picker=picker)
-        try:
-            b.capture()
-            b.launch()
-            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-                  for _ in range(repeats)]
-            for e0, e1 in ev:
-                e0.record(stream)
+        for sh in short_shares:
+            st = dict(setting or {})
+            st["short_share"] = sh
+            b = Batch(dg, queries, wr, stream, setting=st, picker=picker)
+            try:
+                b.capture()
                 b.launch()
-                e1.record(stream)
-            stream.synchronize()
-            ms = min(e0.elapsed_time(e1) for e0, e1 in ev)
-            table.append({"wave_rows": wr, "waves": len(b.waves), "ms": ms})
-        finally:
-            b.free()
+                ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                      for _ in range(repeats)]
+                for e0, e1 in ev:
+                    e0.record(stream)
+                    b.launch()
+                    e1.record(stream)
+                stream.synchronize()
+                ms = min(e0.elapsed_time(e1) for e0, e1 in ev)
+                table.append({"wave_rows": wr, "short_share": sh, "waves": len(b.waves), "ms": ms})
+            finally:
+                b.free()
     best = min(table, key=lambda r: r["ms"])
-    return {"wave_rows": best["wave_rows"], "ms": best["ms"], "table": table}
+    return {"wave_rows": best["wave_rows"], "short_share": best["short_share"], "ms": best["ms"], "table": table}

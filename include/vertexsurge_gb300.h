@@ -175,12 +175,12 @@ typedef struct vs_expand_params {
   int32_t pull_kernel;     /* PULL kernel shape 0..3, see vs_expand_plan_set_pull_kernel */
   int32_t reserved;
   double sparse_frac;      /* fixed planner: SPARSE while pair-list edges < this x E (0 = 0.02) */
-  double short_share;      /* short-mode PULL: rows of the frontier with at most 15 bits are read
-                              from a 32-byte slot of their source ids instead of whole, on hops
-                              where at least this share of the frontier's rows are short and the
-                              frontier exceeds half of L2 (0 = 0.1; < 0 = never; > 1 = every PULL
-                              hop); needs S <= 65536 and whole-row passes, and keeps 64 B of slots
-                              per vertex */
+  double short_share;      /* short-mode PULL: rows of the frontier with few bits (at most 15, or 31
+                              / 63 for rows of 128 / more words) are read from a slot of their
+                              source ids instead of whole, on hops where at least this share of
+                              the frontier's rows are short and the frontier exceeds half of L2
+                              (0 = 0.1; < 0 = never; > 1 = every PULL hop); needs S <= 65536 and
+                              whole-row passes, and keeps 36 to 132 B per vertex */
 } vs_expand_params;
 
 #define VS_MAX_HOPS 64
@@ -196,8 +196,8 @@ typedef struct vs_expand_stats {
   float hop_ms[VS_MAX_HOPS + 1];            /* device time of hop h (plans with timing on) */
   float pull_ms[VS_MAX_HOPS + 1];           /* device time of hop h's pull kernels */
   int32_t short_pull[VS_MAX_HOPS + 1];      /* 1: the PULL of hop h ran in short mode */
-  uint64_t short_rows[VS_MAX_HOPS + 1];     /* rows of layer h with 1..15 bits (when a PULL hop wrote
-                                               its slots) */
+  uint64_t short_rows[VS_MAX_HOPS + 1];     /* rows of layer h short enough for a slot (when a PULL
+                                               hop wrote its slots) */
   uint64_t short_edges[VS_MAX_HOPS + 1];    /* active in-edges of hop h's PULL served from a slot */
   uint64_t tiny_rows[VS_MAX_HOPS + 1];      /* rows of layer h with one bit (its id inline in the word) */
 } vs_expand_stats;

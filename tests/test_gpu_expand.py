@@ -329,7 +329,7 @@ def test_short_pull_parity(vs, graphs, path, direction):
     n_short, n_edges = 0, 0
     for name in ("rmat11_skew", "zipf3000", "rmat10"):
         g, dg = graphs[name]
-        for S in (20, 40, 300, 1000, 4000) + ((16384,) if name == "rmat10" else ()):
+        for S in (20, 40, 300, 1000, 4000) + ((8192, 16384) if name == "rmat10" else ()):
             src = graphgen.sample_sources(g.V, min(S, g.V), seed=S + 1)
             if S > g.V:
                 src = np.resize(src, S).astype(np.uint32)
@@ -350,20 +350,25 @@ def test_short_pull_parity(vs, graphs, path, direction):
 
 
 @pytest.mark.parametrize("path", ["any", "shortest"])
-def test_short_rows_counted(vs, graphs, path):
-    """The PULL epilogue's counts of short rows (1..15 bits) and of rows with
-    their id inline in the tiny word (one bit), in every layer it writes
-    words for, equal the counts over the oracle's layer."""
+@pytest.mark.parametrize("S", [700, 8192])
+def test_short_rows_counted(vs, graphs, path, S):
+    """The PULL epilogue's counts of short rows (at most 15 bits for rows of
+    up to 64 words, 31 for 128 words) and of rows with their id inline in
+    the tiny word (one bit), in every layer it writes words for, equal the
+    counts over the oracle's layer."""
     g, dg = graphs["zipf3000"]
-    src = graphgen.sample_sources(g.V, 700, seed=8)
+    src = graphgen.sample_sources(g.V, min(S, g.V), seed=8)
+    if S > g.V:
+        src = np.resize(src, S).astype(np.uint32)
     _, _, st = vs.expand(dg, src, 1, 4, path, "forward", strategy="pull", stats=True, short_share=2.0)
     W = (len(src) + 63) // 64
     W += W & 1
+    short_max = 15 if W <= 64 else 31 if W <= 128 else 63
     checked = 0
     for h in range(1, min(st["hops_run"], 3) + 1):  # hop 4 is the last: no slots
         layer, _, _ = O.vexpand(g, src, h, h, path, "forward")
         bits = words_to_bool(layer, len(src)).sum(axis=0) if layer.size else np.zeros(g.V)
-        assert st["short_rows"][h] == int(((bits >= 1) & (bits <= 15)).sum()), h
+        assert st["short_rows"][h] == int(((bits >= 1) & (bits <= short_max)).sum()), h
         assert st["tiny_rows"][h] == int((bits == 1).sum()), h
         checked += 1
     assert checked == 3

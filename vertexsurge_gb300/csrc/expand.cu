@@ -589,9 +589,10 @@ template <int H> struct L2Pol {
 // graph most frontier rows hold a handful of sources, and a whole-row gather
 // then moves mostly zero words.  Every PULL hop with a successor therefore
 // also writes, for every vertex, a tiny word (uint32: the row's bit count,
-// saturated at 0xFFFF, and for a one-bit row its source id) and a 32-byte
-// slot (entry 0: the count; entries 1..count: the ids, for up to SHORT_MAX
-// bits).  A later PULL hop in short mode reads, per in-neighbour, either its
+// saturated at 0xFFFF, and for a one-bit row its source id) and a slot of
+// slot_n uint16 (entry 0: the count; entries 1..count: the ids, for up to
+// slot_n - 1 bits; slot_n = 16, 32 or 64 as the rows are up to 512 B, 1 KB or
+// wider).  A later PULL hop in short mode reads, per in-neighbour, either its
 // tiny word (word mode: 4 bytes per vertex, an array L2 can hold, loaded with
 // an evict-last hint; the slot follows only for rows of more than TINY_MAX
 // bits) or its slot alone (slot mode, for frontiers of mostly longer rows):
@@ -601,7 +602,7 @@ template <int H> struct L2Pol {
 // build pass (k_slot_build) when the next hop reads them.
 using Tiny = uint32_t;                                       // count, then ids, as uint16
 constexpr uint32_t TINY_MAX = sizeof(Tiny) / 2 - 1;          // ids in a tiny word
-constexpr uint32_t SHORT_MAX = 15;  // ids in a slot (16 uint16, entry 0 = the count)
+constexpr uint32_t CHUNK_IDS = 16;  // uint16 entries per 32-byte chunk of a slot
 
 // Bulk prefetch of `bytes` (a multiple of 16, 16-byte aligned) into L2.
 __device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
@@ -633,15 +634,27 @@ __device__ __forceinline__ void or_tiny_ids(uint32_t *row32, Tiny t, uint32_t cn
   }
 }
 
-// OR the ids of a slot (count in [TINY_MAX + 1, SHORT_MAX], ids at entries
-// 1..count) into a shared row; the loop leaves at the warp's longest list
-__device__ __forceinline__ void or_slot_ids(uint32_t *row32, const uint4 s0, const uint4 s1, uint32_t cnt) {
+// OR entries first..last (last < CHUNK_IDS) of one 32-byte slot chunk into
+// a shared row; the loop leaves at the warp's longest list
+__device__ __forceinline__ void or_chunk_ids(uint32_t *row32, const uint4 s0, const uint4 s1, uint32_t first,
+                                             uint32_t last) {
   const uint32_t w[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
 #pragma unroll
-  for (uint32_t i = 1; i <= SHORT_MAX; i++) {
-    if (i > cnt) break;
+  for (uint32_t i = 0; i < CHUNK_IDS; i++) {
+    if (i > last) break;
+    if (i < first) continue;
     const uint32_t id = (w[i >> 1] >> ((i & 1) * 16)) & 0xFFFFu;
     atomicOr(row32 + (id >> 5), 1u << (id & 31));
+  }
+}
+
+// OR the ids of a slot (count in [1, slot_n - 1]) whose first chunk is s0/s1
+__device__ __forceinline__ void or_slot_ids(uint32_t *row32, const uint4 *sp, const uint4 s0, const uint4 s1,
+                                            uint32_t cnt) {
+  or_chunk_ids(row32, s0, s1, 1, cnt < CHUNK_IDS - 1 ? cnt : CHUNK_IDS - 1);
+  for (uint32_t c0 = CHUNK_IDS; c0 <= cnt; c0 += CHUNK_IDS) {
+    const uint32_t left = cnt - c0;  // entries c0..cnt remain
+    or_chunk_ids(row32, __ldg(sp + c0 / 8), __ldg(sp + c0 / 8 + 1), 0, left < CHUNK_IDS - 1 ? left : CHUNK_IDS - 1);
   }
 }
 
@@ -659,7 +672,7 @@ __device__ __forceinline__ void gather_chunk(const PullArgs &a, const L2Pol<H> &
     // slot mode (frontiers of mostly 4..15-bit rows): the slot alone, its
     // entry 0 holds the count; word mode: the word, then the slot when the
     // row has more ids than the word holds
-    const uint4 *sp = a.slot_in + (size_t)u * 2;
+    const uint4 *sp = a.slot_in + (size_t)u * (a.slot_n / 8);
     uint4 s0 = make_uint4(0, 0, 0, 0), s1 = s0;
     uint32_t cnt;
     if (slotmode) {
@@ -675,12 +688,12 @@ __device__ __forceinline__ void gather_chunk(const PullArgs &a, const L2Pol<H> &
       or_tiny_ids(row32, tv, cnt);
       act = false;
       se++;
-    } else if (cnt <= SHORT_MAX) {
+    } else if (cnt < a.slot_n) {
       if (!slotmode) {
         s0 = __ldg(sp);
         s1 = __ldg(sp + 1);
       }
-      or_slot_ids(row32, s0, s1, cnt);
+      or_slot_ids(row32, sp, s0, s1, cnt);
       act = false;
       se++;
     }
@@ -741,7 +754,7 @@ __device__ __forceinline__ void gather_rows(const PullArgs &a, const L2Pol<H> &p
   }
 }
 
-// The tiny word (and, for TINY_MAX+1..SHORT_MAX bits, the slot) of the
+// The tiny word and the slot (ids for up to slot_n - 1 bits) of the
 // non-zero row of v held by lanes 0..L-1 (uint4 q = lane + k * L).
 template <int L, int UPL>
 __device__ __forceinline__ void write_short(const PullArgs &a, uint32_t v, const uint4 (&acc)[UPL], uint32_t qn,
@@ -761,8 +774,8 @@ __device__ __forceinline__ void write_short(const PullArgs &a, uint32_t v, const
   }
   const uint32_t total = __shfl_sync(FULL, incl, 31);
   Tiny tv = total < 0xFFFFu ? total : 0xFFFFu;
-  uint16_t *slot = a.slot_out + (size_t)v * 16;
-  if (total <= SHORT_MAX) {
+  uint16_t *slot = a.slot_out + (size_t)v * a.slot_n;
+  if (total < a.slot_n) {
     Tiny part = 0;
     uint32_t pos = 1 + incl - c;
     if (c) {
@@ -867,7 +880,7 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
         write_short<L, UPL>(a, v, acc, qn, ns);
       else if (lane == 0) {
         a.tiny_out[v] = 0;
-        a.slot_out[(size_t)v * 16] = 0;
+        a.slot_out[(size_t)v * a.slot_n] = 0;
       }
     }
     if (lane == 0) {
@@ -1098,7 +1111,8 @@ __global__ void __launch_bounds__(512) k_pull_hub_short(PullArgs a) {
 }
 
 // Word and slot of row r held in one chunk (Q <= 32: lane q holds uint4 q).
-__device__ __forceinline__ void short_from_chunk(uint4 x, uint32_t r, Tiny *tiny, uint16_t *slots) {
+__device__ __forceinline__ void short_from_chunk(uint4 x, uint32_t r, Tiny *tiny, uint16_t *slots,
+                                                 uint32_t slot_n) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t n = popc4(x);
   uint32_t incl = n;
@@ -1109,8 +1123,8 @@ __device__ __forceinline__ void short_from_chunk(uint4 x, uint32_t r, Tiny *tiny
   }
   const uint32_t total = __shfl_sync(FULL, incl, 31);
   Tiny tv = total < 0xFFFFu ? total : 0xFFFFu;
-  uint16_t *slot = slots + (size_t)r * 16;
-  if (total <= SHORT_MAX) {
+  uint16_t *slot = slots + (size_t)r * slot_n;
+  if (total < slot_n) {
     Tiny part = 0;
     uint32_t at = 1 + incl - n;
     const uint32_t w[4] = {x.x, x.y, x.z, x.w};
@@ -1143,8 +1157,8 @@ __device__ __forceinline__ void short_from_chunk(uint4 x, uint32_t r, Tiny *tiny
 // flagged row counts its bits and writes its word (and slot); every other
 // vertex gets the count 0.
 __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__restrict__ F, uint32_t V,
-                             uint32_t Q, Tiny *__restrict__ tiny, uint16_t *__restrict__ slots, const Ctr *ctr,
-                             int h) {
+                             uint32_t Q, Tiny *__restrict__ tiny, uint16_t *__restrict__ slots, uint32_t slot_n,
+                             const Ctr *ctr, int h) {
   if (ctr->hop[h].strategy != ST_PULL || !ctr->hop[h].short_pull || ctr->hop[h - 1].strategy == ST_PULL) return;
   const int lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
@@ -1153,7 +1167,7 @@ __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__
     const bool f = v < V && flagF[v];
     if (v < V && !f) {  // empty row
       tiny[v] = 0;
-      slots[(size_t)v * 16] = 0;
+      slots[(size_t)v * slot_n] = 0;
     }
     unsigned m = __ballot_sync(FULL, f);
     if (Q <= 32) {  // one chunk per row: four rows' loads in flight at once
@@ -1173,7 +1187,7 @@ __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__
           x[k] = (k < n && (uint32_t)lane < Q) ? F[(size_t)rr[k] * Q + lane] : make_uint4(0, 0, 0, 0);
 #pragma unroll
         for (int k = 0; k < 4; k++)
-          if (k < n) short_from_chunk(x[k], rr[k], tiny, slots);
+          if (k < n) short_from_chunk(x[k], rr[k], tiny, slots, slot_n);
       }
       continue;
     }
@@ -1186,8 +1200,8 @@ __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__
       for (uint32_t q = lane; q < Q; q += 32) c += popc4(row[q]);
       const uint32_t total = warp_sum(c);
       Tiny tv = total < 0xFFFFu ? total : 0xFFFFu;
-      uint16_t *slot = slots + (size_t)r * 16;
-      if (total <= SHORT_MAX) {
+      uint16_t *slot = slots + (size_t)r * slot_n;
+      if (total < slot_n) {
         Tiny part = 0;
         uint32_t pos = 1;
         for (uint32_t q0 = 0; q0 < Q; q0 += 32) {
@@ -1457,6 +1471,7 @@ struct vs_expand_plan {
   // row lists of sparse frontier rows (PULL over lists); none when S > 65536 or multi-slice
   Tiny *tiny[2] = {nullptr, nullptr};      // short-row words of the two frontier buffers' layers
   uint16_t *slot[2] = {nullptr, nullptr};  // ... and their slots
+  uint32_t slot_n = 16;                    // uint16 entries per slot
   double short_min = 0.0;                  // share of short rows for a short-mode PULL (0: off)
   bool use_hmask = false;
   int hop_forced[VS_MAX_HOPS + 1] = {};
@@ -1476,6 +1491,10 @@ inline bool needs_acc(const vs_expand_params &p) {
   return (p.path_type == VS_PATH_ANY && p.k_min != p.k_max) ||
          (p.path_type == VS_PATH_SHORTEST && p.k_min >= 2);
 }
+
+// uint16 entries of a short-row slot for rows of W words: a sixteenth of
+// the row's bytes at 64 and 128 words, 128 bytes beyond.
+inline uint32_t slot_entries(uint32_t W) { return W <= 64 ? 16 : W <= 128 ? 32 : 64; }
 
 // Short-row slots (uint16 ids: S <= 65536) need rows in one slice.
 inline bool short_slots_ok(uint32_t S, uint32_t nslices, double share) {
@@ -1578,8 +1597,9 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   if (short_slots_ok(S, pl->nslices, p->short_share)) {
     PL_ALLOC(pl->tiny[0], V);
     PL_ALLOC(pl->tiny[1], V);
-    PL_ALLOC(pl->slot[0], (size_t)V * 16);
-    PL_ALLOC(pl->slot[1], (size_t)V * 16);
+    pl->slot_n = slot_entries(pl->W);
+    PL_ALLOC(pl->slot[0], (size_t)V * pl->slot_n);
+    PL_ALLOC(pl->slot[1], (size_t)V * pl->slot_n);
   } else {
     pl->short_min = 0;
   }
@@ -1654,7 +1674,7 @@ int vs_expand_plan_footprint(const vs_graph *g, uint32_t S, const vs_expand_para
   qs = std::max<uint32_t>(1, std::min<uint32_t>(qs, 256));
   const uint32_t nslices = (uint32_t)((W / 2 + qs - 1) / qs);
   if (short_slots_ok(S, nslices, p->short_share))
-    b += 2 * V * (32 + sizeof(Tiny));  // short-row words and slots of both buffers
+    b += 2 * V * (2 * slot_entries(W) + sizeof(Tiny));  // short-row words and slots of both buffers
   *bytes = b;
   return VS_OK;
 }
@@ -1829,10 +1849,11 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.slot_in = pl->slot[0] ? reinterpret_cast<const uint4 *>(pl->slot[fb]) : nullptr;
     a.tiny_out = keep_short ? pl->tiny[nbuf] : nullptr;
     a.slot_out = keep_short ? pl->slot[nbuf] : nullptr;
+    a.slot_n = pl->slot_n;
     if (timing) cudaEventRecord(pl->ev[3 * h + 1], st);
     if (pl->slot[0])  // slots of a layer SPARSE or PUSH wrote, when this hop reads them
       { k_slot_build<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<const uint4 *>(pl->buf[fb]), V, Q,
-                                               pl->tiny[fb], pl->slot[fb], pl->ctr, h); vs::note_launch(); }
+                                               pl->tiny[fb], pl->slot[fb], pl->slot_n, pl->ctr, h); vs::note_launch(); }
     { var.pull[pl->pull_kind]<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a); vs::note_launch(); }
     if (pl->nhubs)
       { var.hub<<<dim3(pl->grid_hub, pl->nslices), 512, 16 * 32 * 16 * var.UPL, st>>>(a); vs::note_launch(); }

@@ -22,7 +22,7 @@ struct HopCtr {
   int strategy;                        // strategy run at hop h (0 = not run)
   int short_pull;                      // PULL reads the short rows of layer h-1 through their slots
   int short_slots;                     // ... reading slots (count in entry 0) instead of tiny words
-  unsigned long long short_rows;       // rows of layer h with 1..15 bits (low 32 bits) and with at most
+  unsigned long long short_rows;       // rows of layer h with 1..slot_n-1 bits (low 32 bits) and with at most
                                        // TINY_MAX bits (high 32 bits), counted when its words are written
   unsigned long long short_edges;      // active in-edges of a short-mode PULL served from a slot
 };
@@ -122,7 +122,8 @@ struct PullArgs {
   const uint32_t *tiny_in;  // short-row words of layer h-1, one per vertex (NULL: no short mode)
   const uint4 *slot_in;     // slots of layer h-1 (two uint4 per vertex)
   uint32_t *tiny_out;       // words of layer h, written for every vertex (NULL: not kept)
-  uint16_t *slot_out;       // slots of layer h, written for rows of TINY_MAX+1..SHORT_MAX bits
+  uint16_t *slot_out;       // slots of layer h (count, then the ids of a row of < slot_n bits)
+  uint32_t slot_n;          // uint16 entries per slot (16, 32 or 64)
   uint32_t hub_threshold;
   const uint32_t *hubs;
   uint32_t nhubs;

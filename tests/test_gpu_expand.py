@@ -374,6 +374,26 @@ def test_short_rows_counted(vs, graphs, path, S):
     assert checked == 3
 
 
+@pytest.mark.parametrize("share", [2.0, 0.0])
+@pytest.mark.parametrize("hops", [["pull", "push", "pull", "pull"], ["pull", "pull", "push", "pull"],
+                                  ["sparse", "pull", "pull", "push"], ["pull", "pull", "pull", "pull"]])
+def test_slot_only_rows_materialize(vs, graphs, share, hops):
+    """Short rows a PULL hop leaves only in their slots (flag 2) are written
+    out whole before a hop that reads rows (PUSH, or a dense PULL when short
+    mode is not chosen) and are skipped by the row clears; a reused plan
+    stays exact across runs and path types."""
+    for name in ("zipf3000", "rmat11_skew"):
+        g, dg = graphs[name]
+        for path in ("shortest", "any"):
+            plan = vs.ExpandPlan(dg, 300, vs.make_params(1, 4, path, "forward", short_share=share))
+            plan.set_hop_strategies([0] + hops)
+            for seed in (1, 2):
+                src = graphgen.sample_sources(g.V, 300, seed=seed)
+                plan.run(src)
+                exp, _, _ = O.vexpand(g, src, 1, 4, path, "forward")
+                assert np.array_equal(plan.result().download(), exp), (name, path, hops, share, seed)
+
+
 def test_short_pull_default_rule(vs, graphs):
     """With the default share, frontiers that fit in half of L2 keep the
     dense PULL (every small test graph), and the results agree."""

@@ -12,7 +12,9 @@
 // visited matrix (Shortest/FindShortest) and the accumulator (the union of
 // layers k_min..k_max when it differs from visited).  Each frontier buffer
 // has one uint32 flag per vertex with the invariant "flag == 0 => row is
-// zero", which lets a hop skip inactive rows and clear only what it wrote.
+// zero", which lets a hop skip inactive rows and clear only what it wrote
+// (flag 2: a non-zero short row kept only in its short-row slot, the buffer
+// row being zero; see the short-row notes at the PULL kernels).
 //
 // Per hop one of three strategies runs; the choice is made ON THE DEVICE by a
 // one-block decide kernel from the previous hop's counters, so a whole query
@@ -82,7 +84,7 @@ __global__ void k_clear_flagged(uint4 *__restrict__ buf, uint32_t *__restrict__ 
        base += warps * 32) {
     uint32_t v = base + lane;
     uint32_t f = v < V ? flag[v] : 0u;
-    unsigned m = __ballot_sync(FULL, f != 0);
+    unsigned m = __ballot_sync(FULL, f == 1);  // flag 2: the row lives in its slot, the buffer row is zero
     if (f) flag[v] = 0;
     while (m) {
       int b = __ffs(m) - 1;
@@ -757,7 +759,7 @@ __device__ __forceinline__ void gather_rows(const PullArgs &a, const L2Pol<H> &p
 // The tiny word and the slot (ids for up to slot_n - 1 bits) of the
 // non-zero row of v held by lanes 0..L-1 (uint4 q = lane + k * L).
 template <int L, int UPL>
-__device__ __forceinline__ void write_short(const PullArgs &a, uint32_t v, const uint4 (&acc)[UPL], uint32_t qn,
+__device__ __forceinline__ bool write_short(const PullArgs &a, uint32_t v, const uint4 (&acc)[UPL], uint32_t qn,
                                             unsigned long long &ns) {
   const int lane = threadIdx.x & 31;
   uint32_t c = 0;
@@ -811,6 +813,7 @@ __device__ __forceinline__ void write_short(const PullArgs &a, uint32_t v, const
     a.tiny_out[v] = tv;
     slot[0] = (uint16_t)tv;
   }
+  return total < a.slot_n;
 }
 
 // Fused epilogue for the row of v held by lanes 0..L-1 after the group reduction:
@@ -853,9 +856,9 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
   if (lane == 0 && rownz && (a.res_vis || a.acc_on)) a.resflag[v] = 1;
   if (!a.multislice && a.last) {
     // layer k_max is not kept: clear the rows an earlier layer left in this
-    // buffer, so the next run finds it clean
+    // buffer, so the next run finds it clean (a flag-2 row is zero already)
     const uint32_t oldf = a.flagN[v];
-    if (leader_group && oldf) {
+    if (leader_group && oldf == 1) {
 #pragma unroll
       for (int k = 0; k < UPL; k++) {
         const uint32_t q = lane + k * L;
@@ -867,24 +870,26 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
       if (rownz) nv++;
     }
   } else if (!a.multislice) {
-    const uint32_t oldf = a.flagN[v];
-    if (leader_group && (rownz || oldf)) {
-#pragma unroll
-      for (int k = 0; k < UPL; k++) {
-        const uint32_t q = lane + k * L;
-        if (q < qn) pol.st(a.N + (size_t)v * a.Q + q0 + q, acc[k]);
-      }
-    }
+    const uint32_t oldf = a.flagN[v];  // 1: the buffer row holds an older layer's bits
+    bool virt = false;                 // the row is left in its slot only (flag 2)
     if (a.tiny_out) {  // every vertex gets a tiny word: the count is 0 for an empty row
       if (rownz)
-        write_short<L, UPL>(a, v, acc, qn, ns);
+        virt = write_short<L, UPL>(a, v, acc, qn, ns) && a.virt_out;
       else if (lane == 0) {
         a.tiny_out[v] = 0;
         a.slot_out[(size_t)v * a.slot_n] = 0;
       }
     }
+    if (leader_group && ((rownz && !virt) || oldf == 1)) {
+#pragma unroll
+      for (int k = 0; k < UPL; k++) {
+        const uint32_t q = lane + k * L;
+        if (q < qn) pol.st(a.N + (size_t)v * a.Q + q0 + q, virt ? make_uint4(0, 0, 0, 0) : acc[k]);
+      }
+    }
     if (lane == 0) {
-      if ((rownz ? 1u : 0u) != oldf) a.flagN[v] = rownz ? 1u : 0u;
+      const uint32_t nf = rownz ? (virt ? 2u : 1u) : 0u;
+      if (nf != oldf) a.flagN[v] = nf;
       if (rownz) nv++;
     }
   } else if (rownz) {
@@ -1108,6 +1113,40 @@ template <int L, int UPL>
 __global__ void __launch_bounds__(512) k_pull_hub_short(PullArgs a) {
   if (a.ctr->hop[a.h].strategy != ST_PULL || !a.ctr->hop[a.h].short_pull || !a.tiny_in || a.nhubs == 0) return;
   pull_hubs<L, UPL, true>(a);
+}
+
+// Rows of layer h-1 left in their slots (flag 2), written out whole when hop
+// h reads rows: a dense PULL or a PUSH (a short-mode PULL reads the slots).
+// prev_virt: the PULL of hop h-1 was allowed to leave rows in their slots.
+__global__ void k_materialize(uint32_t *__restrict__ flagF, uint4 *__restrict__ F, uint32_t V, uint32_t Q,
+                              const uint16_t *__restrict__ slots, uint32_t slot_n, const Ctr *ctr, int h,
+                              int prev_virt) {
+  const HopCtr &p = ctr->hop[h - 1], &c = ctr->hop[h];
+  if (!prev_virt || p.strategy != ST_PULL || (p.short_rows & 0xFFFFFFFFull) == 0) return;
+  if (c.strategy == 0 || (c.strategy == ST_PULL && c.short_pull)) return;
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < V; base += warps * 32) {
+    const uint32_t v = base + lane;
+    unsigned m = __ballot_sync(FULL, v < V && flagF[v] == 2);
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      const uint32_t r = base + b;
+      const uint16_t *slot = slots + (size_t)r * slot_n;
+      const uint32_t cnt = slot[0];
+      for (uint32_t q0 = 0; q0 < Q; q0 += 32) {
+        const uint32_t q = q0 + lane;
+        uint32_t w[4] = {0, 0, 0, 0};
+        for (uint32_t i = 1; i <= cnt; i++) {
+          const uint32_t id = slot[i];
+          if (id >> 7 == q) w[(id >> 5) & 3] |= 1u << (id & 31);
+        }
+        if (q < Q) F[(size_t)r * Q + q] = make_uint4(w[0], w[1], w[2], w[3]);
+      }
+      if (lane == 0) flagF[r] = 1;
+    }
+  }
 }
 
 // Word and slot of row r held in one chunk (Q <= 32: lane q holds uint4 q).
@@ -1743,6 +1782,13 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
                      : p.strategy == VS_STRAT_PUSH ? ST_PUSH
                      : p.strategy == VS_STRAT_SPARSE ? ST_SPARSE
                                                      : 0;
+  // a PULL hop may leave the short rows of its layer in their slots when the
+  // layer has a successor and nothing reads its rows directly (FindShortest
+  // checks every layer's rows; a kept layer is copied out)
+  auto leave_in_slots = [&](uint32_t hh) {
+    return pl->slot[0] != nullptr && hh >= 1 && hh < p.k_max && p.path_type != VS_PATH_FIND_SHORTEST &&
+           pl->layer_out[hh] == nullptr;
+  };
   for (uint32_t h = 1; h <= p.k_max; h++) {
     const int fb = (h - 1) & 1, nbuf = h & 1;
     DecideArgs da;
@@ -1770,6 +1816,9 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     if (pl->collect_stats || pl->log_features || (pl->picker && p.use_picker))
       { k_hop_stats<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], outl, V, pl->ctr, h); vs::note_launch(); }
     { k_decide<<<1, 64, 0, st>>>(da); vs::note_launch(); }
+    if (pl->slot[0] && leave_in_slots(h - 1))  // whole rows back for a hop that reads rows
+      { k_materialize<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<uint4 *>(pl->buf[fb]), V, Q,
+                                                pl->slot[fb], pl->slot_n, pl->ctr, h, 1); vs::note_launch(); }
 
     { k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[nbuf]),
                                                 pl->flag[nbuf], V, Q, pl->ctr, h, 1); vs::note_launch(); }
@@ -1845,6 +1894,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.ctr = pl->ctr;
     a.h = h;
     const bool keep_short = pl->slot[0] && h < p.k_max && !a.last;  // the next hop may read this layer's words
+    a.virt_out = keep_short && leave_in_slots(h);
     a.tiny_in = pl->slot[0] ? pl->tiny[fb] : nullptr;
     a.slot_in = pl->slot[0] ? reinterpret_cast<const uint4 *>(pl->slot[fb]) : nullptr;
     a.tiny_out = keep_short ? pl->tiny[nbuf] : nullptr;

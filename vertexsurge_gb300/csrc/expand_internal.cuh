@@ -115,7 +115,7 @@ struct PullArgs {
   const uint4 *F;
   uint4 *N, *vis, *acc;
   const uint32_t *flagF;
-  uint32_t *flagN;
+  uint32_t *flagN;  // 0: empty row; 1: non-zero row in the buffer; 2: non-zero row held in its slot only
   uint32_t V, Q, qslice;
   int multislice, shortest, acc_on;
   int last;  // the run's last hop and nothing reads its layer: zero the buffer instead of writing it
@@ -124,6 +124,7 @@ struct PullArgs {
   uint32_t *tiny_out;       // words of layer h, written for every vertex (NULL: not kept)
   uint16_t *slot_out;       // slots of layer h (count, then the ids of a row of < slot_n bits)
   uint32_t slot_n;          // uint16 entries per slot (16, 32 or 64)
+  int virt_out;             // short rows of layer h may stay in their slots (flag 2, buffer row zero)
   uint32_t hub_threshold;
   const uint32_t *hubs;
   uint32_t nhubs;

@@ -224,10 +224,6 @@ int vs_expand_plan_footprint(const vs_graph *g, uint32_t S, const vs_expand_para
 int vs_expand_plan_set_tuning(vs_expand_plan *plan, double sparse_frac, double push_frac,
                               int collect_stats, int timing);
 
-/* One-shot expand: plan, run, hand the result matrix to the caller.
- * FindShortest: targets[i] is the target of source i, distances[i] receives
- * the hop count (0 when source == target, -1 when not found) and *out may be
- * NULL. */
 /* VExpand with path_params.with_distance, Dense strategy (replaces
  * VExpand::copy_to_multi_MT, vexpand.cpp:356-378, and MultipleMatrixTable,
  * matrix_table.hh:132-149): every layer h in [k_min, k_actual] as its own
@@ -243,9 +239,18 @@ int vs_expand_layers(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_
  * distance column I64. */
 int vs_layers_to_flat(const vs_bitmat *const *layers, const int32_t *distances, uint32_t n, vs_flat **out,
                       vs_stream_t stream);
+/* One-shot expand (VExpand::run_internal, vexpand.cpp:448-483): plan, run,
+ * hand the result matrix to the caller.  FindShortest: targets[i] is the
+ * target of source i, distances[i] receives the hop count (0 when source ==
+ * target, -1 when not found) and *out may be NULL.  The library keeps the
+ * plans of one-shot calls (at most 8 idle, 48 GB): a call with the same
+ * graph, source count and parameters reuses one, and the returned matrix is
+ * that plan's result, lent until vs_bitmat_free (treat it as read-only). */
 int vs_expand(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_params *p,
               const uint32_t *targets, int32_t *distances, vs_bitmat **out,
               vs_expand_stats *stats, vs_stream_t stream);
+/* Frees the idle plans kept for one-shot expands (no reference counterpart). */
+int vs_release_cached(void);
 
 /* ---- hash join (replaces HashJoin, src/objects/operator/join.cpp:26-449) --
  * A table operand is a flat table with the key in column key_col, or a

@@ -427,3 +427,47 @@ def test_short_pull_with_row_limits_and_layers(vs, graphs):
     for h, m in vs.expand_layers(dg, src, 1, 4, "shortest", "forward", strategy="pull", short_share=2.0):
         exp, _, _ = O.vexpand(g, src, h, h, "shortest", "forward")
         assert np.array_equal(m.download(), exp), h
+
+
+def test_one_shot_plan_cache(vs, graphs):
+    """One-shot expands keep their plans: results lent out at the same time
+    stay exact, a plan reused for other sources gives exact results, FindShortest
+    reuses without a matrix, a result outlives its graph, and a result is
+    read-only."""
+    g, dg = graphs["zipf3000"]
+    srcs = [graphgen.sample_sources(g.V, 200, seed=s) for s in (1, 2, 3, 4)]
+    exp = [O.vexpand(g, s, 1, 3, "shortest", "forward")[0] for s in srcs]
+    m0, _, _ = vs.expand(dg, srcs[0], 1, 3, "shortest", "forward")
+    m1, _, _ = vs.expand(dg, srcs[1], 1, 3, "shortest", "forward")  # m0 still lent: another plan
+    assert np.array_equal(m0.download(), exp[0]) and np.array_equal(m1.download(), exp[1])
+    m0.free()
+    m2, _, _ = vs.expand(dg, srcs[2], 1, 3, "shortest", "forward")  # reuses m0's plan
+    assert np.array_equal(m2.download(), exp[2]) and np.array_equal(m1.download(), exp[1])
+    import ctypes
+    zeros = np.zeros_like(exp[2])
+    assert vs.lib().vs_bitmat_upload(m2.h, zeros.ctypes.data_as(ctypes.c_void_p), None) != 0  # read-only
+    m1.free()
+    m2.free()
+    for s, e in zip(srcs, exp):  # every call on a reused plan
+        m, _, _ = vs.expand(dg, s, 1, 3, "shortest", "forward")
+        assert np.array_equal(m.download(), e)
+        assert m.count() == O.matrix_count(e, len(s), g.V)
+        m.free()
+    tgt = graphgen.sample_sources(g.V, 200, seed=9)
+    for _ in range(2):
+        _, dist, _ = vs.expand(dg, srcs[0], 1, 20, "find_shortest", "forward", targets=tgt)
+        _, odist, _ = O.vexpand(g, srcs[0], 1, 20, "find_shortest", "forward", targets=tgt)
+        assert np.array_equal(dist, odist)
+    # a result outlives its graph; the plan is freed, not kept, on release
+    h = graphgen.from_edges(64, list(range(63)), list(range(1, 64)))
+    dh = vs.DeviceGraph.from_host(h)
+    src = np.array([0, 5, 9], np.uint32)
+    m, _, _ = vs.expand(dh, src, 1, 2, "any", "forward")
+    e, _, _ = O.vexpand(h, src, 1, 2, "any", "forward")
+    dh.free()
+    assert np.array_equal(m.download(), e)
+    m.free()
+    vs.release_cached()
+    m, _, _ = vs.expand(dg, srcs[3], 1, 3, "shortest", "forward")
+    assert np.array_equal(m.download(), exp[3])
+    m.free()

@@ -172,6 +172,7 @@ _SIGS += [
     ("vs_semi_join", C.c_int, [TableRef, TableRef, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int,
                                C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_void_p]),
     ("vs_expand_plan_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("vs_release_cached", C.c_int, []),
 ]
 
 # internal entry points (not part of the header)
@@ -210,6 +211,11 @@ def init(device: int = 0) -> None:
 
 def kernel_launches() -> int:
     return int(lib().vs_kernel_launches())
+
+
+def release_cached() -> None:
+    """Free the idle expand plans the library keeps for one-shot expands."""
+    check(lib().vs_release_cached())
 
 
 def _ptr(a) -> C.c_void_p:

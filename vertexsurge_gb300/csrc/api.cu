@@ -422,6 +422,7 @@ int vs_graph_upload(uint32_t V, uint64_t E, const int64_t *fwd_off, const uint32
     return fail(VS_ERR_ARG, "vs_graph_upload: missing CSR arrays");
   cudaStream_t st = S(stream);
   vs_graph *g = new vs_graph();
+  g->serial = vs::next_graph_serial();
   g->V = V;
   g->E = E;
   g->directed = directed ? 1 : 0;
@@ -479,6 +480,7 @@ int vs_graph_info(const vs_graph *g, uint32_t *V, uint64_t *E, int *directed) {
 
 int vs_graph_free(vs_graph *g) {
   if (!g) return VS_OK;
+  vs::plan_cache_drop_graph(g->serial);
   cudaFree(g->fwd_off);
   cudaFree(g->rev_off);
   cudaFree(g->fwd_dst);
@@ -498,6 +500,7 @@ int vs_bitmat_create(uint32_t rows, uint32_t cols, int kind, vs_stream_t stream,
 
 int vs_bitmat_upload(vs_bitmat *m, const uint64_t *logical_words, vs_stream_t stream) {
   if (!m || (!logical_words && m->rows && m->cols)) return fail(VS_ERR_ARG, "null argument");
+  if (m->view) return fail(VS_ERR_ARG, "vs_bitmat_upload: the matrix is a read-only view (an expand result)");
   cudaStream_t st = S(stream);
   if (st != m->st) {  // the matrix was allocated in another stream's order
     VS_CK(cudaStreamSynchronize(m->st));
@@ -570,6 +573,11 @@ int vs_bitmat_get_info(const vs_bitmat *m, vs_bitmat_info *info) {
 
 int vs_bitmat_free(vs_bitmat *m) {
   if (!m) return VS_OK;
+  if (m->pool_plan) {  // a one-shot expand result: its plan goes back to the cache
+    vs::plan_cache_return(m->pool_plan, m->st);
+    delete m;
+    return VS_OK;
+  }
   if (!m->view) {  // stream-ordered after the handle's last work, no device-wide wait
     if (m->owns_words) dfree(m->words, m->st);
     dfree(m->row_map, m->st);

@@ -31,6 +31,8 @@
 //   PUSH    active rows OR-ed into their out-neighbours with 64-bit atomics,
 //           followed by a fused dedup/accumulate pass over the touched rows.
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <cstring>
 #include <vector>
 
@@ -1507,8 +1509,8 @@ struct vs_expand_plan {
   uint64_t *hmask = nullptr;  // (k_max + 1) x W words: rows allowed to grow at hop h
   uint32_t *rowk = nullptr;   // [0] largest row limit, [1] a limit exceeded k_max (device-set limits)
   uint64_t *layer_out[VS_MAX_HOPS + 1] = {};  // with_distance: layer h is copied here (zeroed, V x W words)
-  // row lists of sparse frontier rows (PULL over lists); none when S > 65536 or multi-slice
-  Tiny *tiny[2] = {nullptr, nullptr};      // short-row words of the two frontier buffers' layers
+  // short-row index of the two frontier buffers' layers; none when S > 65536 or multi-slice
+  Tiny *tiny[2] = {nullptr, nullptr};      // short-row words
   uint16_t *slot[2] = {nullptr, nullptr};  // ... and their slots
   uint32_t slot_n = 16;                    // uint16 entries per slot
   double short_min = 0.0;                  // share of short rows for a short-mode PULL (0: off)
@@ -1518,6 +1520,11 @@ struct vs_expand_plan {
   uint32_t timed_hops = 0;
   cudaStream_t last_stream = 0;  // frees are ordered after the last run on it
   cudaEvent_t ev[3 * (VS_MAX_HOPS + 1)] = {};
+  // one-shot cache: the caller's parameters, the graph's serial, the plan's
+  // device bytes and the event its last user's stream recorded
+  vs_expand_params key{};
+  uint64_t graph_serial = 0, bytes = 0;
+  cudaEvent_t cache_ev = nullptr;
 };
 
 namespace vs {
@@ -1551,9 +1558,106 @@ int plan_free(vs_expand_plan *pl) {
     if (p) dfree(p, st);
   for (cudaEvent_t e : pl->ev)
     if (e) cudaEventDestroy(e);
+  if (pl->cache_ev) cudaEventDestroy(pl->cache_ev);
   delete pl;
   return VS_OK;
 }
+
+// The one-shot vs_expand keeps its plans: a call takes an idle plan built for
+// the same graph, source count and parameters (or builds one), runs it and
+// hands out the result as a view whose release returns the plan.  Reuse skips
+// the allocations, the full-matrix clears of a new plan and its hub list; a
+// run clears only what the previous run wrote.  At most kCacheIdle idle plans
+// and kCacheBytes of them are kept; vs_release_cached frees them all.
+constexpr size_t kCacheIdle = 8;
+constexpr uint64_t kCacheBytes = 48ull << 30;
+
+struct PlanCache {
+  std::mutex mu;
+  std::vector<vs_expand_plan *> idle;  // oldest first
+  std::vector<uint64_t> dead;          // serials of freed graphs (plans lent out then are freed on return)
+};
+PlanCache &plan_cache() {
+  static PlanCache c;
+  return c;
+}
+
+bool same_params(const vs_expand_params &a, const vs_expand_params &b) {
+  return a.k_min == b.k_min && a.k_max == b.k_max && a.path_type == b.path_type && a.direction == b.direction &&
+         a.strategy == b.strategy && a.use_picker == b.use_picker && a.hub_threshold == b.hub_threshold &&
+         a.slice_words == b.slice_words && a.pair_capacity == b.pair_capacity && a.pull_kernel == b.pull_kernel &&
+         a.sparse_frac == b.sparse_frac && a.short_share == b.short_share;
+}
+
+vs_expand_plan *plan_cache_take(const vs_graph *g, uint32_t S, const vs_expand_params &p) {
+  PlanCache &c = plan_cache();
+  std::lock_guard<std::mutex> lk(c.mu);
+  for (size_t i = c.idle.size(); i-- > 0;) {
+    vs_expand_plan *pl = c.idle[i];
+    if (pl->graph_serial == g->serial && pl->S == S && same_params(pl->key, p)) {
+      c.idle.erase(c.idle.begin() + (long)i);
+      return pl;
+    }
+  }
+  return nullptr;
+}
+
+void plan_cache_trim(PlanCache &c, std::vector<vs_expand_plan *> &drop) {
+  uint64_t bytes = 0;
+  for (vs_expand_plan *pl : c.idle) bytes += pl->bytes;
+  while (!c.idle.empty() && (c.idle.size() > kCacheIdle || bytes > kCacheBytes)) {
+    bytes -= c.idle.front()->bytes;
+    drop.push_back(c.idle.front());
+    c.idle.erase(c.idle.begin());
+  }
+}
+
+}  // namespace ex
+
+uint64_t next_graph_serial() {
+  static std::atomic<uint64_t> n{1};
+  return n++;
+}
+
+void plan_cache_return(vs_expand_plan *pl, cudaStream_t st) {
+  using namespace ex;
+  if (!pl->cache_ev) cudaEventCreateWithFlags(&pl->cache_ev, cudaEventDisableTiming);
+  if (pl->cache_ev) cudaEventRecord(pl->cache_ev, st);  // the next user's stream waits for this one
+  pl->last_stream = st;
+  std::vector<vs_expand_plan *> drop;
+  {
+    PlanCache &c = plan_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (std::find(c.dead.begin(), c.dead.end(), pl->graph_serial) != c.dead.end() || !pl->cache_ev) {
+      drop.push_back(pl);
+    } else {
+      c.idle.push_back(pl);
+      plan_cache_trim(c, drop);
+    }
+  }
+  for (vs_expand_plan *d : drop) plan_free(d);
+}
+
+void plan_cache_drop_graph(uint64_t serial) {
+  using namespace ex;
+  std::vector<vs_expand_plan *> drop;
+  {
+    PlanCache &c = plan_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.dead.push_back(serial);
+    for (size_t i = 0; i < c.idle.size();) {
+      if (c.idle[i]->graph_serial == serial) {
+        drop.push_back(c.idle[i]);
+        c.idle.erase(c.idle.begin() + (long)i);
+      } else {
+        i++;
+      }
+    }
+  }
+  for (vs_expand_plan *d : drop) plan_free(d);
+}
+
+namespace ex {
 
 template <typename K> int occupancy_grid(K kernel, int threads, size_t smem, int cap_per_sm) {
   int per_sm = 0;
@@ -2152,60 +2256,60 @@ int vs_expand(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_
     if (stats) std::memset(stats, 0, sizeof(*stats));
     return VS_OK;
   }
-  vs_expand_plan *pl = nullptr;
-  VS_TRY(vs_expand_plan_create(g, S, p, &pl));
+  cudaStream_t st = vs::S(stream);
+  vs_expand_plan *pl = plan_cache_take(g, S, *p);
+  if (pl) {
+    if (pl->cache_ev) VS_CK(cudaStreamWaitEvent(st, pl->cache_ev, 0));
+  } else {
+    int rc0 = vs_expand_plan_create(g, S, p, &pl);
+    if (rc0 == VS_ERR_OOM) {  // the cached plans may hold the memory: release them and retry once
+      vs_release_cached();
+      rc0 = vs_expand_plan_create(g, S, p, &pl);
+    }
+    if (rc0 != VS_OK) return rc0;
+    pl->key = *p;
+    pl->graph_serial = g->serial;
+    vs_expand_plan_footprint(g, S, p, &pl->bytes);
+  }
   pl->collect_stats = stats != nullptr;
   int rc = vs_expand_plan_run(pl, sources, targets, distances, stream);
   if (rc == VS_OK && stats) rc = vs_expand_plan_stats(pl, stats, stream);
   if (rc == VS_OK && !stats) {
     int err = 0;
-    cudaError_t e = cudaMemcpyAsync(&err, &pl->ctr->error, sizeof(int), cudaMemcpyDeviceToHost,
-                                    vs::S(stream));
-    if (e == cudaSuccess) e = cudaStreamSynchronize(vs::S(stream));
+    cudaError_t e = cudaMemcpyAsync(&err, &pl->ctr->error, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess)
       rc = cuda_fail(e, "vs_expand", __FILE__, __LINE__);
     else if (err)
       rc = fail(VS_ERR_ARG, "a source or target vertex id is >= V (%u)", g->V);
   }
-  if (rc == VS_OK && out && p->path_type != VS_PATH_FIND_SHORTEST) {
-    cudaStream_t st = vs::S(stream);
-    vs_bitmat *m = new vs_bitmat();
-    m->rows = S;
-    m->cols = g->V;
-    m->wpc = pl->W;
-    m->kind = VS_KIND_VARROW;
-    m->owns_words = true;
-    // hand the result buffer over instead of copying it
-    const int lb = p->k_max & 1;
-    if (pl->use_acc) {
-      m->words = pl->acc;
-      pl->acc = nullptr;
-    } else if (pl->use_vis) {
-      m->words = pl->vis;
-      pl->vis = nullptr;
-    } else {  // Any [k, k]: the last layer's buffer and its row flags
-      m->words = pl->buf[lb];
-      pl->buf[lb] = nullptr;
-    }
-    m->row_map = pl->d_src;
-    pl->d_src = nullptr;
-    if (pl->use_acc || pl->use_vis) {
-      m->colnz = pl->resflag;
-      pl->resflag = nullptr;
-    } else {
-      m->colnz = pl->flag[lb];
-      pl->flag[lb] = nullptr;
-    }
+  if (rc != VS_OK) {  // a failed run leaves the plan out of the cache
+    plan_free(pl);
+    return rc;
+  }
+  if (out && p->path_type != VS_PATH_FIND_SHORTEST) {
+    // the result is the plan's own result matrix, lent until the handle is freed
+    vs_bitmat *m = new vs_bitmat(pl->result);
+    m->view = true;
+    m->owns_words = false;
+    m->pool_plan = pl;
     m->st = st;
     *out = m;
-    (void)st;
+    return VS_OK;
   }
-  if (rc == VS_OK) {
-    cudaError_t e = cudaStreamSynchronize(vs::S(stream));
-    if (e != cudaSuccess) rc = cuda_fail(e, "vs_expand", __FILE__, __LINE__);
+  plan_cache_return(pl, st);
+  return VS_OK;
+}
+
+int vs_release_cached(void) {
+  std::vector<vs_expand_plan *> drop;
+  {
+    PlanCache &c = plan_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    drop.swap(c.idle);
   }
-  plan_free(pl);
-  return rc;
+  for (vs_expand_plan *d : drop) plan_free(d);
+  return VS_OK;
 }
 
 }  // extern "C"

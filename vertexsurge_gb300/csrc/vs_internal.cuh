@@ -70,6 +70,7 @@ struct vs_hub_index {
 };
 
 struct vs_graph {
+  uint64_t serial;  // unique per upload (never reused): keys cached plans of this graph
   uint32_t V;
   uint64_t E;
   int directed;
@@ -90,6 +91,7 @@ struct vs_bitmat {
   cudaStream_t st;  // stream of the last work on the handle; frees are ordered on it
   bool owns_words;
   bool view;  // borrowed view: vs_bitmat_free only releases the struct
+  vs_expand_plan *pool_plan = nullptr;  // a one-shot expand result: freeing it returns this plan to the cache
 };
 
 struct vs_flat {
@@ -101,6 +103,11 @@ struct vs_flat {
 };
 
 namespace vs {
+// Cache of expand plans behind the one-shot vs_expand (expand.cu).
+void plan_cache_return(vs_expand_plan *pl, cudaStream_t st);  // a result handle was freed
+void plan_cache_drop_graph(uint64_t serial);                   // the graph is being freed
+uint64_t next_graph_serial();
+
 inline size_t type_size(int t) { return t == VS_T_I64 ? 8 : 4; }
 int exclusive_scan_u64(const unsigned long long *in, unsigned long long *out, size_t n,
                        cudaStream_t st);

@@ -192,7 +192,7 @@ def test_autotuner_settings_keep_results(vs, graphs):
     src = graphgen.sample_sources(g.V, 200, seed=12)
     t = autotune.tune(dg, src, 1, 3, "shortest", "forward", repeats=1, pull_kinds=(0, 3),
                       sparse_fracs=(0.001, 0.05), hub_thresholds=(0, 64))
-    assert len(t["table"]) == 16 and t["ms"] > 0  # x2: row lists on and off
+    assert len(t["table"]) == 16 and t["ms"] > 0  # x2: short mode on and off
     assert {r["short_share"] for r in t["table"]} == {0.0, -1.0}
     exp, _, _ = O.vexpand(g, src, 1, 3, "shortest", "forward")
     for row in t["table"]:

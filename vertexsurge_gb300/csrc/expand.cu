@@ -669,19 +669,26 @@ __device__ __forceinline__ void or_slot_ids(uint32_t *row32, const uint4 *sp, co
 template <int L, int UPL, int H, bool SHORT>
 __device__ __forceinline__ void gather_chunk(const PullArgs &a, const L2Pol<H> &pol, uint32_t *s_u, uint32_t *row32,
                                              const uint32_t q0, const uint32_t qn, uint4 (&acc)[UPL], uint32_t u,
-                                             bool act, Tiny tv, bool slotmode, unsigned long long &se) {
+                                             bool act, Tiny tv, bool slotmode, unsigned long long &se,
+                                             const uint4 *pre = nullptr) {
   constexpr int G = 32 / L;
   const int lane = threadIdx.x & 31, g = lane / L, gl = lane % L;
   if (SHORT && act) {
     // slot mode (frontiers of mostly 4..15-bit rows): the slot alone, its
-    // entry 0 holds the count; word mode: the word, then the slot when the
-    // row has more ids than the word holds
+    // entry 0 holds the count (pre: its first chunk, loaded ahead); word
+    // mode: the word, then the slot when the row has more ids than the word
+    // holds
     const uint4 *sp = a.slot_in + (size_t)u * (a.slot_n / 8);
     uint4 s0 = make_uint4(0, 0, 0, 0), s1 = s0;
     uint32_t cnt;
     if (slotmode) {
-      s0 = __ldg(sp);
-      s1 = __ldg(sp + 1);
+      if (pre) {
+        s0 = pre[0];
+        s1 = pre[1];
+      } else {
+        s0 = __ldg(sp);
+        s1 = __ldg(sp + 1);
+      }
       cnt = s0.x & 0xFFFFu;
     } else {
       cnt = (uint32_t)tv & 0xFFFFu;
@@ -965,14 +972,21 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
   uint32_t v = blockIdx.x * 8 + wib;
   int64_t beg = 0, end = 0;  // list 0 of target v
   uint32_t pu = 0;           // this lane's in-neighbour in v's first chunk
-  Tiny pt = 0;               // ... and its tiny word
+  Tiny pt = 0;               // ... and its tiny word (word mode)
+  uint4 ps[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};  // ... or its slot's first chunk (slot mode)
   bool pact = false;
+  const uint32_t sq = a.slot_n / 8;  // uint4 per slot
   if (v < a.V) {
     beg = __ldg(off0 + v);
     end = __ldg(off0 + v + 1);
     if (beg + lane < end) {
       pu = __ldg(adj0 + beg + lane);
-      if (!slotmode) pt = ld_keep(a.tiny_in + pu);
+      if (slotmode) {
+        ps[0] = __ldg(a.slot_in + (size_t)pu * sq);
+        ps[1] = __ldg(a.slot_in + (size_t)pu * sq + 1);
+      } else {
+        pt = ld_keep(a.tiny_in + pu);
+      }
       pact = true;
     }
   }
@@ -987,6 +1001,7 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
     if (a.in.n > 1) d += a.in.off[1][v + 1] - a.in.off[1][v];
     uint32_t pun = 0;
     Tiny ptn = 0;
+    uint4 psn[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
     const bool pactn = nbeg + lane < nend;
     if (!(a.hub_threshold && d > (int64_t)a.hub_threshold)) {  // hubs: k_pull_hub_short
       if (lane == 0) {  // the epilogue's read-modify-write rows, fetched while the gather runs
@@ -996,7 +1011,7 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
       uint4 acc[UPL];
 #pragma unroll
       for (int k = 0; k < UPL; k++) acc[k] = make_uint4(0, 0, 0, 0);
-      gather_chunk<L, UPL, 0, true>(a, pol, s_u[wib], row32, 0, qn, acc, pu, pact, pt, slotmode, se);
+      gather_chunk<L, UPL, 0, true>(a, pol, s_u[wib], row32, 0, qn, acc, pu, pact, pt, slotmode, se, ps);
       if (pactn) pun = __ldg(adj0 + nbeg + lane);  // in flight during the rest of v
       gather_rows<L, UPL, 0, true>(a, pol, s_u[wib], row32, 0, qn, acc, adj0, beg + 32, end, 0, 32, se, slotmode);
       if (a.in.n > 1)
@@ -1018,16 +1033,30 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
         }
       }
       __syncwarp();
-      if (pactn && !slotmode) ptn = ld_keep(a.tiny_in + pun);  // in flight during the epilogue
+      if (pactn) {  // in flight during the epilogue
+        if (slotmode) {
+          psn[0] = __ldg(a.slot_in + (size_t)pun * sq);
+          psn[1] = __ldg(a.slot_in + (size_t)pun * sq + 1);
+        } else {
+          ptn = ld_keep(a.tiny_in + pun);
+        }
+      }
       pull_epilogue<L, UPL, 0>(a, pol, v, 0, qn, acc, nb, nv, ns);
     } else if (pactn) {
       pun = __ldg(adj0 + nbeg + lane);
-      if (!slotmode) ptn = ld_keep(a.tiny_in + pun);
+      if (slotmode) {
+        psn[0] = __ldg(a.slot_in + (size_t)pun * sq);
+        psn[1] = __ldg(a.slot_in + (size_t)pun * sq + 1);
+      } else {
+        ptn = ld_keep(a.tiny_in + pun);
+      }
     }
     beg = nbeg;
     end = nend;
     pu = pun;
     pt = ptn;
+    ps[0] = psn[0];
+    ps[1] = psn[1];
     pact = pactn;
   }
   pull_counters(a, nb, nv, ns, se);

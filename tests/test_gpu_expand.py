@@ -394,6 +394,24 @@ def test_slot_only_rows_materialize(vs, graphs, share, hops):
                 assert np.array_equal(plan.result().download(), exp), (name, path, hops, share, seed)
 
 
+@pytest.mark.parametrize("cap", [0, 300])
+def test_short_words_from_pairs_or_rows(vs, graphs, cap):
+    """After a SPARSE hop (or the seed) the short-row words and slots come
+    from its pair list; when that list overflowed (cap 300) they come from the
+    rows.  Both give the oracle's result."""
+    for name in ("rmat10", "zipf3000"):
+        g, dg = graphs[name]
+        src = graphgen.sample_sources(g.V, 200, seed=5)
+        for hops in (["sparse", "pull", "pull", "pull"], ["pull", "sparse", "pull", "pull"]):
+            for path in ("shortest", "any"):
+                plan = vs.ExpandPlan(dg, len(src), vs.make_params(1, 4, path, "forward", short_share=2.0,
+                                                                  pair_capacity=cap))
+                plan.set_hop_strategies([0] + hops)
+                plan.run(src)
+                exp, _, _ = O.vexpand(g, src, 1, 4, path, "forward")
+                assert np.array_equal(plan.result().download(), exp), (name, hops, path, cap)
+
+
 def test_short_pull_default_rule(vs, graphs):
     """With the default share, frontiers that fit in half of L2 keep the
     dense PULL (every small test graph), and the results agree."""

@@ -1222,14 +1222,56 @@ __device__ __forceinline__ void short_from_chunk(uint4 x, uint32_t r, Tiny *tiny
   }
 }
 
+// Hop h pulls in short mode over a layer that SPARSE (without overflow) or
+// the seed wrote: that hop left exactly one (vertex, source) pair per bit, so
+// the words and slots are built from the pair list instead of the rows.
+__device__ __forceinline__ bool pairs_build(const Ctr *c, int h) {
+  const HopCtr &cur = c->hop[h], &p = c->hop[h - 1];
+  return cur.strategy == ST_PULL && cur.short_pull && (h == 1 || (p.strategy == ST_SPARSE && !p.overflow));
+}
+
+__global__ void k_pairs_zero(uint32_t *__restrict__ cnt, uint32_t V, const Ctr *ctr, int h) {
+  if (!pairs_build(ctr, h)) return;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) cnt[v] = 0;
+}
+
+// every pair's source id into its vertex's slot (entries 1.., in any order)
+__global__ void k_pairs_slots(const uint2 *__restrict__ pairs, uint32_t *__restrict__ cnt, uint16_t *__restrict__ slots,
+                              uint32_t slot_n, uint64_t cap, const Ctr *ctr, int h) {
+  if (!pairs_build(ctr, h)) return;
+  const unsigned long long np_raw = ctr->hop[h - 1].pairs;
+  const uint64_t np = np_raw < cap ? np_raw : cap;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < np; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint2 pr = pairs[k];
+    const uint32_t at = atomicAdd(&cnt[pr.x], 1u) + 1;
+    if (at < slot_n) slots[(size_t)pr.x * slot_n + at] = (uint16_t)pr.y;
+  }
+}
+
+// the tiny word of every vertex from its pair count (0 for an empty row)
+__global__ void k_pairs_words(const uint32_t *__restrict__ flagF, const uint32_t *__restrict__ cnt,
+                              Tiny *__restrict__ tiny, uint16_t *__restrict__ slots, uint32_t slot_n, uint32_t V,
+                              const Ctr *ctr, int h) {
+  if (!pairs_build(ctr, h)) return;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    const uint32_t c = flagF[v] ? cnt[v] : 0u;
+    Tiny tv = c < 0xFFFFu ? c : 0xFFFFu;
+    if (c == 1) tv |= (Tiny)slots[(size_t)v * slot_n + 1] << 16;
+    tiny[v] = tv;
+    if (c) slots[(size_t)v * slot_n] = (uint16_t)tv;
+  }
+}
+
 // Tiny words and slots of layer h-1 when hop h pulls in short mode and that
-// layer was not written by a PULL hop (SPARSE, PUSH or the seed): a warp per
+// layer was written by PUSH or by a SPARSE hop whose pair list overflowed: a warp per
 // flagged row counts its bits and writes its word (and slot); every other
 // vertex gets the count 0.
 __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__restrict__ F, uint32_t V,
                              uint32_t Q, Tiny *__restrict__ tiny, uint16_t *__restrict__ slots, uint32_t slot_n,
                              const Ctr *ctr, int h) {
-  if (ctr->hop[h].strategy != ST_PULL || !ctr->hop[h].short_pull || ctr->hop[h - 1].strategy == ST_PULL) return;
+  if (ctr->hop[h].strategy != ST_PULL || !ctr->hop[h].short_pull || ctr->hop[h - 1].strategy == ST_PULL ||
+      pairs_build(ctr, h))
+    return;
   const int lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < V; base += warps * 32) {
@@ -2034,9 +2076,15 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.slot_out = keep_short ? pl->slot[nbuf] : nullptr;
     a.slot_n = pl->slot_n;
     if (timing) cudaEventRecord(pl->ev[3 * h + 1], st);
-    if (pl->slot[0])  // slots of a layer SPARSE or PUSH wrote, when this hop reads them
+    if (pl->slot[0]) {  // words and slots of a layer SPARSE, PUSH or the seed wrote, when this hop reads them
+      { k_pairs_zero<<<pl->grid_v, 256, 0, st>>>(pl->touched, V, pl->ctr, h); vs::note_launch(); }
+      { k_pairs_slots<<<pl->grid_v, 256, 0, st>>>(pl->pairs[fb], pl->touched, pl->slot[fb], pl->slot_n, pl->pair_cap,
+                                                pl->ctr, h); vs::note_launch(); }
+      { k_pairs_words<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], pl->touched, pl->tiny[fb], pl->slot[fb], pl->slot_n, V,
+                                                pl->ctr, h); vs::note_launch(); }
       { k_slot_build<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<const uint4 *>(pl->buf[fb]), V, Q,
                                                pl->tiny[fb], pl->slot[fb], pl->slot_n, pl->ctr, h); vs::note_launch(); }
+    }
     { var.pull[pl->pull_kind]<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a); vs::note_launch(); }
     if (pl->nhubs)
       { var.hub<<<dim3(pl->grid_hub, pl->nslices), 512, 16 * 32 * 16 * var.UPL, st>>>(a); vs::note_launch(); }

@@ -278,15 +278,19 @@ __global__ void __launch_bounds__(256) k_isect(Args a) {
 // k_isect.
 constexpr int ISECT_SAMPLE = 4096;
 
-__global__ void __launch_bounds__(256) k_isect_decide(Args a, uint32_t V, uint64_t E, int has_hubs,
-                                                      const void *picker, float *feat_out, int *method) {
+__global__ void __launch_bounds__(1024) k_isect_decide(Args a, uint32_t V, uint64_t E, int has_hubs,
+                                                       const void *picker, float *feat_out, int *method) {
   __shared__ float acc[32];
   __shared__ float f[pk::NF], h1[pk::H1], h2[pk::H2], out[pk::NO];
   if (threadIdx.x < 32) acc[threadIdx.x] = 0.f;
   __syncthreads();
   const uint64_t n = a.nbase < (uint64_t)ISECT_SAMPLE ? a.nbase : (uint64_t)ISECT_SAMPLE;
   // acc: 0 samples, 1 empty, 2 sum log len_walk, 3 sum log len_other, 4 sum log ratio, 5 hub, 6 ratio<=8,
-  //      7 bitmap rule, 8 other-list count, 16..23 hist log len_walk, 24..31 hist log ratio
+  //      7 bitmap rule, 8 other-list count, 16..23 hist log len_walk, 24..31 hist log ratio;
+  // summed per thread, then per warp, then once per warp into shared memory
+  float loc[32];
+#pragma unroll
+  for (int j = 0; j < 32; j++) loc[j] = 0.f;
   for (uint64_t k = threadIdx.x; k < n; k += blockDim.x) {
     const uint64_t t = n == a.nbase ? k : k * a.nbase / n;
     float lw = 0.f;
@@ -300,15 +304,17 @@ __global__ void __launch_bounds__(256) k_isect_decide(Args a, uint32_t V, uint64
       if (len == 0) empty = true;
       if (walk < 0 || len < walk) walk = len;
     }
-    atomicAdd(&acc[0], 1.f);
+    loc[0] += 1.f;
     if (walk < 0) continue;
     if (empty) {
-      atomicAdd(&acc[1], 1.f);
+      loc[1] += 1.f;
       continue;
     }
     lw = log2f(1.f + (float)walk);
-    atomicAdd(&acc[2], lw);
-    atomicAdd(&acc[16 + min(7, (int)(lw * 0.5f))], 1.f);
+    loc[2] += lw;
+    const int hb = min(7, (int)(lw * 0.5f));
+#pragma unroll
+    for (int b = 0; b < 8; b++) loc[16 + b] += hb == b ? 1.f : 0.f;
     bool walked = false;
     for (int i = 0; i < a.ndeps; i++) {
       const Dep &d = a.dep[i];
@@ -321,14 +327,22 @@ __global__ void __launch_bounds__(256) k_isect_decide(Args a, uint32_t V, uint64
       }
       const float lo = log2f(1.f + (float)len), lr = log2f((float)len / (float)walk);
       const bool hub = d.hub_slot && d.hub_slot[u] >= 0;
-      atomicAdd(&acc[3], lo);
-      atomicAdd(&acc[4], lr);
-      atomicAdd(&acc[8], 1.f);
-      if (hub) atomicAdd(&acc[5], 1.f);
-      if (walk >= 512 && len <= 4 * walk) atomicAdd(&acc[6], 1.f);
-      if (hub) atomicAdd(&acc[7], 1.f);
-      atomicAdd(&acc[24 + max(0, min(7, (int)lr))], 1.f);
+      loc[3] += lo;
+      loc[4] += lr;
+      loc[8] += 1.f;
+      if (hub) loc[5] += 1.f;
+      if (walk >= 512 && len <= 4 * walk) loc[6] += 1.f;
+      if (hub) loc[7] += 1.f;
+      const int rb = max(0, min(7, (int)lr));
+#pragma unroll
+      for (int b = 0; b < 8; b++) loc[24 + b] += rb == b ? 1.f : 0.f;
     }
+  }
+#pragma unroll
+  for (int j = 0; j < 32; j++) {
+    float v = loc[j];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.f) atomicAdd(&acc[j], v);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -695,7 +709,7 @@ int vs_mintersect_ex(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps
     VS_TRY(sc.get(&d_method, 1));
     VS_TRY(sc.get(&d_feat, pk::NF));
     VS_CK(cudaMemsetAsync(d_method, 0, sizeof(int), st));  // VS_ISECT_AUTO until the network decides
-    { k_isect_decide<<<1, 256, 0, st>>>(a, fg->V, fg->E, hubs ? 1 : 0,
+    { k_isect_decide<<<1, 1024, 0, st>>>(a, fg->V, fg->E, hubs ? 1 : 0,
                                       method_picker ? vs_picker_device_weights(method_picker) : nullptr, d_feat,
                                       d_method); vs::note_launch(); }
     a.method = method_picker ? d_method : nullptr;

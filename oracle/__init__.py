@@ -1,2 +1,3 @@
 """ORACLE — test infrastructure only: the CPU restatement of the reference
-operators (oracle.cpp) used as the checker and the timed CPU baseline."""
+operators (oracle.cpp), against which the parity tests compare the CUDA path, and
+the timed CPU baseline."""

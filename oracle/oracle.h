@@ -2,8 +2,8 @@
  * ORACLE — test infrastructure only.
  *
  * A portable CPU restatement (C++17 + OpenMP, no SIMD) of VertexSurge's
- * variable-length graph pattern matching operators, used as the checker for
- * the CUDA path and as the timed CPU baseline.  Only tests/, the smoke check
+ * variable-length graph pattern matching operators, the reference the parity
+ * tests compare the CUDA path with and the timed CPU baseline.  Only tests/, the smoke check
  * in __graft_entry__.py and bench.py's CPU-baseline leg may load it; nothing
  * in the product links or calls it.
  *

@@ -7,7 +7,7 @@ expand), dependencies = the adjacency lists of a and of b (forward, or both
 backward).  Each call is timed (CUDA events around the whole call, best of
 two after a warm run) under every method the network can choose — binary
 search everywhere, hub bitmap wherever one exists, and the per-tuple rule
-(`algo='auto'`, which is also the fixed planner it is judged against); the
+(`algo='auto'`, which is also the fixed planner it is compared with); the
 call's 32 features come from the same device code that feeds the network.
 Results never depend on the method (checked on every logged call).
 Evaluation on held-out calls: the network's slowdown against the best

@@ -412,6 +412,20 @@ def test_short_words_from_pairs_or_rows(vs, graphs, cap):
                 assert np.array_equal(plan.result().download(), exp), (name, hops, path, cap)
 
 
+def test_short_pull_find_shortest(vs, graphs):
+    """FindShortest with short mode forced on every PULL hop (its layers keep
+    their rows, which the target check reads) gives the oracle's distances."""
+    for name, (g, dg) in graphs.items():
+        src = graphgen.sample_sources(g.V, 150, seed=41)
+        tgt = graphgen.sample_sources(g.V, 150, seed=42)
+        tgt[:5] = src[:5]
+        for strategy in ("pull", "auto"):
+            _, dist, _ = vs.expand(dg, src, 1, 30, "find_shortest", "forward", targets=tgt, strategy=strategy,
+                                   short_share=2.0)
+            _, odist, _ = O.vexpand(g, src, 1, 30, "find_shortest", "forward", targets=tgt)
+            assert np.array_equal(dist, odist), (name, strategy)
+
+
 def test_short_pull_default_rule(vs, graphs):
     """With the default share, frontiers that fit in half of L2 keep the
     dense PULL (every small test graph), and the results agree."""

@@ -49,11 +49,11 @@ class Samples:
                 np.asarray(self.query, np.int64))
 
 
-def graph_suite(scales=(20, 21, 22, 23, 24), skews=(0.45, 0.57, 0.65), zipf=((10_000_000, 300_000_000),),
-                small=(16,)):
+def graph_suite(scales=(20, 21, 22, 23, 24), skews=(0.45, 0.57, 0.65),
+                zipf=((1_000_000, 30_000_000), (10_000_000, 300_000_000)), small=(16,)):
     """R-MAT graphs at `scales` x skews a (b = c = (1 - a - 0.05) / 2), the
-    small R-MAT of the plain-method configuration and the power-law graph of
-    the pattern query."""
+    small R-MAT of the plain-method configuration and the power-law graphs of
+    the pattern query (10M vertices, and its 1M-vertex instance)."""
     gs = []
     for sc in scales:
         for a in skews:
@@ -191,12 +191,13 @@ def main():
     ap.add_argument("--out", default=str(WEIGHTS_FILE))
     ap.add_argument("--report", default="")
     ap.add_argument("--scales", default="20,21,22,23,24")
-    ap.add_argument("--no-zipf", action="store_true", help="leave out the 10M-vertex power-law graph")
+    ap.add_argument("--no-zipf", action="store_true", help="leave out the power-law graphs")
     args = ap.parse_args()
     vs.init(0)
     scales = tuple(int(x) for x in args.scales.split(","))
     t0 = time.time()
-    graphs = graph_suite(scales=scales, zipf=() if args.no_zipf else ((10_000_000, 300_000_000),))
+    graphs = graph_suite(scales=scales, zipf=() if args.no_zipf else ((1_000_000, 30_000_000),
+                                                                       (10_000_000, 300_000_000)))
     samples = collect(args.queries, graphs=graphs, minutes=args.minutes, target_samples=args.samples)
     t_log = time.time() - t0
     pk, rep = train_and_evaluate(samples, epochs=args.epochs)

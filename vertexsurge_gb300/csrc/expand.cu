@@ -602,8 +602,12 @@ template <int H> struct L2Pol {
 // bits) or its slot alone (slot mode, for frontiers of mostly longer rows):
 // count 0 is an empty row, short rows OR their ids into a per-warp
 // shared-memory row with 32-bit atomics, and only longer rows are gathered
-// whole.  Layers written by SPARSE or PUSH get their words and slots from a
-// build pass (k_slot_build) when the next hop reads them.
+// whole.  Short rows of a layer with a successor stay in their slots only
+// (flag 2, buffer row zero) unless the layer's rows are read directly;
+// k_materialize writes them out before a hop that reads rows.  Layers
+// written by SPARSE or the seed get their words and slots from the hop's
+// pair list (k_pairs_*), layers written by PUSH or an overflowed SPARSE hop
+// from their rows (k_slot_build), when the next hop reads them.
 using Tiny = uint32_t;                                       // count, then ids, as uint16
 constexpr uint32_t TINY_MAX = sizeof(Tiny) / 2 - 1;          // ids in a tiny word
 constexpr uint32_t CHUNK_IDS = 16;  // uint16 entries per 32-byte chunk of a slot

@@ -243,7 +243,8 @@ int vs_layers_to_flat(const vs_bitmat *const *layers, const int32_t *distances, 
  * hand the result matrix to the caller.  FindShortest: targets[i] is the
  * target of source i, distances[i] receives the hop count (0 when source ==
  * target, -1 when not found) and *out may be NULL.  The library keeps the
- * plans of one-shot calls (at most 8 idle, 48 GB): a call with the same
+ * plans of one-shot calls (at most 8 idle, a quarter of the device's memory
+ * and at least 48 GB): a call with the same
  * graph, source count and parameters reuses one, and the returned matrix is
  * that plan's result, lent until vs_bitmat_free (treat it as read-only). */
 int vs_expand(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_expand_params *p,

@@ -1643,9 +1643,19 @@ int plan_free(vs_expand_plan *pl) {
 // hands out the result as a view whose release returns the plan.  Reuse skips
 // the allocations, the full-matrix clears of a new plan and its hub list; a
 // run clears only what the previous run wrote.  At most kCacheIdle idle plans
-// and kCacheBytes of them are kept; vs_release_cached frees them all.
+// are kept, holding at most a quarter of the device's memory (48 GB at
+// least); vs_release_cached frees them all.
 constexpr size_t kCacheIdle = 8;
-constexpr uint64_t kCacheBytes = 48ull << 30;
+
+uint64_t cache_bytes_cap() {
+  static uint64_t cap = 0;
+  if (cap == 0) {
+    size_t free_b = 0, total_b = 0;
+    cap = 48ull << 30;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) cap = std::max<uint64_t>(cap, total_b / 4);
+  }
+  return cap;
+}
 
 struct PlanCache {
   std::mutex mu;
@@ -1680,7 +1690,8 @@ vs_expand_plan *plan_cache_take(const vs_graph *g, uint32_t S, const vs_expand_p
 void plan_cache_trim(PlanCache &c, std::vector<vs_expand_plan *> &drop) {
   uint64_t bytes = 0;
   for (vs_expand_plan *pl : c.idle) bytes += pl->bytes;
-  while (!c.idle.empty() && (c.idle.size() > kCacheIdle || bytes > kCacheBytes)) {
+  const uint64_t cap = cache_bytes_cap();
+  while (!c.idle.empty() && (c.idle.size() > kCacheIdle || bytes > cap)) {
     bytes -= c.idle.front()->bytes;
     drop.push_back(c.idle.front());
     c.idle.erase(c.idle.begin());

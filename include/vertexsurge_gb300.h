@@ -180,7 +180,8 @@ typedef struct vs_expand_params {
                               source ids instead of whole, on hops where at least this share of
                               the frontier's rows are short and the frontier exceeds half of L2
                               (0 = 0.1; < 0 = never; > 1 = every PULL hop); needs S <= 65536 and
-                              whole-row passes, and keeps 36 to 132 B per vertex */
+                              whole-row passes, and keeps 36 to 132 B per vertex, except in plans
+                              whose V x S matrix fits in half of L2 (short mode never runs there) */
 } vs_expand_params;
 
 #define VS_MAX_HOPS 64

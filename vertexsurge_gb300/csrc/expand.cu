@@ -1617,9 +1617,11 @@ inline bool needs_acc(const vs_expand_params &p) {
 // the row's bytes at 64 and 128 words, 128 bytes beyond.
 inline uint32_t slot_entries(uint32_t W) { return W <= 64 ? 16 : W <= 128 ? 32 : 64; }
 
-// Short-row slots (uint16 ids: S <= 65536) need rows in one slice.
-inline bool short_slots_ok(uint32_t S, uint32_t nslices, double share) {
-  return share >= 0 && S <= 65536 && nslices == 1;
+// Short-row slots (uint16 ids: S <= 65536) need rows in one slice, and short
+// mode runs only on frontiers larger than half of L2 (unless forced: share >
+// 1): a graph whose whole V x W matrix fits there never uses them.
+inline bool short_slots_ok(uint32_t S, uint32_t nslices, double share, uint64_t V, uint32_t W) {
+  return share >= 0 && S <= 65536 && nslices == 1 && (share > 1.0 || V * 8ull * W > l2_bytes() / 2);
 }
 
 int plan_free(vs_expand_plan *pl) {
@@ -1823,7 +1825,7 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   PL_ALLOC(pl->hmask, (size_t)(p->k_max + 1) * pl->W);
   PL_ALLOC(pl->rowk, 2);
   pl->short_min = p->short_share == 0 ? 0.1 : p->short_share;
-  if (short_slots_ok(S, pl->nslices, p->short_share)) {
+  if (short_slots_ok(S, pl->nslices, p->short_share, V, pl->W)) {
     PL_ALLOC(pl->tiny[0], V);
     PL_ALLOC(pl->tiny[1], V);
     pl->slot_n = slot_entries(pl->W);
@@ -1902,8 +1904,8 @@ int vs_expand_plan_footprint(const vs_graph *g, uint32_t S, const vs_expand_para
   uint32_t qs = p->slice_words ? (p->slice_words + 1) / 2 : (uint32_t)(W / 2);
   qs = std::max<uint32_t>(1, std::min<uint32_t>(qs, 256));
   const uint32_t nslices = (uint32_t)((W / 2 + qs - 1) / qs);
-  if (short_slots_ok(S, nslices, p->short_share))
-    b += 2 * V * (2 * slot_entries(W) + sizeof(Tiny));  // short-row words and slots of both buffers
+  if (short_slots_ok(S, nslices, p->short_share, V, (uint32_t)W))
+    b += 2 * V * (2 * slot_entries((uint32_t)W) + sizeof(Tiny));  // short-row words and slots of both buffers
   *bytes = b;
   return VS_OK;
 }
@@ -1979,6 +1981,11 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     return pl->slot[0] != nullptr && hh >= 1 && hh < p.k_max && p.path_type != VS_PATH_FIND_SHORTEST &&
            pl->layer_out[hh] == nullptr;
   };
+  // PUSH runs only when forced (for the run or a hop), enabled in the fixed
+  // planner (push_frac > 0) or left to the picker
+  bool any_forced_push = forced == ST_PUSH;
+  for (uint32_t hh = 1; hh <= p.k_max; hh++) any_forced_push |= pl->hop_forced[hh] == ST_PUSH;
+  const bool can_push = any_forced_push || pl->push_frac > 0 || (pl->picker && p.use_picker);
   for (uint32_t h = 1; h <= p.k_max; h++) {
     const int fb = (h - 1) & 1, nbuf = h & 1;
     DecideArgs da;
@@ -2053,10 +2060,12 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     pa.W = W;
     pa.shortest = pl->use_vis;
     pa.acc_on = acc_on;
-    { k_push_reset<<<1, 1, 0, st>>>(pl->ctr); vs::note_launch(); }
-    { k_push_compact<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], V, pl->push_list, pl->ctr, h); vs::note_launch(); }
-    { k_push<<<pl->grid_push, 256, 0, st>>>(pa); vs::note_launch(); }
-    { k_push_epilogue<<<pl->grid_push, 256, 0, st>>>(pa); vs::note_launch(); }
+    if (can_push) {  // PUSH kernels only when the hop can run PUSH
+      { k_push_reset<<<1, 1, 0, st>>>(pl->ctr); vs::note_launch(); }
+      { k_push_compact<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], V, pl->push_list, pl->ctr, h); vs::note_launch(); }
+      { k_push<<<pl->grid_push, 256, 0, st>>>(pa); vs::note_launch(); }
+      { k_push_epilogue<<<pl->grid_push, 256, 0, st>>>(pa); vs::note_launch(); }
+    }
     PullArgs a;
     a.resflag = pl->resflag;
     a.res_vis = pl->use_vis && !pl->use_acc;

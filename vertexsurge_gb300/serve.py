@@ -65,13 +65,15 @@ def make_trace(g, n: int, rate_qps: float, s_range=(64, 2048), l_max=5, join_row
 
 
 class Server:
-    def __init__(self, dg: vs.DeviceGraph, budget_bytes: int, slots: int = 4, picker=None, tuned=None):
+    def __init__(self, dg: vs.DeviceGraph, budget_bytes: int, slots: int = 4, picker=None, tuned=None,
+                 make_stream=None):
         self.dg = dg
         self.budget = int(budget_bytes)
         self.slots = slots
         self.picker = picker
         self.tuned = tuned or {}
         self.adj = [dict(graph=dg, direction="forward", base_col=0), dict(graph=dg, direction="forward", base_col=1)]
+        self.make_stream = make_stream  # a slot's stream (default: a new CUDA stream per slot)
 
     def _params(self, S, k_min, k_max, path):
         from .autotune import params_kw
@@ -113,8 +115,12 @@ class Server:
     def serve(self, trace: list, time_scale: float = 1.0) -> dict:
         """Replay the trace: arrivals follow the trace clock (scaled), admission is
         continuous under the slot and byte limits."""
-        import torch
         pending = sorted(trace, key=lambda r: r.arrival)
+        if self.make_stream is None:
+            import torch
+            make_stream = torch.cuda.Stream
+        else:
+            make_stream = self.make_stream
         for r in pending:
             r.bytes = self.footprint(r)
             if r.bytes > self.budget:
@@ -125,7 +131,7 @@ class Server:
         errors = []
 
         def worker():
-            stream = torch.cuda.Stream()
+            stream = make_stream()
             while True:
                 with lock:
                     while True:

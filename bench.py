@@ -151,31 +151,42 @@ def expand_bytes(V, W, e_act, shortest, acc, gathers=True):
     active edge (32-byte sector minimum) and P streaming passes over the V x S
     matrices (P = 4 for the frontier/next pair plus visited or accumulator
     read+write each).  gathers=False gives the compulsory bytes alone (every
-    frontier row read once instead of once per edge)."""
+    frontier row read once instead of once per edge):
+    8(V+1) + 4 E_act + P 8W V."""
     P = 2 + (2 if shortest else 0) + (2 if acc else 0)
     return 8 * (V + 1) + 4 * e_act + (e_act * max(32, 8 * W) if gathers else 0) + P * 8 * W * V
 
 
-def short_bytes(V, W, e_act, e_short, active_prev, built, shortest, acc, gathers=True):
-    """Algorithmic bytes of a short-mode PULL hop: CSR offsets + targets, one
-    32-byte sector per active in-edge whose row is short (its tiny word or
-    slot) and a whole-row gather (at least one sector) for the others, the
-    layer's tiny words and slots (36 B per vertex), the build of the
-    frontier's words and slots when SPARSE wrote it (its rows read once), and
-    the same P passes over the V x S matrices as the dense hop."""
-    P = 2 + (2 if shortest else 0) + (2 if acc else 0)
-    per_edge = (32 * e_short + max(32, 8 * W) * (e_act - e_short)) if gathers else 0
-    build = (8 * W + 36) * active_prev if built else 0
-    return 8 * (V + 1) + 4 * e_act + per_edge + 36 * V + build + P * 8 * W * V
+def pattern_config(args, g, w, world):
+    """The workload's `config` object, the same in the GPU and reference arms."""
+    Sa, Sb = w["S_a"], w["S_b"]
+    W = (Sa + 63) // 64
+    csr_gb = (16 * (g.V + 1) + 8 * g.E) / 1e9
+    mat_gb = 8 * (W + (W & 1)) * g.V / 1e9
+    return {"workload": args.workload, "V": g.V, "E": g.E, "S_a": Sa, "hops_a": list(w["hops_a"]),
+            "S_b": Sb, "hops_b": list(w["hops_b"]), "join": "A x B on vertex id, exact count",
+            "intersect": "triangle closing over out-lists, exact count",
+            "l2": f"inputs larger than L2 (CSR {csr_gb:.1f} GB, {mat_gb:.2f} GB per bit matrix)"
+            if mat_gb > 0.126 else "matrices fit in L2 (launch-bound workload)",
+            "parallelism": f"replicas{world}"}
+
+
+def batched_config(args, g, queries, world):
+    """The batched workload's `config` object, the same in both arms."""
+    return {"workload": args.workload, "V": g.V, "E": g.E, "queries": len(queries),
+            "sources": int(sum(len(q.sources) for q in queries)),
+            "key_rows": int(sum(len(q.keys) for q in queries)), "l2": "inputs larger than L2",
+            "parallelism": f"replicas{world}"}
 
 
 def cpu_baseline(g, w, sa):
-    """Oracle VExpand on the host cores: the bounded sample and its throughput."""
+    """Oracle VExpand on the host cores: the bounded sample and its throughput,
+    and the sample's matrix (logical words, V x S/64) for the parity check."""
     from oracle import pyoracle as O
     S = w["cpu_S"]
     src = sa[:S]
     k0, k1 = w["hops_a"]
-    _, _, st = O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False, hop_stats=True)
+    words, _, st = O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=True, hop_stats=True)
     src_edges = S * sum(st["active_edges"][1:])
     t = time.perf_counter()
     O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False)
@@ -183,7 +194,7 @@ def cpu_baseline(g, w, sa):
     return {"value": src_edges / dt / 1e9, "unit": "Gsrc-edges/s", "cores": O.lib().oracle_get_threads(),
             "kind": "port",
             "sample": f"VExpand(Shortest, [{k0},{k1}], Forward) from the first {S} A sources on the full "
-                      f"graph, one run of {dt:.1f} s ({src_edges / 1e9:.2f} Gsrc-edges)"}, dt
+                      f"graph, one run of {dt:.1f} s ({src_edges / 1e9:.2f} Gsrc-edges)"}, words
 
 
 def batched_queries(g, w):
@@ -232,7 +243,7 @@ def run_reference_batched(args, w):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": min(args.warmup, 1),
             "ms_per_step": 1000 * sum(times) / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded power-law graph, uniform sources)",
-            "config": {"workload": args.workload, "V": g.V, "E": g.E, "queries": len(queries)},
+            "config": batched_config(args, g, queries, args.gpus),
             "cpu_baseline": {"value": value, "unit": "queries/s", "cores": cores, "kind": "port",
                              "sample": desc},
             "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -371,9 +382,13 @@ def run_gpu_batched(args, w, rank, world, local_rank):
             dist.destroy_process_group()
         return
     cpu = None
+    parity = None
     if world == 1 and not args.no_cpu:
         sample, ccounts, dt = cpu_batched(g, w, queries)
         assert [int(counts[i]) for i in sample] == ccounts, "oracle counts differ from the batch"
+        parity = {"queries": len(sample), "equal": True,
+                  "against": "oracle VExpand(Shortest, [1,l]) + TableConvert + HashJoin count per query "
+                             f"(queries {sample}); the batch also equals {len(chk)} solo GPU runs"}
         from oracle import pyoracle as O
         cpu = {"value": len(sample) / dt, "unit": "queries/s", "cores": O.lib().oracle_get_threads(),
                "kind": "port", "sample": f"{len(sample)} queries with <= 2048 sources, one at a time, {dt:.1f} s"}
@@ -381,14 +396,13 @@ def run_gpu_batched(args, w, rank, world, local_rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (seeded power-law graph, uniform sources and keys)",
-            "config": {"workload": args.workload, "V": g.V, "E": g.E, "queries": nq, "sources": src_rows,
-                       "key_rows": key_rows, "wave_rows": waves["wave_rows"], "waves": len(bt.waves),
-                       "graph_kernels": kernels, "l2": "inputs larger than L2",
-                       "parallelism": f"replicas{world}"},
+            "config": batched_config(args, g, queries, world),
+            "batch": {"wave_rows": waves["wave_rows"], "waves": len(bt.waves), "graph_kernels": kernels},
             "queries_per_s": {"plain": value, "learned": learned["queries_per_s"] if learned else None},
             "learned_picker": learned, "autotune": {"planner": setting, "waves": waves},
             "results": {"count_sum": int(counts.sum()), "checked_against_solo": len(chk)},
-            "roofline": None, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+            "roofline": None, "cpu_baseline": cpu, "parity": parity, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -429,7 +443,7 @@ def run_reference(args, w, rank, world):
             "unit": "Gsrc-edges/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": min(args.warmup, 1),
             "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded power-law graph, uniform sources)",
-            "config": {"workload": args.workload, "V": g.V, "E": g.E, "S": S, "hops": [k0, k1]},
+            "config": pattern_config(args, g, w, args.gpus),
             "cpu_baseline": {"value": value, "unit": "Gsrc-edges/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "Gsrc-edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -506,7 +520,8 @@ def run_gpu(args, w, rank, world, local_rank):
     clocks = ClockSampler(local_rank)
     launches0 = vs.kernel_launches()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    pull_ms, pull_bytes, pull_comp = 0.0, 0.0, 0.0
+    pull_ms, pull_comp, pull_launches = 0.0, 0.0, 0
+    pull_hop_ms = {}
     W = (Sa + 63) // 64
     W += W & 1
     torch.cuda.nvtx.range_push("timed")
@@ -517,14 +532,12 @@ def run_gpu(args, w, rank, world, local_rank):
         for h in range(1, st["hops_run"] + 1):
             if st["strategy"][h] == vs.STRAT_PULL:
                 pull_ms += st["pull_ms"][h]
-                if stA["short_pull"][h]:
-                    args_sh = (g.V, W, stA["active_edges"][h], stA["short_edges"][h],
-                               stA["active_vertices"][h - 1], stA["strategy"][h - 1] != vs.STRAT_PULL, True, False)
-                    pull_bytes += short_bytes(*args_sh)
-                    pull_comp += short_bytes(*args_sh, gathers=False)
-                else:
-                    pull_bytes += expand_bytes(g.V, W, stA["active_edges"][h], True, False)
-                    pull_comp += expand_bytes(g.V, W, stA["active_edges"][h], True, False, gathers=False)
+                pull_hop_ms[h] = pull_hop_ms.get(h, 0.0) + st["pull_ms"][h]
+                pull_launches += 1
+                # compulsory bytes of the hop: CSR offsets, the
+                # active in-list entries and P = 4 passes over the V x S
+                # matrices (frontier read, next layer write, visited read + write)
+                pull_comp += expand_bytes(g.V, W, stA["active_edges"][h], True, False, gathers=False)
     ev1.record(stream)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
@@ -615,36 +628,53 @@ def run_gpu(args, w, rank, world, local_rank):
             dist.destroy_process_group()
         return
     peak, peak_kind = peaks()
-    achieved = pull_bytes / (pull_ms / 1e3) / 1e9 if pull_ms else None
-    rl_kernel = "k_pull_short" if any(stA["short_pull"][1:]) else "k_pull"
+    achieved = pull_comp / (pull_ms / 1e3) / 1e9 if pull_ms else None
+    short_hops = [h for h in range(1, len(stA["short_pull"])) if stA["short_pull"][h]]
+    rl_kernel = "k_pull_short" if short_hops else "k_pull"
+    traffic = profiled_traffic(args.workload, rl_kernel)
+    per_launch_ms = pull_ms / max(1, pull_launches)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if achieved else None, "traffic": profiled_traffic(args.workload, rl_kernel),
+                "frac": achieved / peak if achieved else None,
+                "bytes": "compulsory bytes per PULL hop, 8(V+1) + 4 E_act + 4 * 8W V (CSR offsets, active "
+                         "in-list entries, frontier read, next-layer write, visited read + write), E_act exact "
+                         "from the stats pass",
+                "bytes_per_launch": pull_comp / max(1, pull_launches),
+                "traffic": traffic,
+                "dram_frac": (traffic / (per_launch_ms / 1e3) / 1e9) / peak if traffic and per_launch_ms else None,
                 "traffic_source": f"profiles/{rl_kernel}_{args.workload}.md (ncu dram__bytes_read.sum + "
                                   "dram__bytes_write.sum per working launch)",
-                "kernel": ("k_pull, short mode on hops " + str([h for h in range(1, len(stA["short_pull"]))
-                                                             if stA["short_pull"][h]]) + " (expand A, pull hops)"
-                           if any(stA["short_pull"][1:]) else "k_pull (expand A, pull hops)"), "peak_source": peak_kind,
-                "compulsory_frac": (pull_comp / (pull_ms / 1e3) / 1e9) / peak if pull_ms else None,
-                "per_launch_ms": pull_ms / max(1, args.steps * sum(1 for s in stA["strategy"][1:] if s == 1))}
+                "kernel": (f"{rl_kernel} (expand A, PULL hops {sorted(pull_hop_ms)}, short mode on {short_hops})"),
+                "peak_source": peak_kind,
+                "per_launch_ms": per_launch_ms,
+                "per_hop_ms": {str(h): t / args.steps for h, t in sorted(pull_hop_ms.items())}}
     cpu = None
+    parity = None
     if world == 1 and not args.no_cpu:
-        cpu, _ = cpu_baseline(g, w, sa)
+        cpu, ow = cpu_baseline(g, w, sa)
+        # the oracle's sample (the first cpu_S A sources) against the same rows
+        # of the GPU's A result from the timed plan: rows are independent BFSs,
+        # so the sample's matrix is words [0, cpu_S/64) of every GPU column
+        gw = pA.result().download(stream)
+        nw = ow.shape[1]
+        equal = bool(np.array_equal(gw[:, :nw], ow))
+        parity = {"rows": int(w["cpu_S"]), "equal": equal,
+                  "against": f"oracle VExpand(Shortest, {list(ka)}, Forward) from the first {w['cpu_S']} A "
+                             "sources, whole bit matrix (rows x V) compared bit for bit"}
+        del gw
+        if not equal:
+            raise SystemExit("parity: the GPU's A rows differ from the oracle's")
     line = {"metric": "multi-source expand Gsrc-edges/s", "value": value, "unit": "Gsrc-edges/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (seeded power-law graph, uniform sources)",
-            "config": {"workload": args.workload, "V": g.V, "E": g.E, "S_a": Sa, "hops_a": list(ka),
-                       "S_b": Sb, "hops_b": list(kb), "join": "A x B on vertex id, exact count",
-                       "intersect": "triangle closing over out-lists, exact count",
-                       "l2": "inputs larger than L2 (CSR 2.5 GB, 5.1 GB per bit matrix)",
-                       "parallelism": f"replicas{world}"},
+            "config": pattern_config(args, g, w, world),
             "queries_per_s": {"plain": 1000.0 / ms_per_step,
                               "learned": learned["queries_per_s"] if learned else None},
             "learned_picker": learned, "autotune": tuned,
             "results": {"join_count": jc, "triangles": tc, "visited_a": stA["visit_count"],
                         "hops_run_a": stA["hops_run"], "strategies_a": stA["strategy"][1:],
                         "src_edges_per_step": src_edges},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk}
     print(json.dumps(line), flush=True)
     if dist:

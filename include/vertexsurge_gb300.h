@@ -196,7 +196,7 @@ typedef struct vs_expand_stats {
   int32_t strategy[VS_MAX_HOPS + 1];        /* strategy run at hop h */
   float hop_ms[VS_MAX_HOPS + 1];            /* device time of hop h (plans with timing on) */
   float pull_ms[VS_MAX_HOPS + 1];           /* device time of hop h's pull kernels */
-  int32_t short_pull[VS_MAX_HOPS + 1];      /* 1: the PULL of hop h ran in short mode */
+  int32_t short_pull[VS_MAX_HOPS + 1];      /* the PULL of hop h ran in short mode: 1 reading words, 2 slots */
   uint64_t short_rows[VS_MAX_HOPS + 1];     /* rows of layer h short enough for a slot (when a PULL
                                                hop wrote its slots) */
   uint64_t short_edges[VS_MAX_HOPS + 1];    /* active in-edges of hop h's PULL served from a slot */
@@ -278,14 +278,16 @@ int vs_hash_join(vs_table_ref a, vs_table_ref b, int only_count, uint64_t max_ro
  * where an allocation mid-query could fail under memory pressure, take the
  * driver's allocation lock or synchronise the device and stall other work.
  * keys_a / keys_b are device arrays of na / nb keys (VS_T_VID = uint32,
- * VS_T_I64 = int64); *count (host or device memory) receives
+ * VS_T_I64 = int64; a host pointer is refused with VS_ERR_ARG before any
+ * launch); *count (host or device memory) receives
  * sum_k multiplicity_a(k) * multiplicity_b(k), the same number as
  * vs_hash_join(only_count = 1) on tables holding these key columns.
  * The hash table lives in a fixed device array of this library: 2^19 slots,
  * 8 MiB per GPU, held from the first call on that GPU until process exit.
  * The smaller side may have at most 262,144 rows; larger inputs are rejected
  * with VS_ERR_CAPACITY before any work is queued.  The first call on a device
- * looks up the array's device address (make it before any stream capture).
+ * looks up the array's device address (make it before any stream capture);
+ * after cudaDeviceReset the next call looks it up again.
  * Every call reuses the same array and clears the part it needs: calls whose
  * work overlaps on the GPU (concurrent streams, or host threads sharing a
  * device) race on it and must be serialised by the caller. */

@@ -6,7 +6,10 @@ records, in order, the input schemas, the std::vector literals, the shapes of
 the matrices the test builds (Dense*Matrix(rows, cols)), the operator
 constructor arguments and every asserted value (EXPECT_EQ).
 
-    python tests/golden/make_known_answers.py /root/reference
+    python tests/golden/make_known_answers.py <reference checkout>
+
+The reference checkout is a required argument: the script has no default
+location for it.
 """
 import json
 import re
@@ -70,4 +73,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_known_answers.py <reference checkout>")
+    main(sys.argv[1])

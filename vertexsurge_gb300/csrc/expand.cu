@@ -2177,7 +2177,7 @@ int vs_expand_plan_stats(vs_expand_plan *pl, vs_expand_stats *stats, vs_stream_t
     stats->active_edges[i] = h.hop[i].active_edges;
     stats->pairs[i] = h.hop[i].pairs;
     stats->strategy[i] = h.hop[i].strategy;
-    stats->short_pull[i] = h.hop[i].short_pull;
+    stats->short_pull[i] = h.hop[i].short_pull ? (h.hop[i].short_slots ? 2 : 1) : 0;
     stats->short_rows[i] = h.hop[i].short_rows & 0xFFFFFFFFull;
     stats->tiny_rows[i] = h.hop[i].short_rows >> 32;
     stats->short_edges[i] = h.hop[i].short_edges;

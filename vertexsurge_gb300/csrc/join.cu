@@ -449,7 +449,10 @@ constexpr uint64_t NOALLOC_WORDS = 2 * (NOALLOC_SLOTS + 1) + 1;
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[NOALLOC_WORDS];
 
 // Device address of the array, looked up once per device with that device
-// current (host code may not use the symbol itself as a device pointer).
+// current (host code may not use the symbol itself as a device pointer).  A
+// cached address is checked against the runtime before use: after
+// cudaDeviceReset the device's context, and with it the array, is new, and
+// the address is looked up again.
 int noalloc_scratch(unsigned long long **out) {
   static std::mutex mu;
   static unsigned long long *addr[128] = {};
@@ -457,6 +460,14 @@ int noalloc_scratch(unsigned long long **out) {
   VS_CK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 128) return fail(VS_ERR_UNSUPPORTED, "device index %d out of range", dev);
   std::lock_guard<std::mutex> lock(mu);
+  if (addr[dev]) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, addr[dev]) != cudaSuccess || at.type != cudaMemoryTypeDevice ||
+        at.device != dev) {
+      cudaGetLastError();  // a stale address is not an error of this call
+      addr[dev] = nullptr;
+    }
+  }
   if (!addr[dev]) {
     void *p = nullptr;
     VS_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
@@ -577,6 +588,14 @@ int vs_hash_join_count_noalloc(const void *keys_a, uint64_t na, const void *keys
     return fail(VS_ERR_ARG, "vs_hash_join_count_noalloc: null argument");
   if (key_type != VS_T_VID && key_type != VS_T_I64)
     return fail(VS_ERR_ARG, "vs_hash_join_count_noalloc: unknown key type %d", key_type);
+  // the kernels read the keys directly: a host pointer is refused before any launch
+  for (const void *p : {na ? keys_a : nullptr, nb ? keys_b : nullptr}) {
+    if (!p) continue;
+    cudaPointerAttributes at{};
+    VS_CK(cudaPointerGetAttributes(&at, p));
+    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+      return fail(VS_ERR_ARG, "vs_hash_join_count_noalloc: keys_a and keys_b must be device memory");
+  }
   const bool build_a = na < nb;
   const void *bk = build_a ? keys_a : keys_b, *pk = build_a ? keys_b : keys_a;
   const uint64_t nbld = build_a ? na : nb, nprb = build_a ? nb : na;

@@ -475,6 +475,8 @@ def run_gpu(args, w, rank, world, local_rank):
     t0 = time.time()
     tc = args.tune_cache or None
     tA = autotune.tune(dg, sa, ka[0], ka[1], "shortest", "forward", stream=stream, cache_file=tc)
+    if args.expand_a:
+        tA = dict(tA, **json.loads(args.expand_a))
     tB = autotune.tune(dg, sb, kb[0], kb[1], "shortest", "forward", stream=stream, cache_file=tc)
     tP = autotune.tune(dg, sa, 1, 1, "any", "forward", stream=stream, cache_file=tc)
     tuned = {k: {x: t.get(x, 0.0) for x in ("pull_kind", "sparse_frac", "hub_threshold", "slice_words",
@@ -550,6 +552,28 @@ def run_gpu(args, w, rank, world, local_rank):
         ms = float(t.item())
     ms_per_step = ms / args.steps
     value = world * src_edges * args.steps / (ms / 1e3) / 1e9
+
+    # expand A alone with each short-mode kernel (the next target's visited
+    # words and flag loaded ahead, and not: pull kernel bit 2), per-hop
+    # CUDA-event times of the PULL hops
+    short_kernels = None
+    if any(stA["short_pull"][1:]):
+        short_kernels = {}
+        kind0 = int(tA.get("pull_kind", 0))
+        for name, kind in (("preload", kind0 & 3), ("no_preload", (kind0 & 3) | 4)):
+            pA.set_pull_kernel(kind)
+            per_hop = {}
+            for _ in range(3):
+                pA.run(dA, stream=stream)
+            for _ in range(5):
+                pA.run(dA, stream=stream)
+                sth = pA.stats(stream)
+                for h in range(1, sth["hops_run"] + 1):
+                    if sth["strategy"][h] == vs.STRAT_PULL:
+                        per_hop[str(h)] = per_hop.get(str(h), 0.0) + sth["pull_ms"][h] / 5
+            short_kernels[name] = per_hop
+        pA.set_pull_kernel(kind0)
+        pA.run(dA, stream=stream)  # the result the parity check reads comes from the tuned kernel
 
     # e2e: one-shot C-ABI calls, sources from pinned host memory, counts read back
     pA.set_tuning(timing=False)
@@ -675,7 +699,7 @@ def run_gpu(args, w, rank, world, local_rank):
                         "hops_run_a": stA["hops_run"], "strategies_a": stA["strategy"][1:],
                         "src_edges_per_step": src_edges},
             "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clk}
+            "clocks": clk, "short_kernels_ms": short_kernels}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -691,6 +715,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--tune-cache", default="", help="JSON file of autotuner results (read if present, "
                     "written otherwise)")
+    ap.add_argument("--expand-a", default="", help="JSON object overriding tuned knobs of expand A "
+                    "(pull_kind, sparse_frac, hub_threshold, slice_words, short_share), e.g. for profiling")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

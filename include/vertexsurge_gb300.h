@@ -172,7 +172,7 @@ typedef struct vs_expand_params {
   uint32_t hub_threshold;  /* in-degree above which a vertex gets a whole CTA (0 = tuned default) */
   uint32_t slice_words;    /* source words per pass (0 = whole row up to 256 words) */
   uint64_t pair_capacity;  /* sparse (vertex, source) list capacity (0 = default) */
-  int32_t pull_kernel;     /* PULL kernel shape 0..3, see vs_expand_plan_set_pull_kernel */
+  int32_t pull_kernel;     /* PULL kernel shape 0..7, see vs_expand_plan_set_pull_kernel */
   int32_t reserved;
   double sparse_frac;      /* fixed planner: SPARSE while pair-list edges < this x E (0 = 0.02) */
   double short_share;      /* short-mode PULL: rows of the frontier with few bits (at most 15, or 31
@@ -422,9 +422,11 @@ int vs_expand_plan_set_row_limits(vs_expand_plan *plan, const uint8_t *row_kmax,
  * row limit. */
 int vs_expand_plan_set_row_limits_device(vs_expand_plan *plan, const uint8_t *row_kmax, uint32_t n,
                                          vs_stream_t stream);
-/* Kernel shape of PULL hops (the autotuner's knob): kind 0..3, bit 0 = eight
+/* Kernel shape of PULL hops (the autotuner's knob): kind 0..7, bit 0 = eight
  * resident 256-thread blocks per SM, bit 1 = L2 cache policies that keep
- * frontier rows and stream everything else.  Results never depend on it. */
+ * frontier rows and stream everything else, bit 2 = short-mode hops without
+ * loading the next target's visited words and flag ahead.  Results never
+ * depend on it. */
 int vs_expand_plan_set_pull_kernel(vs_expand_plan *plan, int kind);
 /* Feature logging: when on, every run records the 32 features of each hop;
  * vs_expand_plan_features copies (VS_MAX_HOPS + 1) x 32 floats (row h = hop h). */

@@ -832,11 +832,14 @@ __device__ __forceinline__ bool write_short(const PullArgs &a, uint32_t v, const
 // Fused epilogue for the row of v held by lanes 0..L-1 after the group reduction:
 // visited AND-NOT + update, accumulator OR, next-layer write (and its slot),
 // flag, counters.
-template <int L, int UPL, int H>
+// PRE: the visited words of the row (vpre, lanes 0..L-1) and the row's
+// next-layer flag (oldf_pre) were loaded ahead by the caller.
+template <int L, int UPL, int H, bool PRE = false>
 __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> &pol, uint32_t v,
                                               const uint32_t q0, const uint32_t qn, uint4 (&acc)[UPL],
                                               unsigned long long &nb, unsigned long long &nv,
-                                              unsigned long long &ns) {
+                                              unsigned long long &ns, const uint4 *vpre = nullptr,
+                                              uint32_t oldf_pre = 0) {
   const int lane = threadIdx.x & 31;
   const bool leader_group = lane < L;
   bool any = false;
@@ -852,7 +855,7 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
           x = make_uint4(x.x & m.x, x.y & m.y, x.z & m.z, x.w & m.w);
         }
         if (a.shortest && nz4(x)) {
-          const uint4 vv = pol.ld_rw(a.vis + idx);
+          const uint4 vv = PRE ? vpre[k] : pol.ld_rw(a.vis + idx);
           x = andnot4(x, vv);
           if (nz4(x)) pol.st(a.vis + idx, or4(vv, x));
         }
@@ -870,7 +873,7 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
   if (!a.multislice && a.last) {
     // layer k_max is not kept: clear the rows an earlier layer left in this
     // buffer, so the next run finds it clean (a flag-2 row is zero already)
-    const uint32_t oldf = a.flagN[v];
+    const uint32_t oldf = PRE ? oldf_pre : a.flagN[v];
     if (leader_group && oldf == 1) {
 #pragma unroll
       for (int k = 0; k < UPL; k++) {
@@ -883,7 +886,7 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
       if (rownz) nv++;
     }
   } else if (!a.multislice) {
-    const uint32_t oldf = a.flagN[v];  // 1: the buffer row holds an older layer's bits
+    const uint32_t oldf = PRE ? oldf_pre : a.flagN[v];  // 1: the buffer row holds an older layer's bits
     bool virt = false;                 // the row is left in its slot only (flag 2)
     if (a.tiny_out) {  // every vertex gets a tiny word: the count is 0 for an empty row
       if (rownz)
@@ -956,8 +959,10 @@ __device__ __forceinline__ void pull_vertices(const PullArgs &a) {
 
 // Short mode (one slice).  Software-pipelined over the warp's targets: while
 // target v is processed, the next target's list bounds, first 32
-// in-neighbours and their tiny words are already in flight.
-template <int L, int UPL>
+// in-neighbours and their tiny words are already in flight.  PRE: so are the
+// next target's visited words (in registers of lanes 0..L-1) and its
+// next-layer flag, which the epilogue would otherwise wait for.
+template <int L, int UPL, bool PRE = false>
 __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
   const L2Pol<0> pol;
   __shared__ uint32_t s_u[8][32];
@@ -980,6 +985,17 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
   uint4 ps[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};  // ... or its slot's first chunk (slot mode)
   bool pact = false;
   const uint32_t sq = a.slot_n / 8;  // uint4 per slot
+  uint4 vpre[UPL];       // PRE: visited words of v held by lanes 0..L-1
+  uint32_t oldf = 0;     // PRE: next-layer flag of v
+#pragma unroll
+  for (int k = 0; k < UPL; k++) vpre[k] = make_uint4(0, 0, 0, 0);
+  if (PRE && v < a.V) {
+    oldf = a.flagN[v];
+    if (a.shortest && lane < L)
+#pragma unroll
+      for (int k = 0; k < UPL; k++)
+        if (lane + k * L < qn) vpre[k] = pol.ld_rw(a.vis + (size_t)v * a.Q + lane + k * L);
+  }
   if (v < a.V) {
     beg = __ldg(off0 + v);
     end = __ldg(off0 + v + 1);
@@ -1007,9 +1023,20 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
     Tiny ptn = 0;
     uint4 psn[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
     const bool pactn = nbeg + lane < nend;
+    uint4 vpren[UPL];
+    uint32_t oldfn = 0;
+#pragma unroll
+    for (int k = 0; k < UPL; k++) vpren[k] = make_uint4(0, 0, 0, 0);
+    if (PRE && vn < a.V) {  // the next target's visited words and flag, in flight during v
+      oldfn = a.flagN[vn];
+      if (a.shortest && lane < L)
+#pragma unroll
+        for (int k = 0; k < UPL; k++)
+          if (lane + k * L < qn) vpren[k] = pol.ld_rw(a.vis + (size_t)vn * a.Q + lane + k * L);
+    }
     if (!(a.hub_threshold && d > (int64_t)a.hub_threshold)) {  // hubs: k_pull_hub_short
       if (lane == 0) {  // the epilogue's read-modify-write rows, fetched while the gather runs
-        if (a.shortest) prefetch_l2(a.vis + (size_t)v * a.Q, qn * 16);
+        if (a.shortest && !PRE) prefetch_l2(a.vis + (size_t)v * a.Q, qn * 16);
         if (a.acc_on) prefetch_l2(a.acc + (size_t)v * a.Q, qn * 16);
       }
       uint4 acc[UPL];
@@ -1045,7 +1072,7 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
           ptn = ld_keep(a.tiny_in + pun);
         }
       }
-      pull_epilogue<L, UPL, 0>(a, pol, v, 0, qn, acc, nb, nv, ns);
+      pull_epilogue<L, UPL, 0, PRE>(a, pol, v, 0, qn, acc, nb, nv, ns, vpre, oldf);
     } else if (pactn) {
       pun = __ldg(adj0 + nbeg + lane);
       if (slotmode) {
@@ -1062,6 +1089,9 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
     ps[0] = psn[0];
     ps[1] = psn[1];
     pact = pactn;
+    oldf = oldfn;
+#pragma unroll
+    for (int k = 0; k < UPL; k++) vpre[k] = vpren[k];
   }
   pull_counters(a, nb, nv, ns, se);
 }
@@ -1076,8 +1106,15 @@ __global__ void __launch_bounds__(256, MINB) k_pull(PullArgs a) {
 // of the dense kernels' budget)
 template <int L, int UPL>
 __global__ void __launch_bounds__(256, UPL >= 4 ? 2 : 5) k_pull_short(PullArgs a) {
-  if (a.ctr->hop[a.h].strategy != ST_PULL || !a.ctr->hop[a.h].short_pull || !a.tiny_in) return;
+  if (a.ctr->hop[a.h].strategy != ST_PULL || !a.ctr->hop[a.h].short_pull || !a.tiny_in || a.pre) return;
   pull_vertices_short<L, UPL>(a);
+}
+
+// ... with the visited words and flag of the next target loaded ahead
+template <int L, int UPL>
+__global__ void __launch_bounds__(256, UPL >= 4 ? 2 : 4) k_pull_short_pre(PullArgs a) {
+  if (a.ctr->hop[a.h].strategy != ST_PULL || !a.ctr->hop[a.h].short_pull || !a.tiny_in || !a.pre) return;
+  pull_vertices_short<L, UPL, true>(a);
 }
 
 // Hub vertices (in-degree above the threshold): one 512-thread CTA per vertex,
@@ -1530,11 +1567,12 @@ using PullFn = void (*)(PullArgs);
 struct PullVariant {
   int L, UPL;
   PullFn pull[4], hub;  // pull[k]: bit 0 = 8 blocks per SM, bit 1 = L2 cache policies
-  PullFn pull_short, hub_short;
+  PullFn pull_short, hub_short, pull_short_pre;
 };
 
 #define VS_PULLS(L, U) {k_pull<L, U, 1, 0>, k_pull<L, U, 8, 0>, k_pull<L, U, 1, 1>, k_pull<L, U, 8, 1>}
-#define VS_VARIANT(L, U) {L, U, VS_PULLS(L, U), k_pull_hub<L, U>, k_pull_short<L, U>, k_pull_hub_short<L, U>}
+#define VS_VARIANT(L, U) \
+  {L, U, VS_PULLS(L, U), k_pull_hub<L, U>, k_pull_short<L, U>, k_pull_hub_short<L, U>, k_pull_short_pre<L, U>}
 const PullVariant kVariants[] = {
     VS_VARIANT(1, 1),  VS_VARIANT(2, 1),  VS_VARIANT(4, 1),  VS_VARIANT(8, 1), VS_VARIANT(16, 1),
     VS_VARIANT(32, 1), VS_VARIANT(32, 2), VS_VARIANT(32, 4), VS_VARIANT(32, 8),
@@ -1573,7 +1611,7 @@ struct vs_expand_plan {
   uint32_t nhubs = 0, hub_threshold = 0;
   bool use_vis = false, use_acc = false, clear_diag = false;
   bool collect_stats = false;
-  int grid_pull = 0, grid_hub = 0, grid_sparse = 0, grid_v = 0, grid_push = 0, grid_short = 0;
+  int grid_pull = 0, grid_hub = 0, grid_sparse = 0, grid_v = 0, grid_push = 0, grid_short = 0, grid_short_pre = 0;
   vs_bitmat result{};
   bool has_result = false;
   // tuning knobs of the fixed planner
@@ -1771,7 +1809,7 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
     return fail(VS_ERR_ARG, "unknown direction %d", p->direction);
   if (p->strategy < VS_STRAT_AUTO || p->strategy > VS_STRAT_SPARSE)
     return fail(VS_ERR_ARG, "unknown strategy %d", p->strategy);
-  if (p->pull_kernel < 0 || p->pull_kernel > 3) return fail(VS_ERR_ARG, "pull kernel variant must be 0..3");
+  if (p->pull_kernel < 0 || p->pull_kernel > 7) return fail(VS_ERR_ARG, "pull kernel variant must be 0..7");
   if (p->sparse_frac < 0) return fail(VS_ERR_ARG, "sparse_frac must be >= 0");
   if (S == 0) return fail(VS_ERR_ARG, "no start vertex for VExpand");
   cudaStream_t st = 0;
@@ -1873,12 +1911,13 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   const PullVariant &var = pick_variant(pl->qslice);
   const int hub_smem = 16 * 32 * 16 * var.UPL;
   if (hub_smem > 48 * 1024) cudaFuncSetAttribute(var.hub, cudaFuncAttributeMaxDynamicSharedMemorySize, hub_smem);
-  pl->grid_pull = occupancy_grid(var.pull[pl->pull_kind], 256, 0, 8);
+  pl->grid_pull = occupancy_grid(var.pull[pl->pull_kind & 3], 256, 0, 8);
   pl->grid_hub = std::max(1, std::min((int)pl->nhubs, occupancy_grid(var.hub, 512, hub_smem, 2)));
   if (pl->slot[0]) {  // short mode: a row of Q uint4 per warp (PULL) or per CTA (hubs)
     const int hs = hub_smem + (int)pl->Q * 16;
     if (hs > 48 * 1024) cudaFuncSetAttribute(var.hub_short, cudaFuncAttributeMaxDynamicSharedMemorySize, hs);
     pl->grid_short = occupancy_grid(var.pull_short, 256, 8 * (size_t)pl->Q * 16, 8);
+    pl->grid_short_pre = occupancy_grid(var.pull_short_pre, 256, 8 * (size_t)pl->Q * 16, 8);
   }
   pl->grid_sparse = occupancy_grid(k_sparse, 256, 0, 8);
   pl->grid_push = occupancy_grid(k_push, 256, 0, 8);
@@ -2099,6 +2138,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     a.tiny_out = keep_short ? pl->tiny[nbuf] : nullptr;
     a.slot_out = keep_short ? pl->slot[nbuf] : nullptr;
     a.slot_n = pl->slot_n;
+    a.pre = (pl->pull_kind & 4) == 0;
     if (timing) cudaEventRecord(pl->ev[3 * h + 1], st);
     if (pl->slot[0]) {  // words and slots of a layer SPARSE, PUSH or the seed wrote, when this hop reads them
       { k_pairs_zero<<<pl->grid_v, 256, 0, st>>>(pl->touched, V, pl->ctr, h); vs::note_launch(); }
@@ -2109,11 +2149,14 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
       { k_slot_build<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<const uint4 *>(pl->buf[fb]), V, Q,
                                                pl->tiny[fb], pl->slot[fb], pl->slot_n, pl->ctr, h); vs::note_launch(); }
     }
-    { var.pull[pl->pull_kind]<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a); vs::note_launch(); }
+    { var.pull[pl->pull_kind & 3]<<<dim3(pl->grid_pull, pl->nslices), 256, 0, st>>>(a); vs::note_launch(); }
     if (pl->nhubs)
       { var.hub<<<dim3(pl->grid_hub, pl->nslices), 512, 16 * 32 * 16 * var.UPL, st>>>(a); vs::note_launch(); }
     if (pl->slot[0]) {
-      { var.pull_short<<<pl->grid_short, 256, 8 * (size_t)Q * 16, st>>>(a); vs::note_launch(); }
+      if (a.pre)
+        { var.pull_short_pre<<<pl->grid_short_pre, 256, 8 * (size_t)Q * 16, st>>>(a); vs::note_launch(); }
+      else
+        { var.pull_short<<<pl->grid_short, 256, 8 * (size_t)Q * 16, st>>>(a); vs::note_launch(); }
       if (pl->nhubs)
         { var.hub_short<<<pl->grid_hub, 512, 16 * 32 * 16 * var.UPL + (size_t)Q * 16, st>>>(a); vs::note_launch(); }
     }
@@ -2278,12 +2321,14 @@ int vs_expand_plan_set_row_limits_device(vs_expand_plan *pl, const uint8_t *row_
 
 // Kernel shape of the PULL hops (chosen by the autotuner): bit 0 asks for 8
 // resident 256-thread blocks per SM (32 registers), bit 1 adds L2 cache
-// policies (streams evict-first, frontier rows evict-last).
+// policies (streams evict-first, frontier rows evict-last), bit 2 runs
+// short-mode hops without loading the next target's visited words and flag
+// ahead.
 int vs_expand_plan_set_pull_kernel(vs_expand_plan *pl, int kind) {
-  if (!pl || kind < 0 || kind > 3) return fail(VS_ERR_ARG, "pull kernel variant must be 0..3");
+  if (!pl || kind < 0 || kind > 7) return fail(VS_ERR_ARG, "pull kernel variant must be 0..7");
   pl->pull_kind = kind;
   const PullVariant &var = pick_variant(pl->qslice);
-  pl->grid_pull = occupancy_grid(var.pull[kind], 256, 0, 8);
+  pl->grid_pull = occupancy_grid(var.pull[kind & 3], 256, 0, 8);
   return VS_OK;
 }
 

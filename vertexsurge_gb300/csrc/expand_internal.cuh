@@ -125,6 +125,7 @@ struct PullArgs {
   uint16_t *slot_out;       // slots of layer h (count, then the ids of a row of < slot_n bits)
   uint32_t slot_n;          // uint16 entries per slot (16, 32 or 64)
   int virt_out;             // short rows of layer h may stay in their slots (flag 2, buffer row zero)
+  int pre;                  // short mode: the next target's visited words and flag are loaded ahead
   uint32_t hub_threshold;
   const uint32_t *hubs;
   uint32_t nhubs;

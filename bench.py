@@ -56,6 +56,10 @@ WORKLOADS = {
                                batched=dict(n=256, s_range=(64, 8192), l_range=(2, 6),
                                             join_rows=(100_000, 10_000_000), waves=(8192, 16384, 32768),
                                             cpu_queries=3, check=6)),
+    # Flat x Flat count-only HashJoin of two uint32 key columns of N rows each,
+    # keys Zipf-skewed over 10M vertex ids (the key tables of the batched workload)
+    "join_zipf10M": dict(kind="join", V=10_000_000, sizes=(100_000, 1_000_000, 10_000_000), skew=1.2, seed=4,
+                         cpu_rows=1_000_000),
     "zipf1M_batched64": dict(kind="zipf", V=1_000_000, E=30_000_000, alpha=2.1, cap=50_000, seed=3,
                              batched=dict(n=64, s_range=(64, 8192), l_range=(2, 6),
                                           join_rows=(100_000, 1_000_000), waves=(8192, 16384, 32768),
@@ -408,6 +412,110 @@ def run_gpu_batched(args, w, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def join_inputs(w, n):
+    from vertexsurge_gb300 import batch
+    rng = np.random.default_rng(w["seed"] + n)
+    perm = rng.permutation(w["V"]).astype(np.uint32)
+    return (batch.zipf_keys(rng, n, w["V"], perm, w["skew"]), batch.zipf_keys(rng, n, w["V"], perm, w["skew"]))
+
+
+def join_bytes(n_build, n_probe):
+    """Algorithmic bytes of a count-only Flat x Flat join of 4-byte keys
+    (SURVEY 8(d) join formula without output): both key columns read, the
+    table cleared (16 B per slot: key and count, capacity the power of two
+    >= 2 N_b, at least 64), one 16-byte insert per build row and at least one
+    32-byte sector per probe."""
+    cap = 64
+    while cap < 2 * n_build:
+        cap *= 2
+    return 4 * n_build + 4 * n_probe + 16 * cap + 16 * n_build + 32 * n_probe
+
+
+def run_join(args, w, rank, world, local_rank, reference=False):
+    """Count-only Flat x Flat HashJoin of two key columns per size."""
+    from oracle import pyoracle as O
+    rows = []
+    if reference:
+        from vertexsurge_gb300 import build as b
+        b.build_oracle()
+        b.build_gen()
+        n = w["cpu_rows"]
+        ka, kb = join_inputs(w, n)
+        ta, tb = O.Table(O.FLAT, [0, 1], cols=[ka, ka]), O.Table(O.FLAT, [2, 1], cols=[kb, kb])
+        times = []
+        for i in range(args.steps + 1):
+            t = time.perf_counter()
+            cnt = O.hash_join(ta, tb, 1, only_count=True)[2]
+            if i:
+                times.append(time.perf_counter() - t)
+        value = 2 * n * args.steps / sum(times) / 1e6
+        line = {"impl": "reference", "metric": "count-only hash join Mrows/s", "value": value, "unit": "Mrows/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": 1, "ms_per_step": 1000 * sum(times) / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                "data": "synthetic (Zipf-skewed vertex-id keys)",
+                "config": {"workload": args.workload, "V": w["V"], "sizes": list(w["sizes"])},
+                "cpu_baseline": {"value": value, "unit": "Mrows/s", "cores": O.lib().oracle_get_threads(),
+                                 "kind": "port", "sample": f"HashJoin count of two {n}-row key columns"},
+                "e2e": {"value": value, "unit": "Mrows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    import torch
+    import vertexsurge_gb300 as vs
+    from vertexsurge_gb300 import build as b
+    b.build_all()
+    torch.cuda.set_device(local_rank)
+    vs.init(local_rank)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    peak, peak_kind = peaks()
+    launches0 = vs.kernel_launches()
+    total_ms = 0.0
+    total_rows = 0
+    clocks = ClockSampler(local_rank)
+    for n in w["sizes"]:
+        ka, kb = join_inputs(w, n)
+        fa, fb = vs.FlatTable.from_columns([ka], stream), vs.FlatTable.from_columns([kb], stream)
+        exp = None
+        for _ in range(args.warmup):
+            _, c, _ = vs.hash_join(fa, fb, 0, 0, only_count=True, stream=stream)
+        # exact count: sum over keys of multiplicity_a * multiplicity_b
+        ua, ca = np.unique(ka, return_counts=True)
+        ub, cb = np.unique(kb, return_counts=True)
+        _, ia, ib = np.intersect1d(ua, ub, assume_unique=True, return_indices=True)
+        exp = int(np.sum(ca[ia].astype(np.int64) * cb[ib].astype(np.int64)))
+        assert c == exp, (n, c, exp)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            vs.hash_join(fa, fb, 0, 0, only_count=True, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        byt = join_bytes(n, n)
+        rows.append({"rows_per_side": n, "ms": ms, "Mrows_per_s": 2 * n / ms / 1e3, "count": c, "bytes": byt,
+                     "GB_per_s": byt / ms / 1e6, "frac": byt / ms / 1e6 / peak})
+        total_ms += ms
+        total_rows += 2 * n
+        fa.free()
+        fb.free()
+    clk = clocks.stop()
+    big = rows[-1]
+    line = {"metric": "count-only hash join Mrows/s", "value": total_rows / total_ms / 1e3, "unit": "Mrows/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (Zipf-skewed vertex-id keys)",
+            "config": {"workload": args.workload, "V": w["V"], "sizes": list(w["sizes"])},
+            "sizes": rows,
+            "roofline": {"bound": "hbm", "achieved": big["GB_per_s"], "peak": peak, "unit": "GB/s",
+                         "frac": big["frac"], "traffic": None, "peak_source": peak_kind,
+                         "bytes": "4 N_b + 4 N_p + 16 cap + 16 N_b + 32 N_p (largest size)"},
+            "cpu_baseline": None, "parity": {"sizes": len(rows), "equal": True,
+                                             "against": "numpy sum of multiplicity products per key"},
+            "e2e": None, "gpu_launches": vs.kernel_launches() - launches0, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, w, rank, world):
     """--impl reference: the oracle (CPU restatement of the reference) on host cores."""
     if rank != 0:
@@ -722,7 +830,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     w = WORKLOADS[args.workload]
-    if args.impl == "reference":
+    if w.get("kind") == "join":
+        if rank == 0 or args.impl != "reference":
+            run_join(args, w, rank, world, local_rank, reference=args.impl == "reference")
+    elif args.impl == "reference":
         run_reference(args, w, rank, world)
     elif "batched" in w:
         run_gpu_batched(args, w, rank, world, local_rank)

@@ -380,6 +380,37 @@ int vs_semi_join(vs_table_ref a, vs_table_ref b, uint32_t nkeys, const uint32_t 
                  const uint32_t *b_key_cols, int only_count, vs_flat **out_flat, vs_bitmat **out_mat,
                  uint64_t *count, vs_stream_t stream);
 
+/* MatrixTableFilter (replaces MatrixTableFilter<F>, big_operators2.hh:53-61,
+ * 142-170, over VarRowMatrixTable::filter / ColMainMatrixTable::filter,
+ * matrix_table.hh:153-200): clears, in place, every bit (r, c) of m for which
+ * the predicate is false, r and c being the row and column VALUES (row_map[r]
+ * and col_map[c] when the maps exist, else the indices).  The reference takes
+ * a host predicate f(r, c); here it is the AND of up to three device forms:
+ *   row_keep   bitset over row values: keep when bit r is set (values at or
+ *              above row_values fail); NULL = no row condition
+ *   col_keep   the same over column values (col_values bits); NULL = none
+ *   pairs      npairs keys (r << 32 | c) sorted ascending (checked; an
+ *              unsorted list is VS_ERR_ARG); pairs_mode 1 keeps only listed
+ *              pairs, 2 drops listed pairs, 0 ignores the list.
+ * The arrays are device or host memory (host arrays are copied in and the
+ * call syncs the stream before returning).  A MultipleMatrixTable is filtered
+ * layer by layer (one call per layer matrix).  With device arrays and no pair
+ * list the call is stream-ordered; a pair list is checked for order with one
+ * host sync. */
+int vs_matrix_filter(vs_bitmat *m, const uint64_t *row_keep, uint32_t row_values, const uint64_t *col_keep,
+                     uint32_t col_values, const uint64_t *pairs, uint64_t npairs, int pairs_mode,
+                     vs_stream_t stream);
+/* Column predicate of the reference's LDBC-FinBench tcr1 plan
+ * (src/objects/testify/ldbc-finbench/tcr1.cpp:46-57, a VertexNeighborFetcher
+ * and a VertexPropertyFetcher): mask bit v (g->V bits, ceil(V/64) words) is
+ * set when some neighbour u of v in g (out-lists for VS_DIR_FORWARD, in-lists
+ * for VS_DIR_BACKWARD) has prop[u] == value.  Vertices of several types share
+ * g's id space (e.g. mediums numbered after the accounts).  prop holds nprop
+ * uint8 values, host or device; a neighbour id >= nprop is VS_ERR_ARG.  mask
+ * is host or device memory; the call syncs the stream once. */
+int vs_vertex_mask_any_neighbor(const vs_graph *g, int direction, const uint8_t *prop, uint32_t nprop,
+                                uint8_t value, uint64_t *mask, vs_stream_t stream);
+
 /* Scan with a range filter (replaces Scan + VariableFilter over a vertex
  * property, big_operators.hh:21-38, scan.cpp:31-70): the vertex ids i < n with
  * lo <= values[i] <= hi, ascending, as one VID column.  values: device array

@@ -845,6 +845,55 @@ uint64_t oracle_matrix_row_or_sum(const or_table *m, uint32_t *out_col) {
   return n;
 }
 
+// MatrixTableFilter<F>::run_internal (big_operators2.hh:142-170): the matrix
+// table's iterators visit every set bit, map the row through row_map and the
+// column through col_map, and clear the bit when f(r, c) is false
+// (matrix_table.hh:153-200).  f is the AND of the device forms.
+uint64_t oracle_matrix_filter(const or_table *m, const uint64_t *row_keep, uint32_t row_values,
+                              const uint64_t *col_keep, uint32_t col_values, const uint64_t *pairs,
+                              uint64_t npairs, int pairs_mode) {
+  auto in_bits = [](const uint64_t *bits, uint32_t n, uint32_t v) {
+    return v < n && ((bits[v >> 6] >> (v & 63)) & 1ull);
+  };
+  auto f = [&](uint32_t r, uint32_t c) {
+    if (row_keep && !in_bits(row_keep, row_values, r)) return false;
+    if (col_keep && !in_bits(col_keep, col_values, c)) return false;
+    if (pairs_mode) {
+      const bool listed = std::binary_search(pairs, pairs + npairs, ((uint64_t)r << 32) | c);
+      if (listed != (pairs_mode == 1)) return false;
+    }
+    return true;
+  };
+  const size_t wpc = mat_wpc(m);
+  uint64_t cleared = 0;
+  for (size_t c = 0; c < m->mcols; c++)
+    for (size_t w = 0; w < wpc; w++) {
+      uint64_t x = m->words[c * wpc + w];
+      while (x) {
+        const unsigned b = (unsigned)std::countr_zero(x);
+        x &= x - 1;
+        const size_t r = w * 64 + b;
+        if (!f(mat_row_value(m, r), mat_col_value(m, c))) {
+          const_cast<uint64_t *>(m->words)[c * wpc + w] &= ~(1ull << b);
+          cleared++;
+        }
+      }
+    }
+  return cleared;
+}
+
+// VertexNeighborFetcher + VertexPropertyFetcher as tcr1.cpp:46-57 uses them.
+void oracle_vertex_mask_any_neighbor(const int64_t *off, const uint32_t *adj, uint32_t V, const uint8_t *prop,
+                                     uint8_t value, uint64_t *mask) {
+  for (size_t i = 0; i < ((size_t)V + 63) / 64; i++) mask[i] = 0;
+  for (uint32_t v = 0; v < V; v++)
+    for (int64_t j = off[v]; j < off[v + 1]; j++)
+      if (prop[adj[j]] == value) {
+        mask[v >> 6] |= 1ull << (v & 63);
+        break;
+      }
+}
+
 // SemiJoin<N>::build / probe_once / probe (semi_join.cpp:58-262).  Key
 // tuples are compared by value (TupleValue equality); std::set stands in for
 // the reference's concurrent set.

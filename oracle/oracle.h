@@ -131,6 +131,23 @@ uint64_t oracle_matrix_row_or_sum(const or_table *m, uint32_t *out_col);
 int oracle_semi_join(const or_table *a, const or_table *b, const int32_t *key_vars, uint32_t N,
                      int only_count, or_result *out, uint64_t *out_words);
 
+/* MatrixTableFilter<F>::run_internal (big_operators2.hh:142-170) over
+ * VarRowMatrixTable::Iterator::filter / ColMainMatrixTable::Iterator::filter
+ * (matrix_table.hh:153-200): every set bit (r, c) of m is mapped through
+ * row_map / col_map and cleared, in place in m->words, when the predicate is
+ * false.  The predicate is the device forms of vs_matrix_filter: row_keep /
+ * col_keep bitsets over values (NULL = no condition; values at or above
+ * row_values / col_values fail) and a sorted (r << 32 | c) pair list, mode 1
+ * keep listed, 2 drop listed, 0 none.  Returns the number of bits cleared. */
+uint64_t oracle_matrix_filter(const or_table *m, const uint64_t *row_keep, uint32_t row_values,
+                              const uint64_t *col_keep, uint32_t col_values, const uint64_t *pairs,
+                              uint64_t npairs, int pairs_mode);
+
+/* tcr1's column predicate (ldbc-finbench/tcr1.cpp:46-57): bit v of mask set
+ * when a neighbour u of v (CSR off[V+1], adj) has prop[u] == value. */
+void oracle_vertex_mask_any_neighbor(const int64_t *off, const uint32_t *adj, uint32_t V, const uint8_t *prop,
+                                     uint8_t value, uint64_t *mask);
+
 /* Thread count used by every parallel region (0 = OpenMP default). */
 void oracle_set_threads(int n);
 int oracle_get_threads(void);

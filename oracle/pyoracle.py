@@ -62,6 +62,11 @@ def lib():
         L.oracle_matrix_row_or_sum.restype = C.c_uint64
         L.oracle_semi_join.argtypes = [C.POINTER(OrTable), C.POINTER(OrTable), C.c_void_p, C.c_uint32, C.c_int,
                                        C.POINTER(OrResult), C.c_void_p]
+        L.oracle_matrix_filter.argtypes = [C.POINTER(OrTable), C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
+                                           C.c_void_p, C.c_uint64, C.c_int]
+        L.oracle_matrix_filter.restype = C.c_uint64
+        L.oracle_vertex_mask_any_neighbor.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint8,
+                                                      C.c_void_p]
         L.oracle_set_threads.argtypes = [C.c_int]
         L.oracle_get_threads.restype = C.c_int
         _lib = L
@@ -249,3 +254,21 @@ def semi_join(a: Table, b: Table, key_vars, only_count=False):
     count = int(r.count)
     var, cols, _ = _result(r)
     return var, cols, count
+
+
+def matrix_filter(m: Table, row_keep=None, row_values=0, col_keep=None, col_values=0, pairs=None, pairs_mode=0):
+    """MatrixTableFilter in place on m.words; returns the number of bits cleared."""
+    rk = None if row_keep is None else np.ascontiguousarray(row_keep, dtype=np.uint64)
+    ck = None if col_keep is None else np.ascontiguousarray(col_keep, dtype=np.uint64)
+    pk = None if pairs is None else np.ascontiguousarray(pairs, dtype=np.uint64)
+    return int(lib().oracle_matrix_filter(C.byref(m.t), _p(rk), int(row_values), _p(ck), int(col_values), _p(pk),
+                                          0 if pk is None else len(pk), int(pairs_mode)))
+
+
+def vertex_mask_any_neighbor(off, adj, V, prop, value):
+    mask = np.zeros((V + 63) // 64, np.uint64)
+    o = np.ascontiguousarray(off, dtype=np.int64)
+    a = np.ascontiguousarray(adj, dtype=np.uint32)
+    pr = np.ascontiguousarray(prop, dtype=np.uint8)
+    lib().oracle_vertex_mask_any_neighbor(_p(o), _p(a), int(V), _p(pr), int(value), _p(mask))
+    return mask

@@ -97,3 +97,66 @@ def test_semi_join_one_key_against_a_matrix():
     ta2 = O.Table(O.FLAT, [A], cols=[a % 40])
     present_r = set(np.nonzero(m2.any(axis=1))[0].tolist())
     assert O.semi_join(ta2, tb, [A], only_count=True)[2] == sum(int(x) in present_r for x in a % 40)
+
+
+def value_bits(values, universe):
+    """A bitset (uint64 words) over `universe` values with the given values set."""
+    bits = np.zeros((universe + 63) // 64, np.uint64)
+    for v in values:
+        if v < universe:
+            bits[v >> 6] |= np.uint64(1) << np.uint64(v & 63)
+    return bits
+
+
+@pytest.mark.parametrize("kind", [O.VARROW, O.COLMAIN])
+def test_matrix_filter(kind):
+    """MatrixTableFilter (big_operators2.hh:142-170): a bit (r, c) survives when
+    the predicate holds on its mapped (row value, column value), checked against
+    a Python loop over the set bits (the reference has no filter test)."""
+    rng = np.random.default_rng(11)
+    rows, cols = 130, 300
+    m = rand_matrix(rng, rows, cols, 0.08)
+    rmap = rng.permutation(5000)[:rows].astype(np.uint32)
+    cmap = rng.permutation(7000)[:cols].astype(np.uint32)
+    rkeep = set(rng.choice(rmap, rows // 2, replace=False).tolist())
+    ckeep = set(rng.choice(cmap, cols // 3, replace=False).tolist())
+    bits = [(int(rmap[r]), int(cmap[c])) for r, c in zip(*np.nonzero(m))]
+    listed = sorted({(r << 32) | c for r, c in bits[::3]} | {(4999 << 32) | 1})
+    listed_set = set(listed)
+    cases = [dict(row_keep=value_bits(rkeep, 5000), row_values=5000),
+             dict(col_keep=value_bits(ckeep, 7000), col_values=7000),
+             dict(col_keep=value_bits(ckeep, 6000), col_values=6000),  # values >= 6000 fail
+             dict(pairs=np.array(listed, np.uint64), pairs_mode=1),
+             dict(pairs=np.array(listed, np.uint64), pairs_mode=2),
+             dict(row_keep=value_bits(rkeep, 5000), row_values=5000, col_keep=value_bits(ckeep, 7000),
+                  col_values=7000, pairs=np.array(listed, np.uint64), pairs_mode=2)]
+    for kw in cases:
+        t = O.Table(kind, [A, B], words=bool_to_words(m), mrows=rows, mcols=cols, row_map=rmap, col_map=cmap)
+
+        def keep(r, c):
+            if "row_keep" in kw and not (r < kw["row_values"] and r in rkeep):
+                return False
+            if "col_keep" in kw and not (c < kw["col_values"] and c in ckeep):
+                return False
+            if kw.get("pairs_mode"):
+                return (((r << 32) | c) in listed_set) == (kw["pairs_mode"] == 1)
+            return True
+
+        exp = np.zeros_like(m)
+        for r, c in zip(*np.nonzero(m)):
+            exp[r, c] = keep(int(rmap[r]), int(cmap[c]))
+        cleared = O.matrix_filter(t, **kw)
+        assert np.array_equal(t.words, bool_to_words(exp))
+        assert cleared == int(m.sum() - exp.sum())
+
+
+def test_vertex_mask_any_neighbor():
+    rng = np.random.default_rng(12)
+    V, n_other = 400, 90
+    deg = rng.integers(0, 6, V)
+    off = np.concatenate([[0], np.cumsum(deg)]).astype(np.int64)
+    adj = rng.integers(0, n_other, int(off[-1])).astype(np.uint32)
+    prop = (rng.random(n_other) < 0.2).astype(np.uint8)
+    mask = O.vertex_mask_any_neighbor(off, adj, V, prop, 1)
+    exp = [v for v in range(V) if any(prop[u] == 1 for u in adj[off[v]:off[v + 1]])]
+    assert np.array_equal(mask, value_bits(exp, V))

@@ -173,6 +173,10 @@ _SIGS += [
                                C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_void_p]),
     ("vs_expand_plan_features", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("vs_release_cached", C.c_int, []),
+    ("vs_matrix_filter", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                                   C.c_uint64, C.c_int, C.c_void_p]),
+    ("vs_vertex_mask_any_neighbor", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_uint32, C.c_uint8,
+                                              C.c_void_p, C.c_void_p]),
 ]
 
 # internal entry points (not part of the header)
@@ -708,6 +712,34 @@ def matrix_row_or_sum(m: "BitMatrix", stream=None) -> "FlatTable":
     out = C.c_void_p()
     check(lib().vs_matrix_row_or_sum(m.h, C.byref(out), _stream(stream)))
     return FlatTable(out)
+
+
+def matrix_filter(m: "BitMatrix", row_keep=None, row_values=0, col_keep=None, col_values=0, pairs=None,
+                  pairs_mode=0, stream=None):
+    """MatrixTableFilter in place: keep bit (r, c) when row value r is in the row_keep
+    bitset, column value c in the col_keep bitset and (r, c) passes the pair list
+    (pairs_mode 1: listed pairs only, 2: all but listed; keys r << 32 | c, sorted).
+    Arrays: numpy uint64 (host, copied in by the call) or torch device tensors."""
+    def arr(x):
+        return None if x is None or hasattr(x, "data_ptr") else np.ascontiguousarray(x, dtype=np.uint64)
+
+    rk = row_keep if hasattr(row_keep, "data_ptr") else arr(row_keep)
+    ck = col_keep if hasattr(col_keep, "data_ptr") else arr(col_keep)
+    pk = pairs if hasattr(pairs, "data_ptr") else arr(pairs)
+    npairs = 0 if pk is None else (int(pk.numel()) if hasattr(pk, "numel") else len(pk))
+    check(lib().vs_matrix_filter(m.h, _ptr(rk), int(row_values), _ptr(ck), int(col_values), _ptr(pk), npairs,
+                                 int(pairs_mode), _stream(stream)))
+
+
+def vertex_mask_any_neighbor(graph: "DeviceGraph", prop, value: int, direction="forward", stream=None):
+    """Bitset (numpy uint64, ceil(V/64) words): bit v set when a neighbour u of v in the
+    graph has prop[u] == value (prop: uint8 numpy array or device tensor)."""
+    p = prop if hasattr(prop, "data_ptr") else np.ascontiguousarray(prop, dtype=np.uint8)
+    n = int(p.numel()) if hasattr(p, "numel") else len(p)
+    mask = np.zeros((graph.V + 63) // 64, np.uint64)
+    check(lib().vs_vertex_mask_any_neighbor(graph.h, _DIRS[direction], _ptr(p), n, int(value), _ptr(mask),
+                                            _stream(stream)))
+    return mask
 
 
 def semi_join(a, b, a_keys, b_keys, only_count=False, stream=None):

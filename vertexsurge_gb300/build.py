@@ -29,7 +29,8 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-fno-strict-aliasing", "-I", str(ROOT / "include")]
 CXX_FLAGS = ["-O3", "-std=c++20", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function"]
 
-CU_SOURCES = ["api.cu", "expand.cu", "matrix.cu", "join.cu", "intersect.cu", "picker.cu", "consumers.cu"]
+CU_SOURCES = ["api.cu", "expand.cu", "matrix.cu", "join.cu", "intersect.cu", "picker.cu", "consumers.cu",
+              "filter.cu"]
 
 LIB = PKG / "libvsgb300.so"
 GEN_LIB = PKG / "libvsgen.so"

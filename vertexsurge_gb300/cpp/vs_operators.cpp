@@ -669,6 +669,49 @@ void MatrixTableSelect::run_internal() {
   results = t;
 }
 
+// MatrixTableFilter<F>::finishAddingDependency / run_internal
+// (big_operators2.hh:142-170): one dependency, the same schema, the input
+// table filtered in place.
+MatrixTableFilter::MatrixTableFilter(MatrixFilter f) : f(std::move(f)) {}
+
+void MatrixTableFilter::finishAddingDependency() {
+  if (deps.size() != 1) throw Error(VS_ERR_ARG, "MatrixTableFilter takes one dependency");
+  results_schema = deps[0]->results_schema;
+}
+
+void MatrixTableFilter::run_internal() {
+  results = dep_results[0];
+  std::vector<uint64_t> keys;
+  for (const auto &p : f.pairs) keys.push_back((uint64_t)p.first << 32 | p.second);
+  std::sort(keys.begin(), keys.end());
+  auto apply = [&](MatrixTable *m) {
+    check(vs_matrix_filter(m->h, f.row_keep.empty() ? nullptr : f.row_keep.data(), f.row_values,
+                           f.col_keep.empty() ? nullptr : f.col_keep.data(), f.col_values,
+                           keys.empty() ? nullptr : keys.data(), keys.size(), f.pairs_mode, stream));
+  };
+  if (auto *mm = dynamic_cast<MultipleMatrixTable *>(results.get())) {
+    for (auto &m : mm->mats) apply(m.get());
+    return;
+  }
+  auto *m = results->down_to_matrix_table();
+  if (!m) throw Error(VS_ERR_ARG, "MatrixTableFilter needs a matrix table");  // big_operators2.hh:147
+  apply(m);
+}
+
+std::vector<uint64_t> MatrixFilter::any_neighbor(Graph &g, const std::string &edge_key,
+                                                 const std::vector<uint8_t> &prop, uint8_t value) {
+  auto it = g.edges.find(edge_key);
+  if (it == g.edges.end()) throw Error(VS_ERR_ARG, "no edge type " + edge_key);
+  uint32_t V = 0;
+  uint64_t E = 0;
+  int directed = 0;
+  check(vs_graph_info(it->second.g, &V, &E, &directed));
+  std::vector<uint64_t> mask(((size_t)V + 63) / 64);
+  check(vs_vertex_mask_any_neighbor(it->second.g, VS_DIR_FORWARD, prop.data(), (uint32_t)prop.size(), value,
+                                    mask.data(), BigOperator::stream));
+  return mask;
+}
+
 int64_t single_count(Table *t) {
   auto *f = t->down_to_flat_table();
   if (!f || f->tuple_count() != 1) throw Error(VS_ERR_ARG, "not a count table");

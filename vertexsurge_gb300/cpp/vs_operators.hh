@@ -303,6 +303,35 @@ class MatrixTableSelect : public BigOperator {
   void finishAddingDependency() override;
 };
 
+// MatrixTableFilter (big_operators2.hh:53-61,142-170).  The reference takes a
+// host predicate f(row value, column value) and clears the bits where it is
+// false, in its input table; here the predicate is the AND of device forms
+// (vs_matrix_filter): a bitset over row values, a bitset over column values
+// and a pair list (kept or dropped).  The input table is filtered in place and
+// becomes the result, as in the reference; a MultipleMatrixTable is filtered
+// layer by layer.
+struct MatrixFilter {
+  std::vector<uint64_t> row_keep;  // bitset over row values (empty: no row condition)
+  uint32_t row_values = 0;         // values at or above fail
+  std::vector<uint64_t> col_keep;  // bitset over column values (empty: no column condition)
+  uint32_t col_values = 0;
+  std::vector<std::pair<VID, VID>> pairs;  // (row value, column value)
+  int pairs_mode = 0;                      // 1: keep listed pairs only, 2: drop listed pairs
+  // the bitset of vertices v with a neighbour u (edge type of g) whose uint8
+  // property equals value: tcr1's "signed in to a blocked medium" (tcr1.cpp:46-57)
+  static std::vector<uint64_t> any_neighbor(class Graph &g, const std::string &edge_key,
+                                            const std::vector<uint8_t> &prop, uint8_t value);
+};
+
+class MatrixTableFilter : public BigOperator {
+  MatrixFilter f;
+  void run_internal() override;
+
+ public:
+  explicit MatrixTableFilter(MatrixFilter f);
+  void finishAddingDependency() override;
+};
+
 // Result consumers (big_operators2.hh, big_operators3.hh).
 enum class SortOrder { ASC, DESC };
 

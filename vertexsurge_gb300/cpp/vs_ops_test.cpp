@@ -3,8 +3,9 @@
 //   HashJoin{FlatFlat,FlatMat,MatFlat,MatMat}[CountOnly] == 18   (join.cpp:451-920)
 //   Mintersect{FlatFlatFlat,FlatMatMat} == 3                     (mintersect.cpp:347-511)
 //   TableConvertVRtoCM / _T exactness                            (big_operators2.cpp:215-296)
-// and plan shapes of the query drivers (e1-self-ring, p3-tri3-1, p4-exp4-1)
-// on a small generated graph, checked against host-side breadth-first search.
+// and plan shapes of the query drivers (e1-self-ring, p3-tri3-1, p4-exp4-1,
+// tcr1's expand + MatrixTableFilter) on a small generated graph, checked
+// against host-side breadth-first search.
 // Exit status 0 = every test passed.
 #include <cstdio>
 #include <cstdlib>
@@ -391,6 +392,64 @@ static bool plans_case(const HostGraph &hg) {
   return ok;
 }
 
+// tcr1 plan shape (ldbc-finbench/tcr1.cpp:41-60): VExpand(Shortest, with
+// distances, [1,3]) then MatrixTableFilter keeping the persons signed in to a
+// blocked medium (a signIn edge type to mediums numbered after the persons)
+static bool filter_case(Graph &g, const HostGraph &hg) {
+  bool ok = true;
+  const uint32_t nm = 400, VT = hg.V + nm;
+  std::mt19937_64 gen(11);
+  vector<std::set<uint32_t>> out(VT);
+  for (uint32_t i = 0; i < 3 * hg.V; i++) out[gen() % hg.V].insert(hg.V + (uint32_t)(gen() % nm));
+  vector<int64_t> off(VT + 1, 0), roff(VT + 1, 0);
+  vector<uint32_t> adj, radj;
+  vector<vector<uint32_t>> in(VT);
+  for (uint32_t u = 0; u < VT; u++) {
+    for (uint32_t v : out[u]) {
+      adj.push_back(v);
+      in[v].push_back(u);
+    }
+    off[u + 1] = (int64_t)adj.size();
+  }
+  for (uint32_t v = 0; v < VT; v++) {
+    for (uint32_t u : in[v]) radj.push_back(u);
+    roff[v + 1] = (int64_t)radj.size();
+  }
+  g.add_edge_type("Person", "signIn", "Medium", true, VT, adj.size(), off.data(), adj.data(), roff.data(),
+                  radj.data());
+  vector<uint8_t> blocked(VT, 0);
+  for (uint32_t m = hg.V; m < VT; m++) blocked[m] = gen() % 10 == 0;
+  MatrixFilter f;
+  f.col_keep = MatrixFilter::any_neighbor(g, "Person_signIn_Medium", blocked, 1);
+  f.col_values = hg.V;
+  auto keeps = [&](uint32_t v) {
+    for (uint32_t m : out[v])
+      if (blocked[m]) return true;
+    return false;
+  };
+  size_t bad_mask = 0;
+  for (uint32_t v = 0; v < hg.V; v++) bad_mask += ((f.col_keep[v >> 6] >> (v & 63)) & 1) != (uint64_t)keeps(v);
+  EXPECT_EQ(bad_mask, (size_t)0);
+  vector<uint64_t> sa;
+  for (uint64_t i = 0; i < 100; i++) sa.push_back((i * 29 + 3) % hg.V);
+  auto ve = make_shared<VExpand>("Person", "Person", "knows", Direction::Both, 1, 3,
+                                 VExpandPathParameters::Shortest().set_with_distance(), ExpandStrategy::Dense, "a.id",
+                                 std::optional<VariableName>("b.id"));
+  ve->addLastDependency(ids("a.id", sa));
+  auto flt = make_shared<MatrixTableFilter>(f);
+  flt->addLastDependency(ve);
+  flt->run();
+  auto *multi = dynamic_cast<MultipleMatrixTable *>(flt->results.get());
+  EXPECT_EQ(multi != nullptr, true);
+  int64_t exp = 0;
+  for (auto s : sa) {
+    auto d = bfs(hg, (uint32_t)s);
+    for (uint32_t v = 0; v < hg.V; v++) exp += d[v] >= 1 && d[v] <= 3 && keeps(v);
+  }
+  EXPECT_EQ((int64_t)multi->tuple_count(), exp);
+  return ok;
+}
+
 // Reads a graph directory in the reference's layout through Graph(dir).load()
 // and prints Count(VExpand(sources i*7 mod V for i < 100, Forward, Shortest,
 // [1,3])) over its first self edge type.
@@ -471,6 +530,7 @@ int main(int argc, char **argv) {
   run_test("TableConvertVRtoCM", [] { return table_convert_case(false); });
   run_test("TableConvertVRtoCM_T", [] { return table_convert_case(true); });
   run_test("PlanShapes(e1,p3-tri3-1,p3-tri3-2,p4-exp4-1,consumers,FindShortest)", [&] { return plans_case(hg); });
+  run_test("MatrixTableFilter(tcr1)", [&] { return filter_case(g, hg); });
   std::printf("%d passed, %d failed\n", g_pass, g_fail);
   return g_fail ? 1 : 0;
 }

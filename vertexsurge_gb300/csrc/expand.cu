@@ -440,14 +440,15 @@ __device__ __forceinline__ unsigned long long out_degree(const Lists &L, uint32_
 __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
   Ctr *c = a.ctr;
   if (c->hop[a.h].strategy != ST_SPARSE) return;
+  __shared__ uint2 s_new[8][SPARSE_CHUNK];  // a warp's new pairs of its current chunk
   const unsigned long long np_raw = c->hop[a.h - 1].pairs;
   const uint64_t np = np_raw < a.cap ? np_raw : a.cap;
   const unsigned long long T = a.doff[np];
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
   const uint64_t nchunks = (T + SPARSE_CHUNK - 1) / SPARSE_CHUNK;
   unsigned long long nb = 0, nv = 0, pe = 0;
-  for (uint64_t ck = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ck < nchunks; ck += warps) {
+  for (uint64_t ck = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib; ck < nchunks; ck += warps) {
     const unsigned long long e0 = ck * SPARSE_CHUNK;
     const unsigned long long e1 = min(e0 + SPARSE_CHUNK, T);
     // pairs owning the chunk's first and last edge: largest p with doff[p] <= e
@@ -466,16 +467,28 @@ __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
       }
       phi = lo;
     }
+    // up to 32 pairs: lane j holds the first edge of pair plo + j, and an
+    // edge's pair is found by counting those starts at or below it
+    const uint32_t npr = (uint32_t)(phi - plo + 1);
+    const unsigned long long dj = (npr <= 32 && (uint32_t)lane < npr) ? a.doff[plo + lane] : ~0ull;
+    uint32_t nloc = 0;  // new pairs of this chunk so far (s_new)
     for (unsigned long long eb = e0; eb < e1; eb += 32) {
       const unsigned long long e = eb + lane;
       bool fresh = false;
       uint32_t v = 0, i = 0;
-      if (e < e1) {
-        uint64_t lo = plo, hi = phi + 1;
+      uint64_t lo = plo;
+      if (npr <= 32) {
+        uint32_t cnt = 0;
+        for (uint32_t j = 0; j < npr; j++) cnt += __shfl_sync(FULL, dj, j) <= e;
+        lo = plo + (cnt ? cnt - 1 : 0);
+      } else if (e < e1) {
+        uint64_t hi = phi + 1;
         while (hi - lo > 1) {
           const uint64_t mid = (lo + hi) >> 1;
           if (a.doff[mid] <= e) lo = mid; else hi = mid;
         }
+      }
+      if (e < e1) {
         const uint2 pr = a.pin[lo];
         const uint32_t u = pr.x;
         i = pr.y;
@@ -507,24 +520,29 @@ __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
           }
         }
       }
-      // warp-aggregated append of the new pairs (with their out-degrees)
+      // the chunk's new pairs gather in shared memory (one list append per chunk)
       const unsigned m = __ballot_sync(FULL, fresh);
-      if (m) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&c->hop[a.h].pairs, (unsigned long long)__popc(m));
-        base = __shfl_sync(FULL, base, 0);
-        if (fresh) {
-          const unsigned long long slot = base + __popc(m & lanemask_lt());
-          const unsigned long long d = out_degree(a.out, v);
-          pe += d;
-          if (slot < a.cap) {
-            a.pout[slot] = make_uint2(v, i);
-            a.pdeg_out[slot] = d;
-          } else {
-            c->hop[a.h].overflow = 1;
-          }
+      if (fresh) s_new[wib][nloc + __popc(m & lanemask_lt())] = make_uint2(v, i);
+      nloc += __popc(m);
+    }
+    __syncwarp();
+    if (nloc) {  // append the chunk's new pairs (with their out-degrees) to layer h's list
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(&c->hop[a.h].pairs, (unsigned long long)nloc);
+      base = __shfl_sync(FULL, base, 0);
+      for (uint32_t j = lane; j < nloc; j += 32) {
+        const uint2 pr = s_new[wib][j];
+        const unsigned long long d = out_degree(a.out, pr.x);
+        pe += d;
+        const unsigned long long slot = base + j;
+        if (slot < a.cap) {
+          a.pout[slot] = pr;
+          a.pdeg_out[slot] = d;
+        } else {
+          c->hop[a.h].overflow = 1;
         }
       }
+      __syncwarp();
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) c->hop[a.h].work_edges = T;

@@ -51,12 +51,13 @@ def test_filter_forms_match_oracle(vs, kind):
 
 
 def test_filter_rejects_bad_arguments(vs):
-    m = vs.BitMatrix.from_logical(np.ones((10, 1), np.uint64), 64, 10)
+    full = np.full((10, 1), np.uint64(0xFFFFFFFFFFFFFFFF), np.uint64)
+    m = vs.BitMatrix.from_logical(full, 64, 10)
     with pytest.raises(vs.VsError):  # a pair list out of order
         vs.matrix_filter(m, pairs=np.array([5, 3], np.uint64), pairs_mode=1)
     with pytest.raises(vs.VsError):  # unknown mode
         vs.matrix_filter(m, pairs=np.array([3, 5], np.uint64), pairs_mode=3)
-    assert np.array_equal(m.download(), np.ones((10, 1), np.uint64))
+    assert np.array_equal(m.download(), full)
     # a host bitset is copied in: rows 0..31 kept
     host = np.array([0xFFFFFFFF], np.uint64)
     assert vs.lib().vs_matrix_filter(m.h, host.ctypes.data, 64, None, 0, None, 0, 0, None) == 0

@@ -775,7 +775,8 @@ def run_gpu(args, w, rank, world, local_rank):
                 "dram_frac": (traffic / (per_launch_ms / 1e3) / 1e9) / peak if traffic and per_launch_ms else None,
                 "traffic_source": f"profiles/{rl_kernel}_{args.workload}.md (ncu dram__bytes_read.sum + "
                                   "dram__bytes_write.sum per working launch)",
-                "kernel": (f"{rl_kernel} (expand A, PULL hops {sorted(pull_hop_ms)}, short mode on {short_hops})"),
+                "kernel": (f"{rl_kernel} (expand A, PULL hops {sorted(pull_hop_ms)}, short mode on "
+                           f"{ {h: ('words', 'slots')[stA['short_pull'][h] - 1] for h in short_hops} })"),
                 "peak_source": peak_kind,
                 "per_launch_ms": per_launch_ms,
                 "per_hop_ms": {str(h): t / args.steps for h, t in sorted(pull_hop_ms.items())}}

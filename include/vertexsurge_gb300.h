@@ -179,7 +179,7 @@ typedef struct vs_expand_params {
                               / 63 for rows of 128 / more words) are read from a slot of their
                               source ids instead of whole, on hops where at least this share of
                               the frontier's rows are short and the frontier exceeds half of L2
-                              (0 = 0.1; < 0 = never; > 1 = every PULL hop); needs S <= 65536 and
+                              (0 = 0.1; < 0 = never; > 1 = every PULL hop); needs S <= 32768 and
                               whole-row passes, and keeps 36 to 132 B per vertex, except in plans
                               whose V x S matrix fits in half of L2 (short mode never runs there) */
 } vs_expand_params;
@@ -200,7 +200,7 @@ typedef struct vs_expand_stats {
   uint64_t short_rows[VS_MAX_HOPS + 1];     /* rows of layer h short enough for a slot (when a PULL
                                                hop wrote its slots) */
   uint64_t short_edges[VS_MAX_HOPS + 1];    /* active in-edges of hop h's PULL served from a slot */
-  uint64_t tiny_rows[VS_MAX_HOPS + 1];      /* rows of layer h with one bit (its id inline in the word) */
+  uint64_t tiny_rows[VS_MAX_HOPS + 1];      /* rows of layer h with one or two bits (ids inline in the word) */
 } vs_expand_stats;
 
 /* A plan owns the frontier, next, visited and accumulator matrices for S

@@ -353,9 +353,9 @@ def test_short_pull_parity(vs, graphs, path, direction):
 @pytest.mark.parametrize("S", [700, 8192])
 def test_short_rows_counted(vs, graphs, path, S):
     """The PULL epilogue's counts of short rows (at most 15 bits for rows of
-    up to 64 words, 31 for 128 words) and of rows with their id inline in
-    the tiny word (one bit), in every layer it writes words for, equal the
-    counts over the oracle's layer."""
+    up to 64 words, 31 for 128 words) and of rows with their ids inline in
+    the tiny word (one or two bits), in every layer it writes words for,
+    equal the counts over the oracle's layer."""
     g, dg = graphs["zipf3000"]
     src = graphgen.sample_sources(g.V, min(S, g.V), seed=8)
     if S > g.V:
@@ -369,7 +369,7 @@ def test_short_rows_counted(vs, graphs, path, S):
         layer, _, _ = O.vexpand(g, src, h, h, path, "forward")
         bits = words_to_bool(layer, len(src)).sum(axis=0) if layer.size else np.zeros(g.V)
         assert st["short_rows"][h] == int(((bits >= 1) & (bits <= short_max)).sum()), h
-        assert st["tiny_rows"][h] == int((bits == 1).sum()), h
+        assert st["tiny_rows"][h] == int(((bits >= 1) & (bits <= 2)).sum()), h
         checked += 1
     assert checked == 3
 

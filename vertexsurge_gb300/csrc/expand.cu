@@ -610,8 +610,8 @@ template <int H> struct L2Pol {
 // Short rows.  In the later hops of a many-source expand over a power-law
 // graph most frontier rows hold a handful of sources, and a whole-row gather
 // then moves mostly zero words.  Every PULL hop with a successor therefore
-// also writes, for every vertex, a tiny word (uint32: the row's bit count,
-// saturated at 0xFFFF, and for a one-bit row its source id) and a slot of
+// also writes, for every vertex, a tiny word (uint32: the ids of a row of one
+// or two bits, else its saturated bit count) and a slot of
 // slot_n uint16 (entry 0: the count; entries 1..count: the ids, for up to
 // slot_n - 1 bits; slot_n = 16, 32 or 64 as the rows are up to 512 B, 1 KB or
 // wider).  A later PULL hop in short mode reads, per in-neighbour, either its
@@ -626,9 +626,28 @@ template <int H> struct L2Pol {
 // written by SPARSE or the seed get their words and slots from the hop's
 // pair list (k_pairs_*), layers written by PUSH or an overflowed SPARSE hop
 // from their rows (k_slot_build), when the next hop reads them.
-using Tiny = uint32_t;                                       // count, then ids, as uint16
-constexpr uint32_t TINY_MAX = sizeof(Tiny) / 2 - 1;          // ids in a tiny word
+// A tiny word is 0 for an empty row; otherwise its top two bits are a class:
+// 1 = one id in bits 0..14, 2 = two ids in bits 0..14 and 15..29, 3 = the
+// row's bit count (saturated at 0xFFFF) in bits 0..15, its ids in the slot
+// when the count is below slot_n.  Short mode runs only for rows of at most
+// 512 words (S <= 32768), so source ids fit 15 bits.
+using Tiny = uint32_t;
+constexpr uint32_t TINY_MAX = 2;    // ids a tiny word holds
 constexpr uint32_t CHUNK_IDS = 16;  // uint16 entries per 32-byte chunk of a slot
+
+// Tiny word of a row of `total` bits; part = its first two ids (bits 0..14,
+// 15..29) when total <= TINY_MAX.
+__host__ __device__ __forceinline__ Tiny tiny_word(uint32_t total, uint32_t part) {
+  return total == 0 ? 0u
+         : total <= TINY_MAX ? (total << 30) | part
+                             : (3u << 30) | (total < 0xFFFFu ? total : 0xFFFFu);
+}
+// Bit count of a row from its tiny word: exact up to TINY_MAX, else the
+// saturated count.
+__device__ __forceinline__ uint32_t tiny_count(Tiny t) {
+  const uint32_t cls = t >> 30;
+  return cls < 3 ? cls : (t & 0xFFFFu);
+}
 
 // Bulk prefetch of `bytes` (a multiple of 16, 16-byte aligned) into L2.
 __device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
@@ -652,11 +671,11 @@ __device__ __forceinline__ Tiny ld_keep(const Tiny *p) {
 
 // OR the ids of a tiny word (count in [1, TINY_MAX]) into a shared row
 __device__ __forceinline__ void or_tiny_ids(uint32_t *row32, Tiny t, uint32_t cnt) {
-#pragma unroll
-  for (uint32_t i = 1; i <= TINY_MAX; i++) {
-    if (i > cnt) break;
-    const uint32_t id = (uint32_t)(t >> (16 * i)) & 0xFFFFu;
-    atomicOr(row32 + (id >> 5), 1u << (id & 31));
+  const uint32_t id0 = t & 0x7FFFu;
+  atomicOr(row32 + (id0 >> 5), 1u << (id0 & 31));
+  if (cnt > 1) {
+    const uint32_t id1 = (t >> 15) & 0x7FFFu;
+    atomicOr(row32 + (id1 >> 5), 1u << (id1 & 31));
   }
 }
 
@@ -713,7 +732,7 @@ __device__ __forceinline__ void gather_chunk(const PullArgs &a, const L2Pol<H> &
       }
       cnt = s0.x & 0xFFFFu;
     } else {
-      cnt = (uint32_t)tv & 0xFFFFu;
+      cnt = tiny_count(tv);
     }
     if (cnt == 0) {
       act = false;
@@ -788,63 +807,73 @@ __device__ __forceinline__ void gather_rows(const PullArgs &a, const L2Pol<H> &p
 }
 
 // The tiny word and the slot (ids for up to slot_n - 1 bits) of the
-// non-zero row of v held by lanes 0..L-1 (uint4 q = lane + k * L).
+// non-zero row of v held by lanes 0..L-1 (uint4 q = lane + k * L).  A short
+// row's ids are gathered in the warp's staging slot in shared memory and
+// stored with one 16-byte store per lane of the slot; stale entries past the
+// count are never read.
 template <int L, int UPL>
 __device__ __forceinline__ bool write_short(const PullArgs &a, uint32_t v, const uint4 (&acc)[UPL], uint32_t qn,
                                             unsigned long long &ns) {
-  const int lane = threadIdx.x & 31;
+  __shared__ uint4 s_stage[16][8];  // a slot per warp (at most 64 entries, 16 warps)
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   uint32_t c = 0;
   if (lane < L) {
 #pragma unroll
     for (int k = 0; k < UPL; k++)
       if (lane + k * L < qn) c += popc4(acc[k]);
   }
-  uint32_t incl = c;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(FULL, incl, o);
-    if (lane >= o) incl += y;
-  }
-  const uint32_t total = __shfl_sync(FULL, incl, 31);
-  Tiny tv = total < 0xFFFFu ? total : 0xFFFFu;
+  const uint32_t total = __reduce_add_sync(FULL, c);
   uint16_t *slot = a.slot_out + (size_t)v * a.slot_n;
-  if (total < a.slot_n) {
-    Tiny part = 0;
-    uint32_t pos = 1 + incl - c;
-    if (c) {
+  if (total >= a.slot_n) {  // a long row: its count alone
+    if (lane == 0) {
+      a.tiny_out[v] = tiny_word(total, 0);
+      slot[0] = (uint16_t)(total < 0xFFFFu ? total : 0xFFFFu);
+    }
+    return false;
+  }
+  // position of this lane's first id: exclusive prefix of the bit counts
+  uint32_t excl;
+  if (__ballot_sync(FULL, c > 1) == 0) {
+    excl = __popc(__ballot_sync(FULL, c != 0) & lanemask_lt());
+  } else {
+    uint32_t incl = c;
 #pragma unroll
-      for (int k = 0; k < UPL; k++) {
-        const uint32_t q = lane + k * L;
-        if (q < qn) {
-          const uint32_t w[4] = {acc[k].x, acc[k].y, acc[k].z, acc[k].w};
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += y;
+    }
+    excl = incl - c;
+  }
+  uint16_t *stage = reinterpret_cast<uint16_t *>(s_stage[wib]);
+  if (c) {
+    uint32_t pos = 1 + excl;
 #pragma unroll
-          for (int wi = 0; wi < 4; wi++) {
-            uint32_t bits = w[wi];
-            while (bits) {
-              const uint32_t t = __ffs(bits) - 1;
-              bits &= bits - 1;
-              const uint32_t id = q * 128 + wi * 32 + t;
-              if (total <= TINY_MAX) part |= (Tiny)id << (16 * pos);
-              slot[pos] = (uint16_t)id;
-              pos++;
-            }
+    for (int k = 0; k < UPL; k++) {
+      const uint32_t q = lane + k * L;
+      if (q < qn) {
+        const uint32_t w[4] = {acc[k].x, acc[k].y, acc[k].z, acc[k].w};
+#pragma unroll
+        for (int wi = 0; wi < 4; wi++) {
+          uint32_t bits = w[wi];
+          while (bits) {
+            stage[pos++] = (uint16_t)(q * 128 + wi * 32 + __ffs(bits) - 1);
+            bits &= bits - 1;
           }
         }
       }
     }
-    if (total <= TINY_MAX) {
-#pragma unroll
-      for (int o = 16; o; o >>= 1) part |= (Tiny)__shfl_xor_sync(FULL, part, o);
-      tv |= part;
-    }
-    // short rows in the low half, rows of at most TINY_MAX bits in the high half
-    if (lane == 0) ns += 1ull + (total <= TINY_MAX ? 1ull << 32 : 0ull);
   }
+  if (lane == 0) stage[0] = (uint16_t)total;
+  __syncwarp();
+  if ((uint32_t)lane < a.slot_n / 8) reinterpret_cast<uint4 *>(slot)[lane] = s_stage[wib][lane];
   if (lane == 0) {
-    a.tiny_out[v] = tv;
-    slot[0] = (uint16_t)tv;
+    // up to two ids ride in the word, more stay in the slot
+    a.tiny_out[v] = tiny_word(total, total <= TINY_MAX ? stage[1] | (total > 1 ? (uint32_t)stage[2] << 15 : 0u) : 0u);
+    // short rows in the low half, rows of at most TINY_MAX bits in the high half
+    ns += 1ull + (total <= TINY_MAX ? 1ull << 32 : 0ull);
   }
-  return total < a.slot_n;
+  __syncwarp();  // the staging slot is free for the warp's next row
+  return true;
 }
 
 // Fused epilogue for the row of v held by lanes 0..L-1 after the group reduction:
@@ -1251,10 +1280,9 @@ __device__ __forceinline__ void short_from_chunk(uint4 x, uint32_t r, Tiny *tiny
     if (lane >= (uint32_t)o) incl += y;
   }
   const uint32_t total = __shfl_sync(FULL, incl, 31);
-  Tiny tv = total < 0xFFFFu ? total : 0xFFFFu;
+  uint32_t part = 0;  // ids 1 and 2 of the row, in tiny-word positions
   uint16_t *slot = slots + (size_t)r * slot_n;
   if (total < slot_n) {
-    Tiny part = 0;
     uint32_t at = 1 + incl - n;
     const uint32_t w[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
@@ -1264,20 +1292,16 @@ __device__ __forceinline__ void short_from_chunk(uint4 x, uint32_t r, Tiny *tiny
         const uint32_t t = __ffs(bits) - 1;
         bits &= bits - 1;
         const uint32_t id = lane * 128 + wi * 32 + t;
-        if (total <= TINY_MAX) part |= (Tiny)id << (16 * at);
+        if (at <= TINY_MAX) part |= id << (15 * (at - 1));
         slot[at] = (uint16_t)id;
         at++;
       }
     }
-    if (total <= TINY_MAX) {
-#pragma unroll
-      for (int o = 16; o; o >>= 1) part |= (Tiny)__shfl_xor_sync(FULL, part, o);
-      tv |= part;
-    }
   }
+  part = __reduce_or_sync(FULL, part);
   if (lane == 0) {
-    tiny[r] = tv;
-    slot[0] = (uint16_t)tv;
+    tiny[r] = tiny_word(total, part);
+    slot[0] = (uint16_t)(total < 0xFFFFu ? total : 0xFFFFu);
   }
 }
 
@@ -1314,10 +1338,13 @@ __global__ void k_pairs_words(const uint32_t *__restrict__ flagF, const uint32_t
   if (!pairs_build(ctr, h)) return;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
     const uint32_t c = flagF[v] ? cnt[v] : 0u;
-    Tiny tv = c < 0xFFFFu ? c : 0xFFFFu;
-    if (c == 1) tv |= (Tiny)slots[(size_t)v * slot_n + 1] << 16;
-    tiny[v] = tv;
-    if (c) slots[(size_t)v * slot_n] = (uint16_t)tv;
+    uint32_t part = 0;
+    if (c && c <= TINY_MAX) {
+      part = slots[(size_t)v * slot_n + 1];
+      if (c > 1) part |= (uint32_t)slots[(size_t)v * slot_n + 2] << 15;
+    }
+    tiny[v] = tiny_word(c, part);
+    if (c) slots[(size_t)v * slot_n] = (uint16_t)(c < 0xFFFFu ? c : 0xFFFFu);
   }
 }
 
@@ -1370,10 +1397,9 @@ __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__
       uint32_t c = 0;
       for (uint32_t q = lane; q < Q; q += 32) c += popc4(row[q]);
       const uint32_t total = warp_sum(c);
-      Tiny tv = total < 0xFFFFu ? total : 0xFFFFu;
+      uint32_t part = 0;  // ids 1 and 2 of the row, in tiny-word positions
       uint16_t *slot = slots + (size_t)r * slot_n;
       if (total < slot_n) {
-        Tiny part = 0;
         uint32_t pos = 1;
         for (uint32_t q0 = 0; q0 < Q; q0 += 32) {
           const uint32_t q = q0 + lane;
@@ -1394,22 +1420,18 @@ __global__ void k_slot_build(const uint32_t *__restrict__ flagF, const uint4 *__
               const uint32_t t = __ffs(bits) - 1;
               bits &= bits - 1;
               const uint32_t id = q * 128 + wi * 32 + t;
-              if (total <= TINY_MAX) part |= (Tiny)id << (16 * at);
+              if (at <= TINY_MAX) part |= id << (15 * (at - 1));
               slot[at] = (uint16_t)id;
               at++;
             }
           }
           pos += __shfl_sync(FULL, incl, 31);
         }
-        if (total <= TINY_MAX) {
-#pragma unroll
-          for (int o = 16; o; o >>= 1) part |= (Tiny)__shfl_xor_sync(FULL, part, o);
-          tv |= part;
-        }
       }
+      part = __reduce_or_sync(FULL, part);
       if (lane == 0) {
-        tiny[r] = tv;
-        slot[0] = (uint16_t)tv;
+        tiny[r] = tiny_word(total, part);
+        slot[0] = (uint16_t)(total < 0xFFFFu ? total : 0xFFFFu);
       }
     }
   }
@@ -1640,7 +1662,7 @@ struct vs_expand_plan {
   uint64_t *hmask = nullptr;  // (k_max + 1) x W words: rows allowed to grow at hop h
   uint32_t *rowk = nullptr;   // [0] largest row limit, [1] a limit exceeded k_max (device-set limits)
   uint64_t *layer_out[VS_MAX_HOPS + 1] = {};  // with_distance: layer h is copied here (zeroed, V x W words)
-  // short-row index of the two frontier buffers' layers; none when S > 65536 or multi-slice
+  // short-row index of the two frontier buffers' layers; none when S > 32768 or multi-slice
   Tiny *tiny[2] = {nullptr, nullptr};      // short-row words
   uint16_t *slot[2] = {nullptr, nullptr};  // ... and their slots
   uint32_t slot_n = 16;                    // uint16 entries per slot
@@ -1673,11 +1695,11 @@ inline bool needs_acc(const vs_expand_params &p) {
 // the row's bytes at 64 and 128 words, 128 bytes beyond.
 inline uint32_t slot_entries(uint32_t W) { return W <= 64 ? 16 : W <= 128 ? 32 : 64; }
 
-// Short-row slots (uint16 ids: S <= 65536) need rows in one slice, and short
+// Short-row words and slots (15-bit ids: S <= 32768) need rows in one slice, and short
 // mode runs only on frontiers larger than half of L2 (unless forced: share >
 // 1): a graph whose whole V x W matrix fits there never uses them.
 inline bool short_slots_ok(uint32_t S, uint32_t nslices, double share, uint64_t V, uint32_t W) {
-  return share >= 0 && S <= 65536 && nslices == 1 && (share > 1.0 || V * 8ull * W > l2_bytes() / 2);
+  return share >= 0 && S <= 32768 && nslices == 1 && (share > 1.0 || V * 8ull * W > l2_bytes() / 2);
 }
 
 int plan_free(vs_expand_plan *pl) {

@@ -71,15 +71,27 @@ def test_row_block_counts_reject_bad_blocks(vs, graphs):
     m.free()
 
 
-@pytest.mark.parametrize("wave_rows", [256, 400])
-def test_batch_counts_equal_solo(vs, graphs, wave_rows):
+@pytest.mark.parametrize("wave_rows,lanes", [(256, 1), (400, 1), (256, 3)])
+def test_batch_counts_equal_solo(vs, graphs, wave_rows, lanes):
+    """Every query's count in the batch (eager and replayed as one graph,
+    waves on one or several concurrent lanes) equals the query run alone, and
+    a few equal the oracle's VExpand + TableConvert + HashJoin count."""
     import torch
+    from oracle import pyoracle as O
     from vertexsurge_gb300 import batch
     g, dg = graphs["rmat11_skew"]
     qs = batch.make_queries(g, 14, s_range=(3, 250), l_range=(1, 4), join_rows=(10, 4000), seed=3)
     solo = batch.solo_counts(dg, qs)
+    for i in (0, 5, 13):
+        q = qs[i]
+        words, _, _ = O.vexpand(g, q.sources, 1, q.k_max, "shortest", "forward")
+        cm = O.table_convert(words, len(q.sources), g.V, False)
+        a = O.Table(O.COLMAIN, [0, 1], words=cm, mrows=len(q.sources), mcols=g.V, row_map=q.sources)
+        k = O.Table(O.FLAT, [1], cols=[q.keys])
+        assert O.hash_join(k, a, 1, only_count=True)[2] == solo[i], i
     stream = torch.cuda.Stream()
-    b = batch.Batch(dg, qs, wave_rows, stream)
+    b = batch.Batch(dg, qs, wave_rows, stream, lanes=lanes)
+    assert b.lanes == min(lanes, len(b.waves))
     assert len(b.waves) >= 2, [len(q.sources) for q in qs]
     b.run_eager()
     assert np.array_equal(b.counts(), solo)

@@ -80,21 +80,35 @@ def pack(queries: list, wave_rows: int) -> list:
 
 class Batch:
     """Device-resident batch of queries; `capture` records the whole batch on
-    `stream`, `launch` replays it, `counts` reads the per-query join counts."""
+    `stream`, `launch` replays it, `counts` reads the per-query join counts.
+
+    lanes > 1 runs the waves on that many concurrent branches of the captured
+    graph, wave w on lane w mod lanes, each lane with its own expand plan and
+    stream: while one wave is in a hop that leaves SMs idle (pair-list hops,
+    decide and clear kernels, the tail of a PULL hop) another wave's kernels
+    fill them."""
 
     def __init__(self, dg, queries: list, wave_rows: int, stream, path="shortest", direction="forward",
-                 setting: dict | None = None, picker=None):
+                 setting: dict | None = None, picker=None, lanes: int = 1):
         import torch
         from .autotune import params_kw
         self.dg, self.queries, self.stream = dg, queries, stream
         self.waves = pack(queries, wave_rows)
         self.S = max(sum(len(queries[i].sources) for i in w) for w in self.waves)
         self.k_max = max(q.k_max for q in queries)
-        self.plan = vs.ExpandPlan(dg, self.S, vs.make_params(1, self.k_max, path, direction,
-                                                             use_picker=picker is not None,
-                                                             **params_kw(setting)))
-        if picker is not None:
-            self.plan.set_picker(picker)
+        params = vs.make_params(1, self.k_max, path, direction, use_picker=picker is not None, **params_kw(setting))
+        # every lane holds a plan: no more lanes than the free device memory takes twice over
+        free_b, _ = torch.cuda.mem_get_info()
+        fits = max(1, int(free_b // (2 * vs.plan_footprint(dg, self.S, params))))
+        self.lanes = max(1, min(int(lanes), len(self.waves), fits))
+        self.plans = []
+        for _ in range(self.lanes):
+            pl = vs.ExpandPlan(dg, self.S, params)
+            if picker is not None:
+                pl.set_picker(picker)
+            self.plans.append(pl)
+        self.plan = self.plans[0]
+        self.streams = [stream] + [torch.cuda.Stream() for _ in range(self.lanes - 1)]
         nw = len(self.waves)
         src = np.zeros((nw, self.S), np.uint32)       # padding rows start at vertex 0 and never grow
         lim = np.zeros((nw, self.S), np.uint8)
@@ -130,20 +144,34 @@ class Batch:
         return self.d_src.numel() * 4 + self.d_lim.numel() + self.d_keys.numel() * 4
 
     def run_eager(self):
-        """Every wave: row limits, expand, row-block join counts (stream-ordered)."""
+        """Every wave: row limits, expand, row-block join counts, ordered on its
+        lane's stream; the lanes fork from and join back into `stream`."""
+        import torch
+        if self.lanes > 1:
+            fork = torch.cuda.Event()
+            fork.record(self.stream)
+            for st in self.streams[1:]:
+                st.wait_event(fork)
         off = 0
         for wi, blocks in enumerate(self.waves):
-            self.plan.set_row_limits_device(self.d_lim[wi], self.S, stream=self.stream)
-            self.plan.run(self.d_src[wi], stream=self.stream)
+            k = wi % self.lanes
+            plan, st = self.plans[k], self.streams[k]
+            plan.set_row_limits_device(self.d_lim[wi], self.S, stream=st)
+            plan.run(self.d_src[wi], stream=st)
             nb = len(self.blocks[wi])
-            vs.join_count_row_blocks(self.plan.result(), self.d_keys, self.blocks[wi],
-                                     self.d_counts[off:off + nb], stream=self.stream)
+            vs.join_count_row_blocks(plan.result(), self.d_keys, self.blocks[wi],
+                                     self.d_counts[off:off + nb], stream=st)
             off += nb
+        for st in self.streams[1:]:
+            join = torch.cuda.Event()
+            join.record(st)
+            self.stream.wait_event(join)
 
     def capture(self):
-        self.run_eager()  # the plan's first run on this stream happens outside the capture
-        self.stream.synchronize()
-        with vs.Captured(self.stream, keep=(self.plan, self.d_src, self.d_lim, self.d_keys,
+        self.run_eager()  # every plan's first run on its stream happens outside the capture
+        for st in self.streams:
+            st.synchronize()
+        with vs.Captured(self.stream, keep=(*self.plans, self.d_src, self.d_lim, self.d_keys,
                                             self.d_counts)) as cg:
             self.run_eager()
         self.graph = cg
@@ -161,7 +189,8 @@ class Batch:
         if self.graph is not None:
             self.graph.free()
             self.graph = None
-        self.plan.free()
+        for pl in self.plans:
+            pl.free()
 
 
 def solo_counts(dg, queries: list, path="shortest", direction="forward", stream=None) -> np.ndarray:
@@ -179,33 +208,34 @@ def solo_counts(dg, queries: list, path="shortest", direction="forward", stream=
 
 
 def tune_wave_rows(dg, queries, stream, candidates=(16384, 32768), setting=None, repeats=1,
-                   picker=None, short_shares=(0.0, -1.0)) -> dict:
-    """Time one captured batch per wave width and short-mode setting (the
-    waves' hop limits and mixed sizes decide whether short-row PULL pays, so
-    it is tuned here on the batch itself); returns {'wave_rows',
-    'short_share', 'ms', 'table'}."""
+                   picker=None, short_shares=(0.0, -1.0), lanes=(1,)) -> dict:
+    """Time one captured batch per wave width, short-mode setting and lane
+    count (the waves' hop limits and mixed sizes decide whether short-row PULL
+    and concurrent waves pay, so they are tuned here on the batch itself);
+    returns {'wave_rows', 'short_share', 'lanes', 'ms', 'table'}."""
     import torch
     table = []
-    for wr in candidates:
-        if wr < max(len(q.sources) for q in queries):
+    widest = max(len(q.sources) for q in queries)
+    for wr, sh, ln in [(wr, sh, ln) for wr in candidates for sh in short_shares for ln in lanes]:
+        if wr < widest:
             continue
-        for sh in short_shares:
-            st = dict(setting or {})
-            st["short_share"] = sh
-            b = Batch(dg, queries, wr, stream, setting=st, picker=picker)
-            try:
-                b.capture()
+        st = dict(setting or {})
+        st["short_share"] = sh
+        b = Batch(dg, queries, wr, stream, setting=st, picker=picker, lanes=ln)
+        try:
+            b.capture()
+            b.launch()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(repeats)]
+            for e0, e1 in ev:
+                e0.record(stream)
                 b.launch()
-                ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-                      for _ in range(repeats)]
-                for e0, e1 in ev:
-                    e0.record(stream)
-                    b.launch()
-                    e1.record(stream)
-                stream.synchronize()
-                ms = min(e0.elapsed_time(e1) for e0, e1 in ev)
-                table.append({"wave_rows": wr, "short_share": sh, "waves": len(b.waves), "ms": ms})
-            finally:
-                b.free()
+                e1.record(stream)
+            stream.synchronize()
+            ms = min(e0.elapsed_time(e1) for e0, e1 in ev)
+            table.append({"wave_rows": wr, "short_share": sh, "lanes": b.lanes, "waves": len(b.waves), "ms": ms})
+        finally:
+            b.free()
     best = min(table, key=lambda r: r["ms"])
-    return {"wave_rows": best["wave_rows"], "short_share": best["short_share"], "ms": best["ms"], "table": table}
+    return {"wave_rows": best["wave_rows"], "short_share": best["short_share"], "lanes": best["lanes"],
+            "ms": best["ms"], "table": table}

@@ -1008,7 +1008,9 @@ __device__ __forceinline__ void pull_vertices(const PullArgs &a) {
 // target v is processed, the next target's list bounds, first 32
 // in-neighbours and their tiny words are already in flight.  PRE: so are the
 // next target's visited words (in registers of lanes 0..L-1) and its
-// next-layer flag, which the epilogue would otherwise wait for.
+// next-layer flag, which the epilogue would otherwise wait for, and the list
+// bounds run one target further ahead, so the next target's in-neighbours
+// are requested when v starts.
 template <int L, int UPL, bool PRE = false>
 __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
   const L2Pol<0> pol;
@@ -1043,6 +1045,11 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
       for (int k = 0; k < UPL; k++)
         if (lane + k * L < qn) vpre[k] = pol.ld_rw(a.vis + (size_t)v * a.Q + lane + k * L);
   }
+  int64_t b1 = 0, e1 = 0;  // PRE: list 0 of the next target, loaded one target ahead
+  if (PRE && (uint64_t)v + stride < a.V) {
+    b1 = __ldg(off0 + v + stride);
+    e1 = __ldg(off0 + v + stride + 1);
+  }
   if (v < a.V) {
     beg = __ldg(off0 + v);
     end = __ldg(off0 + v + 1);
@@ -1059,8 +1066,16 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
   }
   for (; v < a.V; v += stride) {
     const uint32_t vn = v + stride;
-    int64_t nbeg = 0, nend = 0;
-    if (vn < a.V) {
+    int64_t nbeg = 0, nend = 0, b2 = 0, e2 = 0;
+    if (PRE) {  // the next target's bounds arrived during v - stride; fetch those of vn + stride
+      nbeg = b1;
+      nend = e1;
+      const uint64_t v2 = (uint64_t)vn + stride;
+      if (v2 < a.V) {
+        b2 = __ldg(off0 + v2);
+        e2 = __ldg(off0 + v2 + 1);
+      }
+    } else if (vn < a.V) {
       nbeg = __ldg(off0 + vn);
       nend = __ldg(off0 + vn + 1);
     }
@@ -1070,6 +1085,7 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
     Tiny ptn = 0;
     uint4 psn[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
     const bool pactn = nbeg + lane < nend;
+    if (PRE && pactn) pun = __ldg(adj0 + nbeg + lane);  // in flight during all of v
     uint4 vpren[UPL];
     uint32_t oldfn = 0;
 #pragma unroll
@@ -1090,7 +1106,7 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
 #pragma unroll
       for (int k = 0; k < UPL; k++) acc[k] = make_uint4(0, 0, 0, 0);
       gather_chunk<L, UPL, 0, true>(a, pol, s_u[wib], row32, 0, qn, acc, pu, pact, pt, slotmode, se, ps);
-      if (pactn) pun = __ldg(adj0 + nbeg + lane);  // in flight during the rest of v
+      if (!PRE && pactn) pun = __ldg(adj0 + nbeg + lane);  // in flight during the rest of v
       gather_rows<L, UPL, 0, true>(a, pol, s_u[wib], row32, 0, qn, acc, adj0, beg + 32, end, 0, 32, se, slotmode);
       if (a.in.n > 1)
         gather_rows<L, UPL, 0, true>(a, pol, s_u[wib], row32, 0, qn, acc, a.in.adj[1], a.in.off[1][v],
@@ -1121,7 +1137,7 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
       }
       pull_epilogue<L, UPL, 0, PRE>(a, pol, v, 0, qn, acc, nb, nv, ns, vpre, oldf);
     } else if (pactn) {
-      pun = __ldg(adj0 + nbeg + lane);
+      if (!PRE) pun = __ldg(adj0 + nbeg + lane);
       if (slotmode) {
         psn[0] = __ldg(a.slot_in + (size_t)pun * sq);
         psn[1] = __ldg(a.slot_in + (size_t)pun * sq + 1);
@@ -1136,6 +1152,8 @@ __device__ __forceinline__ void pull_vertices_short(const PullArgs &a) {
     ps[0] = psn[0];
     ps[1] = psn[1];
     pact = pactn;
+    b1 = b2;
+    e1 = e2;
     oldf = oldfn;
 #pragma unroll
     for (int k = 0; k < UPL; k++) vpre[k] = vpren[k];
@@ -1159,7 +1177,7 @@ __global__ void __launch_bounds__(256, UPL >= 4 ? 2 : 5) k_pull_short(PullArgs a
 
 // ... with the visited words and flag of the next target loaded ahead
 template <int L, int UPL>
-__global__ void __launch_bounds__(256, UPL >= 4 ? 2 : 4) k_pull_short_pre(PullArgs a) {
+__global__ void __launch_bounds__(256, UPL >= 4 ? 2 : UPL == 2 ? 3 : 4) k_pull_short_pre(PullArgs a) {
   if (a.ctr->hop[a.h].strategy != ST_PULL || !a.ctr->hop[a.h].short_pull || !a.tiny_in || !a.pre) return;
   pull_vertices_short<L, UPL, true>(a);
 }

@@ -95,68 +95,6 @@ __global__ void k_probe(Table t, const void *keycol, int ktype, uint64_t n,
   block_add(s, total);
 }
 
-// Count-only Flat x Flat joins use a table whose slot is one 16-byte pair
-// (stored key, multiplicity): a probe reads key and count in one sector, the
-// build's count add hits the line its key CAS just brought in, and the empty
-// table is all zeros (the stored key is ~key, so the all-ones key, stored as
-// 0, gets the extra slot at index cap).
-struct CountTable {
-  unsigned long long *slot;  // 2 x (cap + 1) words: (stored key, count) pairs
-  uint64_t cap;
-};
-
-__device__ __forceinline__ uint64_t ct_insert(const CountTable &t, unsigned long long k) {
-  if (k == ~0ull) return t.cap;
-  const unsigned long long sk = ~k;
-  uint64_t h = ht_hash(k) & (t.cap - 1);
-  for (uint64_t probe = 0; probe <= t.cap; probe++) {
-    const unsigned long long old = atomicCAS(&t.slot[2 * h], 0ull, sk);
-    if (old == 0ull || old == sk) return h;
-    h = (h + 1) & (t.cap - 1);
-  }
-  return ~0ull;
-}
-
-__global__ void k_count_build(CountTable t, const void *keycol, int ktype, uint64_t n) {
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
-    const uint64_t i = i0 + threadIdx.x;
-    const bool valid = i < n;
-    const unsigned long long k = valid ? load_key(keycol, ktype, i) : EMPTY - 1;
-    const unsigned active = __ballot_sync(FULL, valid);
-    const unsigned peers = __match_any_sync(FULL, k) & active;
-    if (valid && (int)(threadIdx.x & 31) == __ffs(peers) - 1) {
-      const uint64_t s = ct_insert(t, k);
-      if (s != ~0ull) atomicAdd(&t.slot[2 * s + 1], (unsigned long long)__popc(peers));
-    }
-  }
-}
-
-// Sum over probe rows of the multiplicity of their key in the table.
-__global__ void k_count_probe(CountTable t, const void *keycol, int ktype, uint64_t n, unsigned long long *total) {
-  unsigned long long s = 0;
-  const ulonglong2 *slots = reinterpret_cast<const ulonglong2 *>(t.slot);
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const unsigned long long k = load_key(keycol, ktype, i);
-    if (k == ~0ull) {
-      s += slots[t.cap].y;
-      continue;
-    }
-    const unsigned long long sk = ~k;
-    uint64_t h = ht_hash(k) & (t.cap - 1);
-    for (uint64_t probe = 0; probe <= t.cap; probe++) {
-      const ulonglong2 x = slots[h];
-      if (x.x == sk) {
-        s += x.y;
-        break;
-      }
-      if (x.x == 0ull) break;
-      h = (h + 1) & (t.cap - 1);
-    }
-  }
-  block_add(s, total);
-}
-
 // Flat x Mat count: sum over matrix columns of multiplicity(key) * popcount.
 __global__ void k_count_mat(Table t, const uint64_t *__restrict__ w, uint32_t cols, uint32_t wpc,
                             const uint32_t *col_map, unsigned long long *total) {
@@ -368,32 +306,23 @@ int join_flat_flat(FlatSide a, FlatSide b, bool only_count, uint64_t max_rows, v
   const bool build_a = a.f->nrows < b.f->nrows;
   const FlatSide &bd = build_a ? a : b, &pr = build_a ? b : a;
   Scratch sc{st};
-  if (only_count) {  // one table of (key, count) pairs, one zero fill, a build and a probe
-    CountTable ct;
-    ct.cap = ht_capacity(std::max<uint64_t>(bd.f->nrows, 1));
-    unsigned long long *d_total;
-    VS_TRY(sc.get(&ct.slot, 2 * (ct.cap + 1) + 1));
-    d_total = ct.slot + 2 * (ct.cap + 1);
-    VS_CK(cudaMemsetAsync(ct.slot, 0, 8 * (2 * (ct.cap + 1) + 1), st));
-    if (bd.f->nrows)
-      { k_count_build<<<grid_for(bd.f->nrows), 256, 0, st>>>(ct, bd.f->cols[bd.key], bd.f->types[bd.key],
-                                                           bd.f->nrows); vs::note_launch(); }
-    if (pr.f->nrows)
-      { k_count_probe<<<grid_for(pr.f->nrows), 256, 0, st>>>(ct, pr.f->cols[pr.key], pr.f->types[pr.key],
-                                                           pr.f->nrows, d_total); vs::note_launch(); }
-    VS_CK(cudaGetLastError());
-    return read_total(d_total, count, st);
-  }
   Table t;
-  VS_TRY(table_alloc(sc, bd.f->nrows, false, true, &t));
+  VS_TRY(table_alloc(sc, bd.f->nrows, false, !only_count, &t));
   uint32_t *slot_of = nullptr;
-  VS_TRY(sc.get(&slot_of, bd.f->nrows));
+  if (!only_count) VS_TRY(sc.get(&slot_of, bd.f->nrows));
   if (bd.f->nrows)
     { k_build<<<grid_for(bd.f->nrows), 256, 0, st>>>(t, bd.f->cols[bd.key], bd.f->types[bd.key],
                                                    bd.f->nrows, slot_of); vs::note_launch(); }
   unsigned long long *d_total;
   VS_TRY(sc.get(&d_total, 1));
   VS_CK(cudaMemsetAsync(d_total, 0, 8, st));
+  if (only_count) {
+    if (pr.f->nrows)
+      { k_probe<<<grid_for(pr.f->nrows), 256, 0, st>>>(t, pr.f->cols[pr.key], pr.f->types[pr.key],
+                                                     pr.f->nrows, nullptr, nullptr, d_total); vs::note_launch(); }
+    VS_CK(cudaGetLastError());
+    return read_total(d_total, count, st);
+  }
   // group build rows by key
   VS_TRY(exclusive_scan_u64(t.cnt, t.off, t.cap + 1, st));
   uint32_t *rows_by_key;

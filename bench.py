@@ -754,11 +754,13 @@ def run_gpu(args, w, rank, world, local_rank):
             step_learned()
         torch.cuda.synchronize()
         l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push("learned")
         l0.record(stream)
         for _ in range(args.steps):
             jc3, tc3 = step_learned()
         l1.record(stream)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         assert (jc3, tc3) == (jc, tc), "learned-picker results differ from the fixed planner"
         ms_l = l0.elapsed_time(l1) / args.steps
         learned = {"queries_per_s": 1000.0 / ms_l, "ms_per_step": ms_l,

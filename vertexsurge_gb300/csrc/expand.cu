@@ -262,9 +262,13 @@ __global__ void __launch_bounds__(64) k_decide(DecideArgs a) {
     }
     __syncthreads();
     if (use_picker) {
-      __shared__ __nv_bfloat16 w[pk::NPARAM];  // the network, staged with coalesced loads
+      // the network, staged with 16-byte loads (the weight buffer is 16-byte aligned)
+      __shared__ __align__(16) __nv_bfloat16 w[(pk::NPARAM + 7) / 8 * 8];
       const __nv_bfloat16 *gw = (const __nv_bfloat16 *)a.picker;
-      for (int i = t; i < pk::NPARAM; i += blockDim.x) w[i] = gw[i];
+      constexpr int NV = pk::NPARAM / 8;
+      for (int i = t; i < NV; i += blockDim.x)
+        reinterpret_cast<uint4 *>(w)[i] = __ldg(reinterpret_cast<const uint4 *>(gw) + i);
+      for (int i = NV * 8 + t; i < pk::NPARAM; i += blockDim.x) w[i] = gw[i];
       __syncthreads();
       {
         float acc = __bfloat162float(w[pk::OFF_B1 + t]);

@@ -474,37 +474,58 @@ __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
     // up to 32 pairs: lane j holds the first edge of pair plo + j, and an
     // edge's pair is found by counting those starts at or below it
     const uint32_t npr = (uint32_t)(phi - plo + 1);
-    const unsigned long long dj = (npr <= 32 && (uint32_t)lane < npr) ? a.doff[plo + lane] : ~0ull;
+    // up to 32 pairs: lane j holds pair plo + j (its first edge, source id,
+    // and its vertex's list starts and first-list length), so the rounds
+    // below take them by shuffle instead of loading them per edge
+    const bool few = npr <= 32;
+    unsigned long long dj = ~0ull;
+    uint32_t pi = 0;
+    int64_t pb0 = 0, pd0 = 0, pb1 = 0;
+    if (few && (uint32_t)lane < npr) {
+      dj = a.doff[plo + lane];
+      const uint2 pr = a.pin[plo + lane];
+      pi = pr.y;
+      pb0 = a.out.off[0][pr.x];
+      pd0 = a.out.off[0][pr.x + 1] - pb0;
+      if (a.out.n > 1) pb1 = a.out.off[1][pr.x];
+    }
     uint32_t nloc = 0;  // new pairs of this chunk so far (s_new)
     for (unsigned long long eb = e0; eb < e1; eb += 32) {
       const unsigned long long e = eb + lane;
       bool fresh = false;
       uint32_t v = 0, i = 0;
-      uint64_t lo = plo;
-      if (npr <= 32) {
+      unsigned long long j = 0;  // the edge's index in its pair's out-lists
+      int64_t b0 = 0, d0 = 0, b1 = 0;
+      if (few) {
         uint32_t cnt = 0;
-        for (uint32_t j = 0; j < npr; j++) cnt += __shfl_sync(FULL, dj, j) <= e;
-        lo = plo + (cnt ? cnt - 1 : 0);
+        for (uint32_t q = 0; q < npr; q++) cnt += __shfl_sync(FULL, dj, q) <= e;
+        const int own = cnt ? (int)cnt - 1 : 0;
+        i = __shfl_sync(FULL, pi, own);
+        b0 = __shfl_sync(FULL, pb0, own);
+        d0 = __shfl_sync(FULL, pd0, own);
+        b1 = __shfl_sync(FULL, pb1, own);
+        j = e - __shfl_sync(FULL, dj, own);
       } else if (e < e1) {
-        uint64_t hi = phi + 1;
+        uint64_t lo = plo, hi = phi + 1;
         while (hi - lo > 1) {
           const uint64_t mid = (lo + hi) >> 1;
           if (a.doff[mid] <= e) lo = mid; else hi = mid;
         }
+        const uint2 pr = a.pin[lo];
+        i = pr.y;
+        j = e - a.doff[lo];
+        b0 = a.out.off[0][pr.x];
+        d0 = a.out.off[0][pr.x + 1] - b0;
+        if (a.out.n > 1) b1 = a.out.off[1][pr.x];
       }
       if (e < e1) {
-        const uint2 pr = a.pin[lo];
-        const uint32_t u = pr.x;
-        i = pr.y;
         const uint32_t wi = i >> 6;
         const unsigned long long bit = 1ull << (i & 63);
         if (!a.hmask || (__ldg(a.hmask + wi) & bit)) {
-          unsigned long long j = e - a.doff[lo];
-          const int64_t b0 = a.out.off[0][u], d0 = a.out.off[0][u + 1] - b0;
           if ((int64_t)j < d0)
             v = a.out.adj[0][b0 + j];
           else
-            v = a.out.adj[1][a.out.off[1][u] + (int64_t)j - d0];
+            v = a.out.adj[1][b1 + (int64_t)j - d0];
           const size_t idx = (size_t)v * a.W + wi;
           if (a.shortest) {
             const unsigned long long old = atomicOr(&a.vis[idx], bit);

@@ -35,7 +35,10 @@ __device__ __forceinline__ uint64_t ht_insert(const HashTable &t, unsigned long 
   }
   uint64_t h = ht_hash(k) & (t.cap - 1);
   for (uint64_t probe = 0; probe <= t.cap; probe++) {
-    unsigned long long old = atomicCAS(&t.keys[h], HT_EMPTY, k);
+    // a slot already holding a key is read, not CAS-ed: a hot key's slot is
+    // then only read by the many warps that meet it
+    unsigned long long old = t.keys[h];
+    if (old == HT_EMPTY) old = atomicCAS(&t.keys[h], HT_EMPTY, k);
     if (old == HT_EMPTY || old == k) return h;
     h = (h + 1) & (t.cap - 1);
   }

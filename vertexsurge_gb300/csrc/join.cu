@@ -60,6 +60,50 @@ __global__ void k_build(Table t, const void *keycol, int ktype, uint64_t n, uint
   }
 }
 
+// Count-only build: each block first counts its rows' keys in a table of
+// its own in shared memory and adds every key's block count to the global
+// table once, so a hot key costs one global atomic per block instead of one
+// per warp (a Zipf-skewed key column sends most warps to the same slot).
+// Keys that find no shared slot within a few probes go to the global table
+// directly.
+constexpr int LOC_SLOTS = 4096;
+__global__ void __launch_bounds__(256) k_build_count(Table t, const void *keycol, int ktype, uint64_t n) {
+  __shared__ unsigned long long s_key[LOC_SLOTS];
+  __shared__ uint32_t s_cnt[LOC_SLOTS];
+  for (int i = threadIdx.x; i < LOC_SLOTS; i += blockDim.x) {
+    s_key[i] = EMPTY;
+    s_cnt[i] = 0;
+  }
+  __syncthreads();
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const unsigned long long k = load_key(keycol, ktype, i);
+    bool done = false;
+    if (k != EMPTY) {  // the all-ones key goes straight to its reserved global slot
+      uint32_t h = (uint32_t)ht_hash(k) & (LOC_SLOTS - 1);
+      for (int probe = 0; probe < 8 && !done; probe++) {
+        unsigned long long old = s_key[h];
+        if (old == EMPTY) old = atomicCAS(&s_key[h], EMPTY, k);
+        if (old == EMPTY || old == k) {
+          atomicAdd(&s_cnt[h], 1u);
+          done = true;
+        }
+        h = (h + 1) & (LOC_SLOTS - 1);
+      }
+    }
+    if (!done) {
+      const uint64_t slot = ht_insert(t, k);
+      atomicAdd(&t.cnt[slot], 1ull);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < LOC_SLOTS; i += blockDim.x)
+    if (s_cnt[i]) {
+      const uint64_t slot = ht_insert(t, s_key[i]);
+      atomicAdd(&t.cnt[slot], (unsigned long long)s_cnt[i]);
+    }
+}
+
 // Build over matrix columns: key = col_map[c] (or c) -> first column index.
 __global__ void k_build_cols(Table t, const uint32_t *col_map, uint32_t cols) {
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < cols; c += gridDim.x * blockDim.x) {
@@ -310,7 +354,10 @@ int join_flat_flat(FlatSide a, FlatSide b, bool only_count, uint64_t max_rows, v
   VS_TRY(table_alloc(sc, bd.f->nrows, false, !only_count, &t));
   uint32_t *slot_of = nullptr;
   if (!only_count) VS_TRY(sc.get(&slot_of, bd.f->nrows));
-  if (bd.f->nrows)
+  if (bd.f->nrows && only_count)
+    { k_build_count<<<std::min(grid_for(bd.f->nrows), 4 * sm_count()), 256, 0, st>>>(
+          t, bd.f->cols[bd.key], bd.f->types[bd.key], bd.f->nrows); vs::note_launch(); }
+  else if (bd.f->nrows)
     { k_build<<<grid_for(bd.f->nrows), 256, 0, st>>>(t, bd.f->cols[bd.key], bd.f->types[bd.key],
                                                    bd.f->nrows, slot_of); vs::note_launch(); }
   unsigned long long *d_total;

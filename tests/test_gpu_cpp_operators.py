@@ -33,16 +33,24 @@ def _undirected(g):
 
 
 @pytest.mark.parametrize("undirected", [False, True])
-def test_graph_directory_through_cpp_loader(tmp_path, undirected):
-    """Graph(dir).load() reads the reference's directory layout; the count of
-    an expand over it equals the oracle's on the same arrays."""
+@pytest.mark.parametrize("layout", ["csr", "flat", "blocks"])
+def test_graph_directory_through_cpp_loader(tmp_path, undirected, layout):
+    """Graph(dir).load() reads the reference's directory layout (CSR files,
+    or only a flat edge list, one file or target blocks, from which it builds
+    the CSR); the count of an expand over it equals the oracle's on the same
+    arrays."""
     from oracle import pyoracle as O
     from tests import graphs as G
     from vertexsurge_gb300 import graph_dir
     g = G.small_graphs()["rmat10"]
     if undirected:
         g = _undirected(g)
-    graph_dir.save(tmp_path, g)
+    if layout == "csr":
+        graph_dir.save(tmp_path, g)
+    elif layout == "flat":
+        graph_dir.save(tmp_path, g, csr=False, flats=("random",))
+    else:
+        graph_dir.save(tmp_path, g, csr=False, partitioned={"hilbert": 6})
     r = subprocess.run([str(build.OPS_TEST), "--graph-dir", str(tmp_path)], capture_output=True, text=True,
                        timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr

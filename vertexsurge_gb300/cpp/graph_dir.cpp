@@ -17,6 +17,7 @@
 #include <sys/stat.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <cctype>
 #include <cstring>
 #include <fstream>
@@ -41,6 +42,12 @@ struct Json {
       for (auto &kv : obj)
         if (kv.first == k) return kv.second;
     throw Error(VS_ERR_ARG, "schema.json: missing key \"" + k + "\"");
+  }
+  const Json *find(const std::string &k) const {
+    if (kind == Obj)
+      for (auto &kv : obj)
+        if (kv.first == k) return &kv.second;
+    return nullptr;
   }
 };
 
@@ -218,6 +225,58 @@ std::string backward_edge_name(const TypeName &src, const TypeName &e, const Typ
   return directed ? dst + "<-" + e + "-" + src : dst + "-" + e + "-" + src;
 }
 
+namespace {
+
+// CSR (offsets, targets sorted per list) of the edges from[i] -> to[i].
+void csr_of_pairs(size_t V, const std::vector<uint32_t> &from, const std::vector<uint32_t> &to,
+                  std::vector<int64_t> &off, std::vector<uint32_t> &adj) {
+  off.assign(V + 1, 0);
+  for (uint32_t a : from) {
+    if (a >= V) throw Error(VS_ERR_ARG, "flat edge list: vertex id out of range");
+    off[a + 1]++;
+  }
+  for (size_t v = 0; v < V; v++) off[v + 1] += off[v];
+  adj.assign(from.size(), 0);
+  std::vector<int64_t> cur(off.begin(), off.end() - 1);
+  for (size_t i = 0; i < from.size(); i++) adj[cur[from[i]]++] = to[i];
+  for (size_t v = 0; v < V; v++) std::sort(adj.begin() + off[v], adj.begin() + off[v + 1]);
+}
+
+// The forward flat edge list of an edge type (its first unpartitioned order,
+// else the blocks of its first partitioned order), as (src, dst) columns:
+// the reference's flat files are VIDPair DiskArrays named
+// "{edge name}_{order}[_{block}]" (meta/schema.cpp:69-97,
+// meta/graph_loader.hh:202-276).
+bool read_forward_flat(const std::filesystem::path &dir, const Json &e, const std::string &edge_name,
+                       std::vector<uint32_t> &src, std::vector<uint32_t> &dst) {
+  const Json *info = e.find("store_info");
+  if (!info) return false;
+  std::vector<std::string> files;
+  const Json *flats = info->find("flats");
+  const Json *parts = info->find("partitioned_flats");
+  const Json *counts = info->find("partition_counts");
+  if (flats && !flats->arr.empty()) {
+    files.push_back(edge_name + "_" + flats->arr[0].str);
+  } else if (parts && counts && !parts->arr.empty() && !counts->arr.empty()) {
+    for (size_t i = 0; i < (size_t)counts->arr[0].num; i++)
+      files.push_back(edge_name + "_" + parts->arr[0].str + "_" + std::to_string(i));
+  } else {
+    return false;
+  }
+  for (const std::string &name : files) {
+    Mapped m;
+    map_disk_array(dir / name, 2 * sizeof(uint32_t), m);
+    const uint32_t *p = static_cast<const uint32_t *>(m.data());
+    for (int64_t i = 0; i < m.count; i++) {
+      src.push_back(p[2 * i]);
+      dst.push_back(p[2 * i + 1]);
+    }
+  }
+  return true;
+}
+
+}  // namespace
+
 void Graph::load_dir() {
   std::ifstream f(dir / "schema.json");
   if (!f) throw Error(VS_ERR_ARG, "no schema.json in " + dir.string());
@@ -257,6 +316,22 @@ void Graph::load_dir() {
     const uint64_t E = (uint64_t)e.at("statistics").at("count").num;
     const size_t V = vertex_count.at(src);
     const std::string fwd = forward_edge_name(src, type, dst, directed) + "_csr_src_dst";
+    if (!std::filesystem::exists(dir / (fwd + "_index"))) {  // no CSR files: build them from a flat list
+      std::vector<uint32_t> s, d;
+      if (!read_forward_flat(dir, e, forward_edge_name(src, type, dst, directed), s, d))
+        throw Error(VS_ERR_ARG, "edge type " + src + "_" + type + "_" + dst + ": neither CSR files nor flat edge lists");
+      if (s.size() != E)
+        throw Error(VS_ERR_ARG, "edge type " + src + "_" + type + "_" + dst + ": flat edge list length " +
+                                    std::to_string(s.size()) + ", expected " + std::to_string(E));
+      std::vector<int64_t> fo, ro;
+      std::vector<uint32_t> fa, ra;
+      csr_of_pairs(V, s, d, fo, fa);
+      if (directed)
+        csr_of_pairs(V, d, s, ro, ra);
+      add_edge_type(src, type, dst, directed, (uint32_t)V, E, fo.data(), fa.data(),
+                    directed ? ro.data() : fo.data(), directed ? ra.data() : fa.data());
+      continue;
+    }
     Mapped fi, fd, bi, bd;
     map_disk_array(dir / (fwd + "_index"), sizeof(int64_t), fi);
     map_disk_array(dir / fwd, sizeof(uint32_t), fd);

@@ -56,9 +56,11 @@ def test_picker_drives_the_planner_and_results_stay_exact(vs, cls, strategy):
     g = graphgen.rmat(12, 16, seed=4)
     dg = vs.DeviceGraph.from_host(g)
     src = graphgen.sample_sources(g.V, 300, seed=8)
-    for path in ("any", "shortest"):
+    for path, push_on in (("any", True), ("shortest", True), ("shortest", False)):
         plan = vs.ExpandPlan(dg, len(src), vs.make_params(1, 4, path, "forward", use_picker=True))
         plan.set_picker(constant_picker(vs, cls))
+        if push_on:  # PUSH is opt-in: the picker chooses it only where the plan launches its kernels
+            plan.set_tuning(push_frac=1e-9)
         plan.run(src)
         st = plan.stats()
         exp, _, _ = O.vexpand(g, src, 1, 4, path, "forward")
@@ -66,6 +68,8 @@ def test_picker_drives_the_planner_and_results_stay_exact(vs, cls, strategy):
         got = st["strategy"][1:]
         if strategy == 3:  # sparse runs while its pair list is valid, then falls back
             assert got[0] == 3
+        elif strategy == 2 and not push_on:  # the next-best class instead
+            assert all(s == 1 for s in got), got
         else:
             assert all(s == strategy for s in got), got
 
@@ -86,6 +90,40 @@ def test_hop_overrides_and_feature_logging(vs):
     f = plan.features()[1:n + 1]
     assert np.all(np.isfinite(f)) and f.max() <= 4.0 and f.min() >= 0.0
     assert np.allclose(f[:, 16:].sum(axis=1), 1.0, atol=1e-5)  # degree histogram normalised
+
+
+@pytest.mark.parametrize("path", ["shortest", "any"])
+def test_frontier_statistics_same_under_every_strategy(vs, path):
+    """E_active and the out-degree histogram of a hop's frontier come from the
+    seed (hop 1), from the SPARSE hop that wrote the layer (counted as its rows
+    became non-zero) or from a pass over the frontier flags after a PULL or
+    PUSH hop: the features they give are the same under every strategy, E_active
+    equals the oracle's, and hop 1's histogram is that of the distinct sources."""
+    g = graphgen.rmat(12, 16, seed=4)
+    dg = vs.DeviceGraph.from_host(g)
+    src = graphgen.sample_sources(g.V, 200, seed=9)
+    src[:6] = src[6:12]  # repeated sources: each distinct vertex is one row
+    _, _, ost = O.vexpand(g, src, 1, 4, path, "forward", hop_stats=True)
+    feats = {}
+    for strat in ("sparse", "pull", "push"):
+        plan = vs.ExpandPlan(dg, len(src), vs.make_params(1, 4, path, "forward"))
+        plan.set_hop_strategies([0] + [strat] * 4)
+        plan.log_features(True)
+        plan.set_tuning(collect_stats=True)
+        plan.run(src)
+        st = plan.stats()
+        n = st["hops_run"]
+        assert st["active_edges"][1:] == ost["active_edges"][1:n + 1], (strat, st["active_edges"])
+        feats[strat] = plan.features()[1:n + 1]
+        plan.free()
+    for strat in ("pull", "push"):
+        k = min(len(feats[strat]), len(feats["sparse"]))
+        assert np.array_equal(feats[strat][:k, 16:], feats["sparse"][:k, 16:]), strat
+        assert np.array_equal(feats[strat][:k, 10:12], feats["sparse"][:k, 10:12]), strat
+    d = np.diff(g.fwd_off)[np.unique(src)]
+    bins = np.minimum(15, np.floor(np.log2(d + 1.0)).astype(int))
+    h1 = np.bincount(bins, minlength=16) / len(d)
+    assert np.allclose(feats["sparse"][0, 16:], h1, atol=1e-6)
 
 
 @pytest.mark.parametrize("cls", [0, 1, 2])

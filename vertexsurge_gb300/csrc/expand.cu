@@ -98,8 +98,15 @@ __global__ void k_clear_flagged(uint4 *__restrict__ buf, uint32_t *__restrict__ 
 }
 
 // Layer 0 (ExpandStatus::init_first_m_layer, expand_impl.hh:252-277).
+__device__ __forceinline__ int degree_bin(unsigned long long d) {
+  return min(pk::NHIST - 1, 63 - __clzll((long long)(d + 1)));
+}
+
 __global__ void k_seed(SeedArgs a) {
-  unsigned long long pe = 0, nv = 0;
+  __shared__ unsigned s_hist[pk::NHIST];  // hop 1's frontier statistics (a.stats)
+  if (threadIdx.x < pk::NHIST) s_hist[threadIdx.x] = 0;
+  __syncthreads();
+  unsigned long long pe = 0, nv = 0, ae = 0;
   if (blockIdx.x == 0 && threadIdx.x == 0) {  // counters set on the device: the run has no host copies
     a.ctr->multislice = a.multislice;
     a.ctr->hop[0].pairs = a.S;
@@ -117,7 +124,8 @@ __global__ void k_seed(SeedArgs a) {
     size_t idx = (size_t)v * a.W + (i >> 6);
     unsigned long long bit = 1ull << (i & 63);
     atomicOr((unsigned long long *)&a.buf0[idx], bit);
-    if (atomicOr(&a.flag0[v], 1u) == 0) nv++;
+    const bool first = atomicOr(&a.flag0[v], 1u) == 0;
+    if (first) nv++;
     if (a.vis) atomicOr((unsigned long long *)&a.vis[idx], bit);
     if (a.acc) atomicOr((unsigned long long *)&a.acc[idx], bit);
     if ((a.vis && a.res_vis) || a.acc) a.resflag[v] = 1;
@@ -126,9 +134,18 @@ __global__ void k_seed(SeedArgs a) {
     _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < a.out.n) d += (unsigned long long)(a.out.off[l][v + 1] - a.out.off[l][v]);
     a.pdeg0[i] = d;
     pe += d;
+    if (a.stats && first) {  // each distinct source vertex once, as the stats pass counts rows
+      ae += d;
+      atomicAdd(&s_hist[degree_bin(d)], 1u);
+    }
   }
   block_add(pe, &a.ctr->hop[0].pair_edges);
   block_add(nv, &a.ctr->hop[0].active_vertices);
+  if (a.stats) {
+    block_add(ae, &a.ctr->hop[1].active_edges);
+    if (threadIdx.x < pk::NHIST && s_hist[threadIdx.x])
+      atomicAdd(&a.ctr->hop[1].hist[threadIdx.x], (unsigned long long)s_hist[threadIdx.x]);
+  }
 }
 
 // FindShortest bookkeeping before hop 1 (VExpand::before_execution, vexpand.cpp:179-195).
@@ -188,12 +205,12 @@ __global__ void k_row_mask(const uint8_t *__restrict__ lim, uint32_t n, uint32_t
   if (over) rowk[1] = 1;
 }
 
-// One block of 64 threads: early-stop checks of hop h-1 (VExpand::after_child,
+// One block of 256 threads: early-stop checks of hop h-1 (VExpand::after_child,
 // vexpand.cpp:222-284), the fixed planner's choice for hop h, and — when a
 // picker is loaded or features are logged — the feature vector of hop h and
 // the picker network's choice.
-__global__ void __launch_bounds__(64) k_decide(DecideArgs a) {
-  __shared__ float f[pk::NF], h1[pk::H1], h2[pk::H2], out[pk::NO];
+__global__ void __launch_bounds__(256) k_decide(DecideArgs a) {
+  __shared__ float f[pk::NF], out[pk::NO];
   __shared__ int s_run, s_choice, s_pairs_ok;
   const int t = threadIdx.x;
   Ctr *c = a.ctr;
@@ -238,61 +255,38 @@ __global__ void __launch_bounds__(64) k_decide(DecideArgs a) {
   if (use_picker || a.log_features) {
     if (t == 0) {
       pk::HopFeatIn in;
-      in.S = a.S;
-      in.V = a.V;
-      in.E = (double)a.E;
-      in.W = a.W;
-      in.h = a.h;
-      in.k_min = a.k_min;
-      in.k_max = a.k_max;
-      in.new_bits_prev = (double)prev.new_bits;
-      in.active_prev = (double)prev.active_vertices;
-      double vis = 0;
-      for (int i = 0; i < a.h; i++) vis += (double)c->hop[i].new_bits;
-      in.visited_bits = vis;
-      in.active_edges = (double)cur.active_edges;
-      in.pair_edges = s_pairs_ok ? (double)prev.pair_edges : 0.0;
-      in.pairs_ok = s_pairs_ok;
-      in.shortest = a.path != VS_PATH_ANY;
-      in.both = a.both;
+      in.S = (float)a.S;
+      in.V = (float)a.V;
+      in.E = (float)a.E;
+      in.W = (float)a.W;
+      in.h = (float)a.h;
+      in.k_min = (float)a.k_min;
+      in.k_max = (float)a.k_max;
+      in.new_bits_prev = (float)prev.new_bits;
+      in.active_prev = (float)prev.active_vertices;
+      unsigned long long vis = 0;
+      for (int i = 0; i < a.h; i++) vis += c->hop[i].new_bits;
+      in.visited_bits = (float)vis;
+      in.active_edges = (float)cur.active_edges;
+      in.pair_edges = s_pairs_ok ? (float)prev.pair_edges : 0.f;
+      in.pairs_ok = (float)s_pairs_ok;
+      in.shortest = a.path != VS_PATH_ANY ? 1.f : 0.f;
+      in.both = (float)a.both;
       in.hist = cur.hist;
       pk::hop_features(in, f);
       if (a.log_features)
         for (int i = 0; i < pk::NF; i++) c->feat[a.h][i] = f[i];
     }
     __syncthreads();
-    if (use_picker) {
-      // the network, staged with 16-byte loads (the weight buffer is 16-byte aligned)
-      __shared__ __align__(16) __nv_bfloat16 w[(pk::NPARAM + 7) / 8 * 8];
-      const __nv_bfloat16 *gw = (const __nv_bfloat16 *)a.picker;
-      constexpr int NV = pk::NPARAM / 8;
-      for (int i = t; i < NV; i += blockDim.x)
-        reinterpret_cast<uint4 *>(w)[i] = __ldg(reinterpret_cast<const uint4 *>(gw) + i);
-      for (int i = NV * 8 + t; i < pk::NPARAM; i += blockDim.x) w[i] = gw[i];
-      __syncthreads();
-      {
-        float acc = __bfloat162float(w[pk::OFF_B1 + t]);
-        for (int i = 0; i < pk::NF; i++) acc += __bfloat162float(w[pk::OFF_W1 + t * pk::NF + i]) * f[i];
-        h1[t] = acc > 0.f ? acc : 0.f;
-      }
-      __syncthreads();
-      {
-        float acc = __bfloat162float(w[pk::OFF_B2 + t]);
-        for (int i = 0; i < pk::H1; i++) acc += __bfloat162float(w[pk::OFF_W2 + t * pk::H1 + i]) * h1[i];
-        h2[t] = acc > 0.f ? acc : 0.f;
-      }
-      __syncthreads();
-      if (t < pk::NO) {
-        float acc = __bfloat162float(w[pk::OFF_B3 + t]);
-        for (int i = 0; i < pk::H2; i++) acc += __bfloat162float(w[pk::OFF_W3 + t * pk::H2 + i]) * h2[i];
-        out[t] = acc;
-      }
-      __syncthreads();
+    // one choice left (no pair list, no PUSH in the plan): PULL without the network
+    if (use_picker && (s_pairs_ok || a.push_ok)) {
+      pk::mlp_block(a.picker, f, out);
       if (t == 0) {
         int best = -1;
         for (int k = 0; k < pk::NO; k++) {
           const int st = pk::class_to_strategy(k);
           if (st == ST_SPARSE && !s_pairs_ok) continue;  // no pair list to expand from
+          if (st == ST_PUSH && !a.push_ok) continue;      // the plan launches no PUSH kernels
           if (best < 0 || out[k] > out[best]) best = k;
         }
         s_choice = pk::class_to_strategy(best);
@@ -322,8 +316,14 @@ __global__ void __launch_bounds__(64) k_decide(DecideArgs a) {
 
 // Per-hop frontier statistics of layer h-1: E_active (out-degrees of its
 // non-zero rows) and the log2(out-degree + 1) histogram of those rows.
-__global__ void k_hop_stats(const uint32_t *__restrict__ flagF, Lists out, uint32_t V, Ctr *ctr, int h) {
-  if (ctr->done) return;
+// Layers written by the seed or by a SPARSE hop already have these counts
+// (counted as their rows became non-zero), so the pass exits at once; so it
+// does when only the picker reads them (picker_only) and the hop has a single
+// choice: no pair list after a PULL or PUSH hop, and no PUSH in the plan.
+__global__ void k_hop_stats(const uint32_t *__restrict__ flagF, Lists out, uint32_t V, Ctr *ctr, int h,
+                            int picker_only, int push_ok) {
+  if (ctr->done || h == 1 || ctr->hop[h - 1].strategy == ST_SPARSE) return;
+  if (picker_only && !push_ok) return;
   __shared__ unsigned long long hist[pk::NHIST];
   if (threadIdx.x < pk::NHIST) hist[threadIdx.x] = 0;
   __syncthreads();
@@ -336,7 +336,7 @@ __global__ void k_hop_stats(const uint32_t *__restrict__ flagF, Lists out, uint3
       unsigned long long d = 0;
       _Pragma("unroll") for (int l = 0; l < 2; l++) if (l < out.n) d += (unsigned long long)(out.off[l][v + 1] - out.off[l][v]);
       s += d;
-      b = min(pk::NHIST - 1, 63 - __clzll((long long)(d + 1)));
+      b = degree_bin(d);
     }
     const unsigned peers = __match_any_sync(FULL, b);
     if (b >= 0 && (peers & lanemask_lt()) == 0) atomicAdd(&hist[b], (unsigned long long)__popc(peers));
@@ -445,13 +445,16 @@ __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
   Ctr *c = a.ctr;
   if (c->hop[a.h].strategy != ST_SPARSE) return;
   __shared__ uint2 s_new[8][SPARSE_CHUNK];  // a warp's new pairs of its current chunk
+  __shared__ unsigned s_hist[pk::NHIST];    // hop h+1's frontier statistics (a.stats)
+  if (threadIdx.x < pk::NHIST) s_hist[threadIdx.x] = 0;
+  __syncthreads();
   const unsigned long long np_raw = c->hop[a.h - 1].pairs;
   const uint64_t np = np_raw < a.cap ? np_raw : a.cap;
   const unsigned long long T = a.doff[np];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
   const uint64_t nchunks = (T + SPARSE_CHUNK - 1) / SPARSE_CHUNK;
-  unsigned long long nb = 0, nv = 0, pe = 0;
+  unsigned long long nb = 0, nv = 0, pe = 0, ae = 0;
   for (uint64_t ck = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib; ck < nchunks; ck += warps) {
     const unsigned long long e0 = ck * SPARSE_CHUNK;
     const unsigned long long e1 = min(e0 + SPARSE_CHUNK, T);
@@ -492,7 +495,7 @@ __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
     uint32_t nloc = 0;  // new pairs of this chunk so far (s_new)
     for (unsigned long long eb = e0; eb < e1; eb += 32) {
       const unsigned long long e = eb + lane;
-      bool fresh = false;
+      bool fresh = false, first = false;
       uint32_t v = 0, i = 0;
       unsigned long long j = 0;  // the edge's index in its pair's out-lists
       int64_t b0 = 0, d0 = 0, b1 = 0;
@@ -540,14 +543,18 @@ __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
           if (fresh) {
             if (a.acc_on) atomicOr(&a.acc[idx], bit);
             if (a.res_vis || a.acc_on) a.resflag[v] = 1;
-            if (atomicOr(&a.flagN[v], 1u) == 0) nv++;
+            if (atomicOr(&a.flagN[v], 1u) == 0) {
+              nv++;
+              first = true;
+            }
             nb++;
           }
         }
       }
       // the chunk's new pairs gather in shared memory (one list append per chunk)
       const unsigned m = __ballot_sync(FULL, fresh);
-      if (fresh) s_new[wib][nloc + __popc(m & lanemask_lt())] = make_uint2(v, i);
+      // bit 31 of the source id (S < 2^31) marks the pair that made its row non-zero
+      if (fresh) s_new[wib][nloc + __popc(m & lanemask_lt())] = make_uint2(v, i | (first ? 0x80000000u : 0u));
       nloc += __popc(m);
     }
     __syncwarp();
@@ -556,9 +563,14 @@ __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
       if (lane == 0) base = atomicAdd(&c->hop[a.h].pairs, (unsigned long long)nloc);
       base = __shfl_sync(FULL, base, 0);
       for (uint32_t j = lane; j < nloc; j += 32) {
-        const uint2 pr = s_new[wib][j];
+        const uint2 pf = s_new[wib][j];
+        const uint2 pr = make_uint2(pf.x, pf.y & 0x7FFFFFFFu);
         const unsigned long long d = out_degree(a.out, pr.x);
         pe += d;
+        if (a.stats && (pf.y >> 31)) {  // each row of layer h once, as the stats pass counts them
+          ae += d;
+          atomicAdd(&s_hist[degree_bin(d)], 1u);
+        }
         const unsigned long long slot = base + j;
         if (slot < a.cap) {
           a.pout[slot] = pr;
@@ -574,6 +586,11 @@ __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
   block_add(nb, &c->hop[a.h].new_bits);
   block_add(nv, &c->hop[a.h].active_vertices);
   block_add(pe, &c->hop[a.h].pair_edges);
+  if (a.stats) {
+    block_add(ae, &c->hop[a.h + 1].active_edges);
+    if (threadIdx.x < pk::NHIST && s_hist[threadIdx.x])
+      atomicAdd(&c->hop[a.h + 1].hist[threadIdx.x], (unsigned long long)s_hist[threadIdx.x]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1895,6 +1912,7 @@ int vs_expand_plan_create(vs_graph *g, uint32_t S, const vs_expand_params *p,
   if (p->pull_kernel < 0 || p->pull_kernel > 7) return fail(VS_ERR_ARG, "pull kernel variant must be 0..7");
   if (p->sparse_frac < 0) return fail(VS_ERR_ARG, "sparse_frac must be >= 0");
   if (S == 0) return fail(VS_ERR_ARG, "no start vertex for VExpand");
+  if (S >= 0x80000000u) return fail(VS_ERR_ARG, "VExpand takes fewer than 2^31 start vertices");
   cudaStream_t st = 0;
   vs_expand_plan *pl = new vs_expand_plan();
   pl->g = g;
@@ -2083,6 +2101,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   sa.V = V;
   sa.multislice = pl->nslices > 1;
   sa.rowk = pl->use_hmask ? pl->rowk : nullptr;
+  sa.stats = pl->collect_stats || pl->log_features || (pl->picker && p.use_picker);
   { k_seed<<<std::max(1u, std::min((S_ + 255) / 256, (uint32_t)sm_count() * 4)), 256, 0, st>>>(sa); vs::note_launch(); }
   VS_CK(cudaGetLastError());
   if (pl->layer_out[0])
@@ -2103,11 +2122,13 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     return pl->slot[0] != nullptr && hh >= 1 && hh < p.k_max && p.path_type != VS_PATH_FIND_SHORTEST &&
            pl->layer_out[hh] == nullptr;
   };
-  // PUSH runs only when forced (for the run or a hop), enabled in the fixed
-  // planner (push_frac > 0) or left to the picker
+  // PUSH runs only when forced (for the run or a hop) or enabled in the
+  // fixed planner (push_frac > 0)
   bool any_forced_push = forced == ST_PUSH;
   for (uint32_t hh = 1; hh <= p.k_max; hh++) any_forced_push |= pl->hop_forced[hh] == ST_PUSH;
-  const bool can_push = any_forced_push || pl->push_frac > 0 || (pl->picker && p.use_picker);
+  // (the picker chooses PUSH only where the plan enables it)
+  const bool can_push = any_forced_push || pl->push_frac > 0;
+  const bool stats = pl->collect_stats || pl->log_features || (pl->picker && p.use_picker);
   for (uint32_t h = 1; h <= p.k_max; h++) {
     const int fb = (h - 1) & 1, nbuf = h & 1;
     DecideArgs da;
@@ -2125,16 +2146,22 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     da.push_frac = pl->push_frac;
     da.picker = pl->picker;
     da.picker_on = p.use_picker;
+    da.push_ok = can_push;
     da.rowk = pl->use_hmask ? pl->rowk : nullptr;
     da.short_min = pl->short_min;
     da.l2_half = l2_bytes() / 2;
     da.W = W;
     da.k_min = p.k_min;
     da.k_max = p.k_max;
+    // the seed and SPARSE hops count their layer's statistics; after a PULL or
+    // PUSH hop only a picker that may choose PUSH (or logging) needs the pass
+    const bool picker_only = !pl->collect_stats && !pl->log_features;
+    if (stats && h > 1 && !(picker_only && !can_push))
+      { k_hop_stats<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], outl, V, pl->ctr, h, picker_only, can_push);
+        vs::note_launch(); }
+    { k_decide<<<1, 256, 0, st>>>(da); vs::note_launch(); }
+    // hop_ms covers what the chosen strategy costs, not the statistics and decision before it
     if (timing) cudaEventRecord(pl->ev[3 * h], st);
-    if (pl->collect_stats || pl->log_features || (pl->picker && p.use_picker))
-      { k_hop_stats<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], outl, V, pl->ctr, h); vs::note_launch(); }
-    { k_decide<<<1, 64, 0, st>>>(da); vs::note_launch(); }
     if (pl->slot[0] && leave_in_slots(h - 1))  // whole rows back for a hop that reads rows
       { k_materialize<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<uint4 *>(pl->buf[fb]), V, Q,
                                                 pl->slot[fb], pl->slot_n, pl->ctr, h, 1); vs::note_launch(); }
@@ -2161,6 +2188,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     sp.acc_on = acc_on;
     sp.doff = pl->doff;
     sp.pdeg_out = pl->pdeg[nbuf];
+    sp.stats = stats && h < p.k_max;
     { k_pscan1<<<pl->grid_v, 256, 0, st>>>(pl->pdeg[fb], pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
     { k_pscan2<<<1, 1024, 0, st>>>(pl->bsum, pl->doff, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
     { k_pscan3<<<pl->grid_v, 256, 0, st>>>(pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap); vs::note_launch(); }

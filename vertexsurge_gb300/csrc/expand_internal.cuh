@@ -59,11 +59,13 @@ struct SeedArgs {
   Ctr *ctr;
   int multislice;  // PULL runs in several source slices
   const uint32_t *rowk;  // row-limit words of the plan (NULL: no row limits)
+  int stats;  // also count hop 1's frontier statistics (active_edges, hist) of layer 0
 };
 
 struct DecideArgs {
   Ctr *ctr;
   int h, path, forced, picker_on, log_features, both;
+  int push_ok;  // the plan launches PUSH kernels (the picker may choose PUSH)
   uint32_t S, V, W, k_min, k_max;
   uint64_t E, pair_cap;
   double sparse_frac, push_frac;
@@ -89,6 +91,7 @@ struct SparseArgs {
   unsigned long long *N, *vis, *acc;
   uint32_t *flagN;
   int shortest, acc_on;
+  int stats;  // also count hop h+1's frontier statistics (active_edges, hist) of the layer it writes
 };
 
 struct PushArgs {

@@ -278,71 +278,103 @@ __global__ void __launch_bounds__(256) k_isect(Args a) {
 // k_isect.
 constexpr int ISECT_SAMPLE = 4096;
 
-__global__ void __launch_bounds__(1024) k_isect_decide(Args a, uint32_t V, uint64_t E, int has_hubs,
-                                                       const void *picker, float *feat_out, int *method) {
+// One sample per thread over ISECT_SAMPLE / 256 blocks; each block writes its
+// sums to part[block][32] and the last block to finish (counted in ctl[1])
+// adds them in block order, so the features do not depend on timing.
+constexpr int ISECT_DECIDE_THREADS = 256;
+constexpr int ISECT_DECIDE_BLOCKS = ISECT_SAMPLE / ISECT_DECIDE_THREADS;
+
+__global__ void __launch_bounds__(ISECT_DECIDE_THREADS) k_isect_decide(Args a, uint32_t V, uint64_t E, int has_hubs,
+                                                                       const void *picker, float *feat_out, int *ctl,
+                                                                       float *part) {
+  __shared__ float wsum[ISECT_DECIDE_THREADS / 32][32];
   __shared__ float acc[32];
-  __shared__ float f[pk::NF], h1[pk::H1], h2[pk::H2], out[pk::NO];
-  if (threadIdx.x < 32) acc[threadIdx.x] = 0.f;
-  __syncthreads();
+  __shared__ float f[pk::NF], out[pk::NO];
+  __shared__ int s_last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint64_t n = a.nbase < (uint64_t)ISECT_SAMPLE ? a.nbase : (uint64_t)ISECT_SAMPLE;
-  // acc: 0 samples, 1 empty, 2 sum log len_walk, 3 sum log len_other, 4 sum log ratio, 5 hub, 6 ratio<=8,
-  //      7 bitmap rule, 8 other-list count, 16..23 hist log len_walk, 24..31 hist log ratio;
-  // summed per thread, then per warp, then once per warp into shared memory
+  // loc: 0 samples, 1 empty, 2 sum log len_walk, 3 sum log len_other, 4 sum log ratio, 5 hub, 6 ratio<=8,
+  //      7 bitmap rule, 8 other-list count, 16..23 hist log len_walk, 24..31 hist log ratio
   float loc[32];
 #pragma unroll
   for (int j = 0; j < 32; j++) loc[j] = 0.f;
-  for (uint64_t k = threadIdx.x; k < n; k += blockDim.x) {
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) {
     const uint64_t t = n == a.nbase ? k : k * a.nbase / n;
-    float lw = 0.f;
+    // every sorted dependency's list length and hub flag, loaded once
+    int64_t len[MAX_DEPS];
+    bool hub[MAX_DEPS], sorted[MAX_DEPS];
     int64_t walk = -1;
     bool empty = false;
-    for (int i = 0; i < a.ndeps; i++) {
-      const Dep &d = a.dep[i];
-      if (d.kind != DEP_SORTED) continue;
-      const uint32_t u = d.base_u[t];
-      const int64_t len = u < d.n_u ? d.off[u + 1] - d.off[u] : 0;
-      if (len == 0) empty = true;
-      if (walk < 0 || len < walk) walk = len;
-    }
-    loc[0] += 1.f;
-    if (walk < 0) continue;
-    if (empty) {
-      loc[1] += 1.f;
-      continue;
-    }
-    lw = log2f(1.f + (float)walk);
-    loc[2] += lw;
-    const int hb = min(7, (int)(lw * 0.5f));
 #pragma unroll
-    for (int b = 0; b < 8; b++) loc[16 + b] += hb == b ? 1.f : 0.f;
-    bool walked = false;
-    for (int i = 0; i < a.ndeps; i++) {
+    for (int i = 0; i < MAX_DEPS; i++) {
+      len[i] = 0;
+      hub[i] = sorted[i] = false;
+      if (i >= a.ndeps) break;
       const Dep &d = a.dep[i];
       if (d.kind != DEP_SORTED) continue;
+      sorted[i] = true;
       const uint32_t u = d.base_u[t];
-      const int64_t len = d.off[u + 1] - d.off[u];
-      if (len == walk && !walked) {
-        walked = true;
-        continue;
+      if (u < d.n_u) {
+        len[i] = d.off[u + 1] - d.off[u];
+        hub[i] = d.hub_slot && d.hub_slot[u] >= 0;
       }
-      const float lo = log2f(1.f + (float)len), lr = log2f((float)len / (float)walk);
-      const bool hub = d.hub_slot && d.hub_slot[u] >= 0;
-      loc[3] += lo;
-      loc[4] += lr;
-      loc[8] += 1.f;
-      if (hub) loc[5] += 1.f;
-      if (walk >= 512 && len <= 4 * walk) loc[6] += 1.f;
-      if (hub) loc[7] += 1.f;
-      const int rb = max(0, min(7, (int)lr));
+      if (len[i] == 0) empty = true;
+      if (walk < 0 || len[i] < walk) walk = len[i];
+    }
+    loc[0] = 1.f;
+    if (walk >= 0 && empty) loc[1] = 1.f;
+    if (walk >= 0 && !empty) {
+      const float lw = log2f(1.f + (float)walk);
+      loc[2] = lw;
+      const int hb = min(7, (int)(lw * 0.5f));
 #pragma unroll
-      for (int b = 0; b < 8; b++) loc[24 + b] += rb == b ? 1.f : 0.f;
+      for (int b = 0; b < 8; b++) loc[16 + b] = hb == b ? 1.f : 0.f;
+      bool walked = false;
+#pragma unroll
+      for (int i = 0; i < MAX_DEPS; i++) {
+        if (i >= a.ndeps) break;
+        if (!sorted[i]) continue;
+        if (len[i] == walk && !walked) {
+          walked = true;
+          continue;
+        }
+        const float lo = log2f(1.f + (float)len[i]), lr = log2f((float)len[i] / (float)walk);
+        loc[3] += lo;
+        loc[4] += lr;
+        loc[8] += 1.f;
+        if (hub[i]) loc[5] += 1.f;
+        if (walk >= 512 && len[i] <= 4 * walk) loc[6] += 1.f;
+        if (hub[i]) loc[7] += 1.f;
+        const int rb = max(0, min(7, (int)lr));
+#pragma unroll
+        for (int b = 0; b < 8; b++) loc[24 + b] += rb == b ? 1.f : 0.f;
+      }
     }
   }
+  // warp sums, then the block's in warp order, then the blocks' in block order
 #pragma unroll
   for (int j = 0; j < 32; j++) {
     float v = loc[j];
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && v != 0.f) atomicAdd(&acc[j], v);
+    if (lane == j) wsum[wid][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = 0.f;
+    for (int w = 0; w < ISECT_DECIDE_THREADS / 32; w++) v += wsum[w][threadIdx.x];
+    part[blockIdx.x * 32 + threadIdx.x] = v;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd((unsigned *)&ctl[1], 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (threadIdx.x < 32) {
+    float v = 0.f;
+    for (unsigned b = 0; b < gridDim.x; b++) v += __ldcg(part + b * 32 + threadIdx.x);
+    acc[threadIdx.x] = v;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -373,32 +405,13 @@ __global__ void __launch_bounds__(1024) k_isect_decide(Args a, uint32_t V, uint6
       for (int i = 0; i < pk::NF; i++) feat_out[i] = f[i];
   }
   __syncthreads();
-  if (!picker || !method) return;
-  const __nv_bfloat16 *w = (const __nv_bfloat16 *)picker;
-  const int t = threadIdx.x;
-  if (t < pk::H1) {
-    float s = __bfloat162float(w[pk::OFF_B1 + t]);
-    for (int i = 0; i < pk::NF; i++) s += __bfloat162float(w[pk::OFF_W1 + t * pk::NF + i]) * f[i];
-    h1[t] = s > 0.f ? s : 0.f;
-  }
-  __syncthreads();
-  if (t < pk::H2) {
-    float s = __bfloat162float(w[pk::OFF_B2 + t]);
-    for (int i = 0; i < pk::H1; i++) s += __bfloat162float(w[pk::OFF_W2 + t * pk::H1 + i]) * h1[i];
-    h2[t] = s > 0.f ? s : 0.f;
-  }
-  __syncthreads();
-  if (t < pk::NO) {
-    float s = __bfloat162float(w[pk::OFF_B3 + t]);
-    for (int i = 0; i < pk::H2; i++) s += __bfloat162float(w[pk::OFF_W3 + t * pk::H2 + i]) * h2[i];
-    out[t] = s;
-  }
-  __syncthreads();
-  if (t == 0) {
+  if (!picker) return;
+  pk::mlp_block(picker, f, out);
+  if (threadIdx.x == 0) {
     int best = 0;
-    for (int k = 1; k < pk::NO; k++)
-      if (out[k] > out[best]) best = k;
-    *method = best == 0 ? VS_ISECT_AUTO : best == 1 ? VS_ISECT_BINARY : VS_ISECT_BITMAP;
+    for (int c = 1; c < pk::NO; c++)
+      if (out[c] > out[best]) best = c;
+    ctl[0] = best == 0 ? VS_ISECT_AUTO : best == 1 ? VS_ISECT_BINARY : VS_ISECT_BITMAP;
   }
 }
 
@@ -704,15 +717,18 @@ int vs_mintersect_ex(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps
       hubs |= a.dep[i].hub_slot != nullptr;
     }
   if ((method_picker || features) && fg && !a.all_mat) {
-    int *d_method = nullptr;
-    float *d_feat = nullptr;
-    VS_TRY(sc.get(&d_method, 1));
+    int *d_ctl = nullptr;  // [0] the method (VS_ISECT_AUTO until the network decides), [1] blocks done
+    float *d_feat = nullptr, *d_part = nullptr;
+    VS_TRY(sc.get(&d_ctl, 2));
     VS_TRY(sc.get(&d_feat, pk::NF));
-    VS_CK(cudaMemsetAsync(d_method, 0, sizeof(int), st));  // VS_ISECT_AUTO until the network decides
-    { k_isect_decide<<<1, 1024, 0, st>>>(a, fg->V, fg->E, hubs ? 1 : 0,
-                                      method_picker ? vs_picker_device_weights(method_picker) : nullptr, d_feat,
-                                      d_method); vs::note_launch(); }
-    a.method = method_picker ? d_method : nullptr;
+    VS_TRY(sc.get(&d_part, ISECT_DECIDE_BLOCKS * 32));
+    VS_CK(cudaMemsetAsync(d_ctl, 0, 2 * sizeof(int), st));
+    const uint64_t ns = std::min<uint64_t>(a.nbase, ISECT_SAMPLE);
+    const int gblocks = std::max<int>(1, (int)((ns + ISECT_DECIDE_THREADS - 1) / ISECT_DECIDE_THREADS));
+    { k_isect_decide<<<gblocks, ISECT_DECIDE_THREADS, 0, st>>>(
+          a, fg->V, fg->E, hubs ? 1 : 0, method_picker ? vs_picker_device_weights(method_picker) : nullptr, d_feat,
+          d_ctl, d_part); vs::note_launch(); }
+    a.method = method_picker ? d_ctl : nullptr;
     if (features) VS_CK(cudaMemcpyAsync(features, d_feat, sizeof(float) * pk::NF, cudaMemcpyDefault, st));
   } else if (features) {
     std::memset(features, 0, sizeof(float) * pk::NF);

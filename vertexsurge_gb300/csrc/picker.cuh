@@ -18,41 +18,100 @@ constexpr int NF = 32, H1 = 64, H2 = 64, NO = 3;
 constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + H1 * NF, OFF_W2 = OFF_B1 + H1, OFF_B2 = OFF_W2 + H2 * H1,
               OFF_W3 = OFF_B2 + H2, OFF_B3 = OFF_W3 + NO * H2, NPARAM = OFF_B3 + NO;
 constexpr int NHIST = 16;
+static_assert((NF & (NF - 1)) == 0 && (H1 & (H1 - 1)) == 0, "rotated dot products need power-of-two widths");
 
 // class index -> strategy code of the expand kernels
 __host__ __device__ inline int class_to_strategy(int c) { return c == 0 ? 1 : (c == 1 ? 2 : 3); }
 __host__ __device__ inline int strategy_to_class(int s) { return s == 1 ? 0 : (s == 2 ? 1 : 2); }
 
 struct HopFeatIn {
-  double S, V, E, W, h, k_min, k_max;
-  double new_bits_prev, active_prev, visited_bits, active_edges, pair_edges;
-  double pairs_ok, shortest, both;
+  float S, V, E, W, h, k_min, k_max;
+  float new_bits_prev, active_prev, visited_bits, active_edges, pair_edges;
+  float pairs_ok, shortest, both;
   const unsigned long long *hist;  // NHIST bins of log2(out-degree + 1) over active rows
 };
 
-__device__ __forceinline__ float lg(double x) { return (float)log2(1.0 + x); }
+__device__ __forceinline__ float lg(float x) { return log2f(1.f + x); }
 
+// Single-precision throughout: the features are fp32 network inputs, and a
+// hop's decide block runs on the critical path of the run.
 __device__ inline void hop_features(const HopFeatIn &in, float *f) {
-  const double SV = in.S * in.V;
-  f[0] = (float)(in.new_bits_prev / SV);
-  f[1] = (float)(in.active_prev / in.V);
+  const float SV = in.S * in.V;
+  f[0] = in.new_bits_prev / SV;
+  f[1] = in.active_prev / in.V;
   f[2] = lg(in.active_prev) / 32.f;
-  f[3] = (float)(in.visited_bits / SV);
+  f[3] = in.visited_bits / SV;
   f[4] = lg(in.S) / 16.f;
-  f[5] = (float)(in.W / 256.0);
+  f[5] = in.W / 256.f;
   f[6] = lg(in.V) / 32.f;
   f[7] = lg(in.E) / 40.f;
-  f[8] = (float)(in.E / in.V / 64.0);
-  f[9] = (float)(in.h / 8.0);
-  f[10] = (float)(in.active_edges / in.E);
+  f[8] = in.E / in.V / 64.f;
+  f[9] = in.h / 8.f;
+  f[10] = in.active_edges / in.E;
   f[11] = lg(in.active_edges) / 40.f;
-  f[12] = (float)in.pairs_ok;
-  f[13] = (float)in.shortest;
-  f[14] = (float)in.both;
+  f[12] = in.pairs_ok;
+  f[13] = in.shortest;
+  f[14] = in.both;
   f[15] = lg(in.pair_edges) / 40.f;
-  double tot = 0;
-  for (int b = 0; b < NHIST; b++) tot += (double)in.hist[b];
-  for (int b = 0; b < NHIST; b++) f[16 + b] = tot > 0 ? (float)((double)in.hist[b] / tot) : 0.f;
+  unsigned long long tot = 0;
+  for (int b = 0; b < NHIST; b++) tot += in.hist[b];
+  const float r = tot ? 1.f / (float)tot : 0.f;
+  for (int b = 0; b < NHIST; b++) f[16 + b] = (float)in.hist[b] * r;
+}
+
+// Inference by a whole block (every thread must call it; blockDim.x = P * H1
+// with P a power of two, P = 2..16): the bf16 parameters (16-byte aligned) are
+// staged in shared memory with 16-byte loads; each hidden unit's dot product
+// is split over P adjacent lanes, each starting at its own offset so a warp's
+// lanes read different banks, and summed by shuffles; each output unit is one
+// warp's.  out[NO] must be shared memory.
+__device__ inline void mlp_block(const void *params, const float *f, float *out) {
+  __shared__ __align__(16) __nv_bfloat16 w[(NPARAM + 7) / 8 * 8];
+  __shared__ float h1[H1], h2[H2];
+  const int t = threadIdx.x, lane = t & 31;
+  const __nv_bfloat16 *gw = (const __nv_bfloat16 *)params;
+  constexpr int NV = NPARAM / 8;
+  for (int i = t; i < NV; i += blockDim.x)
+    reinterpret_cast<uint4 *>(w)[i] = __ldg(reinterpret_cast<const uint4 *>(gw) + i);
+  for (int i = NV * 8 + t; i < NPARAM; i += blockDim.x) w[i] = gw[i];
+  __syncthreads();
+  const int P = blockDim.x / H1, u = t / P, p = t & (P - 1);
+  {
+    const int n = NF / P;
+    float acc = 0.f;
+    for (int k = 0; k < n; k++) {
+      const int i = p * n + ((k + u) & (n - 1));
+      acc += __bfloat162float(w[OFF_W1 + u * NF + i]) * f[i];
+    }
+    for (int o = P >> 1; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (p == 0) {
+      acc += __bfloat162float(w[OFF_B1 + u]);
+      h1[u] = acc > 0.f ? acc : 0.f;
+    }
+  }
+  __syncthreads();
+  {
+    const int n = H1 / P;
+    float acc = 0.f;
+    for (int k = 0; k < n; k++) {
+      const int i = p * n + ((k + 2 * u) & (n - 1));
+      acc += __bfloat162float(w[OFF_W2 + u * H1 + i]) * h1[i];
+    }
+    for (int o = P >> 1; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (p == 0) {
+      acc += __bfloat162float(w[OFF_B2 + u]);
+      h2[u] = acc > 0.f ? acc : 0.f;
+    }
+  }
+  __syncthreads();
+  if (t < NO * 32) {
+    const int o3 = t >> 5;
+    float acc = 0.f;
+    for (int i = lane; i < H2; i += 32) acc += __bfloat162float(w[OFF_W3 + o3 * H2 + i]) * h2[i];
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[o3] = acc + __bfloat162float(w[OFF_B3 + o3]);
+  }
+  __syncthreads();
 }
 
 // One sample through the network, computed by one thread (64 FMAs per

@@ -785,8 +785,11 @@ def run_gpu(args, w, rank, world, local_rank):
                 "bytes_per_launch": pull_comp / max(1, pull_launches),
                 "traffic": traffic,
                 "dram_frac": (traffic / (per_launch_ms / 1e3) / 1e9) / peak if traffic and per_launch_ms else None,
-                "traffic_source": f"profiles/{rl_kernel}_{args.workload}.md (ncu dram__bytes_read.sum + "
-                                  "dram__bytes_write.sum per working launch)",
+                "traffic_source": (f"profiles/{rl_kernel}_{args.workload}.md (ncu dram__bytes_read.sum + "
+                                   "dram__bytes_write.sum per working launch)") if traffic else
+                                  ("not captured at this size (a DRAM-counter capture of a full-size launch holds "
+                                   "too much device memory); the 1M-vertex instance's layers are several times "
+                                   "denser per row, so its traffic does not scale to these hops by units processed"),
                 "kernel": (f"{rl_kernel} (expand A, PULL hops {sorted(pull_hop_ms)}, short mode on "
                            f"{ {h: ('words', 'slots')[stA['short_pull'][h] - 1] for h in short_hops} })"),
                 "peak_source": peak_kind,

@@ -168,7 +168,8 @@ typedef struct vs_expand_params {
   int32_t path_type;       /* VS_PATH_* */
   int32_t direction;       /* VS_DIR_* */
   int32_t strategy;        /* VS_STRAT_*: AUTO lets the planner choose per hop */
-  int32_t use_picker;      /* 1: the learned picker chooses under AUTO (when loaded) */
+  int32_t use_picker;      /* 1: the learned picker chooses under AUTO (when loaded); it may choose
+                              PUSH only where the plan runs PUSH (push_frac > 0 or a forced hop) */
   uint32_t hub_threshold;  /* in-degree above which a vertex gets a whole CTA (0 = tuned default) */
   uint32_t slice_words;    /* source words per pass (0 = whole row up to 256 words) */
   uint64_t pair_capacity;  /* sparse (vertex, source) list capacity (0 = default) */

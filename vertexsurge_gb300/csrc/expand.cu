@@ -354,6 +354,7 @@ __global__ void k_hop_stats(const uint32_t *__restrict__ flagF, Lists out, uint3
 // takes fixed chunks of that edge range, so a pair on a 50k-degree hub is
 // spread over many warps instead of serialising one.
 constexpr int SPARSE_CHUNK = 256;  // edges per warp task
+constexpr int SPARSE_K = 2;        // edges per lane per round
 
 // Pairs the SPARSE hop h scans (0 when the hop runs another strategy).
 __device__ __forceinline__ uint64_t scan_len(const Ctr *ctr, int h, uint64_t cap) {
@@ -441,7 +442,7 @@ __device__ __forceinline__ unsigned long long out_degree(const Lists &L, uint32_
   return d;
 }
 
-__global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
+__global__ void __launch_bounds__(256, 4) k_sparse(SparseArgs a) {
   Ctr *c = a.ctr;
   if (c->hop[a.h].strategy != ST_SPARSE) return;
   __shared__ uint2 s_new[8][SPARSE_CHUNK];  // a warp's new pairs of its current chunk
@@ -493,72 +494,90 @@ __global__ void __launch_bounds__(256) k_sparse(SparseArgs a) {
       if (a.out.n > 1) pb1 = a.out.off[1][pr.x];
     }
     uint32_t nloc = 0;  // new pairs of this chunk so far (s_new)
-    for (unsigned long long eb = e0; eb < e1; eb += 32) {
-      const unsigned long long e = eb + lane;
-      bool fresh = false, first = false;
-      uint32_t v = 0, i = 0;
-      unsigned long long j = 0;  // the edge's index in its pair's out-lists
-      int64_t b0 = 0, d0 = 0, b1 = 0;
-      if (few) {
-        uint32_t cnt = 0;
-        for (uint32_t q = 0; q < npr; q++) cnt += __shfl_sync(FULL, dj, q) <= e;
-        const int own = cnt ? (int)cnt - 1 : 0;
-        i = __shfl_sync(FULL, pi, own);
-        b0 = __shfl_sync(FULL, pb0, own);
-        d0 = __shfl_sync(FULL, pd0, own);
-        b1 = __shfl_sync(FULL, pb1, own);
-        j = e - __shfl_sync(FULL, dj, own);
-      } else if (e < e1) {
-        uint64_t lo = plo, hi = phi + 1;
-        while (hi - lo > 1) {
-          const uint64_t mid = (lo + hi) >> 1;
-          if (a.doff[mid] <= e) lo = mid; else hi = mid;
+    // SPARSE_K edges per lane per round, each phase issued for all of them
+    // before the next: the adjacency loads, then the returning atomics on the
+    // visited (or next-layer) words, then the row flags, so a lane keeps
+    // SPARSE_K dependent chains in flight instead of one
+    for (unsigned long long eb = e0; eb < e1; eb += 32 * SPARSE_K) {
+      uint32_t v[SPARSE_K], i[SPARSE_K];
+      bool act[SPARSE_K];
+#pragma unroll
+      for (int k = 0; k < SPARSE_K; k++) {
+        const unsigned long long e = eb + k * 32 + lane;
+        unsigned long long j = 0;  // the edge's index in its pair's out-lists
+        int64_t b0 = 0, d0 = 0, b1 = 0;
+        v[k] = 0;
+        i[k] = 0;
+        if (few) {  // the last pair whose first edge is at or below e (starts ascend with the lane)
+          int own = 0;
+#pragma unroll
+          for (int step = 16; step; step >>= 1)
+            if (__shfl_sync(FULL, dj, own + step) <= e) own += step;
+          i[k] = __shfl_sync(FULL, pi, own);
+          b0 = __shfl_sync(FULL, pb0, own);
+          d0 = __shfl_sync(FULL, pd0, own);
+          b1 = __shfl_sync(FULL, pb1, own);
+          j = e - __shfl_sync(FULL, dj, own);
+        } else if (e < e1) {
+          uint64_t lo = plo, hi = phi + 1;
+          while (hi - lo > 1) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (a.doff[mid] <= e) lo = mid; else hi = mid;
+          }
+          const uint2 pr = a.pin[lo];
+          i[k] = pr.y;
+          j = e - a.doff[lo];
+          b0 = a.out.off[0][pr.x];
+          d0 = a.out.off[0][pr.x + 1] - b0;
+          if (a.out.n > 1) b1 = a.out.off[1][pr.x];
         }
-        const uint2 pr = a.pin[lo];
-        i = pr.y;
-        j = e - a.doff[lo];
-        b0 = a.out.off[0][pr.x];
-        d0 = a.out.off[0][pr.x + 1] - b0;
-        if (a.out.n > 1) b1 = a.out.off[1][pr.x];
+        act[k] = e < e1 && (!a.hmask || ((__ldg(a.hmask + (i[k] >> 6)) >> (i[k] & 63)) & 1ull));
+        if (act[k]) v[k] = (int64_t)j < d0 ? a.out.adj[0][b0 + j] : a.out.adj[1][b1 + (int64_t)j - d0];
       }
-      if (e < e1) {
-        const uint32_t wi = i >> 6;
-        const unsigned long long bit = 1ull << (i & 63);
-        if (!a.hmask || (__ldg(a.hmask + wi) & bit)) {
-          if ((int64_t)j < d0)
-            v = a.out.adj[0][b0 + j];
-          else
-            v = a.out.adj[1][b1 + (int64_t)j - d0];
-          const size_t idx = (size_t)v * a.W + wi;
-          if (a.shortest) {
-            const unsigned long long old = atomicOr(&a.vis[idx], bit);
-            if (!(old & bit)) {
-              atomicOr(&a.N[idx], bit);
-              fresh = true;
-            }
-          } else {
-            const unsigned long long old = atomicOr(&a.N[idx], bit);
-            fresh = !(old & bit);
-          }
-          if (fresh) {
-            if (a.acc_on) atomicOr(&a.acc[idx], bit);
-            if (a.res_vis || a.acc_on) a.resflag[v] = 1;
-            if (atomicOr(&a.flagN[v], 1u) == 0) {
-              nv++;
-              first = true;
-            }
-            nb++;
-          }
+      unsigned long long old[SPARSE_K];
+#pragma unroll
+      for (int k = 0; k < SPARSE_K; k++) {
+        old[k] = ~0ull;  // an inactive edge sets nothing
+        if (act[k]) {
+          const size_t idx = (size_t)v[k] * a.W + (i[k] >> 6);
+          // Shortest dedups through the visited bit, Any through the next-layer bit
+          old[k] = atomicOr(a.shortest ? &a.vis[idx] : &a.N[idx], 1ull << (i[k] & 63));
         }
       }
-      // the chunk's new pairs gather in shared memory (one list append per chunk)
-      const unsigned m = __ballot_sync(FULL, fresh);
+      bool fresh[SPARSE_K];
+#pragma unroll
+      for (int k = 0; k < SPARSE_K; k++) {
+        fresh[k] = !((old[k] >> (i[k] & 63)) & 1ull);
+        if (fresh[k]) {
+          const size_t idx = (size_t)v[k] * a.W + (i[k] >> 6);
+          const unsigned long long bit = 1ull << (i[k] & 63);
+          if (a.shortest && !a.last) atomicOr(&a.N[idx], bit);
+          if (a.acc_on) atomicOr(&a.acc[idx], bit);
+          if (a.res_vis || a.acc_on) a.resflag[v[k]] = 1;
+          nb++;
+        }
+      }
+      bool first[SPARSE_K];
+#pragma unroll
+      for (int k = 0; k < SPARSE_K; k++) {
+        // a last layer's rows stay zero in the buffer (flag 2: the run start skips them)
+        first[k] = fresh[k] && atomicOr(&a.flagN[v[k]], a.last ? 2u : 1u) == 0;
+        nv += first[k];
+      }
+      // the chunk's new pairs gather in shared memory (one list append per chunk);
       // bit 31 of the source id (S < 2^31) marks the pair that made its row non-zero
-      if (fresh) s_new[wib][nloc + __popc(m & lanemask_lt())] = make_uint2(v, i | (first ? 0x80000000u : 0u));
-      nloc += __popc(m);
+#pragma unroll
+      for (int k = 0; k < SPARSE_K; k++) {
+        const unsigned m = __ballot_sync(FULL, fresh[k]);
+        if (fresh[k])
+          s_new[wib][nloc + __popc(m & lanemask_lt())] = make_uint2(v[k], i[k] | (first[k] ? 0x80000000u : 0u));
+        nloc += __popc(m);
+      }
     }
     __syncwarp();
-    if (nloc) {  // append the chunk's new pairs (with their out-degrees) to layer h's list
+    if (nloc && a.last) {  // a last layer's pairs are counted, not kept
+      if (lane == 0) atomicAdd(&c->hop[a.h].pairs, (unsigned long long)nloc);
+    } else if (nloc) {  // append the chunk's new pairs (with their out-degrees) to layer h's list
       unsigned long long base = 0;
       if (lane == 0) base = atomicAdd(&c->hop[a.h].pairs, (unsigned long long)nloc);
       base = __shfl_sync(FULL, base, 0);
@@ -2189,6 +2208,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     sp.doff = pl->doff;
     sp.pdeg_out = pl->pdeg[nbuf];
     sp.stats = stats && h < p.k_max;
+    sp.last = h == p.k_max && pl->use_vis && p.path_type != VS_PATH_FIND_SHORTEST && !pl->layer_out[h];
     { k_pscan1<<<pl->grid_v, 256, 0, st>>>(pl->pdeg[fb], pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
     { k_pscan2<<<1, 1024, 0, st>>>(pl->bsum, pl->doff, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
     { k_pscan3<<<pl->grid_v, 256, 0, st>>>(pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap); vs::note_launch(); }

@@ -92,6 +92,7 @@ struct SparseArgs {
   uint32_t *flagN;
   int shortest, acc_on;
   int stats;  // also count hop h+1's frontier statistics (active_edges, hist) of the layer it writes
+  int last;   // Shortest, and layer h is read by nothing: no next-layer rows or pairs, rows flagged 2
 };
 
 struct PushArgs {

@@ -269,6 +269,86 @@ __global__ void __launch_bounds__(256) k_isect(Args a) {
   if (!a.emit && lane == 0 && tot) atomicAdd(a.total, tot);
 }
 
+// Count-only intersection of two sorted adjacency dependencies (triangle
+// closing, the pattern query's T).  A warp takes 32 base tuples at a time,
+// lane j loading tuple j's two list bounds, so the tuples' dependent loads
+// overlap; the candidates of the 32 walked (shorter) lists are then laid end
+// to end and dealt one per lane per round, so short lists leave no lane idle.
+// A lane finds its candidate's tuple by a shuffle search over the lanes'
+// first candidate positions and tests it against the other list: one bit of
+// that vertex's adjacency bitmap where it has one (and the method allows),
+// else a binary search.  The count equals the general kernel's.
+__global__ void __launch_bounds__(256) k_isect_pair_count(Args a) {
+  const int lane = threadIdx.x & 31;
+  const Dep &d0 = a.dep[0], &d1 = a.dep[1];
+  const int learned = a.method ? *a.method : VS_ISECT_AUTO;
+  unsigned long long cnt = 0;
+  for (;;) {
+    unsigned long long t0 = 0;
+    if (lane == 0) t0 = atomicAdd(a.next, 32ull);
+    t0 = __shfl_sync(FULLMASK, t0, 0);
+    if (t0 >= a.nbase) break;
+    const uint64_t t = t0 + lane;
+    // this lane's tuple: walked list [wlo, wlo + wn) of dep w1, other list [olo, ohi) with bitmap slot hs
+    int64_t wlo = 0, wn = 0, olo = 0, ohi = 0;
+    int w1 = 0, hs = -1;
+    if (t < a.nbase) {
+      const uint32_t u0 = d0.base_u[t], u1 = d1.base_u[t];
+      int64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
+      if (u0 < d0.n_u) {
+        lo0 = d0.off[u0];
+        hi0 = d0.off[u0 + 1];
+      }
+      if (u1 < d1.n_u) {
+        lo1 = d1.off[u1];
+        hi1 = d1.off[u1 + 1];
+      }
+      if (lo0 < hi0 && lo1 < hi1) {
+        w1 = hi1 - lo1 < hi0 - lo0;  // the shorter list; dep 0 on a tie, as the general kernel
+        const Dep &o = w1 ? d0 : d1;
+        wlo = w1 ? lo1 : lo0;
+        wn = w1 ? hi1 - lo1 : hi0 - lo0;
+        olo = w1 ? lo0 : lo1;
+        ohi = w1 ? hi0 : hi1;
+        const int algo = o.algo == VS_ISECT_AUTO ? learned : o.algo;
+        if (o.hub_slot && algo != VS_ISECT_BINARY) hs = __ldg(o.hub_slot + (w1 ? u0 : u1));
+      }
+    }
+    unsigned long long incl = (unsigned long long)wn;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(FULLMASK, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const unsigned long long total = __shfl_sync(FULLMASK, incl, 31);
+    const unsigned long long start = incl - (unsigned long long)wn;
+    for (unsigned long long c0 = 0; c0 < total; c0 += 32) {
+      const unsigned long long c = c0 + lane;
+      int own = 0;  // the last lane whose first candidate is at or below c (it owns c when c < total)
+#pragma unroll
+      for (int step = 16; step; step >>= 1)
+        if (__shfl_sync(FULLMASK, start, own + step) <= c) own += step;
+      const unsigned long long ost = __shfl_sync(FULLMASK, start, own);
+      const int64_t owlo = __shfl_sync(FULLMASK, wlo, own);
+      const int64_t oolo = __shfl_sync(FULLMASK, olo, own);
+      const int64_t oohi = __shfl_sync(FULLMASK, ohi, own);
+      const int ow1 = __shfl_sync(FULLMASK, w1, own);
+      const int ohs = __shfl_sync(FULLMASK, hs, own);
+      if (c < total) {
+        const Dep &w = ow1 ? d1 : d0, &o = ow1 ? d0 : d1;
+        const uint32_t x = __ldg(w.adj + owlo + (int64_t)(c - ost));
+        if (x < a.cache_rows) {
+          const bool keep = ohs >= 0 ? ((__ldg(o.hub_bm + (size_t)ohs * o.hub_words + (x >> 6)) >> (x & 63)) & 1ull)
+                                     : in_sorted(o.adj, oolo, oohi, x);
+          cnt += keep;
+        }
+      }
+    }
+  }
+  for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULLMASK, cnt, o);
+  if (lane == 0 && cnt) atomicAdd(a.total, cnt);
+}
+
 // Features of one call for the learned membership method, from up to
 // ISECT_SAMPLE base tuples spread over the base table: list lengths of the
 // walked (shortest) list and of the other adjacency lists, their ratios and how
@@ -746,7 +826,13 @@ int vs_mintersect_ex(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps
   const int grid = grid_for(a.nbase * 32);
   VS_TRY(sc.get(&a.next, 1));
   VS_CK(cudaMemsetAsync(a.next, 0, 8, st));
-  if (a.nbase) { k_isect<<<grid, 256, 0, st>>>(a); vs::note_launch(); }
+  // two adjacency lists and only a count: the tuple-flattening kernel (a
+  // forced window merge keeps the general kernel, which implements it)
+  const bool pair_count = only_count && a.ndeps == 2 && a.dep[0].kind == DEP_SORTED && a.dep[1].kind == DEP_SORTED &&
+                          a.dep[0].algo != VS_ISECT_MERGE && a.dep[1].algo != VS_ISECT_MERGE;
+  if (a.nbase && pair_count)
+    { k_isect_pair_count<<<grid_for(a.nbase * 8), 256, 0, st>>>(a); vs::note_launch(); }
+  else if (a.nbase) { k_isect<<<grid, 256, 0, st>>>(a); vs::note_launch(); }
   VS_CK(cudaGetLastError());
   unsigned long long total = 0;
   VS_CK(cudaMemcpyAsync(&total, d_total, 8, cudaMemcpyDeviceToHost, st));

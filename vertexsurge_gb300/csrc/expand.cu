@@ -216,6 +216,9 @@ __global__ void __launch_bounds__(256) k_decide(DecideArgs a) {
   Ctr *c = a.ctr;
   HopCtr &prev = c->hop[a.h - 1];
   HopCtr &cur = c->hop[a.h];
+  const bool use_picker = a.picker && a.picker_on && a.forced == 0;
+  // the network's parameters load while thread 0 reads the counters
+  const __nv_bfloat16 *w = use_picker ? pk::mlp_stage(a.picker) : nullptr;
   if (t == 0) {
     if (!c->done && a.rowk && (uint32_t)a.h > a.rowk[0]) c->done = 1;  // every row is past its last hop
     if (!c->done && a.h >= 2) {
@@ -251,7 +254,6 @@ __global__ void __launch_bounds__(256) k_decide(DecideArgs a) {
     if (t == 0) cur.strategy = 0;
     return;
   }
-  const bool use_picker = a.picker && a.picker_on && a.forced == 0;
   if (use_picker || a.log_features) {
     if (t == 0) {
       pk::HopFeatIn in;
@@ -280,7 +282,7 @@ __global__ void __launch_bounds__(256) k_decide(DecideArgs a) {
     __syncthreads();
     // one choice left (no pair list, no PUSH in the plan): PULL without the network
     if (use_picker && (s_pairs_ok || a.push_ok)) {
-      pk::mlp_block(a.picker, f, out);
+      pk::mlp_run(w, f, out);
       if (t == 0) {
         int best = -1;
         for (int k = 0; k < pk::NO; k++) {

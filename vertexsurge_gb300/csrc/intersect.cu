@@ -270,17 +270,66 @@ __global__ void __launch_bounds__(256) k_isect(Args a) {
 }
 
 // Count-only intersection of two sorted adjacency dependencies (triangle
-// closing, the pattern query's T).  A warp takes 32 base tuples at a time,
-// lane j loading tuple j's two list bounds, so the tuples' dependent loads
-// overlap; the candidates of the 32 walked (shorter) lists are then laid end
-// to end and dealt one per lane per round, so short lists leave no lane idle.
-// A lane finds its candidate's tuple by a shuffle search over the lanes'
-// first candidate positions and tests it against the other list: one bit of
-// that vertex's adjacency bitmap where it has one (and the method allows),
-// else a binary search.  The count equals the general kernel's.
-__global__ void __launch_bounds__(256) k_isect_pair_count(Args a) {
-  const int lane = threadIdx.x & 31;
+// closing, the pattern query's T), in two kernels.
+//
+// k_isect_pair_count: a warp takes 32 base tuples at a time, lane j loading
+// tuple j's two list bounds, so the tuples' dependent loads overlap.  The
+// candidates of the walked (shorter) lists of up to PAIR_INLINE entries are
+// laid end to end and dealt one per lane per round, so short lists leave no
+// lane idle; a lane finds its candidate's tuple by a shuffle search over the
+// lanes' first candidate positions.  A longer walk is cut into pieces of
+// PAIR_PIECE candidates listed for the second kernel, so the 32 neighbours of
+// a hub in one chunk do not make one warp the critical path.
+// k_isect_pair_pieces: a warp per piece.
+// Either tests a candidate against the other list with one bit of that
+// vertex's adjacency bitmap where it has one (and the method allows), else a
+// binary search.  When the piece list is full the caller reruns the general
+// kernel; the count always equals the general kernel's.
+constexpr int PAIR_INLINE = 64;
+constexpr int PAIR_PIECE = 256;
+
+struct PairTuple {
+  int64_t wlo, wn, olo, ohi;  // walked list [wlo, wlo + wn) of dep w1, other list [olo, ohi)
+  int w1, hs;                 // hs: the other vertex's bitmap slot (-1: binary search)
+};
+
+__device__ __forceinline__ PairTuple pair_tuple(const Args &a, uint64_t t, int learned) {
   const Dep &d0 = a.dep[0], &d1 = a.dep[1];
+  PairTuple p{0, 0, 0, 0, 0, -1};
+  const uint32_t u0 = d0.base_u[t], u1 = d1.base_u[t];
+  int64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
+  if (u0 < d0.n_u) {
+    lo0 = d0.off[u0];
+    hi0 = d0.off[u0 + 1];
+  }
+  if (u1 < d1.n_u) {
+    lo1 = d1.off[u1];
+    hi1 = d1.off[u1 + 1];
+  }
+  if (lo0 < hi0 && lo1 < hi1) {
+    p.w1 = hi1 - lo1 < hi0 - lo0;  // the shorter list; dep 0 on a tie, as the general kernel
+    const Dep &o = p.w1 ? d0 : d1;
+    p.wlo = p.w1 ? lo1 : lo0;
+    p.wn = p.w1 ? hi1 - lo1 : hi0 - lo0;
+    p.olo = p.w1 ? lo0 : lo1;
+    p.ohi = p.w1 ? hi0 : hi1;
+    const int algo = o.algo == VS_ISECT_AUTO ? learned : o.algo;
+    if (o.hub_slot && algo != VS_ISECT_BINARY) p.hs = __ldg(o.hub_slot + (p.w1 ? u0 : u1));
+  }
+  return p;
+}
+
+// Candidate x of a walked list in the other list of its tuple.
+__device__ __forceinline__ bool pair_member(const Args &a, int w1, int hs, int64_t olo, int64_t ohi, uint32_t x) {
+  if (x >= a.cache_rows) return false;
+  const Dep &o = w1 ? a.dep[0] : a.dep[1];
+  return hs >= 0 ? ((__ldg(o.hub_bm + (size_t)hs * o.hub_words + (x >> 6)) >> (x & 63)) & 1ull)
+                 : in_sorted(o.adj, olo, ohi, x);
+}
+
+__global__ void __launch_bounds__(256) k_isect_pair_count(Args a, ulonglong2 *pieces, uint64_t piece_cap,
+                                                          unsigned long long *piece_n, int *overflow) {
+  const int lane = threadIdx.x & 31;
   const int learned = a.method ? *a.method : VS_ISECT_AUTO;
   unsigned long long cnt = 0;
   for (;;) {
@@ -289,39 +338,26 @@ __global__ void __launch_bounds__(256) k_isect_pair_count(Args a) {
     t0 = __shfl_sync(FULLMASK, t0, 0);
     if (t0 >= a.nbase) break;
     const uint64_t t = t0 + lane;
-    // this lane's tuple: walked list [wlo, wlo + wn) of dep w1, other list [olo, ohi) with bitmap slot hs
-    int64_t wlo = 0, wn = 0, olo = 0, ohi = 0;
-    int w1 = 0, hs = -1;
-    if (t < a.nbase) {
-      const uint32_t u0 = d0.base_u[t], u1 = d1.base_u[t];
-      int64_t lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0;
-      if (u0 < d0.n_u) {
-        lo0 = d0.off[u0];
-        hi0 = d0.off[u0 + 1];
+    PairTuple p{0, 0, 0, 0, 0, -1};
+    if (t < a.nbase) p = pair_tuple(a, t, learned);
+    if (p.wn > PAIR_INLINE) {  // a long walk: its pieces go to the second kernel
+      const uint64_t np = (uint64_t)(p.wn + PAIR_PIECE - 1) / PAIR_PIECE;
+      const unsigned long long b = atomicAdd(piece_n, (unsigned long long)np);
+      if (b + np <= piece_cap) {
+        for (uint64_t k = 0; k < np; k++) pieces[b + k] = make_ulonglong2(t, k * PAIR_PIECE);
+      } else {
+        *overflow = 1;
       }
-      if (u1 < d1.n_u) {
-        lo1 = d1.off[u1];
-        hi1 = d1.off[u1 + 1];
-      }
-      if (lo0 < hi0 && lo1 < hi1) {
-        w1 = hi1 - lo1 < hi0 - lo0;  // the shorter list; dep 0 on a tie, as the general kernel
-        const Dep &o = w1 ? d0 : d1;
-        wlo = w1 ? lo1 : lo0;
-        wn = w1 ? hi1 - lo1 : hi0 - lo0;
-        olo = w1 ? lo0 : lo1;
-        ohi = w1 ? hi0 : hi1;
-        const int algo = o.algo == VS_ISECT_AUTO ? learned : o.algo;
-        if (o.hub_slot && algo != VS_ISECT_BINARY) hs = __ldg(o.hub_slot + (w1 ? u0 : u1));
-      }
+      p.wn = 0;
     }
-    unsigned long long incl = (unsigned long long)wn;
+    unsigned long long incl = (unsigned long long)p.wn;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const unsigned long long y = __shfl_up_sync(FULLMASK, incl, o);
       if (lane >= o) incl += y;
     }
     const unsigned long long total = __shfl_sync(FULLMASK, incl, 31);
-    const unsigned long long start = incl - (unsigned long long)wn;
+    const unsigned long long start = incl - (unsigned long long)p.wn;
     for (unsigned long long c0 = 0; c0 < total; c0 += 32) {
       const unsigned long long c = c0 + lane;
       int own = 0;  // the last lane whose first candidate is at or below c (it owns c when c < total)
@@ -329,21 +365,36 @@ __global__ void __launch_bounds__(256) k_isect_pair_count(Args a) {
       for (int step = 16; step; step >>= 1)
         if (__shfl_sync(FULLMASK, start, own + step) <= c) own += step;
       const unsigned long long ost = __shfl_sync(FULLMASK, start, own);
-      const int64_t owlo = __shfl_sync(FULLMASK, wlo, own);
-      const int64_t oolo = __shfl_sync(FULLMASK, olo, own);
-      const int64_t oohi = __shfl_sync(FULLMASK, ohi, own);
-      const int ow1 = __shfl_sync(FULLMASK, w1, own);
-      const int ohs = __shfl_sync(FULLMASK, hs, own);
+      const int64_t owlo = __shfl_sync(FULLMASK, p.wlo, own);
+      const int64_t oolo = __shfl_sync(FULLMASK, p.olo, own);
+      const int64_t oohi = __shfl_sync(FULLMASK, p.ohi, own);
+      const int ow1 = __shfl_sync(FULLMASK, p.w1, own);
+      const int ohs = __shfl_sync(FULLMASK, p.hs, own);
       if (c < total) {
-        const Dep &w = ow1 ? d1 : d0, &o = ow1 ? d0 : d1;
+        const Dep &w = ow1 ? a.dep[1] : a.dep[0];
         const uint32_t x = __ldg(w.adj + owlo + (int64_t)(c - ost));
-        if (x < a.cache_rows) {
-          const bool keep = ohs >= 0 ? ((__ldg(o.hub_bm + (size_t)ohs * o.hub_words + (x >> 6)) >> (x & 63)) & 1ull)
-                                     : in_sorted(o.adj, oolo, oohi, x);
-          cnt += keep;
-        }
+        cnt += pair_member(a, ow1, ohs, oolo, oohi, x);
       }
     }
+  }
+  for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULLMASK, cnt, o);
+  if (lane == 0 && cnt) atomicAdd(a.total, cnt);
+}
+
+__global__ void __launch_bounds__(256) k_isect_pair_pieces(Args a, const ulonglong2 *pieces, uint64_t piece_cap,
+                                                           const unsigned long long *piece_n) {
+  const int lane = threadIdx.x & 31;
+  const int learned = a.method ? *a.method : VS_ISECT_AUTO;
+  const uint64_t n = *piece_n < piece_cap ? *piece_n : piece_cap;
+  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  unsigned long long cnt = 0;
+  for (uint64_t k = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < n; k += warps) {
+    const ulonglong2 pc = pieces[k];
+    const PairTuple p = pair_tuple(a, pc.x, learned);
+    const Dep &w = p.w1 ? a.dep[1] : a.dep[0];
+    const int64_t end = min(p.wn, (int64_t)pc.y + PAIR_PIECE);
+    for (int64_t j = (int64_t)pc.y + lane; j < end; j += 32)
+      cnt += pair_member(a, p.w1, p.hs, p.olo, p.ohi, __ldg(w.adj + p.wlo + j));
   }
   for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULLMASK, cnt, o);
   if (lane == 0 && cnt) atomicAdd(a.total, cnt);
@@ -814,8 +865,8 @@ int vs_mintersect_ex(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps
     std::memset(features, 0, sizeof(float) * pk::NF);
   }
   unsigned long long *d_total, *tcnt = nullptr, *toff = nullptr;
-  VS_TRY(sc.get(&d_total, 1));
-  VS_CK(cudaMemsetAsync(d_total, 0, 8, st));
+  VS_TRY(sc.get(&d_total, 3));  // [0] count, [1] pieces of long walks (pair kernels), [2] their overflow flag
+  VS_CK(cudaMemsetAsync(d_total, 0, 24, st));
   if (!only_count) {
     VS_TRY(sc.get(&tcnt, a.nbase));
     VS_TRY(sc.get(&toff, a.nbase + 1));
@@ -830,13 +881,30 @@ int vs_mintersect_ex(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps
   // forced window merge keeps the general kernel, which implements it)
   const bool pair_count = only_count && a.ndeps == 2 && a.dep[0].kind == DEP_SORTED && a.dep[1].kind == DEP_SORTED &&
                           a.dep[0].algo != VS_ISECT_MERGE && a.dep[1].algo != VS_ISECT_MERGE;
-  if (a.nbase && pair_count)
-    { k_isect_pair_count<<<grid_for(a.nbase * 8), 256, 0, st>>>(a); vs::note_launch(); }
-  else if (a.nbase) { k_isect<<<grid, 256, 0, st>>>(a); vs::note_launch(); }
+  const uint64_t piece_cap = pair_count ? std::max<uint64_t>(65536, 2 * a.nbase) : 0;
+  ulonglong2 *pieces = nullptr;
+  if (a.nbase && pair_count) {
+    VS_TRY(sc.get(&pieces, piece_cap));
+    { k_isect_pair_count<<<grid_for(a.nbase * 8), 256, 0, st>>>(a, pieces, piece_cap, d_total + 1,
+                                                                reinterpret_cast<int *>(d_total + 2));
+      vs::note_launch(); }
+    { k_isect_pair_pieces<<<sm_count() * 8, 256, 0, st>>>(a, pieces, piece_cap, d_total + 1); vs::note_launch(); }
+  } else if (a.nbase) {
+    { k_isect<<<grid, 256, 0, st>>>(a); vs::note_launch(); }
+  }
   VS_CK(cudaGetLastError());
-  unsigned long long total = 0;
-  VS_CK(cudaMemcpyAsync(&total, d_total, 8, cudaMemcpyDeviceToHost, st));
+  unsigned long long res[3] = {0, 0, 0};
+  VS_CK(cudaMemcpyAsync(res, d_total, 24, cudaMemcpyDeviceToHost, st));
   VS_CK(cudaStreamSynchronize(st));
+  if (res[2]) {  // the long walks did not fit the piece list: count again with the general kernel
+    VS_CK(cudaMemsetAsync(d_total, 0, 8, st));
+    VS_CK(cudaMemsetAsync(a.next, 0, 8, st));
+    { k_isect<<<grid, 256, 0, st>>>(a); vs::note_launch(); }
+    VS_CK(cudaGetLastError());
+    VS_CK(cudaMemcpyAsync(res, d_total, 8, cudaMemcpyDeviceToHost, st));
+    VS_CK(cudaStreamSynchronize(st));
+  }
+  unsigned long long total = res[0];
   *count = total;
   if (only_count) return VS_OK;
   VS_TRY(exclusive_scan_u64(tcnt, toff, a.nbase, st));

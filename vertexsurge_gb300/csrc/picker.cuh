@@ -59,21 +59,35 @@ __device__ inline void hop_features(const HopFeatIn &in, float *f) {
   for (int b = 0; b < NHIST; b++) f[16 + b] = (float)in.hist[b] * r;
 }
 
-// Inference by a whole block (every thread must call it; blockDim.x = P * H1
-// with P a power of two, P = 2..16): the bf16 parameters (16-byte aligned) are
-// staged in shared memory with 16-byte loads; each hidden unit's dot product
-// is split over P adjacent lanes, each starting at its own offset so a warp's
-// lanes read different banks, and summed by shuffles; each output unit is one
-// warp's.  out[NO] must be shared memory.
-__device__ inline void mlp_block(const void *params, const float *f, float *out) {
+// Inference by a whole block, in two calls every thread makes.
+// mlp_stage starts copying the bf16 parameters (16-byte aligned) into shared
+// memory with asynchronous 16-byte copies and returns the buffer; a kernel
+// can call it first and compute its features while the copies are in flight.
+// mlp_run (blockDim.x = P * H1, P a power of two, 2..16) waits for them, then
+// splits each hidden unit's dot product over P adjacent lanes, each starting
+// at its own offset so a warp's lanes read different banks, sums them by
+// shuffles, and computes each output unit in one warp.  out[NO] must be
+// shared memory.
+__device__ inline __nv_bfloat16 *mlp_stage(const void *params) {
   __shared__ __align__(16) __nv_bfloat16 w[(NPARAM + 7) / 8 * 8];
-  __shared__ float h1[H1], h2[H2];
-  const int t = threadIdx.x, lane = t & 31;
+  const int t = threadIdx.x;
   const __nv_bfloat16 *gw = (const __nv_bfloat16 *)params;
   constexpr int NV = NPARAM / 8;
-  for (int i = t; i < NV; i += blockDim.x)
-    reinterpret_cast<uint4 *>(w)[i] = __ldg(reinterpret_cast<const uint4 *>(gw) + i);
-  for (int i = NV * 8 + t; i < NPARAM; i += blockDim.x) w[i] = gw[i];
+  // asynchronous 16-byte copies: no thread waits for them before mlp_run
+  for (int i = t; i < NV; i += blockDim.x) {
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(reinterpret_cast<uint4 *>(w) + i);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(reinterpret_cast<const uint4 *>(gw) + i)
+                 : "memory");
+  }
+  // the few tail elements by the block's last threads (thread 0 often has other work)
+  for (int i = NV * 8 + (int)(blockDim.x - 1 - t); i < NPARAM; i += blockDim.x) w[i] = gw[i];
+  return w;
+}
+
+__device__ inline void mlp_run(const __nv_bfloat16 *w, const float *f, float *out) {
+  __shared__ float h1[H1], h2[H2];
+  const int t = threadIdx.x, lane = t & 31;
+  asm volatile("cp.async.wait_all;" ::: "memory");
   __syncthreads();
   const int P = blockDim.x / H1, u = t / P, p = t & (P - 1);
   {
@@ -112,6 +126,10 @@ __device__ inline void mlp_block(const void *params, const float *f, float *out)
     if (lane == 0) out[o3] = acc + __bfloat162float(w[OFF_B3 + o3]);
   }
   __syncthreads();
+}
+
+__device__ inline void mlp_block(const void *params, const float *f, float *out) {
+  mlp_run(mlp_stage(params), f, out);
 }
 
 // One sample through the network, computed by one thread (64 FMAs per

@@ -444,6 +444,34 @@ __device__ __forceinline__ unsigned long long out_degree(const Lists &L, uint32_
   return d;
 }
 
+// Largest p in [0, np) with doff[p] <= x for x0 (lanes 0-15) and x1 (lanes
+// 16-31), doff ascending with doff[0] = 0 <= x: each step a half-warp probes
+// 15 positions spread over its range at once and keeps the part between the
+// last probe at or below x and the next, so a range shrinks 16-fold per
+// dependent load instead of 2-fold.  Every lane receives both answers.
+__device__ __forceinline__ void owner_pairs(const unsigned long long *__restrict__ doff, uint64_t np,
+                                            unsigned long long x0, unsigned long long x1, int lane, uint64_t &p0,
+                                            uint64_t &p1) {
+  const int hl = lane & 15;
+  const unsigned long long x = lane < 16 ? x0 : x1;
+  uint64_t lo = 0, hi = np;  // doff[lo] <= x, and doff[hi] > x unless hi == np
+  while (__any_sync(FULL, hi - lo > 1)) {
+    const uint64_t span = hi - lo;
+    const uint64_t pos = lo + (span * (uint64_t)hl + 15) / 16;  // probe hl; probe 0 is lo itself
+    const bool ok = span > 1 && (hl == 0 || (pos < hi && doff[pos] <= x));
+    const unsigned b = __ballot_sync(FULL, ok);
+    const unsigned half = lane < 16 ? (b & 0xFFFFu) : (b >> 16);
+    if (span > 1) {
+      const int k = 31 - __clz(half);
+      const uint64_t nhi = k == 15 ? hi : lo + (span * (uint64_t)(k + 1) + 15) / 16;
+      lo = lo + (span * (uint64_t)k + 15) / 16;
+      hi = nhi < hi ? nhi : hi;
+    }
+  }
+  p0 = __shfl_sync(FULL, lo, 0);
+  p1 = __shfl_sync(FULL, lo, 16);
+}
+
 __global__ void __launch_bounds__(256, 4) k_sparse(SparseArgs a) {
   Ctr *c = a.ctr;
   if (c->hop[a.h].strategy != ST_SPARSE) return;
@@ -461,119 +489,97 @@ __global__ void __launch_bounds__(256, 4) k_sparse(SparseArgs a) {
   for (uint64_t ck = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib; ck < nchunks; ck += warps) {
     const unsigned long long e0 = ck * SPARSE_CHUNK;
     const unsigned long long e1 = min(e0 + SPARSE_CHUNK, T);
-    // pairs owning the chunk's first and last edge: largest p with doff[p] <= e
-    uint64_t plo = 0, phi = np;
-    {
-      uint64_t lo = 0, hi = np;
-      while (hi - lo > 1) {
-        const uint64_t mid = (lo + hi) >> 1;
-        if (a.doff[mid] <= e0) lo = mid; else hi = mid;
-      }
-      plo = lo;
-      hi = np;
-      while (hi - lo > 1) {
-        const uint64_t mid = (lo + hi) >> 1;
-        if (a.doff[mid] <= e1 - 1) lo = mid; else hi = mid;
-      }
-      phi = lo;
-    }
-    // up to 32 pairs: lane j holds the first edge of pair plo + j, and an
-    // edge's pair is found by counting those starts at or below it
-    const uint32_t npr = (uint32_t)(phi - plo + 1);
-    // up to 32 pairs: lane j holds pair plo + j (its first edge, source id,
-    // and its vertex's list starts and first-list length), so the rounds
-    // below take them by shuffle instead of loading them per edge
-    const bool few = npr <= 32;
-    unsigned long long dj = ~0ull;
-    uint32_t pi = 0;
-    int64_t pb0 = 0, pd0 = 0, pb1 = 0;
-    if (few && (uint32_t)lane < npr) {
-      dj = a.doff[plo + lane];
-      const uint2 pr = a.pin[plo + lane];
-      pi = pr.y;
-      pb0 = a.out.off[0][pr.x];
-      pd0 = a.out.off[0][pr.x + 1] - pb0;
-      if (a.out.n > 1) pb1 = a.out.off[1][pr.x];
-    }
+    // pairs owning the chunk's first and last edge: largest p with doff[p] <= e,
+    // both found at once by a 16-way search per half-warp
+    uint64_t plo, phi;
+    owner_pairs(a.doff, np, e0, e1 - 1, lane, plo, phi);
     uint32_t nloc = 0;  // new pairs of this chunk so far (s_new)
-    // SPARSE_K edges per lane per round, each phase issued for all of them
-    // before the next: the adjacency loads, then the returning atomics on the
-    // visited (or next-layer) words, then the row flags, so a lane keeps
-    // SPARSE_K dependent chains in flight instead of one
-    for (unsigned long long eb = e0; eb < e1; eb += 32 * SPARSE_K) {
-      uint32_t v[SPARSE_K], i[SPARSE_K];
-      bool act[SPARSE_K];
+    // the chunk's pairs 32 at a time: lane j holds pair g0 + j (its first
+    // edge, source id, and its vertex's list starts and first-list length),
+    // and an edge of the group's range finds its pair by a shuffle search over
+    // the lanes' first edges instead of loading it
+    for (uint64_t g0 = plo; g0 <= phi; g0 += 32) {
+      unsigned long long dj = ~0ull;  // lanes past the last pair never own an edge
+      uint32_t pi = 0;
+      int64_t pb0 = 0, pd0 = 0, pb1 = 0;
+      if (g0 + lane <= phi) {
+        dj = a.doff[g0 + lane];
+        const uint2 pr = a.pin[g0 + lane];
+        pi = pr.y;
+        pb0 = a.out.off[0][pr.x];
+        pd0 = a.out.off[0][pr.x + 1] - pb0;
+        if (a.out.n > 1) pb1 = a.out.off[1][pr.x];
+      }
+      // the group's edges inside the chunk
+      const unsigned long long d0j = __shfl_sync(FULL, dj, 0);
+      const unsigned long long gs = d0j > e0 ? d0j : e0;
+      unsigned long long ge = e1;
+      if (g0 + 32 <= phi) {
+        const unsigned long long nx = a.doff[g0 + 32];
+        ge = nx < e1 ? nx : e1;
+      }
+      // SPARSE_K edges per lane per round, each phase issued for all of them
+      // before the next: the adjacency loads, then the returning atomics on
+      // the visited (or next-layer) words, then the row flags, so a lane keeps
+      // SPARSE_K dependent chains in flight instead of one
+      for (unsigned long long eb = gs; eb < ge; eb += 32 * SPARSE_K) {
+        uint32_t v[SPARSE_K], i[SPARSE_K];
+        bool act[SPARSE_K];
 #pragma unroll
-      for (int k = 0; k < SPARSE_K; k++) {
-        const unsigned long long e = eb + k * 32 + lane;
-        unsigned long long j = 0;  // the edge's index in its pair's out-lists
-        int64_t b0 = 0, d0 = 0, b1 = 0;
-        v[k] = 0;
-        i[k] = 0;
-        if (few) {  // the last pair whose first edge is at or below e (starts ascend with the lane)
-          int own = 0;
+        for (int k = 0; k < SPARSE_K; k++) {
+          const unsigned long long e = eb + k * 32 + lane;
+          int own = 0;  // the last pair whose first edge is at or below e (starts ascend with the lane)
 #pragma unroll
           for (int step = 16; step; step >>= 1)
             if (__shfl_sync(FULL, dj, own + step) <= e) own += step;
           i[k] = __shfl_sync(FULL, pi, own);
-          b0 = __shfl_sync(FULL, pb0, own);
-          d0 = __shfl_sync(FULL, pd0, own);
-          b1 = __shfl_sync(FULL, pb1, own);
-          j = e - __shfl_sync(FULL, dj, own);
-        } else if (e < e1) {
-          uint64_t lo = plo, hi = phi + 1;
-          while (hi - lo > 1) {
-            const uint64_t mid = (lo + hi) >> 1;
-            if (a.doff[mid] <= e) lo = mid; else hi = mid;
+          const int64_t b0 = __shfl_sync(FULL, pb0, own);
+          const int64_t d0 = __shfl_sync(FULL, pd0, own);
+          const int64_t b1 = __shfl_sync(FULL, pb1, own);
+          const unsigned long long j = e - __shfl_sync(FULL, dj, own);  // the edge's index in its pair's out-lists
+          v[k] = 0;
+          act[k] = e < ge && (!a.hmask || ((__ldg(a.hmask + (i[k] >> 6)) >> (i[k] & 63)) & 1ull));
+          if (act[k]) v[k] = (int64_t)j < d0 ? a.out.adj[0][b0 + j] : a.out.adj[1][b1 + (int64_t)j - d0];
+        }
+        unsigned long long old[SPARSE_K];
+#pragma unroll
+        for (int k = 0; k < SPARSE_K; k++) {
+          old[k] = ~0ull;  // an inactive edge sets nothing
+          if (act[k]) {
+            const size_t idx = (size_t)v[k] * a.W + (i[k] >> 6);
+            // Shortest dedups through the visited bit, Any through the next-layer bit
+            old[k] = atomicOr(a.shortest ? &a.vis[idx] : &a.N[idx], 1ull << (i[k] & 63));
           }
-          const uint2 pr = a.pin[lo];
-          i[k] = pr.y;
-          j = e - a.doff[lo];
-          b0 = a.out.off[0][pr.x];
-          d0 = a.out.off[0][pr.x + 1] - b0;
-          if (a.out.n > 1) b1 = a.out.off[1][pr.x];
         }
-        act[k] = e < e1 && (!a.hmask || ((__ldg(a.hmask + (i[k] >> 6)) >> (i[k] & 63)) & 1ull));
-        if (act[k]) v[k] = (int64_t)j < d0 ? a.out.adj[0][b0 + j] : a.out.adj[1][b1 + (int64_t)j - d0];
-      }
-      unsigned long long old[SPARSE_K];
+        bool fresh[SPARSE_K];
 #pragma unroll
-      for (int k = 0; k < SPARSE_K; k++) {
-        old[k] = ~0ull;  // an inactive edge sets nothing
-        if (act[k]) {
-          const size_t idx = (size_t)v[k] * a.W + (i[k] >> 6);
-          // Shortest dedups through the visited bit, Any through the next-layer bit
-          old[k] = atomicOr(a.shortest ? &a.vis[idx] : &a.N[idx], 1ull << (i[k] & 63));
+        for (int k = 0; k < SPARSE_K; k++) {
+          fresh[k] = !((old[k] >> (i[k] & 63)) & 1ull);
+          if (fresh[k]) {
+            const size_t idx = (size_t)v[k] * a.W + (i[k] >> 6);
+            const unsigned long long bit = 1ull << (i[k] & 63);
+            if (a.shortest && !a.last) atomicOr(&a.N[idx], bit);
+            if (a.acc_on) atomicOr(&a.acc[idx], bit);
+            if (a.res_vis || a.acc_on) a.resflag[v[k]] = 1;
+            nb++;
+          }
         }
-      }
-      bool fresh[SPARSE_K];
+        bool first[SPARSE_K];
 #pragma unroll
-      for (int k = 0; k < SPARSE_K; k++) {
-        fresh[k] = !((old[k] >> (i[k] & 63)) & 1ull);
-        if (fresh[k]) {
-          const size_t idx = (size_t)v[k] * a.W + (i[k] >> 6);
-          const unsigned long long bit = 1ull << (i[k] & 63);
-          if (a.shortest && !a.last) atomicOr(&a.N[idx], bit);
-          if (a.acc_on) atomicOr(&a.acc[idx], bit);
-          if (a.res_vis || a.acc_on) a.resflag[v[k]] = 1;
-          nb++;
+        for (int k = 0; k < SPARSE_K; k++) {
+          // a last layer's rows stay zero in the buffer (flag 2: the run start skips them)
+          first[k] = fresh[k] && atomicOr(&a.flagN[v[k]], a.last ? 2u : 1u) == 0;
+          nv += first[k];
         }
-      }
-      bool first[SPARSE_K];
+        // the chunk's new pairs gather in shared memory (one list append per chunk);
+        // bit 31 of the source id (S < 2^31) marks the pair that made its row non-zero
 #pragma unroll
-      for (int k = 0; k < SPARSE_K; k++) {
-        // a last layer's rows stay zero in the buffer (flag 2: the run start skips them)
-        first[k] = fresh[k] && atomicOr(&a.flagN[v[k]], a.last ? 2u : 1u) == 0;
-        nv += first[k];
-      }
-      // the chunk's new pairs gather in shared memory (one list append per chunk);
-      // bit 31 of the source id (S < 2^31) marks the pair that made its row non-zero
-#pragma unroll
-      for (int k = 0; k < SPARSE_K; k++) {
-        const unsigned m = __ballot_sync(FULL, fresh[k]);
-        if (fresh[k])
-          s_new[wib][nloc + __popc(m & lanemask_lt())] = make_uint2(v[k], i[k] | (first[k] ? 0x80000000u : 0u));
-        nloc += __popc(m);
+        for (int k = 0; k < SPARSE_K; k++) {
+          const unsigned m = __ballot_sync(FULL, fresh[k]);
+          if (fresh[k])
+            s_new[wib][nloc + __popc(m & lanemask_lt())] = make_uint2(v[k], i[k] | (first[k] ? 0x80000000u : 0u));
+          nloc += __popc(m);
+        }
       }
     }
     __syncwarp();

@@ -60,6 +60,10 @@ WORKLOADS = {
     # keys Zipf-skewed over 10M vertex ids (the key tables of the batched workload)
     "join_zipf10M": dict(kind="join", V=10_000_000, sizes=(100_000, 1_000_000, 10_000_000), skew=1.2, seed=4,
                          cpu_rows=1_000_000),
+    # config 5: the serving loop on a resident R-MAT graph (scale 27: 134M vertices, 2.1B edges), Poisson
+    # arrivals of pattern queries (expand + join + triangles), admission by plan bytes under a budget
+    "serving_rmat27": dict(kind="serving", scale=27, queries=100, rate=1.5, budget_gb=150.0, slots=8,
+                           s_max=2048, l_max=5, check=20, oracle_queries=2),
     "zipf1M_batched64": dict(kind="zipf", V=1_000_000, E=30_000_000, alpha=2.1, cap=50_000, seed=3,
                              batched=dict(n=64, s_range=(64, 8192), l_range=(2, 6),
                                           join_rows=(100_000, 1_000_000), waves=(8192, 16384, 32768),
@@ -526,6 +530,128 @@ def run_join(args, w, rank, world, local_rank, reference=False):
     print(json.dumps(line), flush=True)
 
 
+def serving_oracle(g, trace, n):
+    """The n queries of the trace with the fewest source-hops, each on the CPU:
+    visited = the oracle's VExpand(Shortest, [1, l]) bit count; join = the
+    count of HashJoin(A, key table) on the vertex id, i.e. the sum over key
+    rows of the popcount of A's column for that key (numpy over the oracle's
+    words); triangles = sum over the sources' edges a -> b of |N+(a) & N+(b)|
+    (numpy over the sorted, duplicate-free lists)."""
+    from oracle import pyoracle as O
+    idx = sorted(range(len(trace)), key=lambda i: (len(trace[i].sources) * trace[i].k_max, i))[:n]
+    out = []
+    t = time.perf_counter()
+    for i in idx:
+        r = trace[i]
+        words, _, _ = O.vexpand(g, r.sources, 1, r.k_max, "shortest", "forward")
+        colcnt = np.bitwise_count(words).sum(axis=1, dtype=np.int64)
+        del words
+        tri = 0
+        for a in r.sources:
+            na = g.fwd_dst[g.fwd_off[a]:g.fwd_off[a + 1]]
+            for b in na:
+                nb = g.fwd_dst[g.fwd_off[b]:g.fwd_off[b + 1]]
+                if len(nb):  # members of na in the sorted nb
+                    tri += int(np.count_nonzero(nb[np.minimum(np.searchsorted(nb, na), len(nb) - 1)] == na))
+        out.append((int(colcnt.sum()), int(colcnt[r.keys].sum()), tri))
+    return idx, out, time.perf_counter() - t
+
+
+def run_serving(args, w, rank, world, local_rank):
+    """Config 5: the serving loop (vertexsurge_gb300.serve) replaying a Poisson
+    trace under a byte budget, the fixed planner and the learned pickers on the
+    same trace; latency = completion - arrival.  Every query's host inputs are
+    copied in and its three counts read back inside the served interval."""
+    from vertexsurge_gb300 import graphgen, picker_train, serve
+    if args.impl == "reference":  # the oracle on the sample the GPU arm checks, one query at a time
+        from vertexsurge_gb300 import build as b
+        b.build_oracle()
+        b.build_gen()
+        g = graphgen.rmat(w["scale"], 16, 0.57, 0.19, 0.19, seed=27)
+        trace = serve.make_trace(g, w["queries"], w["rate"], s_range=(64, w["s_max"]), l_max=w["l_max"])
+        idx, _, dt = serving_oracle(g, trace, w["oracle_queries"])
+        from oracle import pyoracle as O
+        value = len(idx) / dt
+        print(json.dumps({"impl": "reference", "metric": "served queries/s", "value": value, "unit": "queries/s",
+                          "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1000 * dt,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+                          "data": "synthetic (seeded R-MAT graph, Poisson arrivals)",
+                          "config": {"workload": args.workload, "V": g.V, "E": g.E},
+                          "cpu_baseline": {"value": value, "unit": "queries/s", "cores": O.lib().oracle_get_threads(),
+                                           "kind": "port", "sample": f"queries {idx} of the trace, one at a time"},
+                          "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    import torch
+    import vertexsurge_gb300 as vs
+    from vertexsurge_gb300 import build as b
+    b.build_all()
+    torch.cuda.set_device(local_rank)
+    vs.init(local_rank)
+    t0 = time.time()
+    g = graphgen.rmat(w["scale"], 16, 0.57, 0.19, 0.19, seed=27)
+    log(f"graph {g.V} vertices {g.E} edges in {time.time() - t0:.1f}s")
+    dg = vs.DeviceGraph.from_host(g)
+    trace = serve.make_trace(g, w["queries"], w["rate"], s_range=(64, w["s_max"]), l_max=w["l_max"])
+    budget = int(w["budget_gb"] * (1 << 30))
+    pickers = {"plain": None}
+    if picker_train.WEIGHTS_FILE.exists():
+        pk = vs.Picker()
+        pk.set_params(np.load(picker_train.WEIGHTS_FILE))
+        pickers["learned"] = pk
+    # warm-up: the first queries alone (kernels loaded, hub indexes built)
+    solo_srv = serve.Server(dg, budget_bytes=1 << 62, slots=1)
+    wstream = torch.cuda.Stream()
+    for r in trace[: max(3, args.warmup)]:
+        solo_srv.run_query(r, wstream)
+    torch.cuda.synchronize()
+    launches0 = vs.kernel_launches()
+    clocks = ClockSampler(local_rank)
+    reports, results = {}, {}
+    for name, pk in pickers.items():
+        for r in trace:
+            r.result = ()
+        reports[name] = serve.Server(dg, budget, slots=w["slots"], picker=pk).serve(trace)
+        results[name] = [r.result for r in trace]
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = vs.kernel_launches() - launches0
+    solo = serve.solo_results(dg, trace[: w["check"]])
+    same_mix = all(results["plain"][i] == solo[i] for i in range(len(solo)))
+    same_picker = all(res == results["plain"] for res in results.values())
+    assert same_mix and same_picker, "served answers differ alone / in the mix / under the picker"
+    parity = None
+    if not args.no_cpu:
+        idx, want, dt = serving_oracle(g, trace, w["oracle_queries"])
+        got = [results["plain"][i] for i in idx]
+        parity = {"queries": len(idx), "equal": got == want,
+                  "against": f"queries {idx}: oracle VExpand bit count, numpy join and triangle counts",
+                  "oracle_s": dt}
+        if got != want:
+            print(json.dumps({"parity": parity, "got": got, "want": want}), flush=True)
+            raise SystemExit("parity: served counts differ from the oracle's")
+    rep = reports["plain"]
+    h2d = sum(r.sources.nbytes + r.keys.nbytes + r.payload.nbytes for r in trace)
+    line = {"metric": "served queries/s", "value": rep["queries_per_s"], "unit": "queries/s", "n_gpus": world,
+            "steps": 1, "warmup": max(3, args.warmup), "ms_per_step": 1000 * rep["wall_s"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded R-MAT graph a=0.57, Poisson arrivals, Zipf join keys)",
+            "config": {"workload": args.workload, "V": g.V, "E": g.E, "queries": w["queries"],
+                       "rate_qps": w["rate"], "budget_gb": w["budget_gb"], "slots": w["slots"],
+                       "s_range": [64, w["s_max"]], "l_max": w["l_max"], "l2": "inputs larger than L2",
+                       "parallelism": f"replicas{world}"},
+            "latency": {name: {k: rep_[k] for k in ("p50_ms", "p99_ms", "service_p50_ms", "queries_per_s",
+                                                    "peak_bytes", "peak_concurrent")}
+                        for name, rep_ in reports.items()},
+            "queries_per_s": {name: rep_["queries_per_s"] for name, rep_ in reports.items()},
+            "check": {"same_alone_and_in_mix": same_mix, "queries": len(solo), "same_under_picker": same_picker},
+            "roofline": None, "cpu_baseline": None, "parity": parity,
+            "e2e": {"value": rep["queries_per_s"], "unit": "queries/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": 3 * 8 * len(trace)},
+            "gpu_launches": launches, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, w, rank, world):
     """--impl reference: the oracle (CPU restatement of the reference) on host cores."""
     if rank != 0:
@@ -849,6 +975,9 @@ def main():
     if w.get("kind") == "join":
         if rank == 0 or args.impl != "reference":
             run_join(args, w, rank, world, local_rank, reference=args.impl == "reference")
+    elif w.get("kind") == "serving":
+        if rank == 0 or args.impl != "reference":
+            run_serving(args, w, rank, world, local_rank)
     elif args.impl == "reference":
         run_reference(args, w, rank, world)
     elif "batched" in w:

@@ -142,6 +142,30 @@ def test_adjacency_triangle_closing(vs, hub_graphs, algo, gname):
         assert c3 == count
 
 
+@pytest.mark.parametrize("algo", ["auto", "binary"])
+def test_pair_count_long_walks_beyond_the_piece_list(vs, algo):
+    """Count-only closing over two adjacency lists cuts walks above 64
+    candidates into pieces; here 600 base tuples each walk 30,000 candidates
+    (70,800 pieces, more than the first pass's list holds), so the call counts
+    again with room for every piece.  Source 0 reaches 1..30000; hubs 1..600
+    each reach 10000..39999: every hub tuple closes 20,001 triangles."""
+    V, D, H = 40_000, 30_000, 600
+    src = np.concatenate([np.zeros(D, np.uint32), np.repeat(np.arange(1, H + 1, dtype=np.uint32), D)])
+    dst = np.concatenate([np.arange(1, D + 1, dtype=np.uint32), np.tile(np.arange(10_000, 10_000 + D, dtype=np.uint32), H)])
+    g = graphgen.from_edges(V, src, dst)
+    dg = vs.DeviceGraph.from_host(g)
+    a = np.zeros(D, np.uint32)
+    b = np.arange(1, D + 1, dtype=np.uint32)
+    base = vs.FlatTable.from_columns([a, b])
+    deps = [dict(graph=dg, direction="forward", base_col=0, algo=algo),
+            dict(graph=dg, direction="forward", base_col=1, algo=algo)]
+    _, count, _ = vs.mintersect(base, deps, V, True)
+    # the general kernel (a forced window merge keeps it) on the same base
+    merge = [dict(d, algo="merge") for d in deps]
+    _, c_general, _ = vs.mintersect(base, merge, V, True)
+    assert count == c_general == H * (D - 10_000 + 1)
+
+
 @pytest.mark.parametrize("algo", ["auto", "merge", "bitmap"])
 def test_adjacency_in_lists(vs, hub_graphs, algo):
     """Backward (in-list) adjacency on a directed graph: common in-neighbours of

@@ -382,7 +382,10 @@ __global__ void __launch_bounds__(256) k_isect_pair_count(Args a, ulonglong2 *pi
 }
 
 __global__ void __launch_bounds__(256) k_isect_pair_pieces(Args a, const ulonglong2 *pieces, uint64_t piece_cap,
-                                                           const unsigned long long *piece_n) {
+                                                           const unsigned long long *piece_n, const int *overflow) {
+  // a full list holds unwritten entries (a reservation that crossed the end
+  // is not written): the caller counts again with room for every piece
+  if (*overflow) return;
   const int lane = threadIdx.x & 31;
   const int learned = a.method ? *a.method : VS_ISECT_AUTO;
   const uint64_t n = *piece_n < piece_cap ? *piece_n : piece_cap;
@@ -881,21 +884,39 @@ int vs_mintersect_ex(vs_table_ref base, const vs_isect_dep *deps, uint32_t ndeps
   // forced window merge keeps the general kernel, which implements it)
   const bool pair_count = only_count && a.ndeps == 2 && a.dep[0].kind == DEP_SORTED && a.dep[1].kind == DEP_SORTED &&
                           a.dep[0].algo != VS_ISECT_MERGE && a.dep[1].algo != VS_ISECT_MERGE;
-  const uint64_t piece_cap = pair_count ? std::max<uint64_t>(65536, 2 * a.nbase) : 0;
-  ulonglong2 *pieces = nullptr;
+  unsigned long long res[3] = {0, 0, 0};
   if (a.nbase && pair_count) {
-    VS_TRY(sc.get(&pieces, piece_cap));
-    { k_isect_pair_count<<<grid_for(a.nbase * 8), 256, 0, st>>>(a, pieces, piece_cap, d_total + 1,
-                                                                reinterpret_cast<int *>(d_total + 2));
-      vs::note_launch(); }
-    { k_isect_pair_pieces<<<sm_count() * 8, 256, 0, st>>>(a, pieces, piece_cap, d_total + 1); vs::note_launch(); }
+    // a first pass with room for 2 pieces per tuple; when the long walks need
+    // more, the pass counted exactly how many, and a second pass gets that room
+    uint64_t piece_cap = std::max<uint64_t>(65536, 2 * a.nbase);
+    int *overflow = reinterpret_cast<int *>(d_total + 2);
+    for (int pass = 0; pass < 2; pass++) {
+      ulonglong2 *pieces = nullptr;
+      if (pass && sc.get(&pieces, piece_cap) != VS_OK) {  // no room: the general kernel below
+        cudaGetLastError();
+        break;
+      }
+      if (!pass) VS_TRY(sc.get(&pieces, piece_cap));
+      if (pass) {
+        VS_CK(cudaMemsetAsync(d_total, 0, 24, st));
+        VS_CK(cudaMemsetAsync(a.next, 0, 8, st));
+      }
+      { k_isect_pair_count<<<grid_for(a.nbase * 8), 256, 0, st>>>(a, pieces, piece_cap, d_total + 1, overflow);
+        vs::note_launch(); }
+      { k_isect_pair_pieces<<<sm_count() * 8, 256, 0, st>>>(a, pieces, piece_cap, d_total + 1, overflow);
+        vs::note_launch(); }
+      VS_CK(cudaGetLastError());
+      VS_CK(cudaMemcpyAsync(res, d_total, 24, cudaMemcpyDeviceToHost, st));
+      VS_CK(cudaStreamSynchronize(st));
+      if (!res[2]) break;
+      piece_cap = res[1];
+    }
   } else if (a.nbase) {
     { k_isect<<<grid, 256, 0, st>>>(a); vs::note_launch(); }
+    VS_CK(cudaGetLastError());
+    VS_CK(cudaMemcpyAsync(res, d_total, 24, cudaMemcpyDeviceToHost, st));
+    VS_CK(cudaStreamSynchronize(st));
   }
-  VS_CK(cudaGetLastError());
-  unsigned long long res[3] = {0, 0, 0};
-  VS_CK(cudaMemcpyAsync(res, d_total, 24, cudaMemcpyDeviceToHost, st));
-  VS_CK(cudaStreamSynchronize(st));
   if (res[2]) {  // the long walks did not fit the piece list: count again with the general kernel
     VS_CK(cudaMemsetAsync(d_total, 0, 8, st));
     VS_CK(cudaMemsetAsync(a.next, 0, 8, st));

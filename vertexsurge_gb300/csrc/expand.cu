@@ -560,7 +560,6 @@ __global__ void __launch_bounds__(256, 4) k_sparse(SparseArgs a) {
             const unsigned long long bit = 1ull << (i[k] & 63);
             if (a.shortest && !a.last) atomicOr(&a.N[idx], bit);
             if (a.acc_on) atomicOr(&a.acc[idx], bit);
-            if (a.res_vis || a.acc_on) a.resflag[v[k]] = 1;
             nb++;
           }
         }
@@ -570,6 +569,8 @@ __global__ void __launch_bounds__(256, 4) k_sparse(SparseArgs a) {
           // a last layer's rows stay zero in the buffer (flag 2: the run start skips them)
           first[k] = fresh[k] && atomicOr(&a.flagN[v[k]], a.last ? 2u : 1u) == 0;
           nv += first[k];
+          // the result column is marked once per row and hop, by the bit that made the row non-zero
+          if (first[k] && (a.res_vis || a.acc_on)) a.resflag[v[k]] = 1;
         }
         // the chunk's new pairs gather in shared memory (one list append per chunk);
         // bit 31 of the source id (S < 2^31) marks the pair that made its row non-zero
@@ -2193,8 +2194,9 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
       { k_materialize<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<uint4 *>(pl->buf[fb]), V, Q,
                                                 pl->slot[fb], pl->slot_n, pl->ctr, h, 1); vs::note_launch(); }
 
-    { k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[nbuf]),
-                                                pl->flag[nbuf], V, Q, pl->ctr, h, 1); vs::note_launch(); }
+    if (h > 1)  // hop 1 writes a buffer the run start cleared
+      { k_clear_flagged<<<pl->grid_v, 256, 0, st>>>(reinterpret_cast<uint4 *>(pl->buf[nbuf]),
+                                                  pl->flag[nbuf], V, Q, pl->ctr, h, 1); vs::note_launch(); }
     const bool acc_on = pl->use_acc && h >= p.k_min && h <= p.k_max;
     SparseArgs sp;
     sp.ctr = pl->ctr;

@@ -135,6 +135,28 @@ def test_plan_rerun_is_clean(vs, graphs, path, k0, k1):
         assert plan.result().count() == O.matrix_count(exp, 256, g.V), seed
 
 
+@pytest.mark.parametrize("path,k0,k1", [("shortest", 1, 2), ("shortest", 2, 3), ("any", 1, 2)])
+def test_rerun_across_strategies(vs, graphs, path, k0, k1):
+    """One plan run under alternating per-hop strategies: a Shortest run whose
+    last hop is SPARSE keeps no next-layer rows (flag 2), and the runs after
+    it (PULL, PUSH, SPARSE) still find clean buffers; every run equals the
+    oracle, and so do the stats' per-hop new-bit counts."""
+    g, dg = graphs["rmat11_skew"]
+    plan = vs.ExpandPlan(dg, 192, vs.make_params(k0, k1, path, "forward"))
+    plan.set_tuning(push_frac=0.5)
+    seq = [("sparse", 1), ("pull", 2), ("sparse", 3), ("push", 1), ("sparse", 2), ("auto", 4)]
+    for strat, seed in seq:
+        plan.set_hop_strategies([0] + [strat] * k1)
+        src = graphgen.sample_sources(g.V, 192, seed=seed)
+        plan.run(src)
+        exp, _, ost = O.vexpand(g, src, k0, k1, path, "forward", hop_stats=True)
+        assert np.array_equal(plan.result().download(), exp), (strat, seed)
+        assert plan.result().count() == O.matrix_count(exp, 192, g.V), (strat, seed)
+        st = plan.stats()
+        if path == "shortest":
+            assert st["visit_count"] == ost["visit_count"][st["hops_run"]], (strat, seed)
+
+
 def test_expand_empty_and_isolated(vs):
     # a graph with isolated vertices and a single edge
     g = graphgen.from_edges(10, [1], [2])

@@ -882,16 +882,11 @@ __device__ __forceinline__ void gather_rows(const PullArgs &a, const L2Pol<H> &p
 // stored with one 16-byte store per lane of the slot; stale entries past the
 // count are never read.
 template <int L, int UPL>
+// c: this lane's bit count of the row (0 past the row's lanes), counted by the caller
 __device__ __forceinline__ bool write_short(const PullArgs &a, uint32_t v, const uint4 (&acc)[UPL], uint32_t qn,
-                                            unsigned long long &ns) {
+                                            uint32_t c, unsigned long long &ns) {
   __shared__ uint4 s_stage[16][8];  // a slot per warp (at most 64 entries, 16 warps)
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  uint32_t c = 0;
-  if (lane < L) {
-#pragma unroll
-    for (int k = 0; k < UPL; k++)
-      if (lane + k * L < qn) c += popc4(acc[k]);
-  }
   const uint32_t total = __reduce_add_sync(FULL, c);
   uint16_t *slot = a.slot_out + (size_t)v * a.slot_n;
   if (total >= a.slot_n) {  // a long row: its count alone
@@ -960,6 +955,7 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
   const int lane = threadIdx.x & 31;
   const bool leader_group = lane < L;
   bool any = false;
+  uint32_t bits = 0;  // this lane's new bits of the row
   if (leader_group) {
 #pragma unroll
     for (int k = 0; k < UPL; k++) {
@@ -978,13 +974,14 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
         }
         if (nz4(x)) {
           any = true;
-          nb += popc4(x);
+          bits += popc4(x);
           if (a.acc_on) a.acc[idx] = or4(a.acc[idx], x);
         }
         acc[k] = x;
       }
     }
   }
+  nb += bits;
   const bool rownz = __any_sync(FULL, any);
   if (lane == 0 && rownz && (a.res_vis || a.acc_on)) a.resflag[v] = 1;
   if (!a.multislice && a.last) {
@@ -1007,7 +1004,7 @@ __device__ __forceinline__ void pull_epilogue(const PullArgs &a, const L2Pol<H> 
     bool virt = false;                 // the row is left in its slot only (flag 2)
     if (a.tiny_out) {  // every vertex gets a tiny word: the count is 0 for an empty row
       if (rownz)
-        virt = write_short<L, UPL>(a, v, acc, qn, ns) && a.virt_out;
+        virt = write_short<L, UPL>(a, v, acc, qn, bits, ns) && a.virt_out;
       else if (lane == 0) {
         a.tiny_out[v] = 0;
         a.slot_out[(size_t)v * a.slot_n] = 0;

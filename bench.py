@@ -435,7 +435,7 @@ def join_inputs(w, n):
 
 def join_bytes(n_build, n_probe):
     """Algorithmic bytes of a count-only Flat x Flat join of 4-byte keys
-    (SURVEY 8(d) join formula without output): both key columns read, the
+    (the hash join's compulsory bytes, no output): both key columns read, the
     table cleared (16 B per slot: key and count, capacity the power of two
     >= 2 N_b, at least 64), one 16-byte insert per build row and at least one
     32-byte sector per probe."""
@@ -780,7 +780,7 @@ def run_gpu(args, w, rank, world, local_rank):
                 pull_ms += st["pull_ms"][h]
                 pull_hop_ms[h] = pull_hop_ms.get(h, 0.0) + st["pull_ms"][h]
                 pull_launches += 1
-                # compulsory bytes of the hop (SURVEY 8(d)): CSR offsets, the
+                # compulsory bytes of the hop: CSR offsets, the
                 # active in-list entries and P = 4 passes over the V x S
                 # matrices (frontier read, next layer write, visited read + write)
                 pull_comp += expand_bytes(g.V, W, stA["active_edges"][h], True, False, gathers=False)

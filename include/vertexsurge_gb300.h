@@ -241,6 +241,13 @@ int vs_expand_layers(vs_graph *g, const uint32_t *sources, uint32_t S, const vs_
  * distance column I64. */
 int vs_layers_to_flat(const vs_bitmat *const *layers, const int32_t *distances, uint32_t n, vs_flat **out,
                       vs_stream_t stream);
+/* The same with each (row value, column value) pair once, at the smallest
+ * distance it appears (VExpand::merge_to_Flat for Any paths,
+ * vexpand.cpp:383-405, which de-duplicates pairs across layers k_min..k_actual;
+ * Shortest layers are disjoint, so both calls agree there).  Layers of one
+ * shape, distances ascending. */
+int vs_layers_to_flat_first(const vs_bitmat *const *layers, const int32_t *distances, uint32_t n, vs_flat **out,
+                            vs_stream_t stream);
 /* One-shot expand (VExpand::run_internal, vexpand.cpp:448-483): plan, run,
  * hand the result matrix to the caller.  FindShortest: targets[i] is the
  * target of source i, distances[i] receives the hop count (0 when source ==

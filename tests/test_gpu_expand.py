@@ -327,6 +327,31 @@ def test_expand_layers_with_distance(vs, graphs, path, krange):
             assert len(set(zip(r.tolist(), c.tolist()))) == total
 
 
+@pytest.mark.parametrize("path,krange", [("any", (1, 3)), ("any", (2, 4)), ("any", (0, 2)), ("shortest", (1, 3))])
+def test_layers_to_flat_first_distance(vs, graphs, path, krange):
+    """VExpand's CSR output with distances: each (source, vertex) pair once at
+    the smallest layer it appears in (merge_to_Flat; for Any a pair reached by
+    walks of several lengths keeps the shortest in range).  Checked against the
+    oracle's per-layer matrices; for Shortest it equals the plain layer list."""
+    g, dg = graphs["rmat11_skew"]
+    src = graphgen.sample_sources(g.V, 130, seed=8)
+    k0, k1 = krange
+    layers = vs.expand_layers(dg, src, k0, k1, path, "forward")
+    first = {}
+    for h, _ in layers:
+        exp, _, _ = O.vexpand(g, src, h, h, path, "forward")
+        bits = np.unpackbits(exp.view(np.uint8), axis=1, bitorder="little")[:, : len(src)]
+        for v, i in zip(*np.nonzero(bits)):
+            first.setdefault((int(src[i]), int(v)), h)
+    r, c, d = vs.layers_to_flat(layers, first=True).columns()
+    got = {(int(a), int(b)): int(x) for a, b, x in zip(r, c, d)}
+    assert len(got) == len(r) == len(first)
+    assert got == first
+    if path == "shortest":
+        r2, c2, d2 = vs.layers_to_flat(layers).columns()
+        assert sorted(zip(r2.tolist(), c2.tolist(), d2.tolist())) == sorted(zip(r.tolist(), c.tolist(), d.tolist()))
+
+
 def test_malformed_csr_is_rejected(vs):
     g = graphgen.from_edges(10, [1, 2], [2, 3])
     bad = g.fwd_dst.copy()

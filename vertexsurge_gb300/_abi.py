@@ -168,6 +168,8 @@ _SIGS += [
                                    C.POINTER(C.c_void_p), C.POINTER(C.c_uint32), C.c_void_p]),
     ("vs_layers_to_flat", C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p),
                                     C.c_void_p]),
+    ("vs_layers_to_flat_first", C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.c_uint32,
+                                          C.POINTER(C.c_void_p), C.c_void_p]),
     ("vs_matrix_row_or_sum", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_void_p]),
     ("vs_semi_join", C.c_int, [TableRef, TableRef, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int,
                                C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_void_p]),
@@ -677,12 +679,14 @@ def expand_layers(graph: "DeviceGraph", sources, k_min, k_max, path="shortest", 
     return [(k_min + i, BitMatrix(C.c_void_p(arr[i]))) for i in range(got.value)]
 
 
-def layers_to_flat(layers: list, stream=None) -> "FlatTable":
-    """(row value, column value, distance) tuples of [(distance, BitMatrix)]."""
+def layers_to_flat(layers: list, stream=None, first=False) -> "FlatTable":
+    """(row value, column value, distance) tuples of [(distance, BitMatrix)];
+    first=True keeps each (row, column) pair once, at its smallest distance."""
     hs = (C.c_void_p * max(1, len(layers)))(*[m.h for _, m in layers])
     d = np.ascontiguousarray([h for h, _ in layers], dtype=np.int32)
     out = C.c_void_p()
-    check(lib().vs_layers_to_flat(hs, _ptr(d), len(layers), C.byref(out), _stream(stream)))
+    fn = lib().vs_layers_to_flat_first if first else lib().vs_layers_to_flat
+    check(fn(hs, _ptr(d), len(layers), C.byref(out), _stream(stream)))
     return FlatTable(out)
 
 

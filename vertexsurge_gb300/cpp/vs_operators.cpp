@@ -71,6 +71,14 @@ std::shared_ptr<FlatTable> MultipleMatrixTable::output_to_flat() const {
   check(vs_layers_to_flat(hs.data(), dis.data(), (uint32_t)hs.size(), &f, BigOperator::stream));
   return std::make_shared<FlatTable>(schema, f);
 }
+
+std::shared_ptr<FlatTable> MultipleMatrixTable::output_to_flat_first() const {
+  std::vector<const vs_bitmat *> hs;
+  for (auto &m : mats) hs.push_back(m->h);
+  vs_flat *f = nullptr;
+  check(vs_layers_to_flat_first(hs.data(), dis.data(), (uint32_t)hs.size(), &f, BigOperator::stream));
+  return std::make_shared<FlatTable>(schema, f);
+}
 MatrixTable *Table::down_to_matrix_table() { return dynamic_cast<MatrixTable *>(this); }
 
 static int32_t abi_type(Type t) { return t == Type::Int64 ? VS_T_I64 : VS_T_VID; }
@@ -359,7 +367,8 @@ void VExpand::run_internal() {
   if (path_params.with_distance) {
     // copy_to_multi_MT (vexpand.cpp:356-378); the CSR strategy's flat output
     // with distances (merge_to_Flat, :380-446) is the same layers as tuples,
-    // for Shortest (Any de-duplicates pairs across layers there: not built)
+    // each (source, vertex) pair once at its smallest distance for Any (the
+    // Shortest layers are disjoint)
     std::vector<vs_bitmat *> layers(k_max - k_min + 1, nullptr);
     uint32_t n = 0;
     check(vs_expand_layers(et.g, src.data(), (uint32_t)src.size(), &p, layers.data(), &n, stream));
@@ -372,9 +381,7 @@ void VExpand::run_internal() {
       multi->add_mat(t, (int32_t)(k_min + i));
     }
     if (strategy == ExpandStrategy::CSR) {
-      if (path_params.path_type == ExpandPathType::Any)
-        throw Error(VS_ERR_UNSUPPORTED, "CSR strategy with distances for Any (per-pair de-duplication)");
-      results = multi->output_to_flat();
+      results = path_params.path_type == ExpandPathType::Any ? multi->output_to_flat_first() : multi->output_to_flat();
     } else {
       results = multi;
     }

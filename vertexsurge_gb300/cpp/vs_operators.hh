@@ -129,6 +129,9 @@ class MultipleMatrixTable : public Table {
   size_t tuple_count() override;
   // (row value, column value, distance) tuples, layer by layer (bit_matrix_table.cpp:302-340)
   std::shared_ptr<FlatTable> output_to_flat() const;
+  // the same with each (row, column) pair once, at its smallest distance
+  // (VExpand::merge_to_Flat for Any paths, vexpand.cpp:383-405)
+  std::shared_ptr<FlatTable> output_to_flat_first() const;
 };
 class ColMainMatrixTable : public MatrixTable {
  public:

@@ -375,6 +375,35 @@ static bool plans_case(const HostGraph &hg) {
     EXPECT_EQ((int64_t)r.size(), exp);
     EXPECT_EQ(bad, (size_t)0);
   }
+  // VExpand with_distance, CSR strategy, Any: each (a, v) pair once, at the
+  // smallest walk length in 1..3 (merge_to_Flat, vexpand.cpp:383-405): as many
+  // tuples as the Any [1,3] union has bits, each distance in [max(1, BFS distance), 3]
+  {
+    auto ve = make_shared<VExpand>("Person", "Person", "knows", Direction::Both, 1, 3,
+                                   VExpandPathParameters::Any().set_with_distance(), ExpandStrategy::CSR,
+                                   "a.id", std::optional<VariableName>("b.id"));
+    ve->addLastDependency(A);
+    ve->run();
+    auto u = make_shared<VExpand>("Person", "Person", "knows", Direction::Both, 1, 3, ExpandPathType::Any,
+                                  ExpandStrategy::Dense, "a.id", std::optional<VariableName>("b.id"));
+    u->addLastDependency(A);
+    u->run();
+    auto *flat = ve->results->down_to_flat_table();
+    EXPECT_EQ(flat != nullptr, true);
+    EXPECT_EQ(ve->results->tuple_count(), u->results->tuple_count());
+    auto r = flat->column(0), c = flat->column(1), d = flat->column(2);
+    std::map<uint64_t, size_t> row_of;
+    for (size_t i = 0; i < sa.size(); i++) row_of.emplace(sa[i], i);
+    size_t bad = 0;
+    std::set<std::pair<uint64_t, uint64_t>> pairs;
+    for (size_t t = 0; t < r.size(); t++) {
+      const int64_t dd = (int64_t)d[t], bfs = da[row_of.at(r[t])][c[t]];
+      bad += dd < 1 || dd > 3 || bfs < 0 || dd < bfs;
+      pairs.emplace(r[t], c[t]);
+    }
+    EXPECT_EQ(bad, (size_t)0);
+    EXPECT_EQ(pairs.size(), r.size());
+  }
   // FindShortest over (start, target) pairs
   {
     vector<uint64_t> tg;

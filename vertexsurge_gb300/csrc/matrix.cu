@@ -155,6 +155,52 @@ __global__ void k_fill_i64(long long *dst, uint64_t n, long long v) {
     dst[i] = v;
 }
 
+// The bits of a layer not seen in an earlier one (first = layer & ~seen),
+// then seen |= layer; n uint4 of each matrix.
+__global__ void k_first_bits(const uint4 *__restrict__ layer, uint4 *__restrict__ seen, uint4 *__restrict__ first,
+                             uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint4 l = layer[i], s = seen[i];
+    first[i] = andnot4(l, s);
+    seen[i] = or4(s, l);
+  }
+}
+
+// (row value, column value, distance) tuples of the parts, part i with distances[i].
+int concat_parts(const std::vector<vs_flat *> &parts, const int32_t *distances, cudaStream_t st, vs_flat **out) {
+  uint64_t total = 0;
+  for (auto *p : parts) total += p->nrows;
+  const int32_t types[3] = {VS_T_VID, VS_T_VID, VS_T_I64};
+  vs_flat *f = nullptr;
+  VS_TRY(flat_alloc(3, types, total, st, &f));
+  uint64_t off = 0;
+  for (size_t i = 0; i < parts.size(); i++) {
+    const uint64_t k = parts[i]->nrows;
+    if (!k) continue;
+    cudaError_t e = cudaMemcpyAsync((uint32_t *)f->cols[0] + off, parts[i]->cols[0], 4 * k, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync((uint32_t *)f->cols[1] + off, parts[i]->cols[1], 4 * k, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) {
+      const int blocks = (int)std::min<uint64_t>((k + 255) / 256, (uint64_t)sm_count() * 8);
+      k_fill_i64<<<blocks, 256, 0, st>>>((long long *)f->cols[2] + off, k, distances[i]);
+      vs::note_launch();
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+      vs_flat_free(f);
+      return cuda_fail(e, "layers to flat", __FILE__, __LINE__);
+    }
+    off += k;
+  }
+  const cudaError_t e = cudaStreamSynchronize(st);  // the parts are freed on return
+  if (e != cudaSuccess) {
+    vs_flat_free(f);
+    return cuda_fail(e, "layers to flat", __FILE__, __LINE__);
+  }
+  *out = f;
+  return VS_OK;
+}
+
 }  // namespace vs
 
 using namespace vs;
@@ -172,41 +218,59 @@ int vs_layers_to_flat(const vs_bitmat *const *layers, const int32_t *distances, 
       for (auto *f : p) vs_flat_free(f);
     }
   } fr{parts};
-  uint64_t total = 0;
   for (uint32_t i = 0; i < n; i++) {
     if (!layers[i]) return fail(VS_ERR_ARG, "layer %u is null", i);
     VS_TRY(bitmat_to_flat(layers[i], st, &parts[i]));
-    total += parts[i]->nrows;
   }
-  const int32_t types[3] = {VS_T_VID, VS_T_VID, VS_T_I64};
-  vs_flat *f = nullptr;
-  VS_TRY(flat_alloc(3, types, total, st, &f));
-  uint64_t off = 0;
+  return concat_parts(parts, distances, st, out);
+}
+
+int vs_layers_to_flat_first(const vs_bitmat *const *layers, const int32_t *distances, uint32_t n, vs_flat **out,
+                            vs_stream_t stream) {
+  if (!out || (n && (!layers || !distances))) return fail(VS_ERR_ARG, "vs_layers_to_flat_first: null argument");
   for (uint32_t i = 0; i < n; i++) {
-    const uint64_t k = parts[i]->nrows;
-    if (!k) continue;
-    cudaError_t e = cudaMemcpyAsync((uint32_t *)f->cols[0] + off, parts[i]->cols[0], 4 * k, cudaMemcpyDeviceToDevice, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync((uint32_t *)f->cols[1] + off, parts[i]->cols[1], 4 * k, cudaMemcpyDeviceToDevice, st);
-    if (e == cudaSuccess) {
-      const int blocks = (int)std::min<uint64_t>((k + 255) / 256, (uint64_t)sm_count() * 8);
-      k_fill_i64<<<blocks, 256, 0, st>>>((long long *)f->cols[2] + off, k, distances[i]);
-      vs::note_launch();
-      e = cudaGetLastError();
-    }
-    if (e != cudaSuccess) {
-      vs_flat_free(f);
-      return cuda_fail(e, "vs_layers_to_flat", __FILE__, __LINE__);
-    }
-    off += k;
+    if (!layers[i]) return fail(VS_ERR_ARG, "layer %u is null", i);
+    const vs_bitmat *l0 = layers[0], *l = layers[i];
+    if (l->rows != l0->rows || l->cols != l0->cols || l->wpc != l0->wpc || l->kind != l0->kind)
+      return fail(VS_ERR_ARG, "layer %u differs in shape from layer 0", i);
+    if (i && distances[i] <= distances[i - 1]) return fail(VS_ERR_ARG, "distances must ascend");
   }
-  const cudaError_t e = cudaStreamSynchronize(st);  // the parts are freed on return
-  if (e != cudaSuccess) {
-    vs_flat_free(f);
-    return cuda_fail(e, "vs_layers_to_flat", __FILE__, __LINE__);
+  cudaStream_t st = S(stream);
+  std::vector<vs_flat *> parts(n, nullptr);
+  struct Free {
+    std::vector<vs_flat *> &p;
+    uint64_t *seen = nullptr, *first = nullptr;
+    cudaStream_t st;
+    ~Free() {
+      for (auto *f : p) vs_flat_free(f);
+      dfree(seen, st);
+      dfree(first, st);
+    }
+  } fr{parts, nullptr, nullptr, st};
+  if (n) {
+    const uint64_t words = (uint64_t)layers[0]->wpc * layers[0]->cols;  // wpc is even: whole uint4
+    VS_TRY(dalloc_n(&fr.seen, words, st));
+    VS_TRY(dalloc_n(&fr.first, words, st));
+    VS_CK(cudaMemsetAsync(fr.seen, 0, 8 * words, st));
+    const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((words / 2 + 255) / 256, (uint64_t)sm_count() * 8));
+    for (uint32_t i = 0; i < n; i++) {
+      if (words) {
+        k_first_bits<<<blocks, 256, 0, st>>>(reinterpret_cast<const uint4 *>(layers[i]->words),
+                                                 reinterpret_cast<uint4 *>(fr.seen),
+                                                 reinterpret_cast<uint4 *>(fr.first), words / 2);
+        vs::note_launch();
+        VS_CK(cudaGetLastError());
+      }
+      vs_bitmat view = *layers[i];  // the layer's maps over the new bits
+      view.words = fr.first;
+      view.colnz = nullptr;
+      view.owns_words = false;
+      view.view = true;
+      view.pool_plan = nullptr;
+      VS_TRY(bitmat_to_flat(&view, st, &parts[i]));
+    }
   }
-  *out = f;
-  return VS_OK;
+  return concat_parts(parts, distances, st, out);
 }
 
 int vs_matrix_select(const vs_bitmat *m, const uint32_t *targets, uint32_t T, vs_bitmat **out,

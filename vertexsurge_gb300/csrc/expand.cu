@@ -82,17 +82,34 @@ __global__ void k_clear_flagged(uint4 *__restrict__ buf, uint32_t *__restrict__ 
   }
   const int lane = threadIdx.x & 31;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < V;
-       base += warps * 32) {
-    uint32_t v = base + lane;
-    uint32_t f = v < V ? flag[v] : 0u;
-    unsigned m = __ballot_sync(FULL, f == 1);  // flag 2: the row lives in its slot, the buffer row is zero
-    if (f) flag[v] = 0;
-    while (m) {
-      int b = __ffs(m) - 1;
-      m &= m - 1;
-      uint4 *row = buf + (size_t)(base + b) * Q;
-      for (uint32_t q = lane; q < Q; q += 32) row[q] = make_uint4(0, 0, 0, 0);
+  // four flags per lane (16-byte loads of the 16-byte aligned flag array):
+  // a warp step covers 128 vertices, so the scan is a quarter as many
+  // dependent loads; flag 2 means the row lives in its slot (buffer row zero)
+  uint4 *flag4 = reinterpret_cast<uint4 *>(flag);
+  const uint32_t nq = V / 4;
+  for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < nq; base += warps * 32) {
+    const uint32_t g = base + lane;
+    const uint4 f = g < nq ? flag4[g] : make_uint4(0, 0, 0, 0);
+    if (f.x | f.y | f.z | f.w) flag4[g] = make_uint4(0, 0, 0, 0);
+    const uint32_t fv[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      unsigned m = __ballot_sync(FULL, fv[k] == 1);
+      while (m) {
+        const int b = __ffs(m) - 1;
+        m &= m - 1;
+        uint4 *row = buf + (size_t)((base + b) * 4u + k) * Q;
+        for (uint32_t q = lane; q < Q; q += 32) row[q] = make_uint4(0, 0, 0, 0);
+      }
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 32) {  // the last V % 4 vertices
+    for (uint32_t v = nq * 4; v < V; v++) {
+      const uint32_t f = flag[v];
+      if (f == 1)
+        for (uint32_t q = lane; q < Q; q += 32) buf[(size_t)v * Q + q] = make_uint4(0, 0, 0, 0);
+      __syncwarp();
+      if (lane == 0 && f) flag[v] = 0;
     }
   }
 }

@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const unsigned long l
                                                            unsigned long long *__restrict__ out) {
   __shared__ unsigned long long base[256];  // next free slot per digit for this block
   __shared__ unsigned wcnt[RS_THREADS / 32][256];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int wid = threadIdx.x >> 5;
   base[threadIdx.x] = off[(uint64_t)threadIdx.x * nblk + blockIdx.x];
   const uint64_t b0 = (uint64_t)blockIdx.x * RS_TILE, b1 = b0 + RS_TILE < n ? b0 + RS_TILE : n;
   for (uint64_t s = b0; s < b1; s += RS_THREADS) {

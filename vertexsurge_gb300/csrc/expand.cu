@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(256, 4) k_sparse(SparseArgs a) {
           if (fresh[k]) {
             const size_t idx = (size_t)v[k] * a.W + (i[k] >> 6);
             const unsigned long long bit = 1ull << (i[k] & 63);
-            if (a.shortest && !a.last) atomicOr(&a.N[idx], bit);
+            if (a.shortest && !a.last && !a.defer) atomicOr(&a.N[idx], bit);
             if (a.acc_on) atomicOr(&a.acc[idx], bit);
             nb++;
           }
@@ -622,6 +622,8 @@ __global__ void __launch_bounds__(256, 4) k_sparse(SparseArgs a) {
           a.pdeg_out[slot] = d;
         } else {
           c->hop[a.h].overflow = 1;
+          // a deferred row gets the bit a full list cannot hold
+          if (a.defer) atomicOr(&a.N[(size_t)pr.x * a.W + (pr.y >> 6)], 1ull << (pr.y & 63));
         }
       }
       __syncwarp();
@@ -1415,6 +1417,29 @@ __device__ __forceinline__ bool pairs_build(const Ctr *c, int h) {
   return cur.strategy == ST_PULL && cur.short_pull && (h == 1 || (p.strategy == ST_SPARSE && !p.overflow));
 }
 
+// Rows of a layer a SPARSE hop left in its pair list (Shortest: the hop
+// dedups through the visited bits and writes no next-layer words), built
+// before hop h reads them.  mode 0, right after hop h's decision: every pair
+// when hop h reads whole rows (PUSH, dense or multi-slice PULL) or builds its
+// short-row index from rows (the list overflowed); mode 1, after the index
+// was built from the pairs: the pairs of rows too long for a slot, which a
+// short-mode PULL gathers whole.  SPARSE reads only pairs.
+__global__ void k_pairs_rows(const uint2 *__restrict__ pairs, const uint32_t *__restrict__ cnt,
+                             unsigned long long *__restrict__ N, uint32_t W, uint32_t slot_n, uint64_t cap,
+                             const Ctr *ctr, int h, int mode) {
+  if (ctr->hop[h - 1].strategy != ST_SPARSE) return;
+  const int s = ctr->hop[h].strategy;
+  const bool go = mode == 0 ? (s == ST_PUSH || (s == ST_PULL && !pairs_build(ctr, h))) : pairs_build(ctr, h);
+  if (!go) return;
+  const unsigned long long np_raw = ctr->hop[h - 1].pairs;
+  const uint64_t np = np_raw < cap ? np_raw : cap;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < np; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint2 pr = pairs[k];
+    if (mode == 1 && cnt[pr.x] < slot_n) continue;
+    atomicOr(&N[(size_t)pr.x * W + (pr.y >> 6)], 1ull << (pr.y & 63));
+  }
+}
+
 __global__ void k_pairs_zero(uint32_t *__restrict__ cnt, uint32_t V, const Ctr *ctr, int h) {
   if (!pairs_build(ctr, h)) return;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) cnt[v] = 0;
@@ -2164,6 +2189,12 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     return pl->slot[0] != nullptr && hh >= 1 && hh < p.k_max && p.path_type != VS_PATH_FIND_SHORTEST &&
            pl->layer_out[hh] == nullptr;
   };
+  // a Shortest SPARSE hop leaves its layer's rows in its pair list when a
+  // later hop may build them (not the last hop, not an exported layer, not
+  // FindShortest, whose target check reads every layer's rows)
+  auto defer_rows = [&](uint32_t hh) {
+    return pl->use_vis && hh >= 1 && hh < p.k_max && p.path_type != VS_PATH_FIND_SHORTEST && !pl->layer_out[hh];
+  };
   // PUSH runs only when forced (for the run or a hop) or enabled in the
   // fixed planner (push_frac > 0)
   bool any_forced_push = forced == ST_PUSH;
@@ -2204,6 +2235,9 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     { k_decide<<<1, 256, 0, st>>>(da); vs::note_launch(); }
     // hop_ms covers what the chosen strategy costs, not the statistics and decision before it
     if (timing) cudaEventRecord(pl->ev[3 * h], st);
+    if (defer_rows(h - 1))  // rows a SPARSE hop h-1 left in its pair list, when hop h reads rows
+      { k_pairs_rows<<<pl->grid_v, 256, 0, st>>>(pl->pairs[fb], pl->touched, reinterpret_cast<unsigned long long *>(pl->buf[fb]),
+                                               W, pl->slot_n, pl->pair_cap, pl->ctr, h, 0); vs::note_launch(); }
     if (pl->slot[0] && leave_in_slots(h - 1))  // whole rows back for a hop that reads rows
       { k_materialize<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<uint4 *>(pl->buf[fb]), V, Q,
                                                 pl->slot[fb], pl->slot_n, pl->ctr, h, 1); vs::note_launch(); }
@@ -2233,6 +2267,7 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
     sp.pdeg_out = pl->pdeg[nbuf];
     sp.stats = stats && h < p.k_max;
     sp.last = h == p.k_max && pl->use_vis && p.path_type != VS_PATH_FIND_SHORTEST && !pl->layer_out[h];
+    sp.defer = defer_rows(h);
     { k_pscan1<<<pl->grid_v, 256, 0, st>>>(pl->pdeg[fb], pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
     { k_pscan2<<<1, 1024, 0, st>>>(pl->bsum, pl->doff, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
     { k_pscan3<<<pl->grid_v, 256, 0, st>>>(pl->doff, pl->bsum, pl->ctr, h, pl->pair_cap); vs::note_launch(); }
@@ -2301,6 +2336,10 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
                                                 pl->ctr, h); vs::note_launch(); }
       { k_pairs_words<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], pl->touched, pl->tiny[fb], pl->slot[fb], pl->slot_n, V,
                                                 pl->ctr, h); vs::note_launch(); }
+      if (defer_rows(h - 1))  // the rows too long for a slot, which the short-mode PULL gathers whole
+        { k_pairs_rows<<<pl->grid_v, 256, 0, st>>>(pl->pairs[fb], pl->touched,
+                                                 reinterpret_cast<unsigned long long *>(pl->buf[fb]), W, pl->slot_n,
+                                                 pl->pair_cap, pl->ctr, h, 1); vs::note_launch(); }
       { k_slot_build<<<pl->grid_v, 256, 0, st>>>(pl->flag[fb], reinterpret_cast<const uint4 *>(pl->buf[fb]), V, Q,
                                                pl->tiny[fb], pl->slot[fb], pl->slot_n, pl->ctr, h); vs::note_launch(); }
     }

@@ -93,6 +93,7 @@ struct SparseArgs {
   int shortest, acc_on;
   int stats;  // also count hop h+1's frontier statistics (active_edges, hist) of the layer it writes
   int last;   // Shortest, and layer h is read by nothing: no next-layer rows or pairs, rows flagged 2
+  int defer;  // Shortest: layer h's rows are built from its pair list by the hop that reads rows (k_pairs_rows)
 };
 
 struct PushArgs {

@@ -306,12 +306,26 @@ def run_gpu_batched(args, w, rank, world, local_rank):
         table = waves["table"] + more["table"]
         if more["ms"] < waves["ms"]:
             waves = more
+        # and the SPARSE threshold, tuned above on one sample query, on the batch itself
+        waves["sparse_frac"] = setting["sparse_frac"]
+        for sf in (0.002, 0.02):
+            if sf == setting["sparse_frac"]:
+                continue
+            alt = batch.tune_wave_rows(dg, queries, stream, candidates=(waves["wave_rows"],),
+                                       setting=dict(setting, sparse_frac=sf, short_share=waves["short_share"]),
+                                       short_shares=(waves["short_share"],), lanes=(waves["lanes"],))
+            for r in alt["table"]:
+                r["sparse_frac"] = sf
+            table += alt["table"]
+            if alt["ms"] < waves["ms"]:
+                waves = dict(alt, sparse_frac=sf)
         waves["table"] = table
         if tc:
             cached = json.loads(Path(tc).read_text()) if Path(tc).exists() else {}
             cached[wkey] = waves
             Path(tc).write_text(json.dumps(cached, indent=1))
     setting["short_share"] = waves.get("short_share", setting["short_share"])
+    setting["sparse_frac"] = waves.get("sparse_frac", setting["sparse_frac"])
     log(f"[rank {rank}] autotune {time.time() - t0:.1f}s: {setting} waves {waves}")
     bt = batch.Batch(dg, queries, waves["wave_rows"], stream, setting=setting, lanes=waves.get("lanes", 1))
     cg = bt.capture()

@@ -26,3 +26,29 @@ def test_reference_arm_line():
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_serving_oracle_counts():
+    """The serving workload's CPU check (bench.serving_oracle): its visited
+    count, its numpy join count (sum of the key columns' popcounts) and its
+    triangle count over sorted lists equal the oracle's VExpand count, the
+    oracle's HashJoin through TableConvert, and an independent sparse-matrix
+    triangle count, on a small trace."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    from oracle import pyoracle as O
+    from tests import pattern_oracle as P
+    from vertexsurge_gb300 import graphgen, serve
+    g = graphgen.rmat(12, 16, seed=3)
+    trace = serve.make_trace(g, 6, 1e6, s_range=(16, 200), l_max=4, join_rows=(100, 2000), seed=9)
+    idx, out, _ = bench.serving_oracle(g, trace, 3)
+    assert len(idx) == 3 and idx == sorted(range(6), key=lambda i: (len(trace[i].sources) * trace[i].k_max, i))[:3]
+    for i, got in zip(idx, out):
+        r = trace[i]
+        words, _, _ = O.vexpand(g, r.sources, 1, r.k_max, "shortest", "forward")
+        cm = O.table_convert(words, len(r.sources), g.V, False)
+        a = O.Table(O.COLMAIN, [0, 1], words=cm, mrows=len(r.sources), mcols=g.V, row_map=r.sources)
+        k = O.Table(O.FLAT, [2, 1], cols=[r.payload, r.keys])
+        want = (O.matrix_count(words, len(r.sources), g.V), O.hash_join(k, a, 1, only_count=True)[2],
+                P.triangle_count(g, r.sources))
+        assert got == want and got[1] > 0 and got[2] > 0

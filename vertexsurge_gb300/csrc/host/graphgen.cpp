@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <random>
 #include <set>
 #include <vector>
 
@@ -307,6 +308,29 @@ int vsg_sample_sources(uint32_t V, uint32_t n, uint64_t seed, uint32_t *out) {
     std::sort(all.begin(), all.begin() + n);
     std::memcpy(out, all.data(), sizeof(uint32_t) * n);
   }
+  return 0;
+}
+
+// Community tags of n vertices in id order, as the reference's social-network
+// importer assigns them (SocialNetworkImporter::set_random_community,
+// src/objects/meta/graph_loader.cpp:229-260): consecutive blocks of
+// 2048 x {1,1,1,10,10,10,100,100,100,1000,1000,1000} vertices get the tags
+// 0..11, the rest tag 12, then the tags are shuffled by std::shuffle with a
+// std::mt19937 seeded as given (the standard library's own shuffle, so the
+// tags equal the reference importer's when both use the same library).
+int vsg_sn_communities(uint64_t n, uint32_t seed, uint8_t *out) {
+  if (!out && n) return 1;
+  static const size_t block = 2048;
+  static const size_t sel[] = {1, 1, 1, 10, 10, 10, 100, 100, 100, 1000, 1000, 1000};
+  const size_t nsel = sizeof(sel) / sizeof(sel[0]);
+  std::vector<uint8_t> tag(n);
+  size_t idx = 0;
+  for (size_t c = 0; c < nsel; c++)
+    for (size_t x = 0; x < block * sel[c] && idx < n; x++) tag[idx++] = (uint8_t)c;
+  while (idx < n) tag[idx++] = (uint8_t)nsel;
+  std::mt19937 gen(seed);
+  std::shuffle(tag.begin(), tag.end(), gen);
+  if (n) std::memcpy(out, tag.data(), n);
   return 0;
 }
 

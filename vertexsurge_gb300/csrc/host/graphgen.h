@@ -53,6 +53,9 @@ void vsg_free(vsg_graph *g);
  * src/include/utils/utils.hh:75-95, which returns a sorted std::set when
  * 2n <= V). */
 int vsg_sample_sources(uint32_t V, uint32_t n, uint64_t seed, uint32_t *out);
+/* Community tags (uint8) of n vertices as the reference's social-network
+ * importer assigns them (std::mt19937(seed) + std::shuffle). */
+int vsg_sn_communities(uint64_t n, uint32_t seed, uint8_t *out);
 
 /* The counter-based hash used by every generator (exposed for tests). */
 uint64_t vsg_hash(uint64_t seed, uint64_t a, uint64_t b);

@@ -217,7 +217,7 @@ PROPERTY_TYPES = {np.dtype(np.uint8): "TagValue8", np.dtype(np.uint16): "TagValu
 
 
 def save(dir_, g: HostGraph, vertex_type="Person", edge_type="knows", graph_name="synthetic",
-         properties: dict | None = None, flats=(), partitioned=None, csr=True) -> None:
+         properties: dict | None = None, flats=(), partitioned=None, csr=True, graph_type="synthetic") -> None:
     """Write one vertex type (with optional properties: name -> per-vertex
     array, stored as "Type.name") and one self edge type (src = dst): its CSR
     files (unless csr is False) and the flat edge lists asked for (`flats`:
@@ -240,7 +240,7 @@ def save(dir_, g: HostGraph, vertex_type="Person", edge_type="knows", graph_name
             write_disk_array(d / names["bwd_data"], g.rev_src.astype(np.uint32))
     store_info = write_flat_edges(d, g, vertex_type, edge_type, vertex_type, flats, partitioned)
     schema = {
-        "graph_name": graph_name, "graph_type": "synthetic",
+        "graph_name": graph_name, "graph_type": graph_type,
         "vertex": [{"type": vertex_type, "statistics": {"count": int(g.V)}, "properties": props}],
         "edge": [{"type": edge_type, "directed": bool(g.directed), "allow_multiple_edge": False,
                   "src": vertex_type, "dst": vertex_type, "properties": {},

@@ -41,6 +41,7 @@ def _lib():
         L.vsg_sample_sources.argtypes = [C.c_uint32, C.c_uint32, C.c_uint64, C.c_void_p]
         L.vsg_hash.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
         L.vsg_hash.restype = C.c_uint64
+        L.vsg_sn_communities.argtypes = [C.c_uint64, C.c_uint32, C.c_void_p]
         _gen = L
     return _gen
 

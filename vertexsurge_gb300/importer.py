@@ -1,0 +1,127 @@
+"""Importer: a social-network edge list (SNAP text or CSV) into the
+reference's graph directory, as the reference's importer writes it for the
+"sn" graph type (src/objects/importer.cpp:120-152; SocialNetworkImporter,
+src/objects/meta/graph_loader.cpp:151-305), so the same input feeds both sides.
+
+Steps, each as the reference takes it:
+  * parse: SNAP text, one "src dst" pair of 64-bit raw ids per line, lines
+    starting with '#' skipped (:151-186); SNAP CSV, a "node_1,node_2" header
+    then one pair per line (:107-117,188-209);
+  * vertices: the distinct raw ids, numbered in ascending raw-id order
+    (rearrange, :262-278; unify_vertex_and_collect_statistics,
+    include/meta/graph_loader.hh:11-23);
+  * communities: set_random_community (:229-260), through the host library's
+    vsg_sn_communities (the standard library's mt19937 and shuffle);
+  * edges: raw ids mapped to the new ids; knows is undirected, so every edge
+    is appended reversed (add_reverse_edges, storage/graph_concepts.hh:100-107),
+    then equal NEIGHBOURING pairs are dropped before the sort by (src, dst) —
+    the reference runs std::unique on the unsorted list
+    (deduplicate_edges, :109-112; unify_edge_and_collect_statistics,
+    graph_loader.hh:59-79), so a pair repeated far apart stays repeated, and
+    this importer keeps that multiset;
+  * output: Person.id and Person.community DiskArrays, the src_dst CSR, the
+    flat lists in src_dst and hilbert order (init_graph_schema, :211-227; with
+    no block count the partitioned forms collapse into the single files),
+    schema.json with graph_type "Social Network".
+Not written: Person.name (random letters drawn in the reference's hash-set
+order, not a value any operator of the path reads).  The reference's CSV path
+collects the vertex set from edge fields that are not yet filled
+(:197-200); here it is the raw ids, as in the text path.
+"""
+from __future__ import annotations
+
+import argparse
+from pathlib import Path
+
+import numpy as np
+
+from . import graph_dir, graphgen
+
+COMMUNITY_SEED = 1234
+
+
+def load_snap_txt(path) -> tuple[np.ndarray, np.ndarray]:
+    """(raw src, raw dst) uint64 arrays of a SNAP edge-list text file."""
+    src, dst = [], []
+    with open(path) as f:
+        for n, line in enumerate(f, 1):
+            if not line.strip() or line.startswith("#"):
+                continue
+            parts = line.split()
+            if len(parts) < 2:
+                raise ValueError(f"{path}:{n}: expected two vertex ids")
+            src.append(int(parts[0]))
+            dst.append(int(parts[1]))
+    return np.asarray(src, np.uint64), np.asarray(dst, np.uint64)
+
+
+def load_snap_csv(path) -> tuple[np.ndarray, np.ndarray]:
+    """(raw src, raw dst) of a CSV with the header node_1,node_2."""
+    with open(path) as f:
+        header = f.readline().strip().split(",")
+        if header != ["node_1", "node_2"]:
+            raise ValueError(f"{path}: header must be node_1,node_2, got {header}")
+        rows = [line.strip().split(",") for line in f if line.strip()]
+    if any(len(r) != 2 for r in rows):
+        raise ValueError(f"{path}: every row holds two vertex ids")
+    a = np.asarray(rows, dtype=np.uint64).reshape(-1, 2)
+    return a[:, 0].copy(), a[:, 1].copy()
+
+
+def communities(n: int, seed: int = COMMUNITY_SEED) -> np.ndarray:
+    out = np.zeros(n, np.uint8)
+    if graphgen._lib().vsg_sn_communities(n, seed, out.ctypes.data if n else None):
+        raise ValueError("community assignment failed")
+    return out
+
+
+def rearrange(raw_src: np.ndarray, raw_dst: np.ndarray):
+    """(raw ids in vertex order, community per vertex, HostGraph of knows)."""
+    raw_ids = np.unique(np.concatenate([raw_src, raw_dst]))  # ascending: vertex i has the i-th smallest raw id
+    V = len(raw_ids)
+    if V >= 1 << 32:
+        raise ValueError("more vertices than 32-bit ids hold")
+    s = np.searchsorted(raw_ids, raw_src).astype(np.uint32)
+    d = np.searchsorted(raw_ids, raw_dst).astype(np.uint32)
+    # undirected: the list and its reverse, neighbouring duplicates dropped, then sorted
+    es = np.concatenate([s, d])
+    ed = np.concatenate([d, s])
+    keep = np.ones(len(es), bool)
+    if len(es) > 1:
+        keep[1:] = (es[1:] != es[:-1]) | (ed[1:] != ed[:-1])
+    es, ed = es[keep], ed[keep]
+    order = np.lexsort((ed, es))
+    es, ed = es[order], ed[order]
+    off = np.zeros(V + 1, np.int64)
+    np.add.at(off, es.astype(np.int64) + 1, 1)
+    off = np.cumsum(off)
+    g = graphgen.HostGraph(V, len(ed), off, ed, off, ed, directed=False)
+    return raw_ids, communities(V), g
+
+
+def output_vlgpm(out_dir, raw_src, raw_dst, partitions: int | None = None) -> graphgen.HostGraph:
+    """Write the directory; partitions: block count of the partitioned flat
+    lists (the reference's -b), none by default."""
+    raw_ids, comm, g = rearrange(raw_src, raw_dst)
+    props = {"id": np.arange(g.V, dtype=np.uint32), "community": comm}
+    part = {"src_dst": partitions, "hilbert": partitions} if partitions else None
+    graph_dir.save(out_dir, g, properties=props, flats=("src_dst", "hilbert"), partitioned=part,
+                   graph_name="Social Network", graph_type="Social Network")
+    return g
+
+
+def main():
+    ap = argparse.ArgumentParser(description="import a social-network edge list into a graph directory")
+    ap.add_argument("-s", "--source", required=True, help="edge list file")
+    ap.add_argument("-d", "--dir", required=True, help="graph directory to write")
+    ap.add_argument("-i", "--input", choices=["snap-txt", "snap-csv"], default="snap-txt")
+    ap.add_argument("-b", "--blocks", type=int, default=None, help="partitioned flat lists in this many blocks")
+    args = ap.parse_args()
+    load = load_snap_txt if args.input == "snap-txt" else load_snap_csv
+    raw_src, raw_dst = load(args.source)
+    g = output_vlgpm(Path(args.dir), raw_src, raw_dst, args.blocks)
+    print(f"{g.V} Person, {g.E} knows (both directions) -> {args.dir}")
+
+
+if __name__ == "__main__":
+    main()

@@ -33,15 +33,15 @@ def _undirected(g):
 
 
 @pytest.mark.parametrize("undirected", [False, True])
-@pytest.mark.parametrize("layout", ["csr", "flat", "blocks"])
+@pytest.mark.parametrize("layout", ["csr", "flat", "blocks", "imported"])
 def test_graph_directory_through_cpp_loader(tmp_path, undirected, layout):
     """Graph(dir).load() reads the reference's directory layout (CSR files,
     or only a flat edge list, one file or target blocks, from which it builds
-    the CSR); the count of an expand over it equals the oracle's on the same
-    arrays."""
+    the CSR, or what the social-network importer wrote from a SNAP edge list);
+    the count of an expand over it equals the oracle's on the same arrays."""
     from oracle import pyoracle as O
     from tests import graphs as G
-    from vertexsurge_gb300 import graph_dir
+    from vertexsurge_gb300 import graph_dir, importer
     g = G.small_graphs()["rmat10"]
     if undirected:
         g = _undirected(g)
@@ -49,8 +49,13 @@ def test_graph_directory_through_cpp_loader(tmp_path, undirected, layout):
         graph_dir.save(tmp_path, g)
     elif layout == "flat":
         graph_dir.save(tmp_path, g, csr=False, flats=("random",))
-    else:
+    elif layout == "blocks":
         graph_dir.save(tmp_path, g, csr=False, partitioned={"hilbert": 6})
+    else:  # the edges as a SNAP file with relabelled raw ids, imported (knows is undirected)
+        rows = np.repeat(np.arange(g.V, dtype=np.uint64), np.diff(g.fwd_off))
+        raw = lambda v: np.uint64(1_000_003) * (np.uint64(g.V) - np.asarray(v, np.uint64)) + np.uint64(7)
+        importer.output_vlgpm(tmp_path, raw(rows), raw(g.fwd_dst))
+        g = graph_dir.load(tmp_path)["Person_knows_Person"]
     r = subprocess.run([str(build.OPS_TEST), "--graph-dir", str(tmp_path)], capture_output=True, text=True,
                        timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr

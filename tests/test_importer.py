@@ -106,3 +106,36 @@ def test_command_line(tmp_path):
     assert out.returncode == 0, out.stderr
     assert "4 Person" in out.stdout
     assert (tmp_path / "db" / "schema.json").exists()
+
+
+def test_ldbc_interactive_and_bi(tmp_path):
+    """LDBC inputs: the vertices are the person files' ids (an isolated person
+    is a vertex), the knows files give the edges; an edge naming an unknown
+    person is refused."""
+    ic = tmp_path / "ic" / "social_network" / "dynamic"
+    ic.mkdir(parents=True)
+    (ic / "person_0_0.csv").write_text("id|firstName|lastName|place\n933|Ann|A|1\n4139|Bo|B|2\n10995|Cy|C|3\n77|Di|D|4\n")
+    (ic / "person_knows_person_0_0.csv").write_text(
+        "Person.id|Person.id|creationDate\n933|4139|2010\n933|10995|2011\n4139|10995|2012\n")
+    persons, rs, rd = importer.load_ldbc_ic(tmp_path / "ic")
+    g = importer.output_vlgpm(tmp_path / "db_ic", rs, rd, persons=persons)
+    assert g.V == 4  # 77 has no edge but is a person
+    ids = [77, 933, 4139, 10995]
+    rank = {v: i for i, v in enumerate(ids)}
+    e = [(rank[a], rank[b]) for a, b in [(933, 4139), (933, 10995), (4139, 10995)]]
+    assert csr_pairs(g) == sorted(e + [(b, a) for a, b in e])
+    bi = tmp_path / "bi" / "graphs" / "csv" / "bi" / "composite-merged-fk" / "initial_snapshot" / "dynamic"
+    (bi / "Person").mkdir(parents=True)
+    (bi / "Person_knows_Person").mkdir(parents=True)
+    (bi / "Person" / "part-0.csv").write_text("creationDate|id|firstName|LocationCityId\n1|933|Ann|5\n2|4139|Bo|6\n")
+    (bi / "Person" / "part-1.csv").write_text("creationDate|id|firstName|LocationCityId\n3|10995|Cy|7\n4|77|Di|8\n")
+    (bi / "Person_knows_Person" / "part-0.csv").write_text(
+        "creationDate|Person1Id|Person2Id\n1|933|4139\n2|933|10995\n")
+    (bi / "Person_knows_Person" / "part-1.csv").write_text("creationDate|Person1Id|Person2Id\n3|4139|10995\n")
+    persons, rs, rd = importer.load_ldbc_bi(tmp_path / "bi")
+    g2 = importer.output_vlgpm(tmp_path / "db_bi", rs, rd, persons=persons)
+    assert g2.V == 4 and csr_pairs(g2) == csr_pairs(g)
+    with pytest.raises(ValueError):
+        importer.rearrange(np.array([933], np.uint64), np.array([5], np.uint64), persons=persons)
+    with pytest.raises(ValueError):
+        importer.rearrange(rs, rd, persons=np.array([933, 933], np.uint64))

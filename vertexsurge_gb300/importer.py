@@ -6,10 +6,17 @@ src/objects/meta/graph_loader.cpp:151-305), so the same input feeds both sides.
 Steps, each as the reference takes it:
   * parse: SNAP text, one "src dst" pair of 64-bit raw ids per line, lines
     starting with '#' skipped (:151-186); SNAP CSV, a "node_1,node_2" header
-    then one pair per line (:107-117,188-209);
-  * vertices: the distinct raw ids, numbered in ascending raw-id order
-    (rearrange, :262-278; unify_vertex_and_collect_statistics,
-    include/meta/graph_loader.hh:11-23);
+    then one pair per line (:107-117,188-209); LDBC SNB interactive, '|'
+    separated social_network/dynamic/person_0_0.csv (column "id") and
+    person_knows_person_0_0.csv (the first two columns) (:44-69,93-105,
+    138-149); LDBC SNB BI, every .csv of the initial snapshot's
+    dynamic/Person (column "id") and dynamic/Person_knows_Person (columns
+    Person1Id, Person2Id) (:17-42,71-91,121-136), files in name order (the
+    reference takes them in directory order);
+  * vertices: the distinct raw ids of the edge list (SNAP) or of the person
+    files (LDBC, which must hold every edge endpoint and no id twice),
+    numbered in ascending raw-id order (rearrange, :262-278;
+    unify_vertex_and_collect_statistics, include/meta/graph_loader.hh:11-23);
   * communities: set_random_community (:229-260), through the host library's
     vsg_sn_communities (the standard library's mt19937 and shuffle);
   * edges: raw ids mapped to the new ids; knows is undirected, so every edge
@@ -68,6 +75,50 @@ def load_snap_csv(path) -> tuple[np.ndarray, np.ndarray]:
     return a[:, 0].copy(), a[:, 1].copy()
 
 
+def _read_psv(path) -> tuple[list, list]:
+    """(titles, rows) of a '|'-separated file with a header line."""
+    with open(path) as f:
+        titles = f.readline().rstrip("\n").split("|")
+        rows = [line.rstrip("\n").split("|") for line in f if line.strip()]
+    return titles, rows
+
+
+def _column(path, titles, rows, name) -> np.ndarray:
+    if name not in titles:
+        raise ValueError(f"{path}: no column {name}")
+    i = titles.index(name)
+    return np.asarray([int(r[i]) for r in rows], np.uint64)
+
+
+def load_ldbc_ic(root) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """(raw person ids, raw src, raw dst) of an LDBC SNB interactive dataset."""
+    dyn = Path(root) / "social_network" / "dynamic"
+    pt, pr = _read_psv(dyn / "person_0_0.csv")
+    persons = _column(dyn / "person_0_0.csv", pt, pr, "id")
+    kt, kr = _read_psv(dyn / "person_knows_person_0_0.csv")
+    if kt[:2] != ["Person.id", "Person.id"]:
+        raise ValueError(f"person_knows_person_0_0.csv: header must start with Person.id|Person.id, got {kt}")
+    k = np.asarray([[int(r[0]), int(r[1])] for r in kr], np.uint64).reshape(-1, 2)
+    return persons, k[:, 0].copy(), k[:, 1].copy()
+
+
+def load_ldbc_bi(root) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """(raw person ids, raw src, raw dst) of an LDBC SNB BI dataset (every .csv
+    of the initial snapshot's Person and Person_knows_Person folders, in name
+    order)."""
+    dyn = Path(root) / "graphs" / "csv" / "bi" / "composite-merged-fk" / "initial_snapshot" / "dynamic"
+    persons, src, dst = [], [], []
+    for path in sorted((dyn / "Person").glob("*.csv")):
+        t, r = _read_psv(path)
+        persons.append(_column(path, t, r, "id"))
+    for path in sorted((dyn / "Person_knows_Person").glob("*.csv")):
+        t, r = _read_psv(path)
+        src.append(_column(path, t, r, "Person1Id"))
+        dst.append(_column(path, t, r, "Person2Id"))
+    cat = lambda xs: np.concatenate(xs) if xs else np.zeros(0, np.uint64)
+    return cat(persons), cat(src), cat(dst)
+
+
 def communities(n: int, seed: int = COMMUNITY_SEED) -> np.ndarray:
     out = np.zeros(n, np.uint8)
     if graphgen._lib().vsg_sn_communities(n, seed, out.ctypes.data if n else None):
@@ -75,14 +126,27 @@ def communities(n: int, seed: int = COMMUNITY_SEED) -> np.ndarray:
     return out
 
 
-def rearrange(raw_src: np.ndarray, raw_dst: np.ndarray):
-    """(raw ids in vertex order, community per vertex, HostGraph of knows)."""
-    raw_ids = np.unique(np.concatenate([raw_src, raw_dst]))  # ascending: vertex i has the i-th smallest raw id
+def rearrange(raw_src: np.ndarray, raw_dst: np.ndarray, persons: np.ndarray | None = None):
+    """(raw ids in vertex order, community per vertex, HostGraph of knows);
+    the vertices are `persons` when given, else the edge endpoints."""
+    raw_src = np.asarray(raw_src, np.uint64)
+    raw_dst = np.asarray(raw_dst, np.uint64)
+    if persons is None:
+        raw_ids = np.unique(np.concatenate([raw_src, raw_dst]))  # ascending: vertex i has the i-th smallest raw id
+    else:
+        raw_ids = np.unique(np.asarray(persons, np.uint64))
+        if len(raw_ids) != len(persons):
+            raise ValueError("a person id occurs twice")
     V = len(raw_ids)
     if V >= 1 << 32:
         raise ValueError("more vertices than 32-bit ids hold")
-    s = np.searchsorted(raw_ids, raw_src).astype(np.uint32)
-    d = np.searchsorted(raw_ids, raw_dst).astype(np.uint32)
+    s = np.searchsorted(raw_ids, raw_src)
+    d = np.searchsorted(raw_ids, raw_dst)
+    if persons is not None and len(s) and (s.max() >= V or d.max() >= V or np.any(raw_ids[np.minimum(s, V - 1)] != raw_src)
+                                           or np.any(raw_ids[np.minimum(d, V - 1)] != raw_dst)):
+        raise ValueError("an edge names a person the person files do not hold")
+    s = s.astype(np.uint32)
+    d = d.astype(np.uint32)
     # undirected: the list and its reverse, neighbouring duplicates dropped, then sorted
     es = np.concatenate([s, d])
     ed = np.concatenate([d, s])
@@ -99,10 +163,12 @@ def rearrange(raw_src: np.ndarray, raw_dst: np.ndarray):
     return raw_ids, communities(V), g
 
 
-def output_vlgpm(out_dir, raw_src, raw_dst, partitions: int | None = None) -> graphgen.HostGraph:
+def output_vlgpm(out_dir, raw_src, raw_dst, partitions: int | None = None,
+                 persons: np.ndarray | None = None) -> graphgen.HostGraph:
     """Write the directory; partitions: block count of the partitioned flat
-    lists (the reference's -b), none by default."""
-    raw_ids, comm, g = rearrange(raw_src, raw_dst)
+    lists (the reference's -b), none by default; persons: the vertex raw ids
+    (LDBC inputs), else the edge endpoints."""
+    raw_ids, comm, g = rearrange(raw_src, raw_dst, persons)
     props = {"id": np.arange(g.V, dtype=np.uint32), "community": comm}
     part = {"src_dst": partitions, "hilbert": partitions} if partitions else None
     graph_dir.save(out_dir, g, properties=props, flats=("src_dst", "hilbert"), partitioned=part,
@@ -112,14 +178,19 @@ def output_vlgpm(out_dir, raw_src, raw_dst, partitions: int | None = None) -> gr
 
 def main():
     ap = argparse.ArgumentParser(description="import a social-network edge list into a graph directory")
-    ap.add_argument("-s", "--source", required=True, help="edge list file")
+    ap.add_argument("-s", "--source", required=True, help="edge list file, or the LDBC dataset directory")
     ap.add_argument("-d", "--dir", required=True, help="graph directory to write")
-    ap.add_argument("-i", "--input", choices=["snap-txt", "snap-csv"], default="snap-txt")
+    ap.add_argument("-i", "--input", choices=["snap-txt", "snap-csv", "ldbc-ic", "ldbc-bi"], default="snap-txt")
     ap.add_argument("-b", "--blocks", type=int, default=None, help="partitioned flat lists in this many blocks")
     args = ap.parse_args()
-    load = load_snap_txt if args.input == "snap-txt" else load_snap_csv
-    raw_src, raw_dst = load(args.source)
-    g = output_vlgpm(Path(args.dir), raw_src, raw_dst, args.blocks)
+    persons = None
+    if args.input == "snap-txt":
+        raw_src, raw_dst = load_snap_txt(args.source)
+    elif args.input == "snap-csv":
+        raw_src, raw_dst = load_snap_csv(args.source)
+    else:
+        persons, raw_src, raw_dst = (load_ldbc_ic if args.input == "ldbc-ic" else load_ldbc_bi)(args.source)
+    g = output_vlgpm(Path(args.dir), raw_src, raw_dst, args.blocks, persons)
     print(f"{g.V} Person, {g.E} knows (both directions) -> {args.dir}")
 
 

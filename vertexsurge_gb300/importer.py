@@ -47,59 +47,60 @@ from . import graph_dir, graphgen
 COMMUNITY_SEED = 1234
 
 
+def _pairs(a: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    a = np.asarray(a, np.uint64).reshape(-1, 2)
+    return a[:, 0].copy(), a[:, 1].copy()
+
+
 def load_snap_txt(path) -> tuple[np.ndarray, np.ndarray]:
-    """(raw src, raw dst) uint64 arrays of a SNAP edge-list text file."""
-    src, dst = [], []
-    with open(path) as f:
-        for n, line in enumerate(f, 1):
-            if not line.strip() or line.startswith("#"):
-                continue
-            parts = line.split()
-            if len(parts) < 2:
-                raise ValueError(f"{path}:{n}: expected two vertex ids")
-            src.append(int(parts[0]))
-            dst.append(int(parts[1]))
-    return np.asarray(src, np.uint64), np.asarray(dst, np.uint64)
+    """(raw src, raw dst) uint64 arrays of a SNAP edge-list text file:
+    whitespace-separated pairs, '#' lines skipped."""
+    try:
+        a = np.loadtxt(path, dtype=np.uint64, comments="#", usecols=(0, 1), ndmin=2)
+    except ValueError as e:
+        raise ValueError(f"{path}: expected two vertex ids per line ({e})") from None
+    return _pairs(a)
 
 
 def load_snap_csv(path) -> tuple[np.ndarray, np.ndarray]:
     """(raw src, raw dst) of a CSV with the header node_1,node_2."""
     with open(path) as f:
         header = f.readline().strip().split(",")
-        if header != ["node_1", "node_2"]:
-            raise ValueError(f"{path}: header must be node_1,node_2, got {header}")
-        rows = [line.strip().split(",") for line in f if line.strip()]
-    if any(len(r) != 2 for r in rows):
+    if header != ["node_1", "node_2"]:
+        raise ValueError(f"{path}: header must be node_1,node_2, got {header}")
+    try:
+        a = np.loadtxt(path, dtype=np.uint64, delimiter=",", skiprows=1, ndmin=2)
+    except ValueError as e:
+        raise ValueError(f"{path}: every row holds two vertex ids ({e})") from None
+    if a.size and a.shape[1] != 2:
         raise ValueError(f"{path}: every row holds two vertex ids")
-    a = np.asarray(rows, dtype=np.uint64).reshape(-1, 2)
-    return a[:, 0].copy(), a[:, 1].copy()
+    return _pairs(a)
 
 
-def _read_psv(path) -> tuple[list, list]:
-    """(titles, rows) of a '|'-separated file with a header line."""
+def _psv_columns(path, names) -> list:
+    """The named columns (uint64) of a '|'-separated file with a header line."""
     with open(path) as f:
         titles = f.readline().rstrip("\n").split("|")
-        rows = [line.rstrip("\n").split("|") for line in f if line.strip()]
-    return titles, rows
-
-
-def _column(path, titles, rows, name) -> np.ndarray:
-    if name not in titles:
-        raise ValueError(f"{path}: no column {name}")
-    i = titles.index(name)
-    return np.asarray([int(r[i]) for r in rows], np.uint64)
+    idx = []
+    for name in names:
+        if name not in titles:
+            raise ValueError(f"{path}: no column {name}")
+        idx.append(titles.index(name))
+    a = np.loadtxt(path, dtype=np.uint64, delimiter="|", skiprows=1, usecols=idx, ndmin=2)
+    return [a[:, k].copy() for k in range(len(idx))]
 
 
 def load_ldbc_ic(root) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     """(raw person ids, raw src, raw dst) of an LDBC SNB interactive dataset."""
     dyn = Path(root) / "social_network" / "dynamic"
-    pt, pr = _read_psv(dyn / "person_0_0.csv")
-    persons = _column(dyn / "person_0_0.csv", pt, pr, "id")
-    kt, kr = _read_psv(dyn / "person_knows_person_0_0.csv")
+    (persons,) = _psv_columns(dyn / "person_0_0.csv", ["id"])
+    kp = dyn / "person_knows_person_0_0.csv"
+    with open(kp) as f:
+        kt = f.readline().rstrip("\n").split("|")
     if kt[:2] != ["Person.id", "Person.id"]:
-        raise ValueError(f"person_knows_person_0_0.csv: header must start with Person.id|Person.id, got {kt}")
-    k = np.asarray([[int(r[0]), int(r[1])] for r in kr], np.uint64).reshape(-1, 2)
-    return persons, k[:, 0].copy(), k[:, 1].copy()
+        raise ValueError(f"{kp}: header must start with Person.id|Person.id, got {kt}")
+    a = np.loadtxt(kp, dtype=np.uint64, delimiter="|", skiprows=1, usecols=(0, 1), ndmin=2)
+    return (persons, *_pairs(a))
 
 
 def load_ldbc_bi(root) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
@@ -107,16 +108,10 @@ def load_ldbc_bi(root) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     of the initial snapshot's Person and Person_knows_Person folders, in name
     order)."""
     dyn = Path(root) / "graphs" / "csv" / "bi" / "composite-merged-fk" / "initial_snapshot" / "dynamic"
-    persons, src, dst = [], [], []
-    for path in sorted((dyn / "Person").glob("*.csv")):
-        t, r = _read_psv(path)
-        persons.append(_column(path, t, r, "id"))
-    for path in sorted((dyn / "Person_knows_Person").glob("*.csv")):
-        t, r = _read_psv(path)
-        src.append(_column(path, t, r, "Person1Id"))
-        dst.append(_column(path, t, r, "Person2Id"))
+    persons = [_psv_columns(p, ["id"])[0] for p in sorted((dyn / "Person").glob("*.csv"))]
+    knows = [_psv_columns(p, ["Person1Id", "Person2Id"]) for p in sorted((dyn / "Person_knows_Person").glob("*.csv"))]
     cat = lambda xs: np.concatenate(xs) if xs else np.zeros(0, np.uint64)
-    return cat(persons), cat(src), cat(dst)
+    return cat(persons), cat([k[0] for k in knows]), cat([k[1] for k in knows])
 
 
 def communities(n: int, seed: int = COMMUNITY_SEED) -> np.ndarray:
@@ -126,15 +121,27 @@ def communities(n: int, seed: int = COMMUNITY_SEED) -> np.ndarray:
     return out
 
 
+def _sorted_unique(x: np.ndarray) -> np.ndarray:
+    """Distinct values ascending (a sort and a neighbour mask: several times
+    faster than np.unique on large uint64 arrays)."""
+    y = np.sort(x)
+    if len(y) < 2:
+        return y
+    keep = np.empty(len(y), bool)
+    keep[0] = True
+    keep[1:] = y[1:] != y[:-1]
+    return y[keep]
+
+
 def rearrange(raw_src: np.ndarray, raw_dst: np.ndarray, persons: np.ndarray | None = None):
     """(raw ids in vertex order, community per vertex, HostGraph of knows);
     the vertices are `persons` when given, else the edge endpoints."""
     raw_src = np.asarray(raw_src, np.uint64)
     raw_dst = np.asarray(raw_dst, np.uint64)
     if persons is None:
-        raw_ids = np.unique(np.concatenate([raw_src, raw_dst]))  # ascending: vertex i has the i-th smallest raw id
+        raw_ids = _sorted_unique(np.concatenate([raw_src, raw_dst]))  # vertex i has the i-th smallest raw id
     else:
-        raw_ids = np.unique(np.asarray(persons, np.uint64))
+        raw_ids = _sorted_unique(np.asarray(persons, np.uint64))
         if len(raw_ids) != len(persons):
             raise ValueError("a person id occurs twice")
     V = len(raw_ids)
@@ -153,12 +160,12 @@ def rearrange(raw_src: np.ndarray, raw_dst: np.ndarray, persons: np.ndarray | No
     keep = np.ones(len(es), bool)
     if len(es) > 1:
         keep[1:] = (es[1:] != es[:-1]) | (ed[1:] != ed[:-1])
-    es, ed = es[keep], ed[keep]
-    order = np.lexsort((ed, es))
-    es, ed = es[order], ed[order]
+    # sorted by (src, dst): one sort of the pairs packed as src << 32 | dst
+    key = np.sort((es[keep].astype(np.uint64) << np.uint64(32)) | ed[keep].astype(np.uint64))
+    es = (key >> np.uint64(32)).astype(np.uint32)
+    ed = (key & np.uint64(0xFFFFFFFF)).astype(np.uint32)
     off = np.zeros(V + 1, np.int64)
-    np.add.at(off, es.astype(np.int64) + 1, 1)
-    off = np.cumsum(off)
+    off[1:] = np.cumsum(np.bincount(es, minlength=V))
     g = graphgen.HostGraph(V, len(ed), off, ed, off, ed, directed=False)
     return raw_ids, communities(V), g
 

@@ -66,6 +66,30 @@ def test_partition_by_dst_blocks():
     assert graph_dir.partition_by_dst(np.array([7, 7, 7], np.uint32), 2) == [(0, 3), (3, 3)]
 
 
+def test_partition_by_dst_matches_the_edge_walk():
+    """The block search (first target change at or after the expected end)
+    equals walking the edges one by one as graph_loader.hh:112-138 does."""
+    def walk(d, count):
+        n, pos, out = len(d), 0, []
+        for i in range(count):
+            if pos >= n:
+                out.append((n, n))
+                continue
+            expected = pos + (n - pos) // (count - i)
+            end = pos + 1
+            while end < n and not (end >= expected and d[end] != d[end - 1]):
+                end += 1
+            out.append((pos, end))
+            pos = end
+        return out
+    rng = np.random.default_rng(3)
+    for _ in range(500):
+        n = int(rng.integers(0, 300))
+        d = np.sort(rng.integers(0, int(rng.integers(1, 60)), n)).astype(np.uint32)
+        c = int(rng.integers(1, 12))
+        assert graph_dir.partition_by_dst(d, c) == walk(d, c)
+
+
 @pytest.mark.parametrize("name", ["rmat10", "rmat9_undirected"])
 def test_flat_edge_lists(tmp_path, name):
     """Every flat list holds the edge set (backward lists as (dst, src)), in

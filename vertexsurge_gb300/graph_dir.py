@@ -133,12 +133,19 @@ def _pow2_at_least(x: int) -> int:
     return p
 
 
+def _pair_order(major: np.ndarray, minor: np.ndarray) -> np.ndarray:
+    """Permutation sorting uint32 pairs by (major, minor): one stable argsort of
+    the pairs packed into uint64 keys (several times faster than lexsort)."""
+    key = (np.asarray(major, np.uint64) << np.uint64(32)) | np.asarray(minor, np.uint64)
+    return np.argsort(key, kind="stable")
+
+
 def order_edges(src: np.ndarray, dst: np.ndarray, order: str, n_src: int, n_dst: int, seed: int = 0) -> np.ndarray:
     """Permutation putting the edges (src, dst) in a flat order."""
     if order == "src_dst":
-        return np.lexsort((dst, src))
+        return _pair_order(src, dst)
     if order == "dst_src":
-        return np.lexsort((src, dst))
+        return _pair_order(dst, src)
     if order == "hilbert":
         return np.argsort(curve_index(_pow2_at_least(max(n_src, n_dst)), src, dst), kind="stable")
     return np.random.default_rng(seed).permutation(len(src))
@@ -149,14 +156,16 @@ def partition_by_dst(dst_sorted: np.ndarray, count: int) -> list:
     first target change at or after pos + (n - pos) / (count - i)
     (graph_loader.hh:112-138); blocks after the last edge are empty."""
     n, pos, out = len(dst_sorted), 0, []
+    d = np.asarray(dst_sorted)
+    changes = np.flatnonzero(d[1:] != d[:-1]) + 1 if n > 1 else np.zeros(0, np.int64)  # i: d[i] != d[i-1]
     for i in range(count):
         if pos >= n:
             out.append((n, n))
             continue
         expected = pos + (n - pos) // (count - i)
-        end = pos + 1
-        while end < n and not (end >= expected and dst_sorted[end] != dst_sorted[end - 1]):
-            end += 1
+        # the first target change at or after max(pos + 1, expected), else the end
+        k = int(np.searchsorted(changes, max(pos + 1, expected)))
+        end = int(changes[k]) if k < len(changes) else n
         out.append((pos, end))
         pos = end
     return out
@@ -182,7 +191,7 @@ def write_flat_edges(dir_, g: HostGraph, src_type: str, etype: str, dst_type: st
             write_disk_array(d / flat_edges_name(src_type, etype, dst_type, g.directed, direction, order),
                              pairs(src[perm], dst[perm], direction))
         for order, count in (partitioned or {}).items():
-            by_dst = np.lexsort((src, dst))
+            by_dst = _pair_order(dst, src)
             s_, t_ = src[by_dst], dst[by_dst]
             for i, (b, e) in enumerate(partition_by_dst(t_, count)):
                 perm = order_edges(s_[b:e], t_[b:e], order, g.V, g.V)
@@ -206,7 +215,7 @@ def read_flat_edges(dir_, src_type: str, etype: str, dst_type: str, directed: bo
 
 def csr_from_pairs(V: int, src: np.ndarray, dst: np.ndarray):
     """(offsets, targets) of the lists of src -> dst, targets sorted per list."""
-    order = np.lexsort((dst, src))
+    order = _pair_order(src, dst)
     off = np.zeros(V + 1, np.int64)
     np.cumsum(np.bincount(src, minlength=V), out=off[1:])
     return off, np.ascontiguousarray(dst[order], np.uint32)

@@ -663,7 +663,8 @@ def run_serving(args, w, rank, world, local_rank):
             "e2e": {"value": rep["queries_per_s"], "unit": "queries/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": 3 * 8 * len(trace)},
             "gpu_launches": launches, "clocks": clk}
-    print(json.dumps(line), flush=True)
+    if rank == 0:  # every rank serves its own replica of the trace; rank 0 reports
+        print(json.dumps(line), flush=True)
 
 
 def run_reference(args, w, rank, world):

@@ -635,7 +635,7 @@ def run_serving(args, w, rank, world, local_rank):
     same_picker = all(res == results["plain"] for res in results.values())
     assert same_mix and same_picker, "served answers differ alone / in the mix / under the picker"
     parity = None
-    if not args.no_cpu:
+    if rank == 0 and not args.no_cpu:
         idx, want, dt = serving_oracle(g, trace, w["oracle_queries"])
         got = [results["plain"][i] for i in idx]
         parity = {"queries": len(idx), "equal": got == want,

@@ -2191,9 +2191,12 @@ int vs_expand_plan_run(vs_expand_plan *pl, const uint32_t *sources, const uint32
   };
   // a Shortest SPARSE hop leaves its layer's rows in its pair list when a
   // later hop may build them (not the last hop, not an exported layer, not
-  // FindShortest, whose target check reads every layer's rows)
+  // FindShortest, whose target check reads every layer's rows) and the plan
+  // has a short-row index (without one every PULL hop reads whole rows, so
+  // building them later only adds a pass)
   auto defer_rows = [&](uint32_t hh) {
-    return pl->use_vis && hh >= 1 && hh < p.k_max && p.path_type != VS_PATH_FIND_SHORTEST && !pl->layer_out[hh];
+    return pl->use_vis && pl->slot[0] != nullptr && hh >= 1 && hh < p.k_max &&
+           p.path_type != VS_PATH_FIND_SHORTEST && !pl->layer_out[hh];
   };
   // PUSH runs only when forced (for the run or a hop) or enabled in the
   // fixed planner (push_frac > 0)

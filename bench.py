@@ -187,22 +187,40 @@ def batched_config(args, g, queries, world):
             "parallelism": f"replicas{world}"}
 
 
+# Block count of the reference's BlockHilbert edge layout in the CPU legs (its
+# importer's -b option): 16 blocks per Grace core, which the guided schedule
+# balances; 256 blocks ran 1.07x faster than 64 on the 10M-vertex graph.
+CPU_BLOCKS = 256
+
+
+def cpu_blocks(g):
+    """The forward direction's BlockHilbert layout (the reference importer's
+    partitioned hilbert lists), built once per graph outside any timed region,
+    as the reference reads it from its graph directory."""
+    from oracle import pyoracle as O
+    return O.FlatBlocks(g, "forward", CPU_BLOCKS)
+
+
 def cpu_baseline(g, w, sa):
     """Oracle VExpand on the host cores: the bounded sample and its throughput,
-    and the sample's matrix (logical words, V x S/64) for the parity check."""
+    and the sample's matrix (logical words, V x S/64) for the parity check.
+    The matrix comes from the CSR pull, the timed run from the reference's
+    BlockHilbert hop; both give the same layers (tests/test_oracle_expand.py)."""
     from oracle import pyoracle as O
     S = w["cpu_S"]
     src = sa[:S]
     k0, k1 = w["hops_a"]
     words, _, st = O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=True, hop_stats=True)
     src_edges = S * sum(st["active_edges"][1:])
+    blk = cpu_blocks(g)
     t = time.perf_counter()
-    O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False)
+    O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False, blocks=blk)
     dt = time.perf_counter() - t
     return {"value": src_edges / dt / 1e9, "unit": "Gsrc-edges/s", "cores": O.lib().oracle_get_threads(),
             "kind": "port",
             "sample": f"VExpand(Shortest, [{k0},{k1}], Forward) from the first {S} A sources on the full "
-                      f"graph, one run of {dt:.1f} s ({src_edges / 1e9:.2f} Gsrc-edges)"}, words
+                      f"graph, the reference's BlockHilbert hop over {CPU_BLOCKS} target blocks, one run of "
+                      f"{dt:.1f} s ({src_edges / 1e9:.2f} Gsrc-edges)"}, words
 
 
 def batched_queries(g, w):
@@ -211,16 +229,17 @@ def batched_queries(g, w):
     return batch.make_queries(g, bw["n"], bw["s_range"], bw["l_range"], bw["join_rows"], seed=4)
 
 
-def cpu_batched(g, w, queries):
-    """Oracle VExpand + TableConvert + HashJoin (count) per query, one query at
-    a time as the reference runs them, on a bounded sample: the first queries
-    of the trace with at most 2,048 sources."""
+def cpu_batched(g, w, queries, blk):
+    """Oracle VExpand (the BlockHilbert hop over `blk`) + TableConvert +
+    HashJoin (count) per query, one query at a time as the reference runs
+    them, on a bounded sample: the first queries of the trace with at most
+    2,048 sources."""
     from oracle import pyoracle as O
     idx = [i for i, q in enumerate(queries) if len(q.sources) <= 2048][: w["batched"]["cpu_queries"]]
     t = time.perf_counter()
     counts = []
     for q in (queries[i] for i in idx):
-        words, _, _ = O.vexpand(g, q.sources, 1, q.k_max, "shortest", "forward")
+        words, _, _ = O.vexpand(g, q.sources, 1, q.k_max, "shortest", "forward", blocks=blk)
         # the reference's HashJoin takes ColMain matrices: TableConvert first
         cm = O.table_convert(words, len(q.sources), g.V, False)
         a = O.Table(O.COLMAIN, [0, 1], words=cm, mrows=len(q.sources), mcols=g.V, row_map=q.sources)
@@ -237,9 +256,10 @@ def run_reference_batched(args, w):
     g = make_graph(w)
     queries = batched_queries(g, w)
     log(f"graph {g.V} vertices {g.E} edges, {len(queries)} queries in {time.time() - t0:.1f}s")
+    blk = cpu_blocks(g)
     times, n = [], 0
     for i in range(args.steps + min(args.warmup, 1)):
-        sample, _, dt = cpu_batched(g, w, queries)
+        sample, _, dt = cpu_batched(g, w, queries, blk)
         if i >= min(args.warmup, 1):
             times.append(dt)
             n += len(sample)
@@ -415,7 +435,7 @@ def run_gpu_batched(args, w, rank, world, local_rank):
     cpu = None
     parity = None
     if world == 1 and not args.no_cpu:
-        sample, ccounts, dt = cpu_batched(g, w, queries)
+        sample, ccounts, dt = cpu_batched(g, w, queries, cpu_blocks(g))
         assert [int(counts[i]) for i in sample] == ccounts, "oracle counts differ from the batch"
         parity = {"queries": len(sample), "equal": True,
                   "against": "oracle VExpand(Shortest, [1,l]) + TableConvert + HashJoin count per query "
@@ -684,20 +704,22 @@ def run_reference(args, w, rank, world):
     S = w["cpu_S"]
     src = sa[:S]
     k0, k1 = w["hops_a"]
-    _, _, st = O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False, hop_stats=True)
+    blk = cpu_blocks(g)
+    _, _, st = O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False, hop_stats=True, blocks=blk)
     src_edges = S * sum(st["active_edges"][1:])
     for _ in range(min(args.warmup, 1)):
-        O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False)
+        O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False, blocks=blk)
     times = []
     for _ in range(args.steps):
         t = time.perf_counter()
-        O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False)
+        O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False, blocks=blk)
         times.append(time.perf_counter() - t)
     total = sum(times)
     value = src_edges * args.steps / total / 1e9
     cores = O.lib().oracle_get_threads()
     sample = (f"VExpand(Shortest, [{k0},{k1}], Forward) from {S} of the A sources on the full graph "
-              f"per step ({src_edges / 1e9:.2f} Gsrc-edges)")
+              f"per step ({src_edges / 1e9:.2f} Gsrc-edges), the reference's BlockHilbert hop over "
+              f"{CPU_BLOCKS} target blocks")
     line = {"impl": "reference", "metric": "multi-source expand Gsrc-edges/s", "value": value,
             "unit": "Gsrc-edges/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": min(args.warmup, 1),
             "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",

@@ -182,9 +182,10 @@ InLists in_lists(const int64_t *fwd_off, const uint32_t *fwd_dst, const int64_t 
   return L;
 }
 
-// One dense hop, Expand<DenseVarStackMatrix>::expand_dense (expand.cpp:210-344):
-// edges are owned by their target column (the BlockHilbert dst partitions);
-// within a partition every stack is processed in turn.
+// One dense hop over the CSR in-lists: edges are owned by their target
+// column, and every stack of a target is finished before the next target.
+// Same OR set as the reference's dense hop (expand.cpp:210-344); the
+// reference's own loop order is expand_blocks below.
 void expand_dense(const InLists &L, uint32_t V, const StackMatrix &base, StackMatrix &out) {
 #pragma omp parallel for num_threads(nthreads()) schedule(dynamic, 256)
   for (size_t v = 0; v < V; v++) {
@@ -214,34 +215,170 @@ uint64_t active_edges(const InLists &L, uint32_t V, const StackMatrix &base) {
   return n;
 }
 
-}  // namespace
+// ---------------------------------------------------------------------------
+// The reference's BlockHilbert edge layout and hop.
+//
+// Layout (graph_loader.hh:239-276): the (u, v) pairs of the expand direction
+// (VIDPair: base column u is OR-ed into column v), sorted by target, cut into
+// blocks by partition_by_dst (graph_loader.hh:110-138: block i ends at the
+// first target change at or after pos + (n - pos) / (count - i)), and each
+// block sorted by the curve index XYToIndex(n, src, dst, RA) of the edge's
+// (source, target) with n the power of two at least V (sort_edge_in_peano2,
+// graph_concepts.hh:164-174; curve utils/peano.hh:20-89).  Blocks are cut on
+// the written column v, so no two blocks write the same column.
+struct VPair {
+  uint32_t u, v;
+};
 
-extern "C" {
+struct FlatBlocks {
+  uint32_t V = 0;
+  std::vector<VPair> pairs;
+  std::vector<uint64_t> off;  // block b holds pairs [off[b], off[b + 1])
+  size_t count() const { return off.empty() ? 0 : off.size() - 1; }
+};
 
-void oracle_set_threads(int n) { g_threads = n; }
-int oracle_get_threads(void) { return nthreads(); }
+// XYToIndex(n, x, y, RA), utils/peano.hh:72-89, one level per iteration.
+// States RA, RD, CA, CD; kPos[state][quadrant] is the quadrant's place in
+// the state's visiting order (order(), peano.hh:27-39), kSub[state][place]
+// the state of that sub-square (subPeanoDirection(), peano.hh:41-53).
+inline uint64_t curve_index(uint64_t n, uint64_t x, uint64_t y) {
+  static const uint8_t kPos[4][4] = {{0, 1, 3, 2}, {2, 3, 1, 0}, {0, 3, 1, 2}, {2, 1, 3, 0}};
+  static const uint8_t kSub[4][4] = {{2, 0, 0, 3}, {3, 1, 1, 2}, {0, 2, 2, 1}, {1, 3, 3, 0}};
+  uint64_t idx = 0;
+  int st = 0;
+  for (uint64_t half = n / 2; half >= 1; half /= 2) {
+    const int q = (x >= half ? 2 : 0) + (y >= half ? 1 : 0);
+    const int p = kPos[st][q];
+    idx = idx * 4 + (uint64_t)p;
+    st = kSub[st][p];
+    if (x >= half) x -= half;
+    if (y >= half) y -= half;
+  }
+  return idx;
+}
 
-// VExpand with ExpandStrategy::Dense over DenseVarStackMatrix:
+FlatBlocks *make_flat_blocks(const InLists &L, uint32_t V, bool fwd_first, uint32_t n_blocks) {
+  auto *B = new FlatBlocks;
+  B->V = V;
+  // pairs grouped by target v in ascending order: the in-lists in CSR order
+  std::vector<uint64_t> start(V + 1, 0);
+  for (size_t v = 0; v < V; v++) {
+    uint64_t d = 0;
+    for (int l = 0; l < L.n; l++) d += (uint64_t)(L.off[l][v + 1] - L.off[l][v]);
+    start[v + 1] = start[v] + d;
+  }
+  const uint64_t n = start[V];
+  B->pairs.resize(n);
+#pragma omp parallel for num_threads(nthreads()) schedule(dynamic, 1024)
+  for (size_t v = 0; v < V; v++) {
+    uint64_t k = start[v];
+    for (int l = 0; l < L.n; l++)
+      for (int64_t j = L.off[l][v]; j < L.off[l][v + 1]; j++) B->pairs[k++] = VPair{L.adj[l][j], (uint32_t)v};
+  }
+  // partition_by_dst over the target-grouped pairs
+  const uint32_t cnt = n_blocks ? n_blocks : 1;
+  B->off.assign(cnt + 1, n);
+  B->off[0] = 0;
+  uint64_t pos = 0;
+  for (uint32_t i = 0; i < cnt; i++) {
+    B->off[i] = pos;
+    if (pos >= n) continue;
+    const uint64_t expected = pos + (n - pos) / (cnt - i);
+    uint64_t e = pos + 1;
+    while (e < n && !(e >= expected && B->pairs[e].v != B->pairs[e - 1].v)) e++;
+    pos = e;
+  }
+  B->off[cnt] = n;
+  // curve order inside every block, over the edge's (source, target): the
+  // pair (u, v) of a forward list is the edge (u, v), of a backward list the
+  // edge (v, u)
+  uint64_t side = 1;
+  while (side < V) side <<= 1;
+#pragma omp parallel for num_threads(nthreads()) schedule(dynamic, 1)
+  for (size_t b = 0; b < cnt; b++) {
+    const uint64_t lo = B->off[b], hi = B->off[b + 1];
+    std::vector<std::pair<uint64_t, VPair>> kp(hi - lo);
+    for (uint64_t i = lo; i < hi; i++) {
+      const VPair e = B->pairs[i];
+      const uint64_t key = fwd_first ? curve_index(side, e.u, e.v) : curve_index(side, e.v, e.u);
+      kp[i - lo] = {key, e};
+    }
+    std::sort(kp.begin(), kp.end(), [](const auto &a, const auto &c) { return a.first < c.first; });
+    for (uint64_t i = lo; i < hi; i++) B->pairs[i] = kp[i - lo].second;
+  }
+  return B;
+}
+
+// DenseVarStackMatrix::prefetch_cols (bitmap.cpp:1173-1185): every 64-byte
+// line of the written and the read column of each pair.
+inline void prefetch_cols(size_t si, const StackMatrix &out, const StackMatrix &base, const VPair *e,
+                          size_t m) {
+  const size_t r = si * out.R;
+  const size_t lines = (out.v_per_stack_col + 7) / 8;
+  for (size_t i = 0; i < m; i++) {
+    const uint64_t *p = &out.bits[out.vidx(r, e[i].v)];
+    const uint64_t *q = &base.bits[base.vidx(r, e[i].u)];
+    for (size_t k = 0; k < lines; k++) {
+      __builtin_prefetch(p + 8 * k, 1);
+      __builtin_prefetch(q + 8 * k, 0);
+    }
+  }
+}
+
+// The BlockHilbert hop (expand.cpp:263-311 with WITH_PREFETCH and
+// BLOCK_PREFETCH, common.hh:52-63): blocks in parallel (guided); inside a
+// block every stack in turn; the pairs in runs of BLOCK_PREFETCH_COUNT = 20,
+// the run's columns prefetched, then OR-ed (prefetch_or_stack_cols_from,
+// bitmap.cpp:1187-1194).
+constexpr size_t kBlockPrefetchCount = 20;
+
+void expand_blocks(const FlatBlocks &B, const StackMatrix &base, StackMatrix &out) {
+#pragma omp parallel for num_threads(nthreads()) schedule(guided)
+  for (size_t b = 0; b < B.count(); b++) {
+    const VPair *e = B.pairs.data() + B.off[b];
+    const size_t n = B.off[b + 1] - B.off[b];
+    for (size_t si = 0; si < base.stack_count; si++) {
+      for (size_t i = 0; i < n; i += kBlockPrefetchCount) {
+        const size_t m = std::min(n - i, kBlockPrefetchCount);
+        prefetch_cols(si, out, base, e + i, m);
+        for (size_t j = 0; j < m; j++) out.or_stack_col_from(si, e[i + j].v, base, e[i + j].u);
+      }
+    }
+  }
+}
+
+uint64_t active_pairs(const FlatBlocks &B, const StackMatrix &base) {
+  uint64_t n = 0;
+  const size_t np = B.pairs.size();
+#pragma omp parallel for reduction(+ : n) num_threads(nthreads()) schedule(static)
+  for (size_t i = 0; i < np; i++) {
+    bool nz = false;
+    for (size_t si = 0; si < base.stack_count && !nz; si++) nz = base.col_nonzero(si, B.pairs[i].u);
+    n += nz;
+  }
+  return n;
+}
+
+// VExpand with ExpandStrategy::Dense over DenseVarStackMatrix, for either hop
+// form (hop(base, out) ORs every edge; active(base) counts the edges whose
+// base column is non-zero):
 //   ExpandStatus init        expand_impl.hh:135-169 (stack size), :252-277 (layer 0 + visit)
 //   hop loop                  PhysicalOperator::run (physical_operator.cpp:62-101) with
 //                             VExpand::after_child (vexpand.cpp:222-284)
 //   one hop + dedup           expand.cpp:263-344
 //   result                    VExpand::merge_to_MT (vexpand.cpp:298-354)
-int oracle_vexpand(uint32_t V, const int64_t *fwd_off, const uint32_t *fwd_dst,
-                   const int64_t *rev_off, const uint32_t *rev_src, int directed,
-                   const uint32_t *sources, uint32_t S, uint32_t k_min, uint32_t k_max,
-                   int path_type, int dir, uint32_t stack_row_count, const uint32_t *targets,
-                   int32_t *dist, uint64_t *out_words, uint64_t *hop_stats) {
+template <class Hop, class Active>
+int vexpand_run(uint32_t V, Hop hop, Active active, const uint32_t *sources, uint32_t S, uint32_t k_min,
+                uint32_t k_max, int path_type, uint32_t stack_row_count, const uint32_t *targets,
+                int32_t *dist, uint64_t *out_words, uint64_t *hop_stats) {
   if (V == 0 || (S > 0 && !sources) || k_min > k_max || k_max > 64) return 1;
-  if (path_type < OR_ANY || path_type > OR_FIND_SHORTEST || dir < 0 || dir > 2) return 1;
+  if (path_type < OR_ANY || path_type > OR_FIND_SHORTEST) return 1;
   if (path_type == OR_FIND_SHORTEST && (!targets || !dist)) return 1;
   for (uint32_t i = 0; i < S; i++)
     if (sources[i] >= V || (targets && targets[i] >= V)) return 1;
   const size_t R = stack_row_count ? stack_row_count : 1024;  // decide_k0, expand.cpp:416-417
   if (R % 512 != 0) return 1;
-  const size_t W = (S + 63) / 64;
   if (S == 0) return 0;  // VExpand::before_execution returns false: empty result
-  InLists L = in_lists(fwd_off, fwd_dst, rev_off, rev_src, directed, dir);
   const bool dedup = path_type != OR_ANY;
 
   std::vector<std::unique_ptr<StackMatrix>> layers;
@@ -273,8 +410,8 @@ int oracle_vexpand(uint32_t V, const int64_t *fwd_off, const uint32_t *fwd_dst,
   for (size_t i = 0; i < k_max; i++) {
     StackMatrix &base = layer(i);
     StackMatrix &out = layer(i + 1);
-    if (hop_stats) hop_stats[2 * 64 + i + 1] = active_edges(L, V, base);
-    expand_dense(L, V, base, out);
+    if (hop_stats) hop_stats[2 * 64 + i + 1] = active(base);
+    hop(base, out);
     if (dedup) visit_count = StackMatrix::dedup_and_update_visit_and_count(*visit, out);
     if (hop_stats) {
       hop_stats[0 * 64 + i + 1] = visit_count;
@@ -311,8 +448,63 @@ int oracle_vexpand(uint32_t V, const int64_t *fwd_off, const uint32_t *fwd_dst,
   StackMatrix merged(S, V, R);
   for (size_t i = k_min; i <= k_actual_max; i++) merged.or_from(layer(i));
   merged.to_logical(out_words);
-  (void)W;
   return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void oracle_set_threads(int n) { g_threads = n; }
+int oracle_get_threads(void) { return nthreads(); }
+
+int oracle_vexpand(uint32_t V, const int64_t *fwd_off, const uint32_t *fwd_dst,
+                   const int64_t *rev_off, const uint32_t *rev_src, int directed,
+                   const uint32_t *sources, uint32_t S, uint32_t k_min, uint32_t k_max,
+                   int path_type, int dir, uint32_t stack_row_count, const uint32_t *targets,
+                   int32_t *dist, uint64_t *out_words, uint64_t *hop_stats) {
+  if (dir < 0 || dir > 2) return 1;
+  InLists L = in_lists(fwd_off, fwd_dst, rev_off, rev_src, directed, dir);
+  return vexpand_run(
+      V, [&](const StackMatrix &base, StackMatrix &out) { expand_dense(L, V, base, out); },
+      [&](const StackMatrix &base) { return active_edges(L, V, base); }, sources, S, k_min, k_max,
+      path_type, stack_row_count, targets, dist, out_words, hop_stats);
+}
+
+void *oracle_flat_blocks(uint32_t V, const int64_t *fwd_off, const uint32_t *fwd_dst,
+                         const int64_t *rev_off, const uint32_t *rev_src, int directed, int dir,
+                         uint32_t n_blocks) {
+  if (V == 0 || dir < 0 || dir > 2 || n_blocks == 0) return nullptr;
+  InLists L = in_lists(fwd_off, fwd_dst, rev_off, rev_src, directed, dir);
+  // a forward (or undirected) list holds the edges u -> v; a backward one v -> u
+  const bool fwd_first = !directed || dir != OR_BACKWARD;
+  return make_flat_blocks(L, V, fwd_first, n_blocks);
+}
+
+void oracle_flat_blocks_free(void *h) { delete static_cast<FlatBlocks *>(h); }
+
+uint64_t oracle_flat_blocks_export(const void *h, uint64_t *off, uint32_t *pairs) {
+  const auto *B = static_cast<const FlatBlocks *>(h);
+  if (off)
+    for (size_t b = 0; b <= B->count(); b++) off[b] = B->off[b];
+  if (pairs)
+    for (size_t i = 0; i < B->pairs.size(); i++) {
+      pairs[2 * i] = B->pairs[i].u;
+      pairs[2 * i + 1] = B->pairs[i].v;
+    }
+  return B->pairs.size();
+}
+
+int oracle_vexpand_blocks(const void *h, const uint32_t *sources, uint32_t S, uint32_t k_min,
+                          uint32_t k_max, int path_type, uint32_t stack_row_count,
+                          const uint32_t *targets, int32_t *dist, uint64_t *out_words,
+                          uint64_t *hop_stats) {
+  if (!h) return 1;
+  const auto &B = *static_cast<const FlatBlocks *>(h);
+  return vexpand_run(
+      B.V, [&](const StackMatrix &base, StackMatrix &out) { expand_blocks(B, base, out); },
+      [&](const StackMatrix &base) { return active_pairs(B, base); }, sources, S, k_min, k_max,
+      path_type, stack_row_count, targets, dist, out_words, hop_stats);
 }
 
 uint64_t oracle_matrix_count(uint32_t rows, uint32_t cols, const uint64_t *words,

@@ -10,7 +10,8 @@
  * It follows the reference's scalar (use_simd == false) branches:
  *   bit matrices  src/objects/storage/bitmap.cpp (DenseVarStackMatrix,
  *                 DenseColMainMatrix), layout src/include/storage/bitmap.hh:329-425
- *   expand        src/objects/operator/expand.cpp:210-344,
+ *   expand        src/objects/operator/expand.cpp:210-344 (the BlockHilbert
+ *                 hop and its edge layout, and a CSR pull with the same result),
  *                 src/include/operator/expand_impl.hh:135-277,
  *                 src/objects/operator/vexpand.cpp:166-354
  *   select/count/convert  src/objects/operator/big_operators2.cpp:6-86,152-213
@@ -56,6 +57,28 @@ int oracle_vexpand(uint32_t V, const int64_t *fwd_off, const uint32_t *fwd_dst,
                    int path_type, int dir, uint32_t stack_row_count,
                    const uint32_t *targets, int32_t *dist, uint64_t *out_words,
                    uint64_t *hop_stats);
+
+/* The reference's default dense hop, ExpandDenseStrategy::BlockHilbert
+ * (big_operators.hh:44-46, expand.cpp:263-311), over its edge layout
+ * (graph_loader.hh:239-276): the (u, v) pairs of the direction (base column u
+ * OR-ed into column v) cut into n_blocks blocks by target with the
+ * reference's partition rule, each block in the order of the curve index
+ * (graph_concepts.hh:164-174); blocks run in parallel, and each pair's columns
+ * are prefetched in runs of 20 pairs.  oracle_flat_blocks returns a handle
+ * (NULL on bad arguments) for oracle_vexpand_blocks, which takes the
+ * remaining arguments of oracle_vexpand and gives the same results.
+ * oracle_flat_blocks_export copies out the n_blocks + 1 block offsets and the
+ * pairs (u, v interleaved) when the pointers are not NULL, and returns the
+ * pair count. */
+void *oracle_flat_blocks(uint32_t V, const int64_t *fwd_off, const uint32_t *fwd_dst,
+                         const int64_t *rev_off, const uint32_t *rev_src, int directed, int dir,
+                         uint32_t n_blocks);
+void oracle_flat_blocks_free(void *blocks);
+uint64_t oracle_flat_blocks_export(const void *blocks, uint64_t *off, uint32_t *pairs);
+int oracle_vexpand_blocks(const void *blocks, const uint32_t *sources, uint32_t S, uint32_t k_min,
+                          uint32_t k_max, int path_type, uint32_t stack_row_count,
+                          const uint32_t *targets, int32_t *dist, uint64_t *out_words,
+                          uint64_t *hop_stats);
 
 /* A table crossing the oracle interface. */
 typedef struct or_table {

@@ -43,6 +43,14 @@ def lib():
         L.oracle_vexpand.argtypes = [C.c_uint32] + [C.c_void_p] * 4 + [C.c_int, C.c_void_p, C.c_uint32,
                                      C.c_uint32, C.c_uint32, C.c_int, C.c_int, C.c_uint32, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_flat_blocks.argtypes = [C.c_uint32] + [C.c_void_p] * 4 + [C.c_int, C.c_int, C.c_uint32]
+        L.oracle_flat_blocks.restype = C.c_void_p
+        L.oracle_flat_blocks_free.argtypes = [C.c_void_p]
+        L.oracle_flat_blocks_export.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_flat_blocks_export.restype = C.c_uint64
+        L.oracle_vexpand_blocks.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
+                                            C.c_int, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                            C.c_void_p]
         L.oracle_hash_join.argtypes = [C.POINTER(OrTable), C.POINTER(OrTable), C.c_int32, C.c_int,
                                        C.POINTER(OrResult)]
         L.oracle_mintersect.argtypes = [C.POINTER(OrTable), C.POINTER(OrTable), C.c_uint32, C.c_int32,
@@ -85,10 +93,39 @@ def set_threads(n: int) -> None:
     lib().oracle_set_threads(int(n))
 
 
+class FlatBlocks:
+    """The reference's BlockHilbert edge layout of one expand direction:
+    n_blocks target-disjoint blocks of (u, v) pairs, each in curve order."""
+
+    def __init__(self, g, direction="forward", n_blocks=64):
+        self.V = g.V
+        self.direction = direction
+        self.n_blocks = int(n_blocks)
+        self._h = lib().oracle_flat_blocks(g.V, _p(g.fwd_off), _p(g.fwd_dst), _p(g.rev_off), _p(g.rev_src),
+                                           1 if g.directed else 0, _DIRS[direction], self.n_blocks)
+        if not self._h:
+            raise ValueError("oracle_flat_blocks rejected its arguments")
+
+    def export(self):
+        """(block offsets (n_blocks + 1,), pairs (n, 2) of (u, v))."""
+        n = lib().oracle_flat_blocks_export(self._h, None, None)
+        off = np.zeros(self.n_blocks + 1, np.uint64)
+        pairs = np.zeros((n, 2), np.uint32)
+        lib().oracle_flat_blocks_export(self._h, _p(off), _p(pairs))
+        return off, pairs
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().oracle_flat_blocks_free(self._h)
+            self._h = None
+
+
 def vexpand(g, sources, k_min, k_max, path="any", direction="forward", targets=None,
-            stack_row_count=1024, want_matrix=True, hop_stats=False):
+            stack_row_count=1024, want_matrix=True, hop_stats=False, blocks=None):
     """VExpand(Dense) on the CPU. Returns (logical words (V, ceil(S/64)) or None,
-    distances or None, hop stats dict or None)."""
+    distances or None, hop stats dict or None).  With `blocks` (a FlatBlocks of
+    this graph and direction) the hops run the reference's BlockHilbert loop
+    over that layout; otherwise a pull over the CSR in-lists."""
     src = np.ascontiguousarray(sources, dtype=np.uint32)
     S = len(src)
     W = (S + 63) // 64
@@ -96,9 +133,15 @@ def vexpand(g, sources, k_min, k_max, path="any", direction="forward", targets=N
     tg = None if targets is None else np.ascontiguousarray(targets, dtype=np.uint32)
     dist = np.zeros(S, dtype=np.int32) if path == "find_shortest" else None
     hs = np.zeros(4 * 64, dtype=np.uint64) if hop_stats else None
-    rc = lib().oracle_vexpand(g.V, _p(g.fwd_off), _p(g.fwd_dst), _p(g.rev_off), _p(g.rev_src),
-                              1 if g.directed else 0, _p(src), S, k_min, k_max, _PATHS[path],
-                              _DIRS[direction], stack_row_count, _p(tg), _p(dist), _p(out), _p(hs))
+    if blocks is not None:
+        if blocks.V != g.V or blocks.direction != direction:
+            raise ValueError("blocks were built for another graph or direction")
+        rc = lib().oracle_vexpand_blocks(blocks._h, _p(src), S, k_min, k_max, _PATHS[path], stack_row_count,
+                                         _p(tg), _p(dist), _p(out), _p(hs))
+    else:
+        rc = lib().oracle_vexpand(g.V, _p(g.fwd_off), _p(g.fwd_dst), _p(g.rev_off), _p(g.rev_src),
+                                  1 if g.directed else 0, _p(src), S, k_min, k_max, _PATHS[path],
+                                  _DIRS[direction], stack_row_count, _p(tg), _p(dist), _p(out), _p(hs))
     if rc:
         raise ValueError("oracle_vexpand rejected its arguments")
     st = None

@@ -25,6 +25,7 @@ def test_reference_arm_line():
     assert d["config"]["workload"] == "rmat16_pattern"
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+    assert "BlockHilbert" in cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
 
@@ -52,3 +53,23 @@ def test_serving_oracle_counts():
         want = (O.matrix_count(words, len(r.sources), g.V), O.hash_join(k, a, 1, only_count=True)[2],
                 P.triangle_count(g, r.sources))
         assert got == want and got[1] > 0 and got[2] > 0
+
+
+def test_batched_cpu_leg_counts():
+    """The batched workload's CPU leg (bench.cpu_batched, the BlockHilbert hop
+    over the bench's block layout) gives, per query, the join count of the
+    CSR-pull oracle and of numpy (sum of the key columns' popcounts)."""
+    import numpy as np
+    sys.path.insert(0, str(ROOT))
+    import bench
+    from oracle import pyoracle as O
+    from vertexsurge_gb300 import batch, graphgen
+    g = graphgen.zipf(5000, 60000, 2.1, 2000, seed=14)
+    queries = batch.make_queries(g, 5, (16, 300), (2, 5), (50, 5000), seed=4)
+    idx, counts, dt = bench.cpu_batched(g, {"batched": {"cpu_queries": 4}}, queries, bench.cpu_blocks(g))
+    assert idx == [0, 1, 2, 3] and dt > 0
+    for i, got in zip(idx, counts):
+        q = queries[i]
+        words, _, _ = O.vexpand(g, q.sources, 1, q.k_max, "shortest", "forward")
+        colcnt = np.bitwise_count(words).sum(axis=1, dtype=np.int64)
+        assert got == int(colcnt[q.keys].sum()) and got > 0

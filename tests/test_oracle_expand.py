@@ -91,3 +91,70 @@ def test_oracle_self_ring_counts(small):
     R = words_to_bool(w2, len(src))
     diag = int(R[np.arange(len(src)), src].sum())
     assert diag == int(G.reach_any(g, src, 1, 3)[np.arange(len(src)), src].sum())
+
+
+# ---- the reference's BlockHilbert hop over its flat edge layout -------------
+
+@pytest.mark.parametrize("path,k_min,k_max,direction", CASES)
+def test_blockhilbert_equals_csr_pull(small, path, k_min, k_max, direction):
+    for name, g in small.items():
+        S = 70
+        src = graphgen.sample_sources(g.V, S, seed=21)
+        want, _, st_want = O.vexpand(g, src, k_min, k_max, path, direction, hop_stats=True)
+        for n_blocks in (1, 7, 64):
+            b = O.FlatBlocks(g, direction, n_blocks)
+            got, _, st = O.vexpand(g, src, k_min, k_max, path, direction, hop_stats=True, blocks=b)
+            assert np.array_equal(got, want), (name, n_blocks)
+            assert st == st_want, (name, n_blocks)
+
+
+def test_blockhilbert_find_shortest_and_stacks(small):
+    g = small["rmat11_skew"]
+    b = O.FlatBlocks(g, "forward", 16)
+    src = graphgen.sample_sources(g.V, 100, seed=31)
+    tgt = graphgen.sample_sources(g.V, 100, seed=32)
+    tgt[:5] = src[:5]
+    _, dist, _ = O.vexpand(g, src, 1, 50, "find_shortest", "forward", targets=tgt, blocks=b)
+    assert np.array_equal(dist, G.find_shortest(g, src, tgt))
+    # three 512-row stacks, the last one partly used
+    src = graphgen.sample_sources(g.V, 1300, seed=33)
+    for path in ("any", "shortest"):
+        want, _, _ = O.vexpand(g, src, 1, 3, path, "forward", stack_row_count=512)
+        got, _, _ = O.vexpand(g, src, 1, 3, path, "forward", stack_row_count=512, blocks=b)
+        assert np.array_equal(got, want), path
+
+
+def test_blockhilbert_layout_is_the_importers(small):
+    """The blocks are the reference importer's partitioned hilbert lists of the
+    forward direction: the same block bounds and pair order as graph_dir's
+    restatement of partition_by_dst + sort_edge_in_peano2."""
+    from vertexsurge_gb300 import graph_dir as GD
+    for name in ("rmat10", "zipf3000"):
+        g = small[name]
+        count = 13
+        off, pairs = O.FlatBlocks(g, "forward", count).export()
+        src = np.repeat(np.arange(g.V, dtype=np.uint32), np.diff(g.fwd_off).astype(np.int64))
+        dst = np.asarray(g.fwd_dst, np.uint32)
+        by_dst = GD._pair_order(dst, src)
+        s_, t_ = src[by_dst], dst[by_dst]
+        bounds = GD.partition_by_dst(t_, count)
+        assert [int(x) for x in off] == [b for b, _ in bounds] + [len(t_)], name
+        for b, e in bounds:
+            perm = GD.order_edges(s_[b:e], t_[b:e], "hilbert", g.V, g.V)
+            assert np.array_equal(pairs[b:e, 0], s_[b:e][perm]), name
+            assert np.array_equal(pairs[b:e, 1], t_[b:e][perm]), name
+
+
+def test_blockhilbert_more_blocks_than_targets():
+    g = graphgen.from_edges(6, np.array([0, 1, 2], np.uint32), np.array([3, 3, 4], np.uint32))
+    b = O.FlatBlocks(g, "forward", 64)
+    off, pairs = b.export()
+    assert len(pairs) == 3 and off[0] == 0 and int(off[-1]) == 3
+    assert np.all(np.diff(off.astype(np.int64)) >= 0)
+    src = np.array([0, 1, 2, 5], np.uint32)
+    for path in ("any", "shortest"):
+        want, _, _ = O.vexpand(g, src, 1, 2, path, "forward")
+        got, _, _ = O.vexpand(g, src, 1, 2, path, "forward", blocks=b)
+        assert np.array_equal(got, want)
+    with pytest.raises(ValueError):
+        O.vexpand(g, src, 1, 2, "any", "backward", blocks=b)

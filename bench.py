@@ -187,10 +187,10 @@ def batched_config(args, g, queries, world):
             "parallelism": f"replicas{world}"}
 
 
-# Block count of the reference's BlockHilbert edge layout in the CPU legs (its
-# importer's -b option): 16 blocks per Grace core, which the guided schedule
-# balances; 256 blocks ran 1.07x faster than 64 on the 10M-vertex graph.
-CPU_BLOCKS = 256
+# Block count of the reference's BlockHilbert edge layout in the CPU legs: the
+# importer's -b 1000 of the reference's documented import commands (256 blocks
+# ran within 4% of it on the 10M-vertex graph).
+CPU_BLOCKS = 1000
 
 
 def cpu_blocks(g):

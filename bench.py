@@ -187,6 +187,27 @@ def batched_config(args, g, queries, world):
             "parallelism": f"replicas{world}"}
 
 
+def cpu_model() -> str:
+    """The host CPU as /proc/cpuinfo names it: the model name on x86, the
+    implementer and part numbers on Arm (0x41 / 0xd4f is Neoverse V2, the
+    Grace core)."""
+    import platform
+    import re
+    try:
+        txt = Path("/proc/cpuinfo").read_text()
+    except OSError:
+        return platform.machine()
+    m = re.search(r"^model name\s*:\s*(.+)$", txt, re.M)
+    if m:
+        return m.group(1).strip()
+    imp = re.search(r"^CPU implementer\s*:\s*(\S+)", txt, re.M)
+    part = re.search(r"^CPU part\s*:\s*(\S+)", txt, re.M)
+    if imp and part:
+        name = " (Neoverse V2)" if (imp.group(1), part.group(1)) == ("0x41", "0xd4f") else ""
+        return f"{platform.machine()} implementer {imp.group(1)} part {part.group(1)}{name}"
+    return platform.machine()
+
+
 # Block count of the reference's BlockHilbert edge layout in the CPU legs: the
 # importer's -b 1000 of the reference's documented import commands (256 blocks
 # ran within 4% of it on the 10M-vertex graph).
@@ -217,7 +238,7 @@ def cpu_baseline(g, w, sa):
     O.vexpand(g, src, k0, k1, "shortest", "forward", want_matrix=False, blocks=blk)
     dt = time.perf_counter() - t
     return {"value": src_edges / dt / 1e9, "unit": "Gsrc-edges/s", "cores": O.lib().oracle_get_threads(),
-            "kind": "port",
+            "kind": "port", "cpu_model": cpu_model(),
             "sample": f"VExpand(Shortest, [{k0},{k1}], Forward) from the first {S} A sources on the full "
                       f"graph, the reference's BlockHilbert hop over {CPU_BLOCKS} target blocks, one run of "
                       f"{dt:.1f} s ({src_edges / 1e9:.2f} Gsrc-edges)"}, words
@@ -272,7 +293,7 @@ def run_reference_batched(args, w):
             "ms_per_step": 1000 * sum(times) / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded power-law graph, uniform sources)",
             "config": batched_config(args, g, queries, args.gpus),
-            "cpu_baseline": {"value": value, "unit": "queries/s", "cores": cores, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": "queries/s", "cores": cores, "kind": "port", "cpu_model": cpu_model(),
                              "sample": desc},
             "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -442,7 +463,7 @@ def run_gpu_batched(args, w, rank, world, local_rank):
                              f"(queries {sample}); the batch also equals {len(chk)} solo GPU runs"}
         from oracle import pyoracle as O
         cpu = {"value": len(sample) / dt, "unit": "queries/s", "cores": O.lib().oracle_get_threads(),
-               "kind": "port", "sample": f"{len(sample)} queries with <= 2048 sources, one at a time, {dt:.1f} s"}
+               "kind": "port", "cpu_model": cpu_model(), "sample": f"{len(sample)} queries with <= 2048 sources, one at a time, {dt:.1f} s"}
     line = {"metric": "batched queries/s", "value": value, "unit": "queries/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64",
@@ -503,7 +524,7 @@ def run_join(args, w, rank, world, local_rank, reference=False):
                 "data": "synthetic (Zipf-skewed vertex-id keys)",
                 "config": {"workload": args.workload, "V": w["V"], "sizes": list(w["sizes"])},
                 "cpu_baseline": {"value": value, "unit": "Mrows/s", "cores": O.lib().oracle_get_threads(),
-                                 "kind": "port", "sample": f"HashJoin count of two {n}-row key columns"},
+                                 "kind": "port", "cpu_model": cpu_model(), "sample": f"HashJoin count of two {n}-row key columns"},
                 "e2e": {"value": value, "unit": "Mrows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -612,7 +633,7 @@ def run_serving(args, w, rank, world, local_rank):
                           "data": "synthetic (seeded R-MAT graph, Poisson arrivals)",
                           "config": {"workload": args.workload, "V": g.V, "E": g.E},
                           "cpu_baseline": {"value": value, "unit": "queries/s", "cores": O.lib().oracle_get_threads(),
-                                           "kind": "port", "sample": f"queries {idx} of the trace, one at a time"},
+                                           "kind": "port", "cpu_model": cpu_model(), "sample": f"queries {idx} of the trace, one at a time"},
                           "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}), flush=True)
         return
@@ -725,7 +746,7 @@ def run_reference(args, w, rank, world):
             "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded power-law graph, uniform sources)",
             "config": pattern_config(args, g, w, args.gpus),
-            "cpu_baseline": {"value": value, "unit": "Gsrc-edges/s", "cores": cores, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": "Gsrc-edges/s", "cores": cores, "kind": "port", "cpu_model": cpu_model(),
                              "sample": sample},
             "e2e": {"value": value, "unit": "Gsrc-edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

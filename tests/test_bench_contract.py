@@ -25,7 +25,7 @@ def test_reference_arm_line():
     assert d["config"]["workload"] == "rmat16_pattern"
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
-    assert "BlockHilbert" in cb["sample"]
+    assert "BlockHilbert" in cb["sample"] and cb["cpu_model"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
 

@@ -40,6 +40,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+NOMINAL_HBM_GBS = 7900.0  # GB300 HBM3e, nominal
 FALLBACK_HBM_GBS = 6800.0
 
 WORKLOADS = {
@@ -577,7 +578,8 @@ def run_join(args, w, rank, world, local_rank, reference=False):
             "config": {"workload": args.workload, "V": w["V"], "sizes": list(w["sizes"])},
             "sizes": rows,
             "roofline": {"bound": "hbm", "achieved": big["GB_per_s"], "peak": peak, "unit": "GB/s",
-                         "frac": big["frac"], "traffic": None, "peak_source": peak_kind,
+                         "frac": big["frac"], "frac_nominal": big["GB_per_s"] / NOMINAL_HBM_GBS,
+                         "traffic": None, "peak_source": peak_kind,
                          "bytes": "4 N_b + 4 N_p + 16 cap + 16 N_b + 32 N_p (largest size)"},
             "cpu_baseline": None, "parity": {"sizes": len(rows), "equal": True,
                                              "against": "numpy sum of multiplicity products per key"},
@@ -963,6 +965,7 @@ def run_gpu(args, w, rank, world, local_rank):
     per_launch_ms = pull_ms / max(1, pull_launches)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if achieved else None,
+                "frac_nominal": achieved / NOMINAL_HBM_GBS if achieved else None,
                 "bytes": "compulsory bytes per PULL hop, 8(V+1) + 4 E_act + 4 * 8W V (CSR offsets, active "
                          "in-list entries, frontier read, next-layer write, visited read + write), E_act exact "
                          "from the stats pass",

@@ -73,3 +73,22 @@ def test_batched_cpu_leg_counts():
         words, _, _ = O.vexpand(g, q.sources, 1, q.k_max, "shortest", "forward")
         colcnt = np.bitwise_count(words).sum(axis=1, dtype=np.int64)
         assert got == int(colcnt[q.keys].sum()) and got > 0
+
+
+def test_cpu_baseline_leg():
+    """The default workload's CPU leg (bench.cpu_baseline) on a small graph:
+    its matrix is the oracle's VExpand of the sample, and its record carries
+    the keys of the line's cpu_baseline."""
+    import numpy as np
+    sys.path.insert(0, str(ROOT))
+    import bench
+    from oracle import pyoracle as O
+    from vertexsurge_gb300 import graphgen
+    g = graphgen.zipf(4000, 50000, 2.1, 1000, seed=14)
+    sa = graphgen.sample_sources(g.V, 300, seed=2)
+    w = {"cpu_S": 128, "hops_a": (1, 4)}
+    rec, words = bench.cpu_baseline(g, w, sa)
+    want, _, _ = O.vexpand(g, sa[:128], 1, 4, "shortest", "forward")
+    assert np.array_equal(words, want)
+    assert rec["value"] > 0 and rec["unit"] == "Gsrc-edges/s" and rec["kind"] == "port"
+    assert rec["cores"] >= 1 and rec["cpu_model"] and "BlockHilbert" in rec["sample"]
